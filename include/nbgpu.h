@@ -1,0 +1,255 @@
+/*
+ * nbgpu.h - C ABI of the GB300 compute cycle for nbodygo (libnbgpu.so).
+ *
+ * One context owns the device copy of a body collection and runs the
+ * reference's compute cycle on it:
+ *
+ *   force + collision detection   cmd/body/body.go:148-225 (Compute,
+ *                                  calcForceFrom, Collided)
+ *   collision resolution          cmd/body/body_collection.go:212-233
+ *                                  (ProcessMods), event.go:53-62,
+ *                                  body.go:228-264, collisioncalc.go:26-186,
+ *                                  fragcalc.go:24-117
+ *   integration                   cmd/body/body.go:114-139 (Update)
+ *   compaction + adds             cmd/body/body_collection.go:253-296 (Cycle)
+ *
+ * nbg_step replaces the block of ComputationRunner.runOneComputation from
+ * "submit slices" to "bc.Cycle(r.R)" (cmd/runner/computation-runner.go:284-322).
+ *
+ * Conventions
+ *  - Every call returns NBG_OK (0) or an NBG_E_* status; nbg_last_error gives
+ *    a message.  Nothing aborts the process or traps on the device.
+ *  - Inputs are copied before a call returns; no caller pointer is kept
+ *    (this satisfies the cgo pointer-passing rules).
+ *  - One thread drives a context at a time (the runner goroutine); calls on
+ *    one context are not synchronised against each other.
+ *  - Body order is the reference's array order: results depend on it exactly
+ *    as in the reference (force summation order, event order, compaction).
+ *  - Strings (Name, Class), colour and light intensity stay with the caller,
+ *    keyed by body id.
+ */
+#ifndef NBGPU_H
+#define NBGPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define NBG_OK 0
+#define NBG_E_CUDA 1     /* a CUDA runtime call failed */
+#define NBG_E_ARG 2      /* bad argument (null pointer, size, enum value) */
+#define NBG_E_OVERFLOW 3 /* a device buffer was too small; state is unchanged */
+#define NBG_E_TIMEOUT 4  /* a bounded device wait gave up */
+#define NBG_E_NAN 5      /* non-finite value where a finite one is required */
+#define NBG_E_STATE 6    /* call not valid in the context's current state */
+
+/* collision behaviours, values of globals.CollisionBehavior
+ * (cmd/globals/globals.go:9-16) */
+#define NBG_NONE 0
+#define NBG_SUBSUME 1
+#define NBG_ELASTIC 2
+#define NBG_FRAGMENT 3
+
+/* body flag bits (Body.Exists, IsSun, Pinned, WithTelemetry and the private
+ * fragmenting / collided flags, cmd/body/body.go:34-52) */
+#define NBG_F_EXISTS 0x01u
+#define NBG_F_IS_SUN 0x02u
+#define NBG_F_PINNED 0x04u
+#define NBG_F_TELEMETRY 0x08u
+#define NBG_F_FRAGMENTING 0x10u
+#define NBG_F_COLLIDED 0x20u
+
+/* precision forms */
+#define NBG_PRECISION_FP64 0  /* plain: the reference's FP64 arithmetic, op for op */
+#define NBG_PRECISION_MIXED 1 /* FP32 pair terms, FP64 everything else */
+
+/* event types reported by nbg_get_events (event.go:18-24) */
+#define NBG_EV_COLLISION 0 /* b1.ResolveCollision(b2) */
+#define NBG_EV_SUBSUME 1   /* b1 subsumes b2 */
+
+typedef struct nbg_ctx nbg_ctx;
+
+/*
+ * Structure-of-arrays view of a body collection in host memory.  Element k of
+ * every array describes body k.  On input, the optional arrays may be NULL:
+ * r defaults to 1 (NewBody, body.go:78), forces and fragment state to 0.
+ * On output, NULL arrays are skipped.
+ */
+typedef struct nbg_soa {
+    /* public Body fields (body.go:34-48) */
+    int64_t *id;
+    double *x, *y, *z, *vx, *vy, *vz, *radius, *mass;
+    double *frag_factor, *frag_step;
+    int32_t *collision; /* NBG_NONE .. NBG_FRAGMENT */
+    uint32_t *flags;    /* NBG_F_* */
+    /* private Body fields (body.go:49-52), optional */
+    double *r;          /* restitution copy used by doElastic */
+    double *fx, *fy, *fz;
+    double *frag_radius, *frag_new_radius, *frag_mass;
+    int64_t *frag_fragments;
+    double *frag_cx, *frag_cy, *frag_cz;
+} nbg_soa;
+
+/* Per-call summary filled by nbg_step. */
+typedef struct nbg_step_info {
+    int64_t steps_done;        /* steps completed by this call */
+    int64_t n_bodies;          /* bodies after the last Cycle */
+    int64_t interactions;      /* sum over steps of N*(N-1), N at step start */
+    int64_t events;            /* collision + subsume events resolved */
+    int64_t fragments_emitted; /* bodies added by fragmentation */
+    int64_t removed;           /* bodies removed by Cycle */
+    int64_t nan_removed;       /* bodies removed because x, y or z became NaN */
+    int64_t next_id;           /* next id NextId() would return */
+} nbg_step_info;
+
+/* Renderable (cmd/body/renderable.go:9-17) minus host-side colour/intensity. */
+typedef struct nbg_renderable {
+    int64_t id;
+    float x, y, z;
+    uint32_t flags; /* NBG_F_EXISTS, NBG_F_IS_SUN */
+    double radius;
+} nbg_renderable;
+
+/* One resolved event of the last step, in the order it was handled. */
+typedef struct nbg_event {
+    int64_t id1, id2; /* b1, b2 of event.go:38-41 */
+    int32_t type;     /* NBG_EV_* */
+    int32_t pad;
+} nbg_event;
+
+/* ModBody edit of one body (body.go:274-313 ApplyMods, after parsing).  Each
+ * bit of `mask` selects one field. */
+#define NBG_M_X 0x0001u
+#define NBG_M_Y 0x0002u
+#define NBG_M_Z 0x0004u
+#define NBG_M_VX 0x0008u
+#define NBG_M_VY 0x0010u
+#define NBG_M_VZ 0x0020u
+#define NBG_M_MASS 0x0040u
+#define NBG_M_RADIUS 0x0080u
+#define NBG_M_FRAG_FACTOR 0x0100u
+#define NBG_M_FRAG_STEP 0x0200u
+#define NBG_M_COLLISION 0x0400u
+#define NBG_M_TELEMETRY 0x0800u
+#define NBG_M_EXISTS 0x1000u
+typedef struct nbg_edit {
+    int64_t id;  /* body to modify */
+    uint32_t mask;
+    int32_t collision;
+    double x, y, z, vx, vy, vz, mass, radius, frag_factor, frag_step;
+    int32_t telemetry, exists;
+} nbg_edit;
+
+/* ---- context ---------------------------------------------------------- */
+
+/* Creates a context on CUDA device `device` able to hold `capacity` bodies
+ * (it grows on demand).  precision: NBG_PRECISION_FP64 or _MIXED.
+ * Replaces NewComputationRunner's worker pool (computation-runner.go:81-98). */
+int nbg_create(int device, int precision, int64_t capacity, nbg_ctx **out);
+void nbg_destroy(nbg_ctx *ctx);
+const char *nbg_last_error(const nbg_ctx *ctx);
+int nbg_set_precision(nbg_ctx *ctx, int precision);
+/* Runs the context's work on the caller's CUDA stream (a cudaStream_t passed
+ * as void *; NULL restores the context's own stream). */
+int nbg_set_stream(nbg_ctx *ctx, void *stream);
+
+/* Seed of the fragment-position generator and the id counter (NextId,
+ * body.go:316-329).  Fragments take ids from this counter. */
+int nbg_set_seed(nbg_ctx *ctx, uint64_t seed);
+int nbg_set_next_id(nbg_ctx *ctx, int64_t next_id);
+int nbg_get_next_id(nbg_ctx *ctx, int64_t *next_id);
+/* Cycle index used to key the fragment generator (starts at 0). */
+int nbg_set_cycle(nbg_ctx *ctx, uint64_t cycle);
+
+/* ---- body set ---------------------------------------------------------- */
+
+/* Replaces the whole collection (NewSimBodyCollection, body_collection.go:45-68). */
+int nbg_set_bodies(nbg_ctx *ctx, const nbg_soa *host, int64_t n);
+/* Number of bodies in the array (BodyCollection.Count, body_collection.go:203-207). */
+int nbg_count(nbg_ctx *ctx, int64_t *n);
+/* Copies up to `cap` bodies out; *n receives the count. */
+int nbg_get_state(nbg_ctx *ctx, nbg_soa *host, int64_t cap, int64_t *n);
+
+/* Enqueue(NewAdd(b)) for n bodies (body_collection.go:82-88, event.go:104-111):
+ * they are appended by the next step's Cycle, newest first, with r = R.
+ * If host->id is NULL or an entry is negative, an id is taken from the
+ * counter; assigned ids are written to ids_out (may be NULL). */
+int nbg_add_bodies(nbg_ctx *ctx, const nbg_soa *host, int64_t n, int64_t *ids_out);
+
+/* ModBody by id (body_collection.go:154-191 HandleModBody): applies each edit
+ * to every body with that id; results[k] = number of bodies matched. */
+int nbg_apply_edits(nbg_ctx *ctx, const nbg_edit *edits, int64_t k, int32_t *results);
+
+/* RemoveBodies (computation-runner.go:171-216 processDeletes): count == -1
+ * removes every body, otherwise `count` unpinned bodies spread evenly through
+ * the array.  *removed receives the number removed (may be NULL). */
+int nbg_remove_bodies(nbg_ctx *ctx, int64_t count, int64_t *removed);
+
+/* GetBody by id (body_collection.go:111-135): copies the first body with that
+ * id into element 0 of `host`; *found = 0 if there is none. */
+int nbg_get_body(nbg_ctx *ctx, int64_t id, nbg_soa *host, int32_t *found);
+
+/* ---- the cycle ---------------------------------------------------------- */
+
+/* Runs `nsteps` compute cycles with time step dt (timeScaling) and
+ * coefficient of restitution R.  nsteps > 1 replays a CUDA graph of one cycle.
+ * On NBG_E_OVERFLOW the context grows the buffer that was short and the
+ * interrupted cycle can be re-run: state is left as it was before it. */
+int nbg_step(nbg_ctx *ctx, double dt, double R, int nsteps, nbg_step_info *info);
+
+/* Runs only the force + collision-detection pass of a cycle on the current
+ * state: the forces of bodies that exist and are not fragmenting are
+ * recomputed; nothing else changes and the detected events are discarded.
+ * For diagnostics and accuracy measurements. */
+int nbg_force_pass(nbg_ctx *ctx);
+
+/* Renderables written by the last cycle's Update (one per body in the array
+ * before compaction; renderable.go:22-40). */
+int nbg_get_renderables(nbg_ctx *ctx, nbg_renderable *host, int64_t cap, int64_t *n);
+
+/* Events resolved by the last cycle, in resolution order.  Self-collisions
+ * (b1 == b2), which the reference enqueues and then resolves as no-ops
+ * (collisioncalc.go:89-92), are not reported. */
+int nbg_get_events(nbg_ctx *ctx, nbg_event *host, int64_t cap, int64_t *n);
+
+/* Net force of the last cycle's force pass for every body (fx, fy, fz of
+ * body.go:49).  Any pointer may be NULL. */
+int nbg_get_forces(nbg_ctx *ctx, double *fx, double *fy, double *fz, int64_t cap, int64_t *n);
+
+/* Total energy (kinetic + pairwise potential, FP64) and momentum of the bodies
+ * that exist; a diagnostic, O(N^2) on the device. */
+int nbg_energy(nbg_ctx *ctx, double *kinetic, double *potential, double momentum[3]);
+
+/* ---- measurement ------------------------------------------------------- */
+
+/* Device time of the kernels of the last nbg_step call, summed over its
+ * cycles, measured with CUDA events on the context's stream.  Slot 0 is the
+ * pair (force + detection) kernel, 1 everything else of the cycle. */
+typedef struct nbg_timing {
+    double pair_ms;
+    double other_ms;
+    int64_t pair_launches;
+    int64_t kernel_launches; /* all kernels of this library launched */
+} nbg_timing;
+int nbg_enable_timing(nbg_ctx *ctx, int on);
+int nbg_get_timing(nbg_ctx *ctx, nbg_timing *t);
+
+/* Tuning knobs of the pair kernels (0 = default). */
+#define NBG_OPT_SPLIT 1      /* mixed: j-range splits per i-tile */
+#define NBG_OPT_GRAPH 2      /* 0 = launch each cycle directly, 1 = CUDA graph */
+#define NBG_OPT_EV_CAP 3     /* event-list capacity (rounded up to a power of two) */
+#define NBG_OPT_FRAG_CAP 4   /* fragments one cycle may emit */
+int nbg_set_option(nbg_ctx *ctx, int key, int64_t value);
+
+/* Peak probes: FFMA (FP32) and DFMA (FP64) throughput of the device in
+ * FLOP/s (an FMA counts 2), measured with dependent-chain kernels. */
+int nbg_probe_peaks(int device, double *fp32_flops, double *fp64_flops, double *sm_clock_mhz);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* NBGPU_H */

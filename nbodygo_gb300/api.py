@@ -1,0 +1,206 @@
+"""Python host binding of libnbgpu.so.
+
+`Simulation` owns one nbg_ctx: the device copy of a body collection and the
+compute cycle on it.  Every method is a thin call into the C ABI
+(include/nbgpu.h); there is no CPU code path - if the CUDA library is missing
+or no GPU is visible, the constructor raises.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import _abi as A
+
+_LIB = None
+LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "libnbgpu.so")
+
+
+class NbgError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"nbg status {code}: {msg}")
+        self.code = code
+
+
+def load_library(path=None):
+    """Loads libnbgpu.so (built in-tree by nbodygo_gb300.build); raises if absent."""
+    global _LIB
+    if _LIB is not None and path is None:
+        return _LIB
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        raise OSError(f"{p} not found: run `python -m nbodygo_gb300.build` (the CUDA library is required)")
+    lib = C.CDLL(p)
+    A.declare(lib)
+    if path is None:
+        _LIB = lib
+    return lib
+
+
+def probe_peaks(device=0):
+    """(fp32 FLOP/s, fp64 FLOP/s, SM MHz) measured by FMA-chain kernels."""
+    lib = load_library()
+    f32, f64, mhz = C.c_double(), C.c_double(), C.c_double()
+    rc = lib.nbg_probe_peaks(device, C.byref(f32), C.byref(f64), C.byref(mhz))
+    if rc != A.NBG_OK:
+        raise NbgError(rc, "peak probe failed")
+    return f32.value, f64.value, mhz.value
+
+
+class Simulation:
+    """A body collection on one GPU with the nbodygo compute cycle."""
+
+    def __init__(self, precision="fp64", capacity=0, device=0, seed=None):
+        self.lib = load_library()
+        self.precision = precision
+        p = A.PRECISION_MIXED if precision == "mixed" else A.PRECISION_FP64
+        ctx = C.c_void_p()
+        rc = self.lib.nbg_create(device, p, int(capacity), C.byref(ctx))
+        if rc != A.NBG_OK:
+            raise NbgError(rc, self.lib.nbg_last_error(None).decode())
+        self.ctx = ctx
+        if seed is not None:
+            self._check(self.lib.nbg_set_seed(self.ctx, int(seed) & (2 ** 64 - 1)))
+
+    def close(self):
+        if getattr(self, "ctx", None):
+            self.lib.nbg_destroy(self.ctx)
+            self.ctx = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def _check(self, rc):
+        if rc != A.NBG_OK:
+            raise NbgError(rc, self.lib.nbg_last_error(self.ctx).decode())
+
+    # ---- configuration ----
+    def set_precision(self, precision):
+        self.precision = precision
+        self._check(self.lib.nbg_set_precision(self.ctx, A.PRECISION_MIXED if precision == "mixed" else A.PRECISION_FP64))
+
+    def set_stream(self, stream_handle):
+        """Run on an external cudaStream_t (an int handle; 0/None = own stream)."""
+        self._check(self.lib.nbg_set_stream(self.ctx, C.c_void_p(stream_handle or None)))
+
+    def set_next_id(self, next_id):
+        self._check(self.lib.nbg_set_next_id(self.ctx, int(next_id)))
+
+    def next_id(self):
+        v = C.c_int64()
+        self._check(self.lib.nbg_get_next_id(self.ctx, C.byref(v)))
+        return v.value
+
+    def set_cycle(self, cycle):
+        self._check(self.lib.nbg_set_cycle(self.ctx, int(cycle)))
+
+    def set_option(self, key, value):
+        self._check(self.lib.nbg_set_option(self.ctx, int(key), int(value)))
+
+    def enable_timing(self, on=True):
+        self._check(self.lib.nbg_enable_timing(self.ctx, 1 if on else 0))
+
+    def timing(self):
+        t = A.NbgTiming()
+        self._check(self.lib.nbg_get_timing(self.ctx, C.byref(t)))
+        return {"pair_ms": t.pair_ms, "other_ms": t.other_ms, "pair_launches": t.pair_launches,
+                "kernel_launches": t.kernel_launches}
+
+    # ---- body set ----
+    def set_bodies(self, bodies):
+        n = len(bodies["x"])
+        soa, keep = A.soa_from_arrays(bodies)
+        self._check(self.lib.nbg_set_bodies(self.ctx, C.byref(soa), n))
+        del keep
+
+    def count(self):
+        v = C.c_int64()
+        self._check(self.lib.nbg_count(self.ctx, C.byref(v)))
+        return v.value
+
+    def state(self, fields=None):
+        n = self.count()
+        out = A.empty_state(n) if fields is None else {f: np.zeros(n, dtype=A.FIELD_DTYPES[f]) for f in fields}
+        soa, keep = A.soa_from_arrays(out)
+        got = C.c_int64()
+        self._check(self.lib.nbg_get_state(self.ctx, C.byref(soa), n, C.byref(got)))
+        del keep
+        return out
+
+    def add_bodies(self, bodies):
+        n = len(bodies["x"])
+        soa, keep = A.soa_from_arrays(bodies)
+        ids = np.zeros(max(n, 1), dtype=np.int64)
+        self._check(self.lib.nbg_add_bodies(self.ctx, C.byref(soa), n, ids.ctypes.data_as(C.POINTER(C.c_int64))))
+        del keep
+        return ids[:n]
+
+    def apply_edits(self, edits):
+        arr = A.edit_array(edits)
+        res = np.zeros(max(1, len(edits)), dtype=np.int32)
+        self._check(self.lib.nbg_apply_edits(self.ctx, arr, len(edits), res.ctypes.data_as(C.POINTER(C.c_int32))))
+        return res[:len(edits)]
+
+    def remove_bodies(self, count):
+        v = C.c_int64()
+        self._check(self.lib.nbg_remove_bodies(self.ctx, int(count), C.byref(v)))
+        return v.value
+
+    def get_body(self, body_id):
+        out = A.empty_state(1)
+        soa, keep = A.soa_from_arrays(out)
+        found = C.c_int32()
+        self._check(self.lib.nbg_get_body(self.ctx, int(body_id), C.byref(soa), C.byref(found)))
+        del keep
+        if not found.value:
+            return None
+        return {k: v[0] for k, v in out.items()}
+
+    # ---- the cycle ----
+    def step(self, dt, R=1.0, nsteps=1):
+        info = A.NbgStepInfo()
+        self._check(self.lib.nbg_step(self.ctx, float(dt), float(R), int(nsteps), C.byref(info)))
+        return {f: getattr(info, f) for f, _ in A.NbgStepInfo._fields_}
+
+    def force_pass(self):
+        """Recomputes the forces of the current state (no other change)."""
+        self._check(self.lib.nbg_force_pass(self.ctx))
+        return self.forces()
+
+    def renderables(self):
+        n = C.c_int64()
+        self._check(self.lib.nbg_get_renderables(self.ctx, None, 0, C.byref(n)))
+        out = np.zeros(n.value, dtype=A.RENDERABLE_DTYPE)
+        self._check(self.lib.nbg_get_renderables(self.ctx, out.ctypes.data_as(C.c_void_p), n.value, C.byref(n)))
+        return out
+
+    def events(self):
+        n = C.c_int64()
+        self._check(self.lib.nbg_get_events(self.ctx, None, 0, C.byref(n)))
+        out = np.zeros(n.value, dtype=A.EVENT_DTYPE)
+        self._check(self.lib.nbg_get_events(self.ctx, out.ctypes.data_as(C.c_void_p), n.value, C.byref(n)))
+        return out
+
+    def forces(self):
+        n = self.count()
+        fx, fy, fz = (np.zeros(n) for _ in range(3))
+        got = C.c_int64()
+        pd = C.POINTER(C.c_double)
+        self._check(self.lib.nbg_get_forces(self.ctx, fx.ctypes.data_as(pd), fy.ctypes.data_as(pd),
+                                            fz.ctypes.data_as(pd), n, C.byref(got)))
+        return fx, fy, fz
+
+    def energy(self):
+        ke, pe = C.c_double(), C.c_double()
+        mom = (C.c_double * 3)()
+        self._check(self.lib.nbg_energy(self.ctx, C.byref(ke), C.byref(pe), mom))
+        return ke.value, pe.value, (mom[0], mom[1], mom[2])

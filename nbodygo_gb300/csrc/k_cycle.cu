@@ -1,0 +1,900 @@
+/*
+ * k_cycle.cu - kernels of one compute cycle except the mixed-precision pair
+ * kernel: the plain FP64 pair kernel, fragment emission, event ordering,
+ * collision resolution, integration, compaction, and the cycle-boundary
+ * edits (RemoveBodies, ModBody, GetBody).
+ *
+ * This file must be compiled with --fmad=false (and -DNBG_NO_FMAD): every
+ * FP64 expression then rounds after each operation exactly like the
+ * reference's Go code on amd64, which is what makes the plain path
+ * bit-identical to the CPU oracle.
+ */
+#ifndef NBG_NO_FMAD
+#error "k_cycle.cu must be compiled with --fmad=false -DNBG_NO_FMAD"
+#endif
+
+#include "nbg_internal.cuh"
+#include "nbg_math.h"
+#include "nbg_shared.h"
+
+#define FULL_MASK 0xffffffffu
+
+/* ------------------------------------------------------------------------ */
+/* block-wide exclusive scan (blockDim.x == NBG_SCAN_BLOCK)                 */
+/* ------------------------------------------------------------------------ */
+
+__device__ static ll block_excl_scan(ll v, ll *total)
+{
+    __shared__ ll warp_tot[NBG_SCAN_BLOCK / 32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    ll x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        ll y = __shfl_up_sync(FULL_MASK, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) warp_tot[w] = x;
+    __syncthreads();
+    if (w == 0) {
+        ll t = warp_tot[lane];
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            ll y = __shfl_up_sync(FULL_MASK, t, o);
+            if (lane >= o) t += y;
+        }
+        warp_tot[lane] = t;
+    }
+    __syncthreads();
+    ll excl = x - v + (w > 0 ? warp_tot[w - 1] : 0);
+    *total = warp_tot[NBG_SCAN_BLOCK / 32 - 1];
+    __syncthreads();
+    return excl;
+}
+
+/* ------------------------------------------------------------------------ */
+/* cycle start                                                              */
+/* ------------------------------------------------------------------------ */
+
+__global__ void k_begin(DevCtl *ctl)
+{
+    if (threadIdx.x != 0 || ctl->error) return;
+    ll n = ctl->n;
+    ctl->n_before = n;
+    ctl->ev_count = 0;
+    ctl->frag_total = 0;
+    ctl->n_keep = n;
+    ctl->rend_n = 0;
+    ctl->last_ev_n = 0;
+    ctl->rmax_bits = 0;
+    ctl->xmax_bits = 0;
+    ctl->m_scale = 0.0;
+}
+
+/* Fragments body k emits this cycle: Compute calls fragment() for a body that
+ * exists and is fragmenting (body.go:148-154); the loop of fragcalc.go:96-111
+ * emits min(fragments, 101) when fragments > 0. */
+__device__ static ll frag_emit_count(const BodyArrays &A, ll k)
+{
+    unsigned f = A.flags[k];
+    if ((f & NBG_LIVE_MASK) != NBG_LIVE_MASK) return 0;
+    ll c = A.fr_cnt[k];
+    if (c <= 0) return 0;
+    return c < NBG_MAX_FRAGS_PER_CYCLE + 1 ? c : NBG_MAX_FRAGS_PER_CYCLE + 1;
+}
+
+__global__ void __launch_bounds__(NBG_SCAN_BLOCK) k_frag_blocksum(BodyArrays A, DevCtl *ctl, ll *blk_sum)
+{
+    if (ctl->error) return;
+    const ll n = ctl->n;
+    const ll base = (ll)blockIdx.x * NBG_SCAN_TILE;
+    if (base >= n) return;
+    ll s = 0;
+    for (int q = 0; q < NBG_SCAN_ITEMS; q++) {
+        ll k = base + (ll)threadIdx.x * NBG_SCAN_ITEMS + q;
+        if (k < n) s += frag_emit_count(A, k);
+    }
+    ll tot;
+    block_excl_scan(s, &tot);
+    if (threadIdx.x == 0) blk_sum[blockIdx.x] = tot;
+}
+
+__global__ void __launch_bounds__(NBG_SCAN_BLOCK) k_keep_blocksum(BodyArrays A, DevCtl *ctl, ll *blk_sum)
+{
+    if (ctl->error) return;
+    const ll n = ctl->n;
+    const ll base = (ll)blockIdx.x * NBG_SCAN_TILE;
+    if (base >= n) return;
+    ll s = 0;
+    for (int q = 0; q < NBG_SCAN_ITEMS; q++) {
+        ll k = base + (ll)threadIdx.x * NBG_SCAN_ITEMS + q;
+        if (k < n) s += (A.flags[k] & NBG_F_EXISTS) ? 1 : 0;
+    }
+    ll tot;
+    block_excl_scan(s, &tot);
+    if (threadIdx.x == 0) blk_sum[blockIdx.x] = tot;
+}
+
+/* Single-block exclusive scan of the per-block sums.  mode 0: fragment
+ * counts (checks capacities); mode 1: surviving bodies. */
+__global__ void __launch_bounds__(NBG_SCAN_BLOCK) k_scan_blocks(DevCtl *ctl, const ll *blk_sum, ll *blk_off, int mode,
+                                                                ll cap, ll frag_cap)
+{
+    if (ctl->error) return;
+    const ll n = ctl->n;
+    const ll nb = (n + NBG_SCAN_TILE - 1) / NBG_SCAN_TILE;
+    ll carry = 0;
+    for (ll b0 = 0; b0 < nb; b0 += NBG_SCAN_BLOCK) {
+        ll b = b0 + threadIdx.x;
+        ll v = b < nb ? blk_sum[b] : 0;
+        ll tot;
+        ll ex = block_excl_scan(v, &tot);
+        if (b < nb) blk_off[b] = carry + ex;
+        carry += tot;
+    }
+    if (threadIdx.x == 0) {
+        if (mode == 0) {
+            ctl->frag_total = carry;
+            ll need = n + carry + ctl->n_host_adds;
+            if (carry > frag_cap) {
+                ctl->error = NBG_E_OVERFLOW;
+                ctl->error_what = 3;
+                ctl->error_need = carry;
+            } else if (need > cap) {
+                ctl->error = NBG_E_OVERFLOW;
+                ctl->error_what = 1;
+                ctl->error_need = need;
+            }
+        } else {
+            ctl->n_keep = carry;
+        }
+    }
+}
+
+/* ------------------------------------------------------------------------ */
+/* K1: plain FP64 force + collision detection                              */
+/* ------------------------------------------------------------------------ */
+
+#define P64_BLOCK 64
+
+/* Detection rule of Compute's second pass (body.go:172-186) for a pair with
+ * Collided(i, j) true. Returns the event type or -1. */
+__device__ static int detect_event(unsigned bi, unsigned bj, double ri, double rj, double dist)
+{
+    bool ei = (bi == NBG_ELASTIC || bi == NBG_FRAGMENT);
+    bool ej = (bj == NBG_ELASTIC || bj == NBG_FRAGMENT);
+    if (ei && ej) return (int)NBG_EVT_COLL_IJ;
+    if (bi == NBG_SUBSUME || bj == NBG_SUBSUME) {
+        if (ri > rj && dist <= ri) return (int)NBG_EVT_SUB_IJ;
+        if (rj > ri && dist <= rj) return (int)NBG_EVT_SUB_JI;
+    }
+    return -1;
+}
+
+__device__ static void emit_event(DevCtl *ctl, ull *keys, ll cap, ll i, ll j, int type)
+{
+    ll slot = atomicAdd((unsigned long long *)&ctl->ev_count, 1ull);
+    if (slot < cap) keys[slot] = ((ull)i << 32) | ((ull)j << 2) | (ull)type;
+}
+
+/*
+ * One thread per body i.  For each j in array order (tiles of P64_BLOCK staged
+ * in shared memory) it evaluates exactly the reference's expressions
+ * (calcForceFrom, body.go:214-225): the sum runs over j in ascending order,
+ * so the result is bit-identical to the sequential loop.  The same dist
+ * decides Collided (body.go:192-208); hits are appended to the event list.
+ */
+__global__ void __launch_bounds__(P64_BLOCK) k_pair_fp64(BodyArrays A, DevCtl *ctl, ull *ev_keys, ll ev_cap)
+{
+    __shared__ double sx[P64_BLOCK], sy[P64_BLOCK], sz[P64_BLOCK], sm[P64_BLOCK], sr[P64_BLOCK];
+    __shared__ unsigned sf[P64_BLOCK];
+    if (ctl->error) return;
+    const ll n = ctl->n;
+    for (ll i0 = (ll)blockIdx.x * P64_BLOCK; i0 < n; i0 += (ll)gridDim.x * P64_BLOCK) {
+        const ll i = i0 + threadIdx.x;
+        const bool valid = i < n;
+        double xi = 0, yi = 0, zi = 0, mi = 0, ri = 0;
+        unsigned fi = 0;
+        if (valid) {
+            xi = A.x[i];
+            yi = A.y[i];
+            zi = A.z[i];
+            mi = A.m[i];
+            ri = A.rad[i];
+            fi = A.flags[i];
+        }
+        const bool live_i = valid && (fi & NBG_LIVE_MASK) == NBG_F_EXISTS;
+        const bool coll_i = (fi & NBG_F_COLLIDED) != 0;
+        const unsigned bi = NBG_BEHAVIOR(fi);
+        const double gmi = NBG_G * mi;
+        double fx = 0.0, fy = 0.0, fz = 0.0;
+        for (ll j0 = 0; j0 < n; j0 += P64_BLOCK) {
+            __syncthreads();
+            const ll jl = j0 + threadIdx.x;
+            if (jl < n) {
+                sx[threadIdx.x] = A.x[jl];
+                sy[threadIdx.x] = A.y[jl];
+                sz[threadIdx.x] = A.z[jl];
+                sm[threadIdx.x] = A.m[jl];
+                sr[threadIdx.x] = A.rad[jl];
+                sf[threadIdx.x] = A.flags[jl];
+            }
+            __syncthreads();
+            if (!live_i) continue;
+            const int cnt = (n - j0) < P64_BLOCK ? (int)(n - j0) : P64_BLOCK;
+            for (int t = 0; t < cnt; t++) {
+                const ll j = j0 + t;
+                const double dx = sx[t] - xi;
+                const double dy = sy[t] - yi;
+                const double dz = sz[t] - zi;
+                const double dist = sqrt(dx * dx + dy * dy + dz * dz);
+                const double rr = ri + sr[t];
+                const unsigned fj = sf[t];
+                const bool live_j = (fj & NBG_LIVE_MASK) == NBG_F_EXISTS;
+                if (live_j && j != i && (coll_i || dist > rr)) {
+                    const double force = gmi * sm[t] / (dist * dist);
+                    fx += force * dx / dist;
+                    fy += force * dy / dist;
+                    fz += force * dz / dist;
+                }
+                if (!coll_i && dist <= rr && j != i) {
+                    int type = detect_event(bi, NBG_BEHAVIOR(fj), ri, sr[t], dist);
+                    if (type >= 0) emit_event(ctl, ev_keys, ev_cap, i, j, type);
+                }
+            }
+        }
+        if (live_i) {
+            A.fx[i] = fx;
+            A.fy[i] = fy;
+            A.fz[i] = fz;
+        }
+    }
+}
+
+/* ------------------------------------------------------------------------ */
+/* K4: order the events (i ascending, then j)                               */
+/* ------------------------------------------------------------------------ */
+
+#define SORT_BLOCK 1024
+#define SORT_SMEM 4096
+
+__global__ void __launch_bounds__(SORT_BLOCK) k_sort_events(DevCtl *ctl, ull *keys, ll cap)
+{
+    __shared__ ull s[SORT_SMEM];
+    __shared__ int bail;
+    if (threadIdx.x == 0) {
+        bail = ctl->error != 0;
+        if (!bail && ctl->ev_count > cap) {
+            ctl->error = NBG_E_OVERFLOW;
+            ctl->error_what = 2;
+            ctl->error_need = ctl->ev_count;
+            bail = 1;
+        }
+    }
+    __syncthreads();
+    if (bail) return;
+    const ll cnt = ctl->ev_count;
+    if (cnt <= 1) return;
+    ll P = 1;
+    while (P < cnt) P <<= 1;
+    ull *d = keys;
+    if (P <= SORT_SMEM) {
+        d = s;
+        for (ll k = threadIdx.x; k < P; k += SORT_BLOCK) s[k] = k < cnt ? keys[k] : ~0ull;
+    } else {
+        for (ll k = cnt + threadIdx.x; k < P; k += SORT_BLOCK) keys[k] = ~0ull;
+    }
+    __syncthreads();
+    for (ll kk = 2; kk <= P; kk <<= 1) {
+        for (ll jj = kk >> 1; jj > 0; jj >>= 1) {
+            for (ll idx = threadIdx.x; idx < P; idx += SORT_BLOCK) {
+                ll ixj = idx ^ jj;
+                if (ixj > idx) {
+                    bool asc = (idx & kk) == 0;
+                    ull a = d[idx], b = d[ixj];
+                    if ((a > b) == asc) {
+                        d[idx] = b;
+                        d[ixj] = a;
+                    }
+                }
+            }
+            __syncthreads();
+        }
+    }
+    if (P <= SORT_SMEM)
+        for (ll k = threadIdx.x; k < cnt; k += SORT_BLOCK) keys[k] = s[k];
+}
+
+/* ------------------------------------------------------------------------ */
+/* K8: fragment emission (fragcalc.go:94-117)                               */
+/* ------------------------------------------------------------------------ */
+
+__global__ void __launch_bounds__(NBG_SCAN_BLOCK) k_frag_emit(BodyArrays A, BodyArrays F, DevCtl *ctl, const ll *blk_off)
+{
+    if (ctl->error) return;
+    const ll n = ctl->n;
+    const ll base = (ll)blockIdx.x * NBG_SCAN_TILE;
+    if (base >= n) return;
+    ll c[NBG_SCAN_ITEMS];
+    ll s = 0;
+    for (int q = 0; q < NBG_SCAN_ITEMS; q++) {
+        ll k = base + (ll)threadIdx.x * NBG_SCAN_ITEMS + q;
+        c[q] = k < n ? frag_emit_count(A, k) : 0;
+        s += c[q];
+    }
+    ll tot;
+    ll off = block_excl_scan(s, &tot) + blk_off[blockIdx.x];
+    const ll id0 = ctl->next_id;
+    const ull seed = ctl->seed, cycle = ctl->cycle;
+    for (int q = 0; q < NBG_SCAN_ITEMS; q++) {
+        ll k = base + (ll)threadIdx.x * NBG_SCAN_ITEMS + q;
+        if (k >= n) break;
+        unsigned fk = A.flags[k];
+        if ((fk & NBG_LIVE_MASK) != NBG_LIVE_MASK) continue;
+        /* for (; fragments > 0;) { fragments--; emit; cnt++; if cnt > 100 break } */
+        const ll parent = A.id[k];
+        const ull key = nbg_frag_key(seed, parent, cycle);
+        const double cx = A.fr_cx[k], cy = A.fr_cy[k], cz = A.fr_cz[k];
+        const double rad9 = A.fr_rad[k] * .9;
+        for (ll e = 0; e < c[q]; e++) {
+            double px, py, pz;
+            nbg_frag_point(key, (int)e, cx, cy, cz, rad9, &px, &py, &pz);
+            const ll slot = off + e;
+            F.id[slot] = id0 + slot;
+            F.x[slot] = px;
+            F.y[slot] = py;
+            F.z[slot] = pz;
+            F.vx[slot] = A.vx[k];
+            F.vy[slot] = A.vy[k];
+            F.vz[slot] = A.vz[k];
+            F.m[slot] = A.fr_mass[k];
+            F.rad[slot] = A.fr_newrad[k];
+            F.fx[slot] = 0;
+            F.fy[slot] = 0;
+            F.fz[slot] = 0;
+            F.ff[slot] = 0;
+            F.fs[slot] = 0;
+            F.rest[slot] = 0;
+            F.fr_rad[slot] = 0;
+            F.fr_newrad[slot] = 0;
+            F.fr_mass[slot] = 0;
+            F.fr_cx[slot] = 0;
+            F.fr_cy[slot] = 0;
+            F.fr_cz[slot] = 0;
+            F.fr_cnt[slot] = 0;
+            F.flags[slot] = NBG_F_EXISTS | ((unsigned)NBG_ELASTIC << NBG_BEHAVIOR_SHIFT);
+        }
+        off += c[q];
+        ll left = A.fr_cnt[k] - c[q];
+        A.fr_cnt[k] = left;
+        if (left <= 0) A.flags[k] = fk & ~NBG_F_EXISTS;
+    }
+}
+
+/* ------------------------------------------------------------------------ */
+/* K5: collision resolution, one thread, newest event first                 */
+/* ------------------------------------------------------------------------ */
+
+struct ElasticOut {
+    bool collided;
+    double vx1, vy1, vz1, vx2, vy2, vz2, vx_cm, vy_cm, vz_cm;
+};
+
+/* calcElasticCollision, collisioncalc.go:42-186 (coll3d), on bodies b and o. */
+__device__ static ElasticOut elastic_calc(const BodyArrays &A, ll b, ll o)
+{
+    ElasticOut res;
+    res.collided = false;
+    res.vx1 = res.vy1 = res.vz1 = res.vx2 = res.vy2 = res.vz2 = 0;
+    res.vx_cm = res.vy_cm = res.vz_cm = 0;
+    const double m1 = A.m[b], m2 = A.m[o], r1 = A.rad[b], r2 = A.rad[o];
+    const double x1 = A.x[b], y1 = A.y[b], z1 = A.z[b];
+    const double X2 = A.x[o], Y2 = A.y[o], Z2 = A.z[o];
+    const double ux1 = A.vx[b], uy1 = A.vy[b], uz1 = A.vz[b];
+    const double vx2 = A.vx[o], vy2 = A.vy[o], vz2 = A.vz[o];
+
+    const double r12 = r1 + r2;
+    const double m21 = m2 / m1;
+    const double x21 = X2 - x1, y21 = Y2 - y1, z21 = Z2 - z1;
+    const double vx21 = vx2 - ux1, vy21 = vy2 - uy1, vz21 = vz2 - uz1;
+    const double vx_cm = (m1 * ux1 + m2 * vx2) / (m1 + m2);
+    const double vy_cm = (m1 * uy1 + m2 * vy2) / (m1 + m2);
+    const double vz_cm = (m1 * uz1 + m2 * vz2) / (m1 + m2);
+    const double d = sqrt(x21 * x21 + y21 * y21 + z21 * z21);
+    const double v = sqrt(vx21 * vx21 + vy21 * vy21 + vz21 * vz21);
+    if (v == 0) return res;
+    /* ball 1 at the origin, ball 2 at rest */
+    const double px = x21, py = y21, pz = z21;
+    const double wx = -vx21, wy = -vy21, wz = -vz21;
+    const double theta2 = nbg_acos(pz / d);
+    const double phi2 = (px == 0 && py == 0) ? 0.0 : nbg_atan2(py, px);
+    const double st = nbg_sin(theta2), ct = nbg_cos(theta2);
+    const double sp = nbg_sin(phi2), cp = nbg_cos(phi2);
+    double vx1r = ct * cp * wx + ct * sp * wy - st * wz;
+    double vy1r = cp * wy - sp * wx;
+    double vz1r = st * cp * wx + st * sp * wy + ct * wz;
+    double fvz1r = vz1r / v;
+    if (fvz1r > 1)
+        fvz1r = 1;
+    else if (fvz1r < -1)
+        fvz1r = -1;
+    const double thetav = nbg_acos(fvz1r);
+    const double phiv = (vx1r == 0 && vy1r == 0) ? 0.0 : nbg_atan2(vy1r, vx1r);
+    const double dr = d * nbg_sin(thetav) / r12;
+    if (thetav > NBG_PIO2_HI || fabs(dr) > 1) return res;
+    const double alpha = nbg_asin(-dr);
+    const double beta = phiv;
+    const double sbeta = nbg_sin(beta), cbeta = nbg_cos(beta);
+    const double a = nbg_tan(thetav + alpha);
+    const double dvz2 = 2 * (vz1r + a * (cbeta * vx1r + sbeta * vy1r)) / ((1 + a * a) * (1 + m21));
+    const double vz2r = dvz2;
+    const double vx2r = a * cbeta * dvz2;
+    const double vy2r = a * sbeta * dvz2;
+    vz1r = vz1r - m21 * vz2r;
+    vx1r = vx1r - m21 * vx2r;
+    vy1r = vy1r - m21 * vy2r;
+    res.collided = true;
+    res.vx1 = ct * cp * vx1r - sp * vy1r + st * cp * vz1r + vx2;
+    res.vy1 = ct * sp * vx1r + cp * vy1r + st * sp * vz1r + vy2;
+    res.vz1 = ct * vz1r - st * vx1r + vz2;
+    res.vx2 = ct * cp * vx2r - sp * vy2r + st * cp * vz2r + vx2;
+    res.vy2 = ct * sp * vx2r + cp * vy2r + st * sp * vz2r + vy2;
+    res.vz2 = ct * vz2r - st * vx2r + vz2;
+    res.vx_cm = vx_cm;
+    res.vy_cm = vy_cm;
+    res.vz_cm = vz_cm;
+    return res;
+}
+
+/* initiateFragmentation, fragcalc.go:67-85.  newRadius is always 1: Go
+ * evaluates the exponent 1/3 as integer division (0) and Pow(x, 0) == 1. */
+__device__ static void initiate_frag(BodyArrays &A, ll b, double fragFactor)
+{
+    const double ffb = A.ff[b];
+    const double fragDelta = ffb > 10 ? 10.0 : fragFactor - ffb;
+    const double fragments = nbg_go_min(fragDelta * A.fs[b], NBG_MAX_FRAGS);
+    unsigned f = A.flags[b];
+    if (fragments <= 1) {
+        A.flags[b] = (f & ~(3u << NBG_BEHAVIOR_SHIFT)) | ((unsigned)NBG_FRAGMENT << NBG_BEHAVIOR_SHIFT);
+        return;
+    }
+    A.flags[b] = f | NBG_F_FRAGMENTING;
+    A.fr_rad[b] = A.rad[b];
+    A.fr_newrad[b] = 1.0;
+    A.fr_mass[b] = A.m[b] / fragments;
+    A.fr_cnt[b] = fragments != fragments ? 0 : (ll)fragments; /* int(NaN): no fragment either way */
+    A.fr_cx[b] = A.x[b];
+    A.fr_cy[b] = A.y[b];
+    A.fr_cz[b] = A.z[b];
+}
+
+/* ResolveCollision, body.go:248-264, with shouldFragment / doFragment /
+ * doElastic (fragcalc.go:24-61, collisioncalc.go:26-35). */
+__device__ static void resolve_collision(BodyArrays &A, ll b, ll o)
+{
+    const unsigned fb = A.flags[b], fo = A.flags[o];
+    if (!(fb & NBG_F_EXISTS) || !(fo & NBG_F_EXISTS)) return;
+    const unsigned bb = NBG_BEHAVIOR(fb), bo = NBG_BEHAVIOR(fo);
+    if (!(bb == NBG_ELASTIC && (bo == NBG_ELASTIC || bo == NBG_FRAGMENT))) return;
+    const ElasticOut r = elastic_calc(A, b, o);
+    if (!r.collided) return;
+    const double rb = A.rest[b];
+    const double nvx1 = (r.vx1 - r.vx_cm) * rb + r.vx_cm;
+    const double nvy1 = (r.vy1 - r.vy_cm) * rb + r.vy_cm;
+    const double nvz1 = (r.vz1 - r.vz_cm) * rb + r.vz_cm;
+    const double nvx2 = (r.vx2 - r.vx_cm) * rb + r.vx_cm;
+    const double nvy2 = (r.vy2 - r.vy_cm) * rb + r.vy_cm;
+    const double nvz2 = (r.vz2 - r.vz_cm) * rb + r.vz_cm;
+    bool frag = false;
+    double tf = 0, of = 0;
+    if (bb == NBG_FRAGMENT || bo == NBG_FRAGMENT) {
+        const double vThis = A.vx[b] + A.vy[b] + A.vz[b];
+        const double dvThis = fabs(A.vx[b] - nvx1) + fabs(A.vy[b] - nvy1) + fabs(A.vz[b] - nvz1);
+        const double thisFactor = dvThis / fabs(vThis);
+        const double vOther = A.vx[o] + A.vy[o] + A.vz[o];
+        const double dvOther = fabs(A.vx[o] - nvx2) + fabs(A.vy[o] - nvy2) + fabs(A.vz[o] - nvz2);
+        const double otherFactor = dvOther / fabs(vOther);
+        if ((bb == NBG_FRAGMENT && thisFactor > A.ff[b]) || (bo == NBG_FRAGMENT && otherFactor > A.ff[o])) {
+            frag = true;
+            tf = thisFactor;
+            of = otherFactor;
+        }
+    }
+    if (frag) {
+        if (bb == NBG_FRAGMENT && tf > A.ff[b]) initiate_frag(A, b, tf);
+        if (NBG_BEHAVIOR(A.flags[o]) == NBG_FRAGMENT && of > A.ff[o]) initiate_frag(A, o, of);
+        return;
+    }
+    A.vx[b] = nvx1;
+    A.vy[b] = nvy1;
+    A.vz[b] = nvz1;
+    A.vx[o] = nvx2;
+    A.vy[o] = nvy2;
+    A.vz[o] = nvz2;
+    A.flags[b] |= NBG_F_COLLIDED;
+    A.flags[o] |= NBG_F_COLLIDED;
+}
+
+/* ResolveSubsume, body.go:228-244 (no Exists checks, radius unchanged). */
+__device__ static void resolve_subsume(BodyArrays &A, ll b, ll o)
+{
+    const double thisMass = A.m[b], otherMass = A.m[o];
+    A.m[b] = thisMass + otherMass;
+    A.m[o] = 0;
+    A.flags[o] &= ~NBG_F_EXISTS;
+}
+
+__global__ void k_resolve(BodyArrays A, DevCtl *ctl, const ull *keys, nbg_event *ev_out)
+{
+    if (threadIdx.x != 0 || blockIdx.x != 0 || ctl->error) return;
+    ctl->next_id += ctl->frag_total; /* fragments took ids next_id .. next_id+total-1 */
+    const ll cnt = ctl->ev_count;
+    for (ll k = cnt - 1; k >= 0; k--) {
+        const ull key = keys[k];
+        const ll i = (ll)(key >> 32);
+        const ll j = (ll)((key >> 2) & 0x3fffffffull);
+        const unsigned type = (unsigned)(key & 3ull);
+        ll b1 = i, b2 = j;
+        if (type == NBG_EVT_SUB_JI) {
+            b1 = j;
+            b2 = i;
+        }
+        nbg_event e;
+        e.id1 = A.id[b1];
+        e.id2 = A.id[b2];
+        e.type = type == NBG_EVT_COLL_IJ ? NBG_EV_COLLISION : NBG_EV_SUBSUME;
+        e.pad = 0;
+        ev_out[cnt - 1 - k] = e;
+        if (type == NBG_EVT_COLL_IJ)
+            resolve_collision(A, b1, b2);
+        else
+            resolve_subsume(A, b1, b2);
+    }
+    ctl->last_ev_n = cnt;
+    ctl->acc_events += cnt;
+    ctl->acc_frags += ctl->frag_total;
+}
+
+/* ------------------------------------------------------------------------ */
+/* K6: integration (Update, body.go:114-139) + renderables                 */
+/* ------------------------------------------------------------------------ */
+
+__global__ void k_integrate(BodyArrays A, DevCtl *ctl, nbg_renderable *rend)
+{
+    if (ctl->error) return;
+    const ll n = ctl->n;
+    const double dt = ctl->dt, R = ctl->R;
+    ll nan_local = 0;
+    for (ll k = (ll)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (ll)gridDim.x * blockDim.x) {
+        unsigned f = A.flags[k];
+        nbg_renderable r;
+        r.id = A.id[k];
+        if (!(f & NBG_F_EXISTS)) {
+            r.x = r.y = r.z = 0.0f;
+            r.flags = 0;
+            r.radius = 0.0;
+            rend[k] = r;
+            continue;
+        }
+        double vx = A.vx[k], vy = A.vy[k], vz = A.vz[k];
+        if (!(f & NBG_F_COLLIDED)) {
+            const double m = A.m[k];
+            vx += dt * A.fx[k] / m;
+            vy += dt * A.fy[k] / m;
+            vz += dt * A.fz[k] / m;
+            A.vx[k] = vx;
+            A.vy[k] = vy;
+            A.vz[k] = vz;
+        }
+        const double x = A.x[k] + dt * vx;
+        const double y = A.y[k] + dt * vy;
+        const double z = A.z[k] + dt * vz;
+        A.x[k] = x;
+        A.y[k] = y;
+        A.z[k] = z;
+        A.rest[k] = R;
+        f &= ~NBG_F_COLLIDED;
+        if (x != x || y != y || z != z) {
+            f &= ~NBG_F_EXISTS;
+            nan_local++;
+        }
+        A.flags[k] = f;
+        r.x = (float)x;
+        r.y = (float)y;
+        r.z = (float)z;
+        r.flags = f & (NBG_F_EXISTS | NBG_F_IS_SUN);
+        r.radius = A.rad[k];
+        if (!(f & NBG_F_EXISTS)) {
+            r.x = r.y = r.z = 0.0f;
+            r.flags = 0;
+            r.radius = 0.0;
+        }
+        rend[k] = r;
+    }
+    if (nan_local) atomicAdd((unsigned long long *)&ctl->acc_nan, (ull)nan_local);
+}
+
+/* ------------------------------------------------------------------------ */
+/* K7: Cycle (body_collection.go:253-296): stable compaction + adds         */
+/* ------------------------------------------------------------------------ */
+
+__device__ static void copy_body(const BodyArrays &S, ll s, BodyArrays &D, ll d)
+{
+    D.x[d] = S.x[s];
+    D.y[d] = S.y[s];
+    D.z[d] = S.z[s];
+    D.vx[d] = S.vx[s];
+    D.vy[d] = S.vy[s];
+    D.vz[d] = S.vz[s];
+    D.m[d] = S.m[s];
+    D.rad[d] = S.rad[s];
+    D.fx[d] = S.fx[s];
+    D.fy[d] = S.fy[s];
+    D.fz[d] = S.fz[s];
+    D.ff[d] = S.ff[s];
+    D.fs[d] = S.fs[s];
+    D.rest[d] = S.rest[s];
+    D.fr_rad[d] = S.fr_rad[s];
+    D.fr_newrad[d] = S.fr_newrad[s];
+    D.fr_mass[d] = S.fr_mass[s];
+    D.fr_cx[d] = S.fr_cx[s];
+    D.fr_cy[d] = S.fr_cy[s];
+    D.fr_cz[d] = S.fr_cz[s];
+    D.fr_cnt[d] = S.fr_cnt[s];
+    D.id[d] = S.id[s];
+    D.flags[d] = S.flags[s];
+}
+
+__device__ static bool cycle_changes(const DevCtl *ctl)
+{
+    return ctl->n_keep != ctl->n || ctl->frag_total > 0 || ctl->n_host_adds > 0;
+}
+
+__global__ void __launch_bounds__(NBG_SCAN_BLOCK) k_compact(BodyArrays A, BodyArrays Bt, DevCtl *ctl, const ll *blk_off)
+{
+    if (ctl->error || !cycle_changes(ctl)) return;
+    const ll n = ctl->n;
+    const ll base = (ll)blockIdx.x * NBG_SCAN_TILE;
+    if (base >= n) return;
+    ll c[NBG_SCAN_ITEMS];
+    ll s = 0;
+    for (int q = 0; q < NBG_SCAN_ITEMS; q++) {
+        ll k = base + (ll)threadIdx.x * NBG_SCAN_ITEMS + q;
+        c[q] = (k < n && (A.flags[k] & NBG_F_EXISTS)) ? 1 : 0;
+        s += c[q];
+    }
+    ll tot;
+    ll off = block_excl_scan(s, &tot) + blk_off[blockIdx.x];
+    for (int q = 0; q < NBG_SCAN_ITEMS; q++) {
+        ll k = base + (ll)threadIdx.x * NBG_SCAN_ITEMS + q;
+        if (c[q]) copy_body(A, k, Bt, off++);
+    }
+}
+
+/* Appends the adds newest first (fragments of this cycle, then host adds),
+ * each with r = R. */
+__global__ void k_append_adds(BodyArrays Bt, BodyArrays F, BodyArrays H, DevCtl *ctl)
+{
+    if (ctl->error || !cycle_changes(ctl)) return;
+    const ll nk = ctl->n_keep, nf = ctl->frag_total, nh = ctl->n_host_adds;
+    const double R = ctl->R;
+    for (ll k = (ll)blockIdx.x * blockDim.x + threadIdx.x; k < nf + nh; k += (ll)gridDim.x * blockDim.x) {
+        ll d = nk + k;
+        if (k < nf) {
+            copy_body(F, nf - 1 - k, Bt, d);
+        } else {
+            ll h = k - nf;
+            copy_body(H, nh - 1 - h, Bt, d);
+        }
+        Bt.rest[d] = R;
+    }
+}
+
+__global__ void k_copy_back(BodyArrays A, BodyArrays Bt, DevCtl *ctl)
+{
+    if (ctl->error || !cycle_changes(ctl)) return;
+    const ll total = ctl->n_keep + ctl->frag_total + ctl->n_host_adds;
+    for (ll k = (ll)blockIdx.x * blockDim.x + threadIdx.x; k < total; k += (ll)gridDim.x * blockDim.x)
+        copy_body(Bt, k, A, k);
+}
+
+__global__ void k_end(DevCtl *ctl)
+{
+    if (threadIdx.x != 0 || ctl->error) return;
+    const ll n = ctl->n;
+    ctl->rend_n = n;
+    ctl->acc_removed += n - ctl->n_keep;
+    ctl->acc_interactions += n * (n > 0 ? n - 1 : 0);
+    ctl->n = ctl->n_keep + ctl->frag_total + ctl->n_host_adds;
+    ctl->n_host_adds = 0;
+    ctl->cycle += 1;
+    ctl->acc_steps += 1;
+}
+
+/* ------------------------------------------------------------------------ */
+/* cycle-boundary edits                                                     */
+/* ------------------------------------------------------------------------ */
+
+/* processDeletes, computation-runner.go:176-216 (sequential by nature). */
+__global__ void k_remove(BodyArrays A, DevCtl *ctl, ll count, ll *removed)
+{
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    const ll n = ctl->n;
+    ll rem = 0;
+    if (count == -1) {
+        for (ll k = 0; k < n; k++) {
+            if (A.flags[k] & NBG_F_EXISTS) {
+                A.m[k] = 0;
+                A.flags[k] &= ~NBG_F_EXISTS;
+                rem++;
+            }
+        }
+    } else {
+        const ll step = count > n ? 1 : n / count;
+        ll iter = 0;
+        bool should = false;
+        for (ll k = 0; k < n; k++) {
+            if (iter % step == 0) should = true;
+            iter++;
+            unsigned f = A.flags[k];
+            if (should && !(f & NBG_F_PINNED) && (f & NBG_F_EXISTS)) {
+                A.m[k] = 0;
+                A.flags[k] = f & ~NBG_F_EXISTS;
+                should = false;
+                rem++;
+            }
+        }
+    }
+    *removed = rem;
+}
+
+/* ApplyMods for bodies matched by id (body.go:274-313, after parsing). */
+__global__ void k_edits(BodyArrays A, DevCtl *ctl, const nbg_edit *E, ll ne, int *results)
+{
+    const ll n = ctl->n;
+    for (ll k = (ll)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (ll)gridDim.x * blockDim.x) {
+        const ll id = A.id[k];
+        for (ll q = 0; q < ne; q++) {
+            const nbg_edit e = E[q];
+            if (e.id != id) continue;
+            atomicAdd(&results[q], 1);
+            const unsigned m = e.mask;
+            if (m & NBG_M_X) A.x[k] = e.x;
+            if (m & NBG_M_Y) A.y[k] = e.y;
+            if (m & NBG_M_Z) A.z[k] = e.z;
+            if (m & NBG_M_VX) A.vx[k] = e.vx;
+            if (m & NBG_M_VY) A.vy[k] = e.vy;
+            if (m & NBG_M_VZ) A.vz[k] = e.vz;
+            if (m & NBG_M_MASS) A.m[k] = e.mass;
+            if (m & NBG_M_RADIUS) A.rad[k] = e.radius;
+            if (m & NBG_M_FRAG_FACTOR) A.ff[k] = e.frag_factor;
+            if (m & NBG_M_FRAG_STEP) A.fs[k] = e.frag_step;
+            unsigned f = A.flags[k];
+            if (m & NBG_M_COLLISION)
+                f = (f & ~(3u << NBG_BEHAVIOR_SHIFT)) | (((unsigned)e.collision & 3u) << NBG_BEHAVIOR_SHIFT);
+            if (m & NBG_M_TELEMETRY) f = e.telemetry ? (f | NBG_F_TELEMETRY) : (f & ~NBG_F_TELEMETRY);
+            if (m & NBG_M_EXISTS) f = e.exists ? (f | NBG_F_EXISTS) : (f & ~NBG_F_EXISTS);
+            A.flags[k] = f;
+        }
+    }
+}
+
+__global__ void k_find(BodyArrays A, DevCtl *ctl, ll id, ll *idx)
+{
+    const ll n = ctl->n;
+    for (ll k = (ll)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (ll)gridDim.x * blockDim.x)
+        if (A.id[k] == id) atomicMin((long long *)idx, (long long)k);
+}
+
+/* Kinetic and pairwise potential energy plus momentum, per-block partials
+ * (out[blockIdx*5 + 0..4]) summed on the host in block order. */
+#define EN_BLOCK 128
+__global__ void __launch_bounds__(EN_BLOCK) k_energy(BodyArrays A, DevCtl *ctl, double *out)
+{
+    __shared__ double red[5][EN_BLOCK];
+    const ll n = ctl->n;
+    double ke = 0, pe = 0, px = 0, py = 0, pz = 0;
+    const ll i = (ll)blockIdx.x * EN_BLOCK + threadIdx.x;
+    if (i < n && (A.flags[i] & NBG_F_EXISTS)) {
+        const double m = A.m[i], vx = A.vx[i], vy = A.vy[i], vz = A.vz[i];
+        ke = 0.5 * m * (vx * vx + vy * vy + vz * vz);
+        px = m * vx;
+        py = m * vy;
+        pz = m * vz;
+        const double xi = A.x[i], yi = A.y[i], zi = A.z[i];
+        for (ll j = i + 1; j < n; j++) {
+            if (!(A.flags[j] & NBG_F_EXISTS)) continue;
+            const double dx = A.x[j] - xi, dy = A.y[j] - yi, dz = A.z[j] - zi;
+            const double r = sqrt(dx * dx + dy * dy + dz * dz);
+            if (r > 0) pe -= NBG_G * m * A.m[j] / r;
+        }
+    }
+    red[0][threadIdx.x] = ke;
+    red[1][threadIdx.x] = pe;
+    red[2][threadIdx.x] = px;
+    red[3][threadIdx.x] = py;
+    red[4][threadIdx.x] = pz;
+    __syncthreads();
+    for (int s = EN_BLOCK / 2; s > 0; s >>= 1) {
+        if (threadIdx.x < s)
+            for (int q = 0; q < 5; q++) red[q][threadIdx.x] += red[q][threadIdx.x + s];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0)
+        for (int q = 0; q < 5; q++) out[(ll)blockIdx.x * 5 + q] = red[q][0];
+}
+
+/* ------------------------------------------------------------------------ */
+/* launchers                                                                */
+/* ------------------------------------------------------------------------ */
+
+static int scan_grid(ll cap) { return (int)((cap + NBG_SCAN_TILE - 1) / NBG_SCAN_TILE); }
+
+static int flat_grid(ll cap)
+{
+    ll g = (cap + 255) / 256;
+    if (g > 152 * 16) g = 152 * 16;
+    return (int)(g < 1 ? 1 : g);
+}
+
+void nbg_launch_begin(const CycleBufs &cb, DevCtl *ctl, cudaStream_t st)
+{
+    (void)cb;
+    k_begin<<<1, 32, 0, st>>>(ctl);
+}
+
+void nbg_launch_frag_count(const CycleBufs &cb, DevCtl *ctl, cudaStream_t st)
+{
+    int g = scan_grid(cb.cap);
+    k_frag_blocksum<<<g, NBG_SCAN_BLOCK, 0, st>>>(cb.a, ctl, cb.blk_sum);
+    k_scan_blocks<<<1, NBG_SCAN_BLOCK, 0, st>>>(ctl, cb.blk_sum, cb.blk_off, 0, cb.cap, cb.frag_cap);
+}
+
+int nbg_pair_fp64_grid(ll cap)
+{
+    ll g = (cap + P64_BLOCK - 1) / P64_BLOCK;
+    return (int)(g < 1 ? 1 : (g > 65535 ? 65535 : g));
+}
+
+void nbg_launch_pair_fp64(const CycleBufs &cb, DevCtl *ctl, cudaStream_t st)
+{
+    k_pair_fp64<<<nbg_pair_fp64_grid(cb.cap), P64_BLOCK, 0, st>>>(cb.a, ctl, cb.ev_keys, cb.ev_cap);
+}
+
+/* everything after the pair kernel: order events, emit fragments, resolve,
+ * integrate, Cycle */
+void nbg_launch_after_pair(const CycleBufs &cb, DevCtl *ctl, cudaStream_t st)
+{
+    const int sg = scan_grid(cb.cap);
+    k_sort_events<<<1, SORT_BLOCK, 0, st>>>(ctl, cb.ev_keys, cb.ev_cap);
+    k_frag_emit<<<sg, NBG_SCAN_BLOCK, 0, st>>>(cb.a, cb.frags, ctl, cb.blk_off);
+    k_resolve<<<1, 32, 0, st>>>(cb.a, ctl, cb.ev_keys, cb.ev_out);
+    k_integrate<<<flat_grid(cb.cap), 256, 0, st>>>(cb.a, ctl, cb.rend);
+    k_keep_blocksum<<<sg, NBG_SCAN_BLOCK, 0, st>>>(cb.a, ctl, cb.blk_sum);
+    k_scan_blocks<<<1, NBG_SCAN_BLOCK, 0, st>>>(ctl, cb.blk_sum, cb.blk_off, 1, cb.cap, cb.frag_cap);
+    k_compact<<<sg, NBG_SCAN_BLOCK, 0, st>>>(cb.a, cb.b, ctl, cb.blk_off);
+    k_append_adds<<<flat_grid(cb.frag_cap + cb.adds_cap), 256, 0, st>>>(cb.b, cb.frags, cb.adds, ctl);
+    k_copy_back<<<flat_grid(cb.cap), 256, 0, st>>>(cb.a, cb.b, ctl);
+    k_end<<<1, 32, 0, st>>>(ctl);
+}
+
+void nbg_launch_remove(const CycleBufs &cb, DevCtl *ctl, ll count, ll *removed_dev, cudaStream_t st)
+{
+    k_remove<<<1, 32, 0, st>>>(cb.a, ctl, count, removed_dev);
+}
+
+void nbg_launch_edits(const CycleBufs &cb, DevCtl *ctl, const nbg_edit *edits_dev, ll k, int *results_dev,
+                      cudaStream_t st)
+{
+    k_edits<<<flat_grid(cb.cap), 256, 0, st>>>(cb.a, ctl, edits_dev, k, results_dev);
+}
+
+void nbg_launch_find(const CycleBufs &cb, DevCtl *ctl, ll id, ll *idx_dev, cudaStream_t st)
+{
+    k_find<<<flat_grid(cb.cap), 256, 0, st>>>(cb.a, ctl, id, idx_dev);
+}
+
+void nbg_launch_energy(const CycleBufs &cb, DevCtl *ctl, double *out_dev, cudaStream_t st)
+{
+    int g = (int)((cb.cap + EN_BLOCK - 1) / EN_BLOCK);
+    k_energy<<<g, EN_BLOCK, 0, st>>>(cb.a, ctl, out_dev);
+}

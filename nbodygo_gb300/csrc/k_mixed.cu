@@ -1,0 +1,480 @@
+/*
+ * k_mixed.cu - mixed-precision force + collision detection.
+ *
+ * Computes the same force pass as calcForceFrom (cmd/body/body.go:214-225)
+ * and the same collision set as Collided (body.go:192-208), with the pair
+ * terms in FP32:
+ *
+ *  - positions are held as hi/lo float pairs (x = hi + lo to ~2^-48 |x|);
+ *    each work item re-centres the j positions on its i-tile's origin c with
+ *    (x_hi - c) + x_lo, so the FP32 coordinates a pair subtracts carry an
+ *    error of 2^-24 |x - c| instead of 2^-24 |x|;
+ *  - pair terms m_j (x_j - x_i) / r^3 use packed f32x2 FMA (two j per
+ *    instruction) and the SFU reciprocal square root;
+ *  - every 256 j the FP32 tile sum is folded into a (hi, lo) float pair with
+ *    TwoSum (Knuth), so the accumulated rounding error stays that of a 128-term
+ *    sum; the item total is written as FP64;
+ *  - any pair closer than a conservative bound (r_i + r_max plus the FP32
+ *    error bound) is re-evaluated in FP64 with the reference's exact
+ *    expressions: that FP64 dist decides the overlap skip and the collision
+ *    test, so the event set is the reference's, and the force of such pairs
+ *    is FP64.
+ *
+ * Work items are (i-tile of 512 bodies, j-range); CTAs take them from an
+ * atomic counter.  Each item writes its partial sums to its own slot, and a
+ * second kernel adds the slots in a fixed order, so results do not depend on
+ * scheduling.
+ */
+#include "nbg_internal.cuh"
+#include "nbg_math.h"
+#include "nbg_shared.h"
+
+#define FULL_MASK 0xffffffffu
+#define SENTINEL_POS 1.0e18f
+
+__device__ __forceinline__ float rsqrt_sfu(float x)
+{
+    float y;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
+/* TwoSum: (hi, lo) += v with the rounding error of hi + v kept in lo. */
+__device__ __forceinline__ void two_sum_add(float &hi, float &lo, float v)
+{
+    float s = hi + v;
+    float bb = s - hi;
+    float e = (hi - (s - bb)) + (v - bb);
+    hi = s;
+    lo += e;
+}
+
+/* A body whose position is not finite or whose radius is NaN interacts with
+ * no other body in the reference's arithmetic except through NaN; the mixed
+ * form keeps it out of every pair (massless, far away) and sets its own force
+ * in k_mix_out. */
+__device__ __forceinline__ bool is_special(double x, double y, double z, double r)
+{
+    return !(fabs(x) <= NBG_DBL_MAX && fabs(y) <= NBG_DBL_MAX && fabs(z) <= NBG_DBL_MAX) || r != r;
+}
+
+/* ---- per-cycle reductions: r_max, |x|_max, m_scale ----------------------- */
+
+__global__ void k_mix_reduce(BodyArrays A, DevCtl *ctl, int split_cap, int slots)
+{
+    if (ctl->error) return;
+    const ll n = ctl->n;
+    float rmax = 0.f, xmax = 0.f;
+    double mmax = 0.0;
+    for (ll k = (ll)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (ll)gridDim.x * blockDim.x) {
+        const double x = A.x[k], y = A.y[k], z = A.z[k], r = A.rad[k];
+        if (is_special(x, y, z, r)) continue;
+        rmax = fmaxf(rmax, (float)fmax(r, 0.0));
+        xmax = fmaxf(xmax, (float)fmax(fabs(x), fmax(fabs(y), fabs(z))));
+        if ((A.flags[k] & NBG_LIVE_MASK) == NBG_F_EXISTS) mmax = fmax(mmax, fabs(A.m[k]));
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        rmax = fmaxf(rmax, __shfl_xor_sync(FULL_MASK, rmax, o));
+        xmax = fmaxf(xmax, __shfl_xor_sync(FULL_MASK, xmax, o));
+        mmax = fmax(mmax, __shfl_xor_sync(FULL_MASK, mmax, o));
+    }
+    if ((threadIdx.x & 31) == 0) {
+        /* rounding up keeps both bounds conservative */
+        atomicMax(&ctl->rmax_bits, __float_as_uint(rmax * (1.0f + 0x1p-20f)));
+        atomicMax(&ctl->xmax_bits, __float_as_uint(xmax * (1.0f + 0x1p-20f)));
+        atomicMax((unsigned long long *)&ctl->m_scale, (ull)__double_as_longlong(mmax));
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        /* j-range splits: enough items for ~8 per resident CTA */
+        const ll ntiles = (n + NBG_MIX_ITILE - 1) / NBG_MIX_ITILE;
+        const ll jtiles = (n + NBG_MIX_JT - 1) / NBG_MIX_JT;
+        ll s = ntiles > 0 ? (8ll * slots + ntiles - 1) / ntiles : 1;
+        if (s > split_cap) s = split_cap;
+        if (s > jtiles) s = jtiles;
+        if (s < 1) s = 1;
+        ctl->splits = (int)s;
+        ctl->work_next = 0;
+    }
+}
+
+/* jhi = (x_hi, y_hi, z_hi, m/m_scale), jlo = (x_lo, y_lo, z_lo, special) */
+__global__ void k_mix_pack(BodyArrays A, DevCtl *ctl, float4 *jhi, float4 *jlo)
+{
+    if (ctl->error) return;
+    const ll n = ctl->n;
+    double ms = ctl->m_scale;
+    if (!(ms > 0.0)) ms = 1.0;
+    for (ll k = (ll)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (ll)gridDim.x * blockDim.x) {
+        const double x = A.x[k], y = A.y[k], z = A.z[k], r = A.rad[k];
+        if (is_special(x, y, z, r)) {
+            jhi[k] = make_float4(SENTINEL_POS, SENTINEL_POS, SENTINEL_POS, 0.f);
+            jlo[k] = make_float4(0.f, 0.f, 0.f, 1.f);
+            continue;
+        }
+        const float xh = (float)x, yh = (float)y, zh = (float)z;
+        const float xl = (float)(x - (double)xh), yl = (float)(y - (double)yh), zl = (float)(z - (double)zh);
+        const bool live = (A.flags[k] & NBG_LIVE_MASK) == NBG_F_EXISTS;
+        const float m = live ? (float)(A.m[k] / ms) : 0.f;
+        jhi[k] = make_float4(xh, yh, zh, m);
+        jlo[k] = make_float4(xl, yl, zl, 0.f);
+    }
+}
+
+/* origin of each i-tile: centre of the bounding box of its bodies */
+__global__ void __launch_bounds__(NBG_MIX_BLOCK) k_mix_tiles(DevCtl *ctl, const float4 *jhi, const float4 *jlo, float4 *tile_c)
+{
+    __shared__ float red[6][NBG_MIX_BLOCK / 32];
+    if (ctl->error) return;
+    const ll n = ctl->n;
+    const ll tile = blockIdx.x;
+    const ll base = tile * NBG_MIX_ITILE;
+    if (base >= n) return;
+    float lo[3] = {3e38f, 3e38f, 3e38f}, hi[3] = {-3e38f, -3e38f, -3e38f};
+    for (int k = 0; k < NBG_MIX_K; k++) {
+        ll i = base + (ll)k * NBG_MIX_BLOCK + threadIdx.x;
+        if (i >= n) continue;
+        if (jlo[i].w != 0.f) continue;
+        float4 h = jhi[i];
+        lo[0] = fminf(lo[0], h.x);
+        lo[1] = fminf(lo[1], h.y);
+        lo[2] = fminf(lo[2], h.z);
+        hi[0] = fmaxf(hi[0], h.x);
+        hi[1] = fmaxf(hi[1], h.y);
+        hi[2] = fmaxf(hi[2], h.z);
+    }
+    for (int o = 16; o > 0; o >>= 1)
+        for (int c = 0; c < 3; c++) {
+            lo[c] = fminf(lo[c], __shfl_xor_sync(FULL_MASK, lo[c], o));
+            hi[c] = fmaxf(hi[c], __shfl_xor_sync(FULL_MASK, hi[c], o));
+        }
+    const int w = threadIdx.x >> 5;
+    if ((threadIdx.x & 31) == 0)
+        for (int c = 0; c < 3; c++) {
+            red[c][w] = lo[c];
+            red[3 + c][w] = hi[c];
+        }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float c3[3];
+        for (int c = 0; c < 3; c++) {
+            float l = red[c][0], h = red[3 + c][0];
+            for (int q = 1; q < NBG_MIX_BLOCK / 32; q++) {
+                l = fminf(l, red[c][q]);
+                h = fmaxf(h, red[3 + c][q]);
+            }
+            c3[c] = (l <= h) ? 0.5f * l + 0.5f * h : 0.f;
+        }
+        tile_c[tile] = make_float4(c3[0], c3[1], c3[2], 0.f);
+    }
+}
+
+/* ---- the pair kernel ----------------------------------------------------- */
+
+__device__ static int detect_event_mixed(unsigned bi, unsigned bj, double ri, double rj, double dist)
+{
+    bool ei = (bi == NBG_ELASTIC || bi == NBG_FRAGMENT);
+    bool ej = (bj == NBG_ELASTIC || bj == NBG_FRAGMENT);
+    if (ei && ej) return (int)NBG_EVT_COLL_IJ;
+    if (bi == NBG_SUBSUME || bj == NBG_SUBSUME) {
+        if (ri > rj && dist <= ri) return (int)NBG_EVT_SUB_IJ;
+        if (rj > ri && dist <= rj) return (int)NBG_EVT_SUB_JI;
+    }
+    return -1;
+}
+
+/* A pair inside the candidate bound: decide overlap and collision in FP64
+ * with the reference's expressions (no contraction: explicit _rn
+ * intrinsics), add the force if the pair does not overlap, and record the
+ * collision event.  Returns the FP64 force term in m_scale-normalised
+ * acceleration units through tx, ty, tz. */
+__device__ static void candidate_pair(const BodyArrays &A, DevCtl *ctl, ull *ev_keys, ll ev_cap, ll i, ll j,
+                                      double inv_ms, double &tx, double &ty, double &tz)
+{
+    tx = ty = tz = 0.0;
+    const unsigned fi = A.flags[i], fj = A.flags[j];
+    const double xi = A.x[i], yi = A.y[i], zi = A.z[i], ri = A.rad[i];
+    const double dx = __dsub_rn(A.x[j], xi);
+    const double dy = __dsub_rn(A.y[j], yi);
+    const double dz = __dsub_rn(A.z[j], zi);
+    const double dist = __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz)));
+    const double rj = A.rad[j];
+    const double rr = __dadd_rn(ri, rj);
+    const bool coll_i = (fi & NBG_F_COLLIDED) != 0;
+    const bool live_j = (fj & NBG_LIVE_MASK) == NBG_F_EXISTS;
+    if (live_j && (coll_i || dist > rr)) {
+        const double w = (A.m[j] * inv_ms) / (dist * dist * dist);
+        tx = w * dx;
+        ty = w * dy;
+        tz = w * dz;
+    }
+    const bool live_i = (fi & NBG_LIVE_MASK) == NBG_F_EXISTS;
+    if (live_i && !coll_i && dist <= rr) {
+        int type = detect_event_mixed(NBG_BEHAVIOR(fi), NBG_BEHAVIOR(fj), ri, rj, dist);
+        if (type >= 0) {
+            ll slot = (ll)atomicAdd((unsigned long long *)&ctl->ev_count, 1ull);
+            if (slot < ev_cap) ev_keys[slot] = ((ull)i << 32) | ((ull)j << 2) | (ull)type;
+        }
+    }
+}
+
+__device__ __forceinline__ void fold64(float &hi, float &lo, double v)
+{
+    float vh = (float)v;
+    float vl = (float)(v - (double)vh);
+    two_sum_add(hi, lo, vh);
+    lo += vl;
+}
+
+template <int K>
+__global__ void __launch_bounds__(NBG_MIX_BLOCK, 3)
+k_pair_mixed(BodyArrays A, DevCtl *ctl, const float4 *__restrict__ jhi, const float4 *__restrict__ jlo,
+             const float4 *__restrict__ tile_c, double *__restrict__ part, ll part_stride, ull *ev_keys, ll ev_cap)
+{
+    constexpr int JP = NBG_MIX_JT / 2; /* j pairs per tile */
+    constexpr int ITILE = NBG_MIX_BLOCK * K;
+    __shared__ float4 sA[JP], sB[JP];
+    __shared__ ll s_item;
+    if (ctl->error) return;
+    const ll n = ctl->n;
+    const int S = ctl->splits;
+    const ll ntiles = (n + ITILE - 1) / ITILE;
+    const ll items = ntiles * S;
+    const ll jc = (((n + S - 1) / S) + NBG_MIX_JT - 1) / NBG_MIX_JT * NBG_MIX_JT;
+    double ms = ctl->m_scale;
+    if (!(ms > 0.0)) ms = 1.0;
+    const double inv_ms = 1.0 / ms;
+    const float rmax = __uint_as_float(ctl->rmax_bits);
+    const float xmax = __uint_as_float(ctl->xmax_bits);
+    const int tid = threadIdx.x;
+
+    for (;;) {
+        if (tid == 0) s_item = (ll)atomicAdd((unsigned long long *)&ctl->work_next, 1ull);
+        __syncthreads();
+        const ll item = s_item;
+        __syncthreads();
+        if (item >= items) break;
+        const ll tile = item / S;
+        const int split = (int)(item % S);
+        const float4 c = tile_c[tile];
+
+        float2 nx[K], ny[K], nz[K];
+        float thr[K];
+        float shx[K], slx[K], shy[K], sly[K], shz[K], slz[K];
+        ll iidx[K];
+#pragma unroll
+        for (int k = 0; k < K; k++) {
+            const ll i = tile * ITILE + (ll)k * NBG_MIX_BLOCK + tid;
+            iidx[k] = i;
+            float xr = 0.f, yr = 0.f, zr = 0.f, t = -1.f;
+            if (i < n) {
+                const float4 h = jhi[i], l = jlo[i];
+                if (l.w == 0.f) {
+                    xr = (h.x - c.x) + l.x;
+                    yr = (h.y - c.y) + l.y;
+                    zr = (h.z - c.z) + l.z;
+                    const double ri = A.rad[i];
+                    const double D = fmax(0.0, ri + (double)rmax);
+                    const double amax = (double)fmaxf(fabsf(xr), fmaxf(fabsf(yr), fabsf(zr)));
+                    const double eps = 0x1p-19 * (amax + D) + 0x1p-44 * (double)xmax + 0x1p-100;
+                    const double b = (D + eps) * (1.0 + 0x1p-18);
+                    t = __double2float_ru(b * b);
+                } else {
+                    xr = yr = zr = SENTINEL_POS;
+                }
+            }
+            nx[k] = make_float2(-xr, -xr);
+            ny[k] = make_float2(-yr, -yr);
+            nz[k] = make_float2(-zr, -zr);
+            thr[k] = t;
+            shx[k] = slx[k] = shy[k] = sly[k] = shz[k] = slz[k] = 0.f;
+        }
+
+        const ll jb = (ll)split * jc;
+        const ll je = jb + jc < n ? jb + jc : n;
+        for (ll jt = jb; jt < je; jt += NBG_MIX_JT) {
+            __syncthreads();
+            {
+                float v[2][4];
+#pragma unroll
+                for (int e = 0; e < 2; e++) {
+                    const ll j = jt + 2 * tid + e;
+                    if (j < je) {
+                        const float4 h = jhi[j], l = jlo[j];
+                        v[e][0] = (h.x - c.x) + l.x;
+                        v[e][1] = (h.y - c.y) + l.y;
+                        v[e][2] = (h.z - c.z) + l.z;
+                        v[e][3] = h.w;
+                        if (l.w != 0.f) {
+                            v[e][0] = v[e][1] = v[e][2] = SENTINEL_POS;
+                            v[e][3] = 0.f;
+                        }
+                    } else {
+                        v[e][0] = v[e][1] = v[e][2] = SENTINEL_POS;
+                        v[e][3] = 0.f;
+                    }
+                }
+                sA[tid] = make_float4(v[0][0], v[1][0], v[0][1], v[1][1]);
+                sB[tid] = make_float4(v[0][2], v[1][2], v[0][3], v[1][3]);
+            }
+            __syncthreads();
+
+            float2 ax[K], ay[K], az[K];
+            float mn[K];
+#pragma unroll
+            for (int k = 0; k < K; k++) {
+                ax[k] = ay[k] = az[k] = make_float2(0.f, 0.f);
+                mn[k] = 3.0e38f;
+            }
+#pragma unroll 2
+            for (int p = 0; p < JP; p++) {
+                const float4 a = sA[p], b = sB[p];
+                const float2 xj = make_float2(a.x, a.y), yj = make_float2(a.z, a.w);
+                const float2 zj = make_float2(b.x, b.y), mj = make_float2(b.z, b.w);
+#pragma unroll
+                for (int k = 0; k < K; k++) {
+                    const float2 dx = __fadd2_rn(xj, nx[k]);
+                    const float2 dy = __fadd2_rn(yj, ny[k]);
+                    const float2 dz = __fadd2_rn(zj, nz[k]);
+                    float2 r2 = __fmul2_rn(dx, dx);
+                    r2 = __ffma2_rn(dy, dy, r2);
+                    r2 = __ffma2_rn(dz, dz, r2);
+                    mn[k] = fminf(mn[k], fminf(r2.x, r2.y));
+                    const float2 inv = make_float2(rsqrt_sfu(r2.x), rsqrt_sfu(r2.y));
+                    const float2 t = __fmul2_rn(mj, inv);
+                    const float2 inv2 = __fmul2_rn(inv, inv);
+                    const float2 s = __fmul2_rn(t, inv2);
+                    ax[k] = __ffma2_rn(s, dx, ax[k]);
+                    ay[k] = __ffma2_rn(s, dy, ay[k]);
+                    az[k] = __ffma2_rn(s, dz, az[k]);
+                }
+            }
+#pragma unroll
+            for (int k = 0; k < K; k++) {
+                if (mn[k] < thr[k]) {
+                    /* slow path: this tile holds a candidate pair for body i */
+                    const ll i = iidx[k];
+                    float tx = 0.f, ty = 0.f, tz = 0.f;
+                    const float xi = -nx[k].x, yi = -ny[k].x, zi = -nz[k].x;
+                    for (int p = 0; p < JP; p++) {
+                        const float4 a = sA[p], b = sB[p];
+#pragma unroll
+                        for (int e = 0; e < 2; e++) {
+                            const ll j = jt + 2 * p + e;
+                            if (j >= je || j == i) continue;
+                            const float xj = e ? a.y : a.x, yj = e ? a.w : a.z;
+                            const float zj = e ? b.y : b.x, m = e ? b.w : b.z;
+                            const float dx = xj - xi, dy = yj - yi, dz = zj - zi;
+                            const float r2 = dx * dx + dy * dy + dz * dz;
+                            if (r2 >= thr[k]) {
+                                const float inv = rsqrt_sfu(r2);
+                                const float s = m * inv * inv * inv;
+                                tx += s * dx;
+                                ty += s * dy;
+                                tz += s * dz;
+                            } else {
+                                double qx, qy, qz;
+                                candidate_pair(A, ctl, ev_keys, ev_cap, i, j, inv_ms, qx, qy, qz);
+                                fold64(shx[k], slx[k], qx);
+                                fold64(shy[k], sly[k], qy);
+                                fold64(shz[k], slz[k], qz);
+                            }
+                        }
+                    }
+                    ax[k] = make_float2(tx, 0.f);
+                    ay[k] = make_float2(ty, 0.f);
+                    az[k] = make_float2(tz, 0.f);
+                }
+                two_sum_add(shx[k], slx[k], ax[k].x + ax[k].y);
+                two_sum_add(shy[k], sly[k], ay[k].x + ay[k].y);
+                two_sum_add(shz[k], slz[k], az[k].x + az[k].y);
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < K; k++) {
+            const ll i = iidx[k];
+            if (i < n) {
+                double *p = part + (ll)split * 3 * part_stride;
+                p[i] = (double)shx[k] + (double)slx[k];
+                p[part_stride + i] = (double)shy[k] + (double)sly[k];
+                p[2 * part_stride + i] = (double)shz[k] + (double)slz[k];
+            }
+        }
+    }
+}
+
+/* f = (G m_i m_scale) * sum over j-range slots, in slot order. */
+__global__ void k_mix_out(BodyArrays A, DevCtl *ctl, const double *part, ll part_stride)
+{
+    if (ctl->error) return;
+    const ll n = ctl->n;
+    const int S = ctl->splits;
+    double ms = ctl->m_scale;
+    if (!(ms > 0.0)) ms = 1.0;
+    for (ll i = (ll)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (ll)gridDim.x * blockDim.x) {
+        const unsigned f = A.flags[i];
+        if ((f & NBG_LIVE_MASK) != NBG_F_EXISTS) continue;
+        const double x = A.x[i], y = A.y[i], z = A.z[i], r = A.rad[i];
+        if (is_special(x, y, z, r)) {
+            /* NaN position or radius: every dist comparison fails, no force;
+             * an infinite coordinate makes the reference's terms NaN */
+            const bool has_nan = x != x || y != y || z != z || r != r;
+            const double v = has_nan ? 0.0 : nbg_nan();
+            A.fx[i] = v;
+            A.fy[i] = v;
+            A.fz[i] = v;
+            continue;
+        }
+        double sx = 0, sy = 0, sz = 0;
+        for (int s = 0; s < S; s++) {
+            const double *p = part + (ll)s * 3 * part_stride;
+            sx += p[i];
+            sy += p[part_stride + i];
+            sz += p[2 * part_stride + i];
+        }
+        const double g = NBG_G * A.m[i] * ms;
+        A.fx[i] = g * sx;
+        A.fy[i] = g * sy;
+        A.fz[i] = g * sz;
+    }
+}
+
+static int g_mixed_slots_cache[64];
+
+int nbg_mixed_slots(int device)
+{
+    if (device >= 0 && device < 64 && g_mixed_slots_cache[device] > 0) return g_mixed_slots_cache[device];
+    int per_sm = 0, sms = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pair_mixed<NBG_MIX_K>, NBG_MIX_BLOCK, 0);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+    int slots = per_sm * sms;
+    if (slots < 1) slots = 1;
+    if (device >= 0 && device < 64) g_mixed_slots_cache[device] = slots;
+    return slots;
+}
+
+static int flat_grid(ll cap)
+{
+    ll g = (cap + 255) / 256;
+    if (g > 152 * 16) g = 152 * 16;
+    return (int)(g < 1 ? 1 : g);
+}
+
+void nbg_launch_mixed_prep(const CycleBufs &cb, DevCtl *ctl, cudaStream_t st)
+{
+    const int fg = flat_grid(cb.cap);
+    k_mix_reduce<<<fg, 256, 0, st>>>(cb.a, ctl, cb.split_cap, cb.slots);
+    k_mix_pack<<<fg, 256, 0, st>>>(cb.a, ctl, cb.jhi, cb.jlo);
+    const ll tiles = (cb.cap + NBG_MIX_ITILE - 1) / NBG_MIX_ITILE;
+    k_mix_tiles<<<(int)tiles, NBG_MIX_BLOCK, 0, st>>>(ctl, cb.jhi, cb.jlo, cb.tile_c);
+}
+
+void nbg_launch_mixed_pair(const CycleBufs &cb, DevCtl *ctl, cudaStream_t st)
+{
+    k_pair_mixed<NBG_MIX_K><<<cb.slots, NBG_MIX_BLOCK, 0, st>>>(cb.a, ctl, cb.jhi, cb.jlo, cb.tile_c, cb.part, cb.cap,
+                                                               cb.ev_keys, cb.ev_cap);
+}
+
+void nbg_launch_mixed_out(const CycleBufs &cb, DevCtl *ctl, cudaStream_t st)
+{
+    k_mix_out<<<flat_grid(cb.cap), 256, 0, st>>>(cb.a, ctl, cb.part, cb.cap);
+}

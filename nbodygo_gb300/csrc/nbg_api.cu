@@ -1,0 +1,985 @@
+/*
+ * nbg_api.cu - the C ABI of include/nbgpu.h: context, device buffers, the
+ * cycle launch sequence (direct or as a replayed CUDA graph), cycle-boundary
+ * edits and the overflow / retry protocol.
+ *
+ * A cycle is the kernel sequence
+ *   begin | fragment count + scan | [mixed: reduce, pack, tile origins]
+ *   | pair kernel | [mixed: partial-sum reduction] | event sort | fragment
+ *   emission | resolution | integration | keep scan | compaction + adds
+ *   | copy back | end
+ * all on one stream, reading and updating a control block in device memory,
+ * so one captured cycle can be replayed nsteps times.  A kernel that finds a
+ * buffer too small sets a sticky error before anything of the cycle is
+ * mutated (the force arrays of live bodies excepted, which every cycle
+ * recomputes); the remaining kernels return at once, the host grows the
+ * buffer and re-runs the cycle.
+ */
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "nbg_internal.cuh"
+
+struct nbg_ctx {
+    int device = 0;
+    int precision = NBG_PRECISION_FP64;
+    cudaStream_t st = nullptr;     /* stream the work runs on */
+    cudaStream_t own_st = nullptr; /* the context's own stream */
+    DevCtl *ctl = nullptr;   /* device */
+    DevCtl *ctl_h = nullptr; /* pinned host copy */
+    CycleBufs cb{};
+    std::string err;
+    ll n_host = 0;          /* bodies in the array, as of the last sync */
+    ll pending_adds = 0;    /* host adds staged for the next cycle */
+    bool timing = false;
+    nbg_timing tacc{};
+    std::vector<cudaEvent_t> evs;
+    int use_graph = 1;
+    cudaGraphExec_t graph = nullptr;
+    bool graph_valid = false;
+    int graph_precision = -1;
+    void *scratch = nullptr;
+    size_t scratch_bytes = 0;
+    ll launches_per_cycle = 0;
+};
+
+static std::string g_last_error;
+
+#define CK(call)                                                                                     \
+    do {                                                                                             \
+        cudaError_t e_ = (call);                                                                     \
+        if (e_ != cudaSuccess) {                                                                     \
+            set_err(ctx, std::string(#call) + ": " + cudaGetErrorString(e_));                        \
+            return NBG_E_CUDA;                                                                       \
+        }                                                                                            \
+    } while (0)
+
+static void set_err(nbg_ctx *ctx, const std::string &m)
+{
+    if (ctx)
+        ctx->err = m;
+    else
+        g_last_error = m;
+}
+
+static int fail(nbg_ctx *ctx, int code, const std::string &m)
+{
+    set_err(ctx, m);
+    return code;
+}
+
+/* ---- small utility kernels --------------------------------------------- */
+
+__global__ void k_fill_f64(double *p, ll n, double v)
+{
+    for (ll k = (ll)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (ll)gridDim.x * blockDim.x) p[k] = v;
+}
+
+__global__ void k_fill_i64(ll *p, ll n, ll v)
+{
+    for (ll k = (ll)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (ll)gridDim.x * blockDim.x) p[k] = v;
+}
+
+static int grid_for(ll n)
+{
+    ll g = (n + 255) / 256;
+    if (g > 4096) g = 4096;
+    return (int)(g < 1 ? 1 : g);
+}
+
+/* ---- BodyArrays allocation ---------------------------------------------- */
+
+/* the 20 FP64 field pointers of a BodyArrays, in declaration order */
+static void f64_fields(BodyArrays &A, double **out[NBG_NF64])
+{
+    double **t[NBG_NF64] = {&A.x,  &A.y,  &A.z,  &A.vx,     &A.vy,        &A.vz,      &A.m,
+                            &A.rad, &A.fx, &A.fy, &A.fz,     &A.ff,        &A.fs,      &A.rest,
+                            &A.fr_rad, &A.fr_newrad, &A.fr_mass, &A.fr_cx, &A.fr_cy, &A.fr_cz};
+    for (int q = 0; q < NBG_NF64; q++) out[q] = t[q];
+}
+
+static void free_arrays(BodyArrays &A)
+{
+    double **f[NBG_NF64];
+    f64_fields(A, f);
+    for (int q = 0; q < NBG_NF64; q++) cudaFree(*f[q]);
+    cudaFree(A.fr_cnt);
+    cudaFree(A.id);
+    cudaFree(A.flags);
+    memset(&A, 0, sizeof A);
+}
+
+static cudaError_t alloc_arrays(BodyArrays &A, ll cap)
+{
+    memset(&A, 0, sizeof A);
+    size_t c = (size_t)(cap > 0 ? cap : 1);
+    double **f[NBG_NF64];
+    f64_fields(A, f);
+    for (int q = 0; q < NBG_NF64; q++) {
+        cudaError_t e = cudaMalloc((void **)f[q], c * sizeof(double));
+        if (e != cudaSuccess) return e;
+    }
+    cudaError_t e = cudaMalloc((void **)&A.fr_cnt, c * sizeof(ll));
+    if (e != cudaSuccess) return e;
+    e = cudaMalloc((void **)&A.id, c * sizeof(ll));
+    if (e != cudaSuccess) return e;
+    return cudaMalloc((void **)&A.flags, c * sizeof(unsigned));
+}
+
+static cudaError_t copy_arrays(BodyArrays &D, const BodyArrays &S, ll n, cudaStream_t st)
+{
+    if (n <= 0) return cudaSuccess;
+    double **fd[NBG_NF64], **fs[NBG_NF64];
+    f64_fields(D, fd);
+    f64_fields(const_cast<BodyArrays &>(S), fs);
+    for (int q = 0; q < NBG_NF64; q++) {
+        cudaError_t e = cudaMemcpyAsync(*fd[q], *fs[q], (size_t)n * sizeof(double), cudaMemcpyDeviceToDevice, st);
+        if (e != cudaSuccess) return e;
+    }
+    cudaError_t e = cudaMemcpyAsync(D.fr_cnt, S.fr_cnt, (size_t)n * sizeof(ll), cudaMemcpyDeviceToDevice, st);
+    if (e != cudaSuccess) return e;
+    e = cudaMemcpyAsync(D.id, S.id, (size_t)n * sizeof(ll), cudaMemcpyDeviceToDevice, st);
+    if (e != cudaSuccess) return e;
+    return cudaMemcpyAsync(D.flags, S.flags, (size_t)n * sizeof(unsigned), cudaMemcpyDeviceToDevice, st);
+}
+
+static ll next_pow2(ll v)
+{
+    ll p = 1;
+    while (p < v) p <<= 1;
+    return p;
+}
+
+static void invalidate_graph(nbg_ctx *ctx)
+{
+    if (ctx->graph) cudaGraphExecDestroy(ctx->graph);
+    ctx->graph = nullptr;
+    ctx->graph_valid = false;
+}
+
+/* (re)allocates the body-capacity dependent buffers, keeping the first
+ * `keep` bodies of the collection */
+static int ensure_cap(nbg_ctx *ctx, ll need, ll keep)
+{
+    if (need <= ctx->cb.cap) return NBG_OK;
+    if (need > NBG_MAX_BODIES) return fail(ctx, NBG_E_ARG, "body count exceeds 2^30");
+    ll cap = ctx->cb.cap > 0 ? ctx->cb.cap : 1024;
+    while (cap < need) cap *= 2;
+    if (cap > NBG_MAX_BODIES) cap = NBG_MAX_BODIES;
+    BodyArrays na;
+    CK(alloc_arrays(na, cap));
+    if (ctx->cb.cap > 0) {
+        CK(copy_arrays(na, ctx->cb.a, keep, ctx->st));
+        CK(cudaStreamSynchronize(ctx->st));
+        free_arrays(ctx->cb.a);
+        free_arrays(ctx->cb.b);
+        cudaFree(ctx->cb.rend);
+        cudaFree(ctx->cb.blk_sum);
+        cudaFree(ctx->cb.blk_off);
+        cudaFree(ctx->cb.jhi);
+        cudaFree(ctx->cb.jlo);
+        cudaFree(ctx->cb.tile_c);
+        cudaFree(ctx->cb.part);
+    }
+    ctx->cb.a = na;
+    CK(alloc_arrays(ctx->cb.b, cap));
+    CK(cudaMalloc((void **)&ctx->cb.rend, (size_t)cap * sizeof(nbg_renderable)));
+    ll nblk = (cap + NBG_SCAN_TILE - 1) / NBG_SCAN_TILE;
+    CK(cudaMalloc((void **)&ctx->cb.blk_sum, (size_t)nblk * sizeof(ll)));
+    CK(cudaMalloc((void **)&ctx->cb.blk_off, (size_t)nblk * sizeof(ll)));
+    ctx->cb.nblk_cap = nblk;
+    CK(cudaMalloc((void **)&ctx->cb.jhi, (size_t)cap * sizeof(float4)));
+    CK(cudaMalloc((void **)&ctx->cb.jlo, (size_t)cap * sizeof(float4)));
+    ll tiles = (cap + NBG_MIX_ITILE - 1) / NBG_MIX_ITILE;
+    CK(cudaMalloc((void **)&ctx->cb.tile_c, (size_t)tiles * sizeof(float4)));
+    CK(cudaMalloc((void **)&ctx->cb.part, (size_t)ctx->cb.split_cap * 3 * (size_t)cap * sizeof(double)));
+    ctx->cb.cap = cap;
+    invalidate_graph(ctx);
+    return NBG_OK;
+}
+
+static int ensure_frag_cap(nbg_ctx *ctx, ll need)
+{
+    if (need <= ctx->cb.frag_cap) return NBG_OK;
+    ll c = ctx->cb.frag_cap > 0 ? ctx->cb.frag_cap : 4096;
+    while (c < need) c *= 2;
+    if (ctx->cb.frag_cap > 0) free_arrays(ctx->cb.frags);
+    CK(alloc_arrays(ctx->cb.frags, c));
+    ctx->cb.frag_cap = c;
+    invalidate_graph(ctx);
+    return NBG_OK;
+}
+
+static int ensure_adds_cap(nbg_ctx *ctx, ll need)
+{
+    if (need <= ctx->cb.adds_cap) return NBG_OK;
+    ll c = ctx->cb.adds_cap > 0 ? ctx->cb.adds_cap : 1024;
+    while (c < need) c *= 2;
+    BodyArrays na;
+    CK(alloc_arrays(na, c));
+    if (ctx->cb.adds_cap > 0) {
+        CK(copy_arrays(na, ctx->cb.adds, ctx->pending_adds, ctx->st));
+        CK(cudaStreamSynchronize(ctx->st));
+        free_arrays(ctx->cb.adds);
+    }
+    ctx->cb.adds = na;
+    ctx->cb.adds_cap = c;
+    invalidate_graph(ctx);
+    return NBG_OK;
+}
+
+static int ensure_ev_cap(nbg_ctx *ctx, ll need)
+{
+    if (need <= ctx->cb.ev_cap) return NBG_OK;
+    ll c = next_pow2(need > 65536 ? need : 65536);
+    cudaFree(ctx->cb.ev_keys);
+    cudaFree(ctx->cb.ev_out);
+    ctx->cb.ev_keys = nullptr;
+    ctx->cb.ev_out = nullptr;
+    CK(cudaMalloc((void **)&ctx->cb.ev_keys, (size_t)c * sizeof(ull)));
+    CK(cudaMalloc((void **)&ctx->cb.ev_out, (size_t)c * sizeof(nbg_event)));
+    ctx->cb.ev_cap = c;
+    invalidate_graph(ctx);
+    return NBG_OK;
+}
+
+static int ensure_scratch(nbg_ctx *ctx, size_t bytes)
+{
+    if (bytes <= ctx->scratch_bytes) return NBG_OK;
+    cudaFree(ctx->scratch);
+    ctx->scratch = nullptr;
+    size_t b = 1 << 16;
+    while (b < bytes) b <<= 1;
+    CK(cudaMalloc(&ctx->scratch, b));
+    ctx->scratch_bytes = b;
+    return NBG_OK;
+}
+
+static int sync_ctl(nbg_ctx *ctx)
+{
+    CK(cudaMemcpyAsync(ctx->ctl_h, ctx->ctl, sizeof(DevCtl), cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
+    ctx->n_host = ctx->ctl_h->n;
+    return NBG_OK;
+}
+
+template <typename T>
+static int put_field(nbg_ctx *ctx, T *dst, const T *src, ll n)
+{
+    if (n <= 0 || !src) return NBG_OK;
+    CK(cudaMemcpyAsync(dst, src, (size_t)n * sizeof(T), cudaMemcpyHostToDevice, ctx->st));
+    return NBG_OK;
+}
+
+template <typename T>
+static int get_field(nbg_ctx *ctx, T *dst, const T *src, ll n)
+{
+    if (n <= 0 || !dst) return NBG_OK;
+    CK(cudaMemcpyAsync(dst, src, (size_t)n * sizeof(T), cudaMemcpyDeviceToHost, ctx->st));
+    return NBG_OK;
+}
+
+/* Uploads n bodies from a host SoA into D at offset `off`; NULL optional
+ * fields get NewBody defaults. */
+static int upload_soa(nbg_ctx *ctx, BodyArrays &D, ll off, const nbg_soa *h, ll n)
+{
+    if (n <= 0) return NBG_OK;
+    if (!h->x || !h->y || !h->z || !h->vx || !h->vy || !h->vz || !h->radius || !h->mass)
+        return fail(ctx, NBG_E_ARG, "x, y, z, vx, vy, vz, radius and mass are required");
+    std::vector<unsigned> flags((size_t)n);
+    for (ll k = 0; k < n; k++) {
+        int32_t c = h->collision ? h->collision[k] : NBG_ELASTIC;
+        if (c < NBG_NONE || c > NBG_FRAGMENT) return fail(ctx, NBG_E_ARG, "collision behaviour out of range");
+        uint32_t f = h->flags ? h->flags[k] : NBG_F_EXISTS;
+        flags[(size_t)k] = (f & 0xffu) | ((unsigned)c << NBG_BEHAVIOR_SHIFT);
+    }
+    int rc;
+#define PUTD(fld, src)                                                                      \
+    if ((src) != nullptr) {                                                                 \
+        if ((rc = put_field(ctx, D.fld + off, (const double *)(src), n)) != NBG_OK) return rc; \
+    }
+#define FILLD(fld, v) k_fill_f64<<<grid_for(n), 256, 0, ctx->st>>>(D.fld + off, n, v)
+    PUTD(x, h->x);
+    PUTD(y, h->y);
+    PUTD(z, h->z);
+    PUTD(vx, h->vx);
+    PUTD(vy, h->vy);
+    PUTD(vz, h->vz);
+    PUTD(rad, h->radius);
+    PUTD(m, h->mass);
+    if (h->frag_factor) { PUTD(ff, h->frag_factor); } else FILLD(ff, 0.0);
+    if (h->frag_step) { PUTD(fs, h->frag_step); } else FILLD(fs, 0.0);
+    if (h->r) { PUTD(rest, h->r); } else FILLD(rest, 1.0);
+    if (h->fx) { PUTD(fx, h->fx); } else FILLD(fx, 0.0);
+    if (h->fy) { PUTD(fy, h->fy); } else FILLD(fy, 0.0);
+    if (h->fz) { PUTD(fz, h->fz); } else FILLD(fz, 0.0);
+    if (h->frag_radius) { PUTD(fr_rad, h->frag_radius); } else FILLD(fr_rad, 0.0);
+    if (h->frag_new_radius) { PUTD(fr_newrad, h->frag_new_radius); } else FILLD(fr_newrad, 0.0);
+    if (h->frag_mass) { PUTD(fr_mass, h->frag_mass); } else FILLD(fr_mass, 0.0);
+    if (h->frag_cx) { PUTD(fr_cx, h->frag_cx); } else FILLD(fr_cx, 0.0);
+    if (h->frag_cy) { PUTD(fr_cy, h->frag_cy); } else FILLD(fr_cy, 0.0);
+    if (h->frag_cz) { PUTD(fr_cz, h->frag_cz); } else FILLD(fr_cz, 0.0);
+#undef PUTD
+#undef FILLD
+    if (h->frag_fragments) {
+        if ((rc = put_field(ctx, D.fr_cnt + off, (const ll *)h->frag_fragments, n)) != NBG_OK) return rc;
+    } else {
+        k_fill_i64<<<grid_for(n), 256, 0, ctx->st>>>(D.fr_cnt + off, n, 0);
+    }
+    if (h->id) {
+        if ((rc = put_field(ctx, D.id + off, (const ll *)h->id, n)) != NBG_OK) return rc;
+    }
+    if ((rc = put_field(ctx, D.flags + off, flags.data(), n)) != NBG_OK) return rc;
+    CK(cudaGetLastError());
+    /* the flag vector is a host temporary */
+    CK(cudaStreamSynchronize(ctx->st));
+    return NBG_OK;
+}
+
+/* ---- public API ---------------------------------------------------------- */
+
+extern "C" {
+
+const char *nbg_last_error(const nbg_ctx *ctx) { return ctx ? ctx->err.c_str() : g_last_error.c_str(); }
+
+int nbg_create(int device, int precision, int64_t capacity, nbg_ctx **out)
+{
+    if (!out) return fail(nullptr, NBG_E_ARG, "out is NULL");
+    *out = nullptr;
+    if (precision != NBG_PRECISION_FP64 && precision != NBG_PRECISION_MIXED)
+        return fail(nullptr, NBG_E_ARG, "unknown precision");
+    if (capacity < 0 || capacity > NBG_MAX_BODIES) return fail(nullptr, NBG_E_ARG, "capacity out of range");
+    int ndev = 0;
+    cudaError_t e = cudaGetDeviceCount(&ndev);
+    if (e != cudaSuccess || ndev == 0)
+        return fail(nullptr, NBG_E_CUDA, std::string("no CUDA device: ") + cudaGetErrorString(e));
+    if (device < 0 || device >= ndev) return fail(nullptr, NBG_E_ARG, "device index out of range");
+    nbg_ctx *ctx = new nbg_ctx();
+    ctx->device = device;
+    ctx->precision = precision;
+    int rc = NBG_OK;
+    do {
+        if (cudaSetDevice(device) != cudaSuccess) {
+            rc = fail(ctx, NBG_E_CUDA, "cudaSetDevice failed");
+            break;
+        }
+        if (cudaStreamCreateWithFlags(&ctx->own_st, cudaStreamNonBlocking) != cudaSuccess) {
+            rc = fail(ctx, NBG_E_CUDA, "cudaStreamCreate failed");
+            break;
+        }
+        ctx->st = ctx->own_st;
+        if (cudaMalloc((void **)&ctx->ctl, sizeof(DevCtl)) != cudaSuccess ||
+            cudaMallocHost((void **)&ctx->ctl_h, sizeof(DevCtl)) != cudaSuccess) {
+            rc = fail(ctx, NBG_E_CUDA, "control block allocation failed");
+            break;
+        }
+        memset(ctx->ctl_h, 0, sizeof(DevCtl));
+        ctx->ctl_h->seed = 0x6e626f6479676f31ull;
+        if (cudaMemcpy(ctx->ctl, ctx->ctl_h, sizeof(DevCtl), cudaMemcpyHostToDevice) != cudaSuccess) {
+            rc = fail(ctx, NBG_E_CUDA, "control block upload failed");
+            break;
+        }
+        ctx->cb.split_cap = 32;
+        ctx->cb.slots = nbg_mixed_slots(device);
+        if ((rc = ensure_cap(ctx, capacity > 0 ? capacity : 1024, 0)) != NBG_OK) break;
+        if ((rc = ensure_frag_cap(ctx, 4096)) != NBG_OK) break;
+        if ((rc = ensure_adds_cap(ctx, 1024)) != NBG_OK) break;
+        if ((rc = ensure_ev_cap(ctx, 65536)) != NBG_OK) break;
+    } while (0);
+    if (rc != NBG_OK) {
+        g_last_error = ctx->err;
+        nbg_destroy(ctx);
+        return rc;
+    }
+    *out = ctx;
+    return NBG_OK;
+}
+
+void nbg_destroy(nbg_ctx *ctx)
+{
+    if (!ctx) return;
+    cudaSetDevice(ctx->device);
+    if (ctx->st) cudaStreamSynchronize(ctx->st);
+    invalidate_graph(ctx);
+    free_arrays(ctx->cb.a);
+    free_arrays(ctx->cb.b);
+    free_arrays(ctx->cb.adds);
+    free_arrays(ctx->cb.frags);
+    cudaFree(ctx->cb.ev_keys);
+    cudaFree(ctx->cb.ev_out);
+    cudaFree(ctx->cb.rend);
+    cudaFree(ctx->cb.blk_sum);
+    cudaFree(ctx->cb.blk_off);
+    cudaFree(ctx->cb.jhi);
+    cudaFree(ctx->cb.jlo);
+    cudaFree(ctx->cb.tile_c);
+    cudaFree(ctx->cb.part);
+    cudaFree(ctx->scratch);
+    cudaFree(ctx->ctl);
+    if (ctx->ctl_h) cudaFreeHost(ctx->ctl_h);
+    for (cudaEvent_t e : ctx->evs) cudaEventDestroy(e);
+    if (ctx->own_st) cudaStreamDestroy(ctx->own_st);
+    delete ctx;
+}
+
+int nbg_set_precision(nbg_ctx *ctx, int precision)
+{
+    if (!ctx) return NBG_E_ARG;
+    if (precision != NBG_PRECISION_FP64 && precision != NBG_PRECISION_MIXED)
+        return fail(ctx, NBG_E_ARG, "unknown precision");
+    ctx->precision = precision;
+    return NBG_OK;
+}
+
+int nbg_set_stream(nbg_ctx *ctx, void *stream)
+{
+    if (!ctx) return NBG_E_ARG;
+    CK(cudaSetDevice(ctx->device));
+    CK(cudaStreamSynchronize(ctx->st));
+    ctx->st = stream ? (cudaStream_t)stream : ctx->own_st;
+    invalidate_graph(ctx);
+    return NBG_OK;
+}
+
+static int ctl_put(nbg_ctx *ctx, size_t off, const void *v, size_t bytes)
+{
+    CK(cudaSetDevice(ctx->device));
+    CK(cudaMemcpyAsync((char *)ctx->ctl + off, v, bytes, cudaMemcpyHostToDevice, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
+    return NBG_OK;
+}
+
+int nbg_set_seed(nbg_ctx *ctx, uint64_t seed)
+{
+    if (!ctx) return NBG_E_ARG;
+    ull s = seed;
+    return ctl_put(ctx, offsetof(DevCtl, seed), &s, sizeof s);
+}
+
+int nbg_set_next_id(nbg_ctx *ctx, int64_t next_id)
+{
+    if (!ctx) return NBG_E_ARG;
+    ll v = next_id;
+    return ctl_put(ctx, offsetof(DevCtl, next_id), &v, sizeof v);
+}
+
+int nbg_get_next_id(nbg_ctx *ctx, int64_t *next_id)
+{
+    if (!ctx || !next_id) return NBG_E_ARG;
+    CK(cudaSetDevice(ctx->device));
+    int rc = sync_ctl(ctx);
+    if (rc != NBG_OK) return rc;
+    *next_id = ctx->ctl_h->next_id;
+    return NBG_OK;
+}
+
+int nbg_set_cycle(nbg_ctx *ctx, uint64_t cycle)
+{
+    if (!ctx) return NBG_E_ARG;
+    ull c = cycle;
+    return ctl_put(ctx, offsetof(DevCtl, cycle), &c, sizeof c);
+}
+
+int nbg_set_bodies(nbg_ctx *ctx, const nbg_soa *host, int64_t n)
+{
+    if (!ctx || n < 0 || (n > 0 && !host)) return fail(ctx, NBG_E_ARG, "bad arguments");
+    CK(cudaSetDevice(ctx->device));
+    int rc = ensure_cap(ctx, n + ctx->pending_adds, 0);
+    if (rc != NBG_OK) return rc;
+    if ((rc = upload_soa(ctx, ctx->cb.a, 0, host, n)) != NBG_OK) return rc;
+    if (!host || !host->id) {
+        /* ids default to the array index, as the reference's tests do */
+        std::vector<ll> ids((size_t)(n > 0 ? n : 1));
+        for (ll k = 0; k < n; k++) ids[(size_t)k] = k;
+        if ((rc = put_field(ctx, ctx->cb.a.id, ids.data(), n)) != NBG_OK) return rc;
+        CK(cudaStreamSynchronize(ctx->st));
+    }
+    ll nn = n;
+    rc = ctl_put(ctx, offsetof(DevCtl, n), &nn, sizeof nn);
+    if (rc != NBG_OK) return rc;
+    ctx->n_host = n;
+    return NBG_OK;
+}
+
+int nbg_count(nbg_ctx *ctx, int64_t *n)
+{
+    if (!ctx || !n) return NBG_E_ARG;
+    CK(cudaSetDevice(ctx->device));
+    int rc = sync_ctl(ctx);
+    if (rc != NBG_OK) return rc;
+    *n = ctx->ctl_h->n;
+    return NBG_OK;
+}
+
+int nbg_get_state(nbg_ctx *ctx, nbg_soa *h, int64_t cap, int64_t *n_out)
+{
+    if (!ctx || !h || cap < 0) return fail(ctx, NBG_E_ARG, "bad arguments");
+    CK(cudaSetDevice(ctx->device));
+    int rc = sync_ctl(ctx);
+    if (rc != NBG_OK) return rc;
+    const ll n0 = ctx->ctl_h->n;
+    const ll n = n0 < cap ? n0 : cap;
+    if (n_out) *n_out = n0;
+    BodyArrays &A = ctx->cb.a;
+#define GETD(hf, df) \
+    if ((rc = get_field(ctx, h->hf, (const double *)A.df, n)) != NBG_OK) return rc;
+    GETD(x, x);
+    GETD(y, y);
+    GETD(z, z);
+    GETD(vx, vx);
+    GETD(vy, vy);
+    GETD(vz, vz);
+    GETD(radius, rad);
+    GETD(mass, m);
+    GETD(frag_factor, ff);
+    GETD(frag_step, fs);
+    GETD(r, rest);
+    GETD(fx, fx);
+    GETD(fy, fy);
+    GETD(fz, fz);
+    GETD(frag_radius, fr_rad);
+    GETD(frag_new_radius, fr_newrad);
+    GETD(frag_mass, fr_mass);
+    GETD(frag_cx, fr_cx);
+    GETD(frag_cy, fr_cy);
+    GETD(frag_cz, fr_cz);
+#undef GETD
+    if ((rc = get_field(ctx, (ll *)h->id, A.id, n)) != NBG_OK) return rc;
+    if ((rc = get_field(ctx, (ll *)h->frag_fragments, A.fr_cnt, n)) != NBG_OK) return rc;
+    std::vector<unsigned> fl;
+    if (h->flags || h->collision) {
+        fl.resize((size_t)(n > 0 ? n : 1));
+        if ((rc = get_field(ctx, fl.data(), A.flags, n)) != NBG_OK) return rc;
+    }
+    CK(cudaStreamSynchronize(ctx->st));
+    for (ll k = 0; k < n && (h->flags || h->collision); k++) {
+        if (h->flags) h->flags[k] = fl[(size_t)k] & 0xffu;
+        if (h->collision) h->collision[k] = (int32_t)NBG_BEHAVIOR(fl[(size_t)k]);
+    }
+    return NBG_OK;
+}
+
+int nbg_add_bodies(nbg_ctx *ctx, const nbg_soa *host, int64_t n, int64_t *ids_out)
+{
+    if (!ctx || n < 0 || (n > 0 && !host)) return fail(ctx, NBG_E_ARG, "bad arguments");
+    if (n == 0) return NBG_OK;
+    CK(cudaSetDevice(ctx->device));
+    int rc = sync_ctl(ctx);
+    if (rc != NBG_OK) return rc;
+    if ((rc = ensure_adds_cap(ctx, ctx->pending_adds + n)) != NBG_OK) return rc;
+    if ((rc = ensure_cap(ctx, ctx->n_host + ctx->pending_adds + n, ctx->n_host)) != NBG_OK) return rc;
+    std::vector<ll> ids((size_t)n);
+    ll next = ctx->ctl_h->next_id;
+    for (ll k = 0; k < n; k++) {
+        ll want = host->id ? host->id[k] : -1;
+        ids[(size_t)k] = want >= 0 ? want : next++;
+    }
+    nbg_soa tmp = *host;
+    tmp.id = (int64_t *)ids.data();
+    if ((rc = upload_soa(ctx, ctx->cb.adds, ctx->pending_adds, &tmp, n)) != NBG_OK) return rc;
+    ctx->pending_adds += n;
+    ll pa = ctx->pending_adds;
+    if ((rc = ctl_put(ctx, offsetof(DevCtl, n_host_adds), &pa, sizeof pa)) != NBG_OK) return rc;
+    if ((rc = ctl_put(ctx, offsetof(DevCtl, next_id), &next, sizeof next)) != NBG_OK) return rc;
+    if (ids_out)
+        for (ll k = 0; k < n; k++) ids_out[k] = ids[(size_t)k];
+    return NBG_OK;
+}
+
+int nbg_apply_edits(nbg_ctx *ctx, const nbg_edit *edits, int64_t k, int32_t *results)
+{
+    if (!ctx || k < 0 || (k > 0 && !edits)) return fail(ctx, NBG_E_ARG, "bad arguments");
+    if (k == 0) return NBG_OK;
+    for (ll q = 0; q < k; q++)
+        if ((edits[q].mask & NBG_M_COLLISION) && (edits[q].collision < NBG_NONE || edits[q].collision > NBG_FRAGMENT))
+            return fail(ctx, NBG_E_ARG, "collision behaviour out of range");
+    CK(cudaSetDevice(ctx->device));
+    size_t eb = (size_t)k * sizeof(nbg_edit), rb = (size_t)k * sizeof(int);
+    int rc = ensure_scratch(ctx, eb + rb + 256);
+    if (rc != NBG_OK) return rc;
+    nbg_edit *ed = (nbg_edit *)ctx->scratch;
+    int *res = (int *)((char *)ctx->scratch + ((eb + 255) / 256) * 256);
+    CK(cudaMemcpyAsync(ed, edits, eb, cudaMemcpyHostToDevice, ctx->st));
+    CK(cudaMemsetAsync(res, 0, rb, ctx->st));
+    nbg_launch_edits(ctx->cb, ctx->ctl, ed, k, res, ctx->st);
+    CK(cudaGetLastError());
+    std::vector<int> hr((size_t)k);
+    CK(cudaMemcpyAsync(hr.data(), res, rb, cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
+    if (results)
+        for (ll q = 0; q < k; q++) results[q] = hr[(size_t)q];
+    return NBG_OK;
+}
+
+int nbg_remove_bodies(nbg_ctx *ctx, int64_t count, int64_t *removed)
+{
+    if (!ctx) return NBG_E_ARG;
+    if (count == 0 || count < -1) return fail(ctx, NBG_E_ARG, "count must be -1 or positive");
+    CK(cudaSetDevice(ctx->device));
+    int rc = ensure_scratch(ctx, sizeof(ll));
+    if (rc != NBG_OK) return rc;
+    nbg_launch_remove(ctx->cb, ctx->ctl, count, (ll *)ctx->scratch, ctx->st);
+    CK(cudaGetLastError());
+    ll r = 0;
+    CK(cudaMemcpyAsync(&r, ctx->scratch, sizeof r, cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
+    if (removed) *removed = r;
+    return NBG_OK;
+}
+
+int nbg_get_body(nbg_ctx *ctx, int64_t id, nbg_soa *h, int32_t *found)
+{
+    if (!ctx || !h || !found) return fail(ctx, NBG_E_ARG, "bad arguments");
+    CK(cudaSetDevice(ctx->device));
+    int rc = ensure_scratch(ctx, sizeof(ll));
+    if (rc != NBG_OK) return rc;
+    ll big = (ll)1 << 62;
+    CK(cudaMemcpyAsync(ctx->scratch, &big, sizeof big, cudaMemcpyHostToDevice, ctx->st));
+    nbg_launch_find(ctx->cb, ctx->ctl, id, (ll *)ctx->scratch, ctx->st);
+    CK(cudaGetLastError());
+    ll idx = 0;
+    CK(cudaMemcpyAsync(&idx, ctx->scratch, sizeof idx, cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
+    if (idx >= big) {
+        *found = 0;
+        return NBG_OK;
+    }
+    *found = 1;
+    BodyArrays &A = ctx->cb.a;
+#define GET1(hf, df) \
+    if ((rc = get_field(ctx, h->hf, (const double *)(A.df + idx), 1)) != NBG_OK) return rc;
+    GET1(x, x);
+    GET1(y, y);
+    GET1(z, z);
+    GET1(vx, vx);
+    GET1(vy, vy);
+    GET1(vz, vz);
+    GET1(radius, rad);
+    GET1(mass, m);
+    GET1(frag_factor, ff);
+    GET1(frag_step, fs);
+    GET1(r, rest);
+    GET1(fx, fx);
+    GET1(fy, fy);
+    GET1(fz, fz);
+    GET1(frag_radius, fr_rad);
+    GET1(frag_new_radius, fr_newrad);
+    GET1(frag_mass, fr_mass);
+    GET1(frag_cx, fr_cx);
+    GET1(frag_cy, fr_cy);
+    GET1(frag_cz, fr_cz);
+#undef GET1
+    if ((rc = get_field(ctx, (ll *)h->id, A.id + idx, 1)) != NBG_OK) return rc;
+    if ((rc = get_field(ctx, (ll *)h->frag_fragments, A.fr_cnt + idx, 1)) != NBG_OK) return rc;
+    unsigned f = 0;
+    if ((rc = get_field(ctx, &f, A.flags + idx, 1)) != NBG_OK) return rc;
+    CK(cudaStreamSynchronize(ctx->st));
+    if (h->flags) h->flags[0] = f & 0xffu;
+    if (h->collision) h->collision[0] = (int32_t)NBG_BEHAVIOR(f);
+    return NBG_OK;
+}
+
+/* ---- the cycle ------------------------------------------------------------ */
+
+static cudaEvent_t get_event(nbg_ctx *ctx, size_t k)
+{
+    while (ctx->evs.size() <= k) {
+        cudaEvent_t e;
+        cudaEventCreate(&e);
+        ctx->evs.push_back(e);
+    }
+    return ctx->evs[k];
+}
+
+/* Launches one cycle.  With ev_base >= 0, events ev_base..ev_base+2 bracket
+ * (cycle start, pair kernel start, pair kernel end, cycle end). */
+static void launch_cycle(nbg_ctx *ctx, int precision, long ev_base)
+{
+    const CycleBufs &cb = ctx->cb;
+    cudaStream_t st = ctx->st;
+    if (ev_base >= 0) cudaEventRecord(get_event(ctx, (size_t)ev_base), st);
+    nbg_launch_begin(cb, ctx->ctl, st);
+    nbg_launch_frag_count(cb, ctx->ctl, st);
+    if (precision == NBG_PRECISION_MIXED) {
+        nbg_launch_mixed_prep(cb, ctx->ctl, st);
+        if (ev_base >= 0) cudaEventRecord(get_event(ctx, (size_t)ev_base + 1), st);
+        nbg_launch_mixed_pair(cb, ctx->ctl, st);
+        if (ev_base >= 0) cudaEventRecord(get_event(ctx, (size_t)ev_base + 2), st);
+        nbg_launch_mixed_out(cb, ctx->ctl, st);
+    } else {
+        if (ev_base >= 0) cudaEventRecord(get_event(ctx, (size_t)ev_base + 1), st);
+        nbg_launch_pair_fp64(cb, ctx->ctl, st);
+        if (ev_base >= 0) cudaEventRecord(get_event(ctx, (size_t)ev_base + 2), st);
+    }
+    nbg_launch_after_pair(cb, ctx->ctl, st);
+    if (ev_base >= 0) cudaEventRecord(get_event(ctx, (size_t)ev_base + 3), st);
+    ctx->launches_per_cycle = precision == NBG_PRECISION_MIXED ? 19 : 14;
+}
+
+static int build_graph(nbg_ctx *ctx)
+{
+    if (ctx->graph_valid && ctx->graph_precision == ctx->precision) return NBG_OK;
+    invalidate_graph(ctx);
+    cudaGraph_t g;
+    CK(cudaStreamBeginCapture(ctx->st, cudaStreamCaptureModeThreadLocal));
+    launch_cycle(ctx, ctx->precision, -1);
+    CK(cudaStreamEndCapture(ctx->st, &g));
+    cudaError_t e = cudaGraphInstantiate(&ctx->graph, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return fail(ctx, NBG_E_CUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e));
+    ctx->graph_valid = true;
+    ctx->graph_precision = ctx->precision;
+    return NBG_OK;
+}
+
+struct StepParams {
+    double dt, R;
+};
+
+int nbg_step(nbg_ctx *ctx, double dt, double R, int nsteps, nbg_step_info *info)
+{
+    if (!ctx || nsteps < 0) return fail(ctx, NBG_E_ARG, "bad arguments");
+    CK(cudaSetDevice(ctx->device));
+    /* dt, R and the per-call accumulators */
+    {
+        DevCtl *h = ctx->ctl_h;
+        int rc = sync_ctl(ctx);
+        if (rc != NBG_OK) return rc;
+        h->dt = dt;
+        h->R = R;
+        h->error = 0;
+        h->error_what = 0;
+        h->error_need = 0;
+        h->acc_steps = h->acc_interactions = h->acc_events = h->acc_frags = h->acc_removed = h->acc_nan = 0;
+        CK(cudaMemcpyAsync(ctx->ctl, h, sizeof(DevCtl), cudaMemcpyHostToDevice, ctx->st));
+    }
+    ctx->tacc = nbg_timing{};
+    int done = 0;
+    int retries = 0;
+    while (done < nsteps) {
+        int rc = ensure_cap(ctx, ctx->n_host + ctx->pending_adds + 1, ctx->n_host);
+        if (rc != NBG_OK) return rc;
+        const int todo = nsteps - done;
+        if (ctx->timing || !ctx->use_graph || todo == 1) {
+            for (int s = 0; s < todo; s++) launch_cycle(ctx, ctx->precision, ctx->timing ? 4L * s : -1L);
+        } else {
+            if ((rc = build_graph(ctx)) != NBG_OK) return rc;
+            for (int s = 0; s < todo; s++) CK(cudaGraphLaunch(ctx->graph, ctx->st));
+        }
+        CK(cudaGetLastError());
+        if ((rc = sync_ctl(ctx)) != NBG_OK) return rc;
+        DevCtl *h = ctx->ctl_h;
+        const int now = (int)h->acc_steps;
+        if (ctx->timing) {
+            for (int s = 0; s < now - done; s++) {
+                float a = 0, b = 0, c = 0;
+                cudaEventElapsedTime(&a, get_event(ctx, 4 * s), get_event(ctx, 4 * s + 1));
+                cudaEventElapsedTime(&b, get_event(ctx, 4 * s + 1), get_event(ctx, 4 * s + 2));
+                cudaEventElapsedTime(&c, get_event(ctx, 4 * s + 2), get_event(ctx, 4 * s + 3));
+                ctx->tacc.pair_ms += b;
+                ctx->tacc.other_ms += a + c;
+                ctx->tacc.pair_launches += 1;
+            }
+        }
+        ctx->tacc.kernel_launches += (ll)(now - done) * ctx->launches_per_cycle;
+        if (now > done) ctx->pending_adds = 0; /* consumed by the first cycle */
+        done = now;
+        if (h->error == 0) continue;
+        if (h->error != NBG_E_OVERFLOW || ++retries > 8) {
+            char m[160];
+            snprintf(m, sizeof m, "cycle %d failed: status %d (what %d, need %lld)", done, h->error, h->error_what,
+                     (long long)h->error_need);
+            return fail(ctx, h->error, m);
+        }
+        /* grow the short buffer and re-run the interrupted cycle */
+        if (h->error_what == 1)
+            rc = ensure_cap(ctx, h->error_need, ctx->n_host);
+        else if (h->error_what == 2)
+            rc = ensure_ev_cap(ctx, h->error_need);
+        else
+            rc = ensure_frag_cap(ctx, h->error_need);
+        if (rc != NBG_OK) return rc;
+        h->error = 0;
+        int z = 0;
+        CK(cudaMemcpyAsync(&ctx->ctl->error, &z, sizeof z, cudaMemcpyHostToDevice, ctx->st));
+    }
+    if (info) {
+        DevCtl *h = ctx->ctl_h;
+        info->steps_done = h->acc_steps;
+        info->n_bodies = h->n;
+        info->interactions = h->acc_interactions;
+        info->events = h->acc_events;
+        info->fragments_emitted = h->acc_frags;
+        info->removed = h->acc_removed;
+        info->nan_removed = h->acc_nan;
+        info->next_id = h->next_id;
+    }
+    return NBG_OK;
+}
+
+int nbg_force_pass(nbg_ctx *ctx)
+{
+    if (!ctx) return NBG_E_ARG;
+    CK(cudaSetDevice(ctx->device));
+    int z = 0;
+    CK(cudaMemcpyAsync(&ctx->ctl->error, &z, sizeof z, cudaMemcpyHostToDevice, ctx->st));
+    nbg_launch_begin(ctx->cb, ctx->ctl, ctx->st);
+    if (ctx->precision == NBG_PRECISION_MIXED) {
+        nbg_launch_mixed_prep(ctx->cb, ctx->ctl, ctx->st);
+        nbg_launch_mixed_pair(ctx->cb, ctx->ctl, ctx->st);
+        nbg_launch_mixed_out(ctx->cb, ctx->ctl, ctx->st);
+    } else {
+        nbg_launch_pair_fp64(ctx->cb, ctx->ctl, ctx->st);
+    }
+    CK(cudaGetLastError());
+    int rc = sync_ctl(ctx);
+    if (rc != NBG_OK) return rc;
+    if (ctx->ctl_h->error) return fail(ctx, ctx->ctl_h->error, "force pass failed");
+    return NBG_OK;
+}
+
+int nbg_get_renderables(nbg_ctx *ctx, nbg_renderable *host, int64_t cap, int64_t *n)
+{
+    if (!ctx || cap < 0) return fail(ctx, NBG_E_ARG, "bad arguments");
+    CK(cudaSetDevice(ctx->device));
+    int rc = sync_ctl(ctx);
+    if (rc != NBG_OK) return rc;
+    ll m = ctx->ctl_h->rend_n;
+    if (n) *n = m;
+    if (host && m > 0) {
+        if ((rc = get_field(ctx, host, ctx->cb.rend, m < cap ? m : cap)) != NBG_OK) return rc;
+        CK(cudaStreamSynchronize(ctx->st));
+    }
+    return NBG_OK;
+}
+
+int nbg_get_events(nbg_ctx *ctx, nbg_event *host, int64_t cap, int64_t *n)
+{
+    if (!ctx || cap < 0) return fail(ctx, NBG_E_ARG, "bad arguments");
+    CK(cudaSetDevice(ctx->device));
+    int rc = sync_ctl(ctx);
+    if (rc != NBG_OK) return rc;
+    ll m = ctx->ctl_h->last_ev_n;
+    if (n) *n = m;
+    if (host && m > 0) {
+        if ((rc = get_field(ctx, host, ctx->cb.ev_out, m < cap ? m : cap)) != NBG_OK) return rc;
+        CK(cudaStreamSynchronize(ctx->st));
+    }
+    return NBG_OK;
+}
+
+int nbg_get_forces(nbg_ctx *ctx, double *fx, double *fy, double *fz, int64_t cap, int64_t *n)
+{
+    if (!ctx || cap < 0) return fail(ctx, NBG_E_ARG, "bad arguments");
+    CK(cudaSetDevice(ctx->device));
+    int rc = sync_ctl(ctx);
+    if (rc != NBG_OK) return rc;
+    ll m = ctx->ctl_h->n;
+    if (n) *n = m;
+    ll c = m < cap ? m : cap;
+    if ((rc = get_field(ctx, fx, (const double *)ctx->cb.a.fx, c)) != NBG_OK) return rc;
+    if ((rc = get_field(ctx, fy, (const double *)ctx->cb.a.fy, c)) != NBG_OK) return rc;
+    if ((rc = get_field(ctx, fz, (const double *)ctx->cb.a.fz, c)) != NBG_OK) return rc;
+    CK(cudaStreamSynchronize(ctx->st));
+    return NBG_OK;
+}
+
+int nbg_energy(nbg_ctx *ctx, double *kinetic, double *potential, double momentum[3])
+{
+    if (!ctx) return NBG_E_ARG;
+    CK(cudaSetDevice(ctx->device));
+    int rc = sync_ctl(ctx);
+    if (rc != NBG_OK) return rc;
+    ll nb = (ctx->cb.cap + 127) / 128;
+    if ((rc = ensure_scratch(ctx, (size_t)nb * 5 * sizeof(double))) != NBG_OK) return rc;
+    CK(cudaMemsetAsync(ctx->scratch, 0, (size_t)nb * 5 * sizeof(double), ctx->st));
+    nbg_launch_energy(ctx->cb, ctx->ctl, (double *)ctx->scratch, ctx->st);
+    CK(cudaGetLastError());
+    std::vector<double> p((size_t)nb * 5);
+    CK(cudaMemcpyAsync(p.data(), ctx->scratch, p.size() * sizeof(double), cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
+    double s[5] = {0, 0, 0, 0, 0};
+    for (ll b = 0; b < nb; b++)
+        for (int q = 0; q < 5; q++) s[q] += p[(size_t)(b * 5 + q)];
+    if (kinetic) *kinetic = s[0];
+    if (potential) *potential = s[1];
+    if (momentum) {
+        momentum[0] = s[2];
+        momentum[1] = s[3];
+        momentum[2] = s[4];
+    }
+    return NBG_OK;
+}
+
+int nbg_enable_timing(nbg_ctx *ctx, int on)
+{
+    if (!ctx) return NBG_E_ARG;
+    ctx->timing = on != 0;
+    return NBG_OK;
+}
+
+int nbg_get_timing(nbg_ctx *ctx, nbg_timing *t)
+{
+    if (!ctx || !t) return NBG_E_ARG;
+    *t = ctx->tacc;
+    return NBG_OK;
+}
+
+int nbg_set_option(nbg_ctx *ctx, int key, int64_t value)
+{
+    if (!ctx) return NBG_E_ARG;
+    switch (key) {
+    case NBG_OPT_SPLIT:
+        if (value < 1 || value > 256) return fail(ctx, NBG_E_ARG, "split cap must be 1..256");
+        if (value != ctx->cb.split_cap) {
+            CK(cudaSetDevice(ctx->device));
+            cudaFree(ctx->cb.part);
+            ctx->cb.part = nullptr;
+            ctx->cb.split_cap = (int)value;
+            CK(cudaMalloc((void **)&ctx->cb.part, (size_t)value * 3 * (size_t)ctx->cb.cap * sizeof(double)));
+            invalidate_graph(ctx);
+        }
+        return NBG_OK;
+    case NBG_OPT_GRAPH:
+        ctx->use_graph = value != 0;
+        return NBG_OK;
+    case NBG_OPT_EV_CAP: {
+        if (value < 1 || value > ((ll)1 << 34)) return fail(ctx, NBG_E_ARG, "event capacity out of range");
+        CK(cudaSetDevice(ctx->device));
+        CK(cudaStreamSynchronize(ctx->st));
+        ctx->cb.ev_cap = 0;
+        ll c = next_pow2(value);
+        cudaFree(ctx->cb.ev_keys);
+        cudaFree(ctx->cb.ev_out);
+        ctx->cb.ev_keys = nullptr;
+        ctx->cb.ev_out = nullptr;
+        CK(cudaMalloc((void **)&ctx->cb.ev_keys, (size_t)c * sizeof(ull)));
+        CK(cudaMalloc((void **)&ctx->cb.ev_out, (size_t)c * sizeof(nbg_event)));
+        ctx->cb.ev_cap = c;
+        invalidate_graph(ctx);
+        return NBG_OK;
+    }
+    case NBG_OPT_FRAG_CAP: {
+        if (value < 1 || value > NBG_MAX_BODIES) return fail(ctx, NBG_E_ARG, "fragment capacity out of range");
+        CK(cudaSetDevice(ctx->device));
+        CK(cudaStreamSynchronize(ctx->st));
+        free_arrays(ctx->cb.frags);
+        CK(alloc_arrays(ctx->cb.frags, value));
+        ctx->cb.frag_cap = value;
+        invalidate_graph(ctx);
+        return NBG_OK;
+    }
+    default:
+        return fail(ctx, NBG_E_ARG, "unknown option");
+    }
+}
+
+int nbg_probe_peaks(int device, double *fp32_flops, double *fp64_flops, double *sm_clock_mhz)
+{
+    return nbg_run_probes(device, fp32_flops, fp64_flops, sm_clock_mhz);
+}
+
+} /* extern "C" */

@@ -1,0 +1,112 @@
+"""Mixed-precision form: FP32 pair terms, FP64 elsewhere.  Forces within
+1e-6 relative L2 of the FP64 force pass; the collision set is exact."""
+import numpy as np
+import pytest
+
+from nbodygo_gb300 import _abi as A
+from nbodygo_gb300 import workloads as W
+from nbodygo_gb300.api import Simulation
+from oracle.oracle import OracleSim
+
+from .helpers import rel_l2
+from .test_gpu_plain_parity import dense_cluster
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-6  # relative L2 acceleration error against FP64
+
+
+def mixed_forces(bodies):
+    sim = Simulation("mixed")
+    sim.set_bodies(bodies)
+    return sim, sim.force_pass()
+
+
+def live(b):
+    return (b["flags"] & (A.F_EXISTS | A.F_FRAGMENTING)) == A.F_EXISTS
+
+
+@pytest.mark.parametrize("n,seed", [(100, 1), (257, 2), (1000, 3), (4096, 4)])
+def test_plummer_forces(n, seed):
+    b = W.plummer(n=n, seed=seed)
+    _, f = mixed_forces(b)
+    ora = OracleSim(threads=8)
+    ora.set_bodies(b)
+    g = ora.forces()
+    err = rel_l2(f, g)
+    assert err <= TOL, f"rel L2 {err:.3e}"
+
+
+def test_disk_forces_and_events():
+    """Central body + disk: the dt = 0 cycle resolves the same events as the
+    oracle's compute pass on the same state."""
+    b = W.disk(n=1000, seed=8)
+    sim, f = mixed_forces(b)
+    ora = OracleSim(threads=8)
+    ora.set_bodies(b)
+    g = ora.forces()
+    assert rel_l2(f, g) <= TOL
+    sim.step(0.0, 1.0, 1)
+    ora.step(0.0, 1.0, 1)
+    ev_g, ev_o = sim.events(), ora.events()
+    assert len(ev_g) == len(ev_o)
+    assert np.array_equal(ev_g["id1"], ev_o["id1"]) and np.array_equal(ev_g["id2"], ev_o["id2"])
+
+
+def test_dense_cluster_events_exact():
+    """Overlapping pairs are decided in FP64: the event list of the first
+    cycle is identical to the oracle's."""
+    b = dense_cluster(400, seed=31)
+    sim = Simulation("mixed", seed=5)
+    sim.set_bodies(b)
+    sim.step(0.05, 0.9, 1)
+    ora = OracleSim(seed=5, threads=8)
+    ora.set_bodies(b)
+    ora.step(0.05, 0.9, 1)
+    ev_g, ev_o = sim.events(), ora.events()
+    assert len(ev_o) > 10
+    for f in ("id1", "id2", "type"):
+        assert np.array_equal(ev_g[f], ev_o[f])
+
+
+def test_plummer_disk_subset_forces():
+    """Workload 2's distribution at 1/8 size, against the FP64 oracle."""
+    b = W.plummer_disk(n_each=8192, seed=3)
+    _, f = mixed_forces(b)
+    ora = OracleSim(threads=8)
+    ora.set_bodies(b)
+    g = ora.forces()
+    assert rel_l2(f, g) <= TOL
+
+
+def test_full_size_plummer_disk_against_fp64_gpu():
+    """Workload 2 at full size (N = 131,072): mixed forces against the plain
+    FP64 GPU forces (themselves bit-identical to the oracle), plus a sampled
+    check of the plain forces against the oracle."""
+    b = W.plummer_disk()
+    _, f = mixed_forces(b)
+    plain = Simulation("fp64")
+    plain.set_bodies(b)
+    g = plain.force_pass()
+    err = rel_l2(f, g)
+    assert err <= TOL, f"rel L2 {err:.3e}"
+    ora = OracleSim(threads=8)
+    ora.set_bodies(b)
+    idx = np.arange(0, len(b["x"]), 4099)
+    ox, oy, oz = ora.forces_subset(idx)
+    assert np.array_equal(g[0][idx], ox) and np.array_equal(g[1][idx], oy) and np.array_equal(g[2][idx], oz)
+
+
+def test_full_size_uniform_sampled():
+    """Workload 4 at full size (N = 1,048,576), one cycle: a sample of 64
+    bodies against the FP64 oracle, and Newton's third law on the total."""
+    b = W.uniform_ball()
+    _, f = mixed_forces(b)
+    ora = OracleSim(threads=8)
+    ora.set_bodies(b)
+    idx = np.arange(0, len(b["x"]), 16411)[:64]
+    g = ora.forces_subset(idx)
+    err = rel_l2([c[idx] for c in f], g)
+    assert err <= TOL, f"rel L2 {err:.3e}"
+    tot = np.sqrt(sum(np.sum(c) ** 2 for c in f))
+    mag = np.sum(np.sqrt(f[0] ** 2 + f[1] ** 2 + f[2] ** 2))
+    assert tot <= 1e-5 * mag
