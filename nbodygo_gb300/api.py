@@ -127,14 +127,22 @@ class Simulation:
         self._check(self.lib.nbg_count(self.ctx, C.byref(v)))
         return v.value
 
-    def state(self, fields=None):
+    def state(self, fields=None, out=None):
+        """Body state as a dict of numpy arrays.  With `out` (a dict of
+        contiguous arrays, e.g. in pinned memory) the state is copied into
+        them, up to their length, and views of the filled part are returned."""
         n = self.count()
-        out = A.empty_state(n) if fields is None else {f: np.zeros(n, dtype=A.FIELD_DTYPES[f]) for f in fields}
+        if out is None:
+            out = A.empty_state(n) if fields is None else {f: np.zeros(n, dtype=A.FIELD_DTYPES[f]) for f in fields}
+            cap = n
+        else:
+            cap = min(len(v) for v in out.values())
         soa, keep = A.soa_from_arrays(out)
         got = C.c_int64()
-        self._check(self.lib.nbg_get_state(self.ctx, C.byref(soa), n, C.byref(got)))
+        self._check(self.lib.nbg_get_state(self.ctx, C.byref(soa), cap, C.byref(got)))
         del keep
-        return out
+        m = min(cap, got.value)
+        return {k: v[:m] for k, v in out.items()}
 
     def add_bodies(self, bodies):
         n = len(bodies["x"])
