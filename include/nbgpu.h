@@ -242,6 +242,9 @@ int nbg_get_timing(nbg_ctx *ctx, nbg_timing *t);
 #define NBG_OPT_GRAPH 2      /* 0 = launch each cycle directly, 1 = CUDA graph */
 #define NBG_OPT_EV_CAP 3     /* event-list capacity (rounded up to a power of two) */
 #define NBG_OPT_FRAG_CAP 4   /* fragments one cycle may emit */
+#define NBG_OPT_NEAR_PPM 5   /* mixed: pairs closer than (value * 1e-6) x the i-tile's
+                                extent around its origin are computed in FP64
+                                (default 70000) */
 int nbg_set_option(nbg_ctx *ctx, int key, int64_t value);
 
 /* Peak probes: FFMA (FP32) and DFMA (FP64) throughput of the device in

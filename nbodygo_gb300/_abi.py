@@ -39,6 +39,7 @@ OPT_SPLIT = 1
 OPT_GRAPH = 2
 OPT_EV_CAP = 3
 OPT_FRAG_CAP = 4
+OPT_NEAR_PPM = 5
 
 _pd = C.POINTER(C.c_double)
 _pi64 = C.POINTER(C.c_int64)

@@ -26,6 +26,7 @@ NVCC_COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompi
 UNITS = {
     "k_cycle.cu": ["--fmad=false", "-DNBG_NO_FMAD"],
     "k_mixed.cu": [],
+    "k_sort.cu": [],
     "k_probe.cu": [],
     "nbg_api.cu": [],
 }

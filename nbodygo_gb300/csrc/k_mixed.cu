@@ -5,24 +5,26 @@
  * and the same collision set as Collided (body.go:192-208), with the pair
  * terms in FP32:
  *
+ *  - bodies are visited in Morton order (k_sort.cu), so each 512-body i-tile
+ *    is compact in space;
  *  - positions are held as hi/lo float pairs (x = hi + lo to ~2^-48 |x|);
- *    each work item re-centres the j positions on its i-tile's origin c with
+ *    each work item re-centres positions on its i-tile's origin c with
  *    (x_hi - c) + x_lo, so the FP32 coordinates a pair subtracts carry an
- *    error of 2^-24 |x - c| instead of 2^-24 |x|;
- *  - pair terms m_j (x_j - x_i) / r^3 use packed f32x2 FMA (two j per
- *    instruction) and the SFU reciprocal square root;
+ *    error of about 2^-24 |x - c|: small for the near pairs, where it matters;
+ *  - pair terms m_j (x_j - x_i) / r^3 use packed f32x2 arithmetic (two j per
+ *    instruction: FFMA2 / FADD2 / FMUL2) and the SFU reciprocal square root;
  *  - every 256 j the FP32 tile sum is folded into a (hi, lo) float pair with
- *    TwoSum (Knuth), so the accumulated rounding error stays that of a 128-term
- *    sum; the item total is written as FP64;
- *  - any pair closer than a conservative bound (r_i + r_max plus the FP32
- *    error bound) is re-evaluated in FP64 with the reference's exact
- *    expressions: that FP64 dist decides the overlap skip and the collision
- *    test, so the event set is the reference's, and the force of such pairs
- *    is FP64.
+ *    TwoSum (Knuth), so the accumulated rounding error stays that of a
+ *    128-term sum; each item's total is written as FP64;
+ *  - a pair closer than a conservative bound - the larger of r_i + r_max plus
+ *    the FP32 error bound, and near_kappa times the i-tile's extent - is
+ *    re-evaluated in FP64 with the reference's exact expressions: that FP64
+ *    dist decides the overlap skip and the collision test, so the event set
+ *    is the reference's, and the force of every near pair is FP64.
  *
- * Work items are (i-tile of 512 bodies, j-range); CTAs take them from an
- * atomic counter.  Each item writes its partial sums to its own slot, and a
- * second kernel adds the slots in a fixed order, so results do not depend on
+ * Work items are (i-tile, j-range) pairs; persistent CTAs take them from an
+ * atomic counter.  Each item writes its partial sums to its own slot, and
+ * k_mix_out adds the slots in a fixed order, so results do not depend on
  * scheduling.
  */
 #include "nbg_internal.cuh"
@@ -58,7 +60,7 @@ __device__ __forceinline__ bool is_special(double x, double y, double z, double 
     return !(fabs(x) <= NBG_DBL_MAX && fabs(y) <= NBG_DBL_MAX && fabs(z) <= NBG_DBL_MAX) || r != r;
 }
 
-/* ---- per-cycle reductions: r_max, |x|_max, m_scale ----------------------- */
+/* ---- per-cycle reductions: r_max, |x|_max, m_scale, splits ---------------- */
 
 __global__ void k_mix_reduce(BodyArrays A, DevCtl *ctl, int split_cap, int slots)
 {
@@ -97,26 +99,28 @@ __global__ void k_mix_reduce(BodyArrays A, DevCtl *ctl, int split_cap, int slots
     }
 }
 
-/* jhi = (x_hi, y_hi, z_hi, m/m_scale), jlo = (x_lo, y_lo, z_lo, special) */
-__global__ void k_mix_pack(BodyArrays A, DevCtl *ctl, float4 *jhi, float4 *jlo)
+/* Packs body perm[p] at sorted position p:
+ * jhi = (x_hi, y_hi, z_hi, m/m_scale), jlo = (x_lo, y_lo, z_lo, special) */
+__global__ void k_mix_pack(BodyArrays A, DevCtl *ctl, const unsigned *perm, float4 *jhi, float4 *jlo)
 {
     if (ctl->error) return;
     const ll n = ctl->n;
     double ms = ctl->m_scale;
     if (!(ms > 0.0)) ms = 1.0;
-    for (ll k = (ll)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (ll)gridDim.x * blockDim.x) {
+    for (ll p = (ll)blockIdx.x * blockDim.x + threadIdx.x; p < n; p += (ll)gridDim.x * blockDim.x) {
+        const ll k = perm[p];
         const double x = A.x[k], y = A.y[k], z = A.z[k], r = A.rad[k];
         if (is_special(x, y, z, r)) {
-            jhi[k] = make_float4(SENTINEL_POS, SENTINEL_POS, SENTINEL_POS, 0.f);
-            jlo[k] = make_float4(0.f, 0.f, 0.f, 1.f);
+            jhi[p] = make_float4(SENTINEL_POS, SENTINEL_POS, SENTINEL_POS, 0.f);
+            jlo[p] = make_float4(0.f, 0.f, 0.f, 1.f);
             continue;
         }
         const float xh = (float)x, yh = (float)y, zh = (float)z;
         const float xl = (float)(x - (double)xh), yl = (float)(y - (double)yh), zl = (float)(z - (double)zh);
         const bool live = (A.flags[k] & NBG_LIVE_MASK) == NBG_F_EXISTS;
         const float m = live ? (float)(A.m[k] / ms) : 0.f;
-        jhi[k] = make_float4(xh, yh, zh, m);
-        jlo[k] = make_float4(xl, yl, zl, 0.f);
+        jhi[p] = make_float4(xh, yh, zh, m);
+        jlo[p] = make_float4(xl, yl, zl, 0.f);
     }
 }
 
@@ -131,10 +135,10 @@ __global__ void __launch_bounds__(NBG_MIX_BLOCK) k_mix_tiles(DevCtl *ctl, const 
     if (base >= n) return;
     float lo[3] = {3e38f, 3e38f, 3e38f}, hi[3] = {-3e38f, -3e38f, -3e38f};
     for (int k = 0; k < NBG_MIX_K; k++) {
-        ll i = base + (ll)k * NBG_MIX_BLOCK + threadIdx.x;
-        if (i >= n) continue;
-        if (jlo[i].w != 0.f) continue;
-        float4 h = jhi[i];
+        ll p = base + (ll)k * NBG_MIX_BLOCK + threadIdx.x;
+        if (p >= n) continue;
+        if (jlo[p].w != 0.f) continue;
+        float4 h = jhi[p];
         lo[0] = fminf(lo[0], h.x);
         lo[1] = fminf(lo[1], h.y);
         lo[2] = fminf(lo[2], h.z);
@@ -182,11 +186,10 @@ __device__ static int detect_event_mixed(unsigned bi, unsigned bj, double ri, do
     return -1;
 }
 
-/* A pair inside the candidate bound: decide overlap and collision in FP64
- * with the reference's expressions (no contraction: explicit _rn
- * intrinsics), add the force if the pair does not overlap, and record the
- * collision event.  Returns the FP64 force term in m_scale-normalised
- * acceleration units through tx, ty, tz. */
+/* A pair inside the candidate bound (body indices i, j): decide overlap and
+ * collision in FP64 with the reference's expressions (no contraction:
+ * explicit _rn intrinsics), return the force term if the pair does not
+ * overlap (m_scale-normalised acceleration units), record the event. */
 __device__ static void candidate_pair(const BodyArrays &A, DevCtl *ctl, ull *ev_keys, ll ev_cap, ll i, ll j,
                                       double inv_ms, double &tx, double &ty, double &tz)
 {
@@ -225,10 +228,14 @@ __device__ __forceinline__ void fold64(float &hi, float &lo, double v)
     lo += vl;
 }
 
+/* Everything in this kernel is indexed by sorted position (p for i, q for
+ * j); perm maps a position to the body index used by the FP64 arrays and the
+ * event keys. */
 template <int K>
 __global__ void __launch_bounds__(NBG_MIX_BLOCK, 3)
 k_pair_mixed(BodyArrays A, DevCtl *ctl, const float4 *__restrict__ jhi, const float4 *__restrict__ jlo,
-             const float4 *__restrict__ tile_c, double *__restrict__ part, ll part_stride, ull *ev_keys, ll ev_cap)
+             const float4 *__restrict__ tile_c, const unsigned *__restrict__ perm, double *__restrict__ part,
+             ll part_stride, ull *ev_keys, ll ev_cap)
 {
     constexpr int JP = NBG_MIX_JT / 2; /* j pairs per tile */
     constexpr int ITILE = NBG_MIX_BLOCK * K;
@@ -245,6 +252,7 @@ k_pair_mixed(BodyArrays A, DevCtl *ctl, const float4 *__restrict__ jhi, const fl
     const double inv_ms = 1.0 / ms;
     const float rmax = __uint_as_float(ctl->rmax_bits);
     const float xmax = __uint_as_float(ctl->xmax_bits);
+    const double kappa = (double)ctl->near_kappa;
     const int tid = threadIdx.x;
 
     for (;;) {
@@ -260,23 +268,21 @@ k_pair_mixed(BodyArrays A, DevCtl *ctl, const float4 *__restrict__ jhi, const fl
         float2 nx[K], ny[K], nz[K];
         float thr[K];
         float shx[K], slx[K], shy[K], sly[K], shz[K], slz[K];
-        ll iidx[K];
 #pragma unroll
         for (int k = 0; k < K; k++) {
-            const ll i = tile * ITILE + (ll)k * NBG_MIX_BLOCK + tid;
-            iidx[k] = i;
+            const ll p = tile * ITILE + (ll)k * NBG_MIX_BLOCK + tid;
             float xr = 0.f, yr = 0.f, zr = 0.f, t = -1.f;
-            if (i < n) {
-                const float4 h = jhi[i], l = jlo[i];
+            if (p < n) {
+                const float4 h = jhi[p], l = jlo[p];
                 if (l.w == 0.f) {
                     xr = (h.x - c.x) + l.x;
                     yr = (h.y - c.y) + l.y;
                     zr = (h.z - c.z) + l.z;
-                    const double ri = A.rad[i];
+                    const double ri = A.rad[perm[p]];
                     const double D = fmax(0.0, ri + (double)rmax);
                     const double amax = (double)fmaxf(fabsf(xr), fmaxf(fabsf(yr), fabsf(zr)));
                     const double eps = 0x1p-19 * (amax + D) + 0x1p-44 * (double)xmax + 0x1p-100;
-                    const double b = (D + eps) * (1.0 + 0x1p-18);
+                    const double b = fmax(D + eps, kappa * amax) * (1.0 + 0x1p-18);
                     t = __double2float_ru(b * b);
                 } else {
                     xr = yr = zr = SENTINEL_POS;
@@ -297,9 +303,9 @@ k_pair_mixed(BodyArrays A, DevCtl *ctl, const float4 *__restrict__ jhi, const fl
                 float v[2][4];
 #pragma unroll
                 for (int e = 0; e < 2; e++) {
-                    const ll j = jt + 2 * tid + e;
-                    if (j < je) {
-                        const float4 h = jhi[j], l = jlo[j];
+                    const ll q = jt + 2 * tid + e;
+                    if (q < je) {
+                        const float4 h = jhi[q], l = jlo[q];
                         v[e][0] = (h.x - c.x) + l.x;
                         v[e][1] = (h.y - c.y) + l.y;
                         v[e][2] = (h.z - c.z) + l.z;
@@ -326,8 +332,8 @@ k_pair_mixed(BodyArrays A, DevCtl *ctl, const float4 *__restrict__ jhi, const fl
                 mn[k] = 3.0e38f;
             }
 #pragma unroll 2
-            for (int p = 0; p < JP; p++) {
-                const float4 a = sA[p], b = sB[p];
+            for (int pp = 0; pp < JP; pp++) {
+                const float4 a = sA[pp], b = sB[pp];
                 const float2 xj = make_float2(a.x, a.y), yj = make_float2(a.z, a.w);
                 const float2 zj = make_float2(b.x, b.y), mj = make_float2(b.z, b.w);
 #pragma unroll
@@ -351,16 +357,17 @@ k_pair_mixed(BodyArrays A, DevCtl *ctl, const float4 *__restrict__ jhi, const fl
 #pragma unroll
             for (int k = 0; k < K; k++) {
                 if (mn[k] < thr[k]) {
-                    /* slow path: this tile holds a candidate pair for body i */
-                    const ll i = iidx[k];
+                    /* slow path: this tile holds a near or overlapping pair for i */
+                    const ll p = tile * ITILE + (ll)k * NBG_MIX_BLOCK + tid;
+                    const ll i = perm[p];
                     float tx = 0.f, ty = 0.f, tz = 0.f;
                     const float xi = -nx[k].x, yi = -ny[k].x, zi = -nz[k].x;
-                    for (int p = 0; p < JP; p++) {
-                        const float4 a = sA[p], b = sB[p];
+                    for (int pp = 0; pp < JP; pp++) {
+                        const float4 a = sA[pp], b = sB[pp];
 #pragma unroll
                         for (int e = 0; e < 2; e++) {
-                            const ll j = jt + 2 * p + e;
-                            if (j >= je || j == i) continue;
+                            const ll q = jt + 2 * pp + e;
+                            if (q >= je || q == p) continue;
                             const float xj = e ? a.y : a.x, yj = e ? a.w : a.z;
                             const float zj = e ? b.y : b.x, m = e ? b.w : b.z;
                             const float dx = xj - xi, dy = yj - yi, dz = zj - zi;
@@ -373,7 +380,7 @@ k_pair_mixed(BodyArrays A, DevCtl *ctl, const float4 *__restrict__ jhi, const fl
                                 tz += s * dz;
                             } else {
                                 double qx, qy, qz;
-                                candidate_pair(A, ctl, ev_keys, ev_cap, i, j, inv_ms, qx, qy, qz);
+                                candidate_pair(A, ctl, ev_keys, ev_cap, i, (ll)perm[q], inv_ms, qx, qy, qz);
                                 fold64(shx[k], slx[k], qx);
                                 fold64(shy[k], sly[k], qy);
                                 fold64(shz[k], slz[k], qz);
@@ -391,26 +398,28 @@ k_pair_mixed(BodyArrays A, DevCtl *ctl, const float4 *__restrict__ jhi, const fl
         }
 #pragma unroll
         for (int k = 0; k < K; k++) {
-            const ll i = iidx[k];
-            if (i < n) {
-                double *p = part + (ll)split * 3 * part_stride;
-                p[i] = (double)shx[k] + (double)slx[k];
-                p[part_stride + i] = (double)shy[k] + (double)sly[k];
-                p[2 * part_stride + i] = (double)shz[k] + (double)slz[k];
+            const ll p = tile * ITILE + (ll)k * NBG_MIX_BLOCK + tid;
+            if (p < n) {
+                double *o = part + (ll)split * 3 * part_stride;
+                o[p] = (double)shx[k] + (double)slx[k];
+                o[part_stride + p] = (double)shy[k] + (double)sly[k];
+                o[2 * part_stride + p] = (double)shz[k] + (double)slz[k];
             }
         }
     }
 }
 
-/* f = (G m_i m_scale) * sum over j-range slots, in slot order. */
-__global__ void k_mix_out(BodyArrays A, DevCtl *ctl, const double *part, ll part_stride)
+/* f = (G m_i m_scale) * sum over j-range slots, in slot order, written to
+ * body perm[p]. */
+__global__ void k_mix_out(BodyArrays A, DevCtl *ctl, const unsigned *perm, const double *part, ll part_stride)
 {
     if (ctl->error) return;
     const ll n = ctl->n;
     const int S = ctl->splits;
     double ms = ctl->m_scale;
     if (!(ms > 0.0)) ms = 1.0;
-    for (ll i = (ll)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (ll)gridDim.x * blockDim.x) {
+    for (ll p = (ll)blockIdx.x * blockDim.x + threadIdx.x; p < n; p += (ll)gridDim.x * blockDim.x) {
+        const ll i = perm[p];
         const unsigned f = A.flags[i];
         if ((f & NBG_LIVE_MASK) != NBG_F_EXISTS) continue;
         const double x = A.x[i], y = A.y[i], z = A.z[i], r = A.rad[i];
@@ -426,10 +435,10 @@ __global__ void k_mix_out(BodyArrays A, DevCtl *ctl, const double *part, ll part
         }
         double sx = 0, sy = 0, sz = 0;
         for (int s = 0; s < S; s++) {
-            const double *p = part + (ll)s * 3 * part_stride;
-            sx += p[i];
-            sy += p[part_stride + i];
-            sz += p[2 * part_stride + i];
+            const double *o = part + (ll)s * 3 * part_stride;
+            sx += o[p];
+            sy += o[part_stride + p];
+            sz += o[2 * part_stride + p];
         }
         const double g = NBG_G * A.m[i] * ms;
         A.fx[i] = g * sx;
@@ -463,18 +472,19 @@ void nbg_launch_mixed_prep(const CycleBufs &cb, DevCtl *ctl, cudaStream_t st)
 {
     const int fg = flat_grid(cb.cap);
     k_mix_reduce<<<fg, 256, 0, st>>>(cb.a, ctl, cb.split_cap, cb.slots);
-    k_mix_pack<<<fg, 256, 0, st>>>(cb.a, ctl, cb.jhi, cb.jlo);
+    nbg_launch_spatial_sort(cb, ctl, st);
+    k_mix_pack<<<fg, 256, 0, st>>>(cb.a, ctl, cb.perm, cb.jhi, cb.jlo);
     const ll tiles = (cb.cap + NBG_MIX_ITILE - 1) / NBG_MIX_ITILE;
     k_mix_tiles<<<(int)tiles, NBG_MIX_BLOCK, 0, st>>>(ctl, cb.jhi, cb.jlo, cb.tile_c);
 }
 
 void nbg_launch_mixed_pair(const CycleBufs &cb, DevCtl *ctl, cudaStream_t st)
 {
-    k_pair_mixed<NBG_MIX_K><<<cb.slots, NBG_MIX_BLOCK, 0, st>>>(cb.a, ctl, cb.jhi, cb.jlo, cb.tile_c, cb.part, cb.cap,
-                                                               cb.ev_keys, cb.ev_cap);
+    k_pair_mixed<NBG_MIX_K><<<cb.slots, NBG_MIX_BLOCK, 0, st>>>(cb.a, ctl, cb.jhi, cb.jlo, cb.tile_c, cb.perm,
+                                                               cb.part, cb.cap, cb.ev_keys, cb.ev_cap);
 }
 
 void nbg_launch_mixed_out(const CycleBufs &cb, DevCtl *ctl, cudaStream_t st)
 {
-    k_mix_out<<<flat_grid(cb.cap), 256, 0, st>>>(cb.a, ctl, cb.part, cb.cap);
+    k_mix_out<<<flat_grid(cb.cap), 256, 0, st>>>(cb.a, ctl, cb.perm, cb.part, cb.cap);
 }

@@ -66,6 +66,17 @@ __global__ void __launch_bounds__(256) k_ffma2_probe(float *out, int iters, floa
     if (blockIdx.x == 0 && threadIdx.x == 0) *cycles = clock64() - c0;
 }
 
+/* one warp, one long dependent chain: SM clock = cycles / event time */
+__global__ void k_clock_probe(float *out, int iters, ll *cycles)
+{
+    const ll c0 = clock64();
+    float x = threadIdx.x * 1e-3f;
+    for (int i = 0; i < iters; i++) x = fmaf(x, 0.999f, 0.001f);
+    const ll c1 = clock64();
+    if (x == -1.0f) out[threadIdx.x] = x;
+    if (threadIdx.x == 0) *cycles = c1 - c0;
+}
+
 int nbg_run_probes(int device, double *fp32, double *fp64, double *mhz)
 {
     if (cudaSetDevice(device) != cudaSuccess) return NBG_E_CUDA;
@@ -97,8 +108,7 @@ int nbg_run_probes(int device, double *fp32, double *fp64, double *mhz)
         cudaMemcpy(&c, cyc, sizeof c, cudaMemcpyDeviceToHost);
         double fl = 2.0 * 8 * 16 * (double)it32 * blocks * threads / (ms * 1e-3);
         if (fl > best32) best32 = fl;
-        double m = (double)c / (ms * 1e3);
-        if (m > clk) clk = m;
+        (void)c;
 
         cudaEventRecord(e0);
         k_ffma2_probe<<<blocks, threads>>>(of, it32 / 2, 0.999f, 0.001f, cyc);
@@ -116,6 +126,16 @@ int nbg_run_probes(int device, double *fp32, double *fp64, double *mhz)
         cudaEventElapsedTime(&ms, e0, e1);
         fl = 2.0 * 8 * 16 * (double)it64 * blocks * threads / (ms * 1e-3);
         if (fl > best64) best64 = fl;
+
+        cudaEventRecord(e0);
+        k_clock_probe<<<1, 32>>>(of, 1 << 22, cyc);
+        cudaEventRecord(e1);
+        cudaEventSynchronize(e1);
+        cudaEventElapsedTime(&ms, e0, e1);
+        ll cc = 0;
+        cudaMemcpy(&cc, cyc, sizeof cc, cudaMemcpyDeviceToHost);
+        const double m = (double)cc / (ms * 1e3);
+        if (m > clk) clk = m;
     }
     cudaError_t err = cudaGetLastError();
     cudaEventDestroy(e0);

@@ -1,0 +1,180 @@
+/*
+ * k_sort.cu - spatial ordering of the i-tiles of the mixed pair kernel.
+ *
+ * Every cycle the bodies are ordered along a Morton (Z-order) curve over a
+ * 1024^3 grid of the symmetric bounding box [-x_max, x_max]^3: 30-bit keys,
+ * sorted with a stable LSD radix sort (8-bit digits, four passes) whose
+ * ranking within a block uses warp match masks, so the order is the same on
+ * every run.  Consecutive 512-body slices of the sorted order are compact in
+ * space; the pair kernel re-centres FP32 coordinates on each slice's origin,
+ * which keeps their error at 2^-24 of the slice size instead of the system
+ * size.  Only the i side uses the order: which j a tile reads, and in which
+ * order, does not matter to the sum's accuracy.
+ *
+ * Bodies with a non-finite position or NaN radius sort last (key 2^30).
+ */
+#include "nbg_internal.cuh"
+
+#define RS_BLOCK 256
+#define RS_ITEMS 16
+#define RS_TILE (RS_BLOCK * RS_ITEMS)
+#define RS_BINS 256
+
+__device__ __forceinline__ unsigned spread10(unsigned v)
+{
+    v &= 0x3ffu;
+    v = (v | (v << 16)) & 0x030000ffu;
+    v = (v | (v << 8)) & 0x0300f00fu;
+    v = (v | (v << 4)) & 0x030c30c3u;
+    v = (v | (v << 2)) & 0x09249249u;
+    return v;
+}
+
+__device__ __forceinline__ unsigned quant10(float x, float inv_span)
+{
+    float t = (x * inv_span + 0.5f) * 1024.0f;
+    t = fminf(fmaxf(t, 0.0f), 1023.0f);
+    return (unsigned)t;
+}
+
+/* keys of the bodies 0..n-1 and the identity permutation */
+__global__ void k_morton_keys(BodyArrays A, DevCtl *ctl, unsigned *keys, unsigned *vals)
+{
+    if (ctl->error) return;
+    const ll n = ctl->n;
+    const float xmax = __uint_as_float(ctl->xmax_bits);
+    const float inv_span = xmax > 0.f ? 0.5f / xmax : 0.f;
+    for (ll k = (ll)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (ll)gridDim.x * blockDim.x) {
+        const double x = A.x[k], y = A.y[k], z = A.z[k], r = A.rad[k];
+        const bool finite = fabs(x) <= 1.7976931348623157e308 && fabs(y) <= 1.7976931348623157e308 &&
+                            fabs(z) <= 1.7976931348623157e308 && r == r;
+        unsigned key = 1u << 30;
+        if (finite)
+            key = spread10(quant10((float)x, inv_span)) | (spread10(quant10((float)y, inv_span)) << 1) |
+                  (spread10(quant10((float)z, inv_span)) << 2);
+        keys[k] = key;
+        vals[k] = (unsigned)k;
+    }
+}
+
+/* per-block digit histogram, digit-major: hist[d * nb + b] */
+__global__ void __launch_bounds__(RS_BLOCK) k_rs_hist(DevCtl *ctl, const unsigned *keys, int shift, ll *hist)
+{
+    __shared__ unsigned cnt[RS_BINS];
+    if (ctl->error) return;
+    const ll n = ctl->n;
+    const ll nb = (n + RS_TILE - 1) / RS_TILE;
+    const ll b = blockIdx.x;
+    if (b >= nb) return;
+    for (int d = threadIdx.x; d < RS_BINS; d += RS_BLOCK) cnt[d] = 0;
+    __syncthreads();
+    const ll base = b * RS_TILE;
+    for (int q = 0; q < RS_ITEMS; q++) {
+        ll k = base + (ll)q * RS_BLOCK + threadIdx.x;
+        if (k < n) atomicAdd(&cnt[(keys[k] >> shift) & 0xffu], 1u);
+    }
+    __syncthreads();
+    for (int d = threadIdx.x; d < RS_BINS; d += RS_BLOCK) hist[(ll)d * nb + b] = cnt[d];
+}
+
+/* exclusive scan of the digit-major histogram (one block) */
+__global__ void __launch_bounds__(1024) k_rs_scan(DevCtl *ctl, ll *hist)
+{
+    __shared__ ll warp_tot[32];
+    if (ctl->error) return;
+    const ll n = ctl->n;
+    const ll nb = (n + RS_TILE - 1) / RS_TILE;
+    const ll total = nb * RS_BINS;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    ll carry = 0;
+    for (ll c0 = 0; c0 < total; c0 += 1024) {
+        const ll c = c0 + threadIdx.x;
+        const ll v = c < total ? hist[c] : 0;
+        ll x = v;
+        for (int o = 1; o < 32; o <<= 1) {
+            ll y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+        }
+        if (lane == 31) warp_tot[w] = x;
+        __syncthreads();
+        if (w == 0) {
+            ll t = warp_tot[lane];
+            for (int o = 1; o < 32; o <<= 1) {
+                ll y = __shfl_up_sync(0xffffffffu, t, o);
+                if (lane >= o) t += y;
+            }
+            warp_tot[lane] = t;
+        }
+        __syncthreads();
+        const ll ex = x - v + (w > 0 ? warp_tot[w - 1] : 0);
+        if (c < total) hist[c] = carry + ex;
+        carry += warp_tot[31];
+        __syncthreads();
+    }
+}
+
+/* stable scatter: element order within a block is kept per digit */
+__global__ void __launch_bounds__(RS_BLOCK) k_rs_scatter(DevCtl *ctl, const unsigned *keys_in, const unsigned *vals_in,
+                                                        unsigned *keys_out, unsigned *vals_out, int shift,
+                                                        const ll *offs)
+{
+    __shared__ ll base[RS_BINS];
+    __shared__ unsigned wcnt[RS_BLOCK / 32][RS_BINS];
+    if (ctl->error) return;
+    const ll n = ctl->n;
+    const ll nb = (n + RS_TILE - 1) / RS_TILE;
+    const ll b = blockIdx.x;
+    if (b >= nb) return;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (int d = threadIdx.x; d < RS_BINS; d += RS_BLOCK) base[d] = offs[(ll)d * nb + b];
+    const unsigned lt = (1u << lane) - 1u;
+    for (int q = 0; q < RS_ITEMS; q++) {
+        for (int d = threadIdx.x; d < RS_BINS * (RS_BLOCK / 32); d += RS_BLOCK) (&wcnt[0][0])[d] = 0;
+        __syncthreads();
+        const ll k = b * RS_TILE + (ll)q * RS_BLOCK + threadIdx.x;
+        const bool ok = k < n;
+        const unsigned key = ok ? keys_in[k] : 0u;
+        const unsigned d = ok ? (key >> shift) & 0xffu : RS_BINS; /* RS_BINS never matches a real digit */
+        const unsigned peers = __match_any_sync(0xffffffffu, d);
+        const unsigned rank = __popc(peers & lt);
+        if (ok && rank == 0) wcnt[w][d] = __popc(peers);
+        __syncthreads();
+        if (ok) {
+            ll pos = base[d] + rank;
+            for (int v = 0; v < w; v++) pos += wcnt[v][d];
+            keys_out[pos] = key;
+            vals_out[pos] = vals_in[k];
+        }
+        __syncthreads();
+        for (int dd = threadIdx.x; dd < RS_BINS; dd += RS_BLOCK) {
+            ll s = 0;
+            for (int v = 0; v < RS_BLOCK / 32; v++) s += wcnt[v][dd];
+            base[dd] += s;
+        }
+        __syncthreads();
+    }
+}
+
+ll nbg_sort_scratch_hist(ll cap) { return ((cap + RS_TILE - 1) / RS_TILE) * RS_BINS; }
+
+/* Leaves the sorted permutation in cb.perm. */
+void nbg_launch_spatial_sort(const CycleBufs &cb, DevCtl *ctl, cudaStream_t st)
+{
+    const int g = (int)((cb.cap + 255) / 256 < 152 * 16 ? (cb.cap + 255) / 256 : 152 * 16);
+    k_morton_keys<<<g > 0 ? g : 1, 256, 0, st>>>(cb.a, ctl, cb.skey[0], cb.perm);
+    const int nb = (int)((cb.cap + RS_TILE - 1) / RS_TILE);
+    unsigned *kin = cb.skey[0], *vin = cb.perm, *kout = cb.skey[1], *vout = cb.sval;
+    for (int pass = 0; pass < 4; pass++) {
+        const int shift = 8 * pass;
+        k_rs_hist<<<nb, RS_BLOCK, 0, st>>>(ctl, kin, shift, cb.shist);
+        k_rs_scan<<<1, 1024, 0, st>>>(ctl, cb.shist);
+        k_rs_scatter<<<nb, RS_BLOCK, 0, st>>>(ctl, kin, vin, kout, vout, shift, cb.shist);
+        unsigned *t = kin;
+        kin = kout;
+        kout = t;
+        t = vin;
+        vin = vout;
+        vout = t;
+    }
+    /* four passes: the result is back in skey[0] / perm */
+}

@@ -160,6 +160,8 @@ static void invalidate_graph(nbg_ctx *ctx)
     ctx->graph_valid = false;
 }
 
+static void free_cap_buffers(CycleBufs &cb);
+
 /* (re)allocates the body-capacity dependent buffers, keeping the first
  * `keep` bodies of the collection */
 static int ensure_cap(nbg_ctx *ctx, ll need, ll keep)
@@ -176,13 +178,7 @@ static int ensure_cap(nbg_ctx *ctx, ll need, ll keep)
         CK(cudaStreamSynchronize(ctx->st));
         free_arrays(ctx->cb.a);
         free_arrays(ctx->cb.b);
-        cudaFree(ctx->cb.rend);
-        cudaFree(ctx->cb.blk_sum);
-        cudaFree(ctx->cb.blk_off);
-        cudaFree(ctx->cb.jhi);
-        cudaFree(ctx->cb.jlo);
-        cudaFree(ctx->cb.tile_c);
-        cudaFree(ctx->cb.part);
+        free_cap_buffers(ctx->cb);
     }
     ctx->cb.a = na;
     CK(alloc_arrays(ctx->cb.b, cap));
@@ -196,9 +192,30 @@ static int ensure_cap(nbg_ctx *ctx, ll need, ll keep)
     ll tiles = (cap + NBG_MIX_ITILE - 1) / NBG_MIX_ITILE;
     CK(cudaMalloc((void **)&ctx->cb.tile_c, (size_t)tiles * sizeof(float4)));
     CK(cudaMalloc((void **)&ctx->cb.part, (size_t)ctx->cb.split_cap * 3 * (size_t)cap * sizeof(double)));
+    CK(cudaMalloc((void **)&ctx->cb.perm, (size_t)cap * sizeof(unsigned)));
+    CK(cudaMalloc((void **)&ctx->cb.sval, (size_t)cap * sizeof(unsigned)));
+    CK(cudaMalloc((void **)&ctx->cb.skey[0], (size_t)cap * sizeof(unsigned)));
+    CK(cudaMalloc((void **)&ctx->cb.skey[1], (size_t)cap * sizeof(unsigned)));
+    CK(cudaMalloc((void **)&ctx->cb.shist, (size_t)nbg_sort_scratch_hist(cap) * sizeof(ll)));
     ctx->cb.cap = cap;
     invalidate_graph(ctx);
     return NBG_OK;
+}
+
+static void free_cap_buffers(CycleBufs &cb)
+{
+    cudaFree(cb.rend);
+    cudaFree(cb.blk_sum);
+    cudaFree(cb.blk_off);
+    cudaFree(cb.jhi);
+    cudaFree(cb.jlo);
+    cudaFree(cb.tile_c);
+    cudaFree(cb.part);
+    cudaFree(cb.perm);
+    cudaFree(cb.sval);
+    cudaFree(cb.skey[0]);
+    cudaFree(cb.skey[1]);
+    cudaFree(cb.shist);
 }
 
 static int ensure_frag_cap(nbg_ctx *ctx, ll need)
@@ -378,6 +395,7 @@ int nbg_create(int device, int precision, int64_t capacity, nbg_ctx **out)
         }
         memset(ctx->ctl_h, 0, sizeof(DevCtl));
         ctx->ctl_h->seed = 0x6e626f6479676f31ull;
+        ctx->ctl_h->near_kappa = 0.07f;
         if (cudaMemcpy(ctx->ctl, ctx->ctl_h, sizeof(DevCtl), cudaMemcpyHostToDevice) != cudaSuccess) {
             rc = fail(ctx, NBG_E_CUDA, "control block upload failed");
             break;
@@ -410,13 +428,7 @@ void nbg_destroy(nbg_ctx *ctx)
     free_arrays(ctx->cb.frags);
     cudaFree(ctx->cb.ev_keys);
     cudaFree(ctx->cb.ev_out);
-    cudaFree(ctx->cb.rend);
-    cudaFree(ctx->cb.blk_sum);
-    cudaFree(ctx->cb.blk_off);
-    cudaFree(ctx->cb.jhi);
-    cudaFree(ctx->cb.jlo);
-    cudaFree(ctx->cb.tile_c);
-    cudaFree(ctx->cb.part);
+    free_cap_buffers(ctx->cb);
     cudaFree(ctx->scratch);
     cudaFree(ctx->ctl);
     if (ctx->ctl_h) cudaFreeHost(ctx->ctl_h);
@@ -716,7 +728,9 @@ static void launch_cycle(nbg_ctx *ctx, int precision, long ev_base)
     }
     nbg_launch_after_pair(cb, ctx->ctl, st);
     if (ev_base >= 0) cudaEventRecord(get_event(ctx, (size_t)ev_base + 3), st);
-    ctx->launches_per_cycle = precision == NBG_PRECISION_MIXED ? 19 : 14;
+    /* begin, fragment count + scan, 10 after the pair kernel, and the pair
+     * kernel; mixed adds reduce, 13 sort, pack, tile origins and the output */
+    ctx->launches_per_cycle = precision == NBG_PRECISION_MIXED ? 31 : 14;
 }
 
 static int build_graph(nbg_ctx *ctx)
@@ -946,6 +960,11 @@ int nbg_set_option(nbg_ctx *ctx, int key, int64_t value)
     case NBG_OPT_GRAPH:
         ctx->use_graph = value != 0;
         return NBG_OK;
+    case NBG_OPT_NEAR_PPM: {
+        if (value < 0 || value > 10000000) return fail(ctx, NBG_E_ARG, "near radius factor out of range");
+        float kappa = (float)((double)value * 1e-6);
+        return ctl_put(ctx, offsetof(DevCtl, near_kappa), &kappa, sizeof kappa);
+    }
     case NBG_OPT_EV_CAP: {
         if (value < 1 || value > ((ll)1 << 34)) return fail(ctx, NBG_E_ARG, "event capacity out of range");
         CK(cudaSetDevice(ctx->device));

@@ -68,6 +68,10 @@ struct DevCtl {
     /* mixed-form reductions (float bits as unsigned for atomicMax) */
     unsigned rmax_bits, xmax_bits;
     double m_scale;
+    /* mixed form: pairs closer than near_kappa * (extent of the i-tile around
+     * its origin) are evaluated in FP64 (set by the host) */
+    float near_kappa;
+    int pad1;
     /* accumulated over the cycles of one nbg_step call */
     ll acc_steps, acc_interactions, acc_events, acc_frags, acc_removed, acc_nan;
     ll rend_n;       /* renderables written by the last cycle */
@@ -88,10 +92,14 @@ struct CycleBufs {
     ll *blk_sum;        /* per-block counts for the scans */
     ll *blk_off;
     ll nblk_cap;
-    /* mixed form */
+    /* mixed form (indexed by sorted position) */
     float4 *jhi, *jlo;
     float4 *tile_c;
     double *part;
+    unsigned *perm;     /* sorted position -> body index */
+    unsigned *skey[2];  /* radix-sort keys (ping-pong) */
+    unsigned *sval;     /* radix-sort values (ping-pong partner of perm) */
+    ll *shist;          /* radix-sort digit histogram / offsets */
     int split_cap;
     int slots;          /* resident CTAs of the mixed kernel on this device */
 };
@@ -121,6 +129,10 @@ void nbg_launch_mixed_prep(const CycleBufs &cb, DevCtl *ctl, cudaStream_t st);
 void nbg_launch_mixed_pair(const CycleBufs &cb, DevCtl *ctl, cudaStream_t st);
 void nbg_launch_mixed_out(const CycleBufs &cb, DevCtl *ctl, cudaStream_t st);
 int nbg_mixed_slots(int device);
+
+/* k_sort.cu */
+void nbg_launch_spatial_sort(const CycleBufs &cb, DevCtl *ctl, cudaStream_t st);
+ll nbg_sort_scratch_hist(ll cap);
 
 /* k_probe.cu */
 int nbg_run_probes(int device, double *fp32, double *fp64, double *mhz);

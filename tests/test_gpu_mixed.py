@@ -8,8 +8,8 @@ from nbodygo_gb300 import workloads as W
 from nbodygo_gb300.api import Simulation
 from oracle.oracle import OracleSim
 
-from .helpers import rel_l2
-from .test_gpu_plain_parity import dense_cluster
+from helpers import rel_l2
+from test_gpu_plain_parity import dense_cluster
 
 pytestmark = pytest.mark.gpu
 TOL = 1e-6  # relative L2 acceleration error against FP64
@@ -110,3 +110,30 @@ def test_full_size_uniform_sampled():
     tot = np.sqrt(sum(np.sum(c) ** 2 for c in f))
     mag = np.sum(np.sqrt(f[0] ** 2 + f[1] ** 2 + f[2] ** 2))
     assert tot <= 1e-5 * mag
+
+
+def test_mixed_is_deterministic():
+    """Persistent CTAs take work items in any order; the sums do not depend
+    on it (per-item slots, fixed-order reduction)."""
+    b = W.plummer_disk(n_each=4096, seed=9)
+    _, f1 = mixed_forces(b)
+    _, f2 = mixed_forces(b)
+    for a, c in zip(f1, f2):
+        assert np.array_equal(a, c)
+
+
+def test_near_pairs_in_fp64_keep_error_down():
+    """With the near-pair radius off, only overlap candidates go to FP64 and
+    the error of close encounters grows; with it on the gate holds."""
+    b = W.plummer_disk(n_each=8192, seed=3)
+    ora = OracleSim(threads=8)
+    ora.set_bodies(b)
+    g = ora.forces()
+    errs = {}
+    for ppm in (0, 70000):
+        sim = Simulation("mixed")
+        sim.set_option(A.OPT_NEAR_PPM, ppm)
+        sim.set_bodies(b)
+        errs[ppm] = rel_l2(sim.force_pass(), g)
+    assert errs[70000] <= TOL
+    assert errs[70000] <= errs[0]

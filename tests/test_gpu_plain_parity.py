@@ -8,7 +8,7 @@ from nbodygo_gb300 import workloads as W
 from nbodygo_gb300.api import Simulation
 from oracle.oracle import OracleSim
 
-from .helpers import assert_events_identical, assert_states_identical, body_set
+from helpers import assert_events_identical, assert_states_identical, body_set
 
 pytestmark = pytest.mark.gpu
 THREADS = 8
