@@ -100,7 +100,9 @@ __global__ void k_mix_reduce(BodyArrays A, DevCtl *ctl, int split_cap, int slots
 }
 
 /* Packs body perm[p] at sorted position p:
- * jhi = (x_hi, y_hi, z_hi, m/m_scale), jlo = (x_lo, y_lo, z_lo, special) */
+ * jhi = (x_hi, y_hi, z_hi, m/m_scale), jlo = (x_lo, y_lo, z_lo, radius).
+ * A special body (see is_special) gets a far sentinel position, no mass and
+ * x_lo = NaN, which is how the kernels recognise it. */
 __global__ void k_mix_pack(BodyArrays A, DevCtl *ctl, const unsigned *perm, float4 *jhi, float4 *jlo)
 {
     if (ctl->error) return;
@@ -112,7 +114,7 @@ __global__ void k_mix_pack(BodyArrays A, DevCtl *ctl, const unsigned *perm, floa
         const double x = A.x[k], y = A.y[k], z = A.z[k], r = A.rad[k];
         if (is_special(x, y, z, r)) {
             jhi[p] = make_float4(SENTINEL_POS, SENTINEL_POS, SENTINEL_POS, 0.f);
-            jlo[p] = make_float4(0.f, 0.f, 0.f, 1.f);
+            jlo[p] = make_float4(__int_as_float(0x7fc00000), 0.f, 0.f, 0.f);
             continue;
         }
         const float xh = (float)x, yh = (float)y, zh = (float)z;
@@ -120,9 +122,11 @@ __global__ void k_mix_pack(BodyArrays A, DevCtl *ctl, const unsigned *perm, floa
         const bool live = (A.flags[k] & NBG_LIVE_MASK) == NBG_F_EXISTS;
         const float m = live ? (float)(A.m[k] / ms) : 0.f;
         jhi[p] = make_float4(xh, yh, zh, m);
-        jlo[p] = make_float4(xl, yl, zl, 0.f);
+        jlo[p] = make_float4(xl, yl, zl, (float)r);
     }
 }
+
+__device__ __forceinline__ bool packed_special(const float4 &lo) { return lo.x != lo.x; }
 
 /* origin of each i-tile: centre of the bounding box of its bodies */
 __global__ void __launch_bounds__(NBG_MIX_BLOCK) k_mix_tiles(DevCtl *ctl, const float4 *jhi, const float4 *jlo, float4 *tile_c)
@@ -137,7 +141,7 @@ __global__ void __launch_bounds__(NBG_MIX_BLOCK) k_mix_tiles(DevCtl *ctl, const 
     for (int k = 0; k < NBG_MIX_K; k++) {
         ll p = base + (ll)k * NBG_MIX_BLOCK + threadIdx.x;
         if (p >= n) continue;
-        if (jlo[p].w != 0.f) continue;
+        if (packed_special(jlo[p])) continue;
         float4 h = jhi[p];
         lo[0] = fminf(lo[0], h.x);
         lo[1] = fminf(lo[1], h.y);
@@ -274,11 +278,11 @@ k_pair_mixed(BodyArrays A, DevCtl *ctl, const float4 *__restrict__ jhi, const fl
             float xr = 0.f, yr = 0.f, zr = 0.f, t = -1.f;
             if (p < n) {
                 const float4 h = jhi[p], l = jlo[p];
-                if (l.w == 0.f) {
+                if (!packed_special(l)) {
                     xr = (h.x - c.x) + l.x;
                     yr = (h.y - c.y) + l.y;
                     zr = (h.z - c.z) + l.z;
-                    const double ri = A.rad[perm[p]];
+                    const double ri = (double)l.w + fabs((double)l.w) * 0x1p-22; /* rounded up */
                     const double D = fmax(0.0, ri + (double)rmax);
                     const double amax = (double)fmaxf(fabsf(xr), fmaxf(fabsf(yr), fabsf(zr)));
                     const double eps = 0x1p-19 * (amax + D) + 0x1p-44 * (double)xmax + 0x1p-100;
@@ -310,7 +314,7 @@ k_pair_mixed(BodyArrays A, DevCtl *ctl, const float4 *__restrict__ jhi, const fl
                         v[e][1] = (h.y - c.y) + l.y;
                         v[e][2] = (h.z - c.z) + l.z;
                         v[e][3] = h.w;
-                        if (l.w != 0.f) {
+                        if (packed_special(l)) {
                             v[e][0] = v[e][1] = v[e][2] = SENTINEL_POS;
                             v[e][3] = 0.f;
                         }
@@ -360,6 +364,7 @@ k_pair_mixed(BodyArrays A, DevCtl *ctl, const float4 *__restrict__ jhi, const fl
                     /* slow path: this tile holds a near or overlapping pair for i */
                     const ll p = tile * ITILE + (ll)k * NBG_MIX_BLOCK + tid;
                     const ll i = perm[p];
+                    const float4 hi_i = jhi[p], lo_i = jlo[p];
                     float tx = 0.f, ty = 0.f, tz = 0.f;
                     const float xi = -nx[k].x, yi = -ny[k].x, zi = -nz[k].x;
                     for (int pp = 0; pp < JP; pp++) {
@@ -370,21 +375,34 @@ k_pair_mixed(BodyArrays A, DevCtl *ctl, const float4 *__restrict__ jhi, const fl
                             if (q >= je || q == p) continue;
                             const float xj = e ? a.y : a.x, yj = e ? a.w : a.z;
                             const float zj = e ? b.y : b.x, m = e ? b.w : b.z;
-                            const float dx = xj - xi, dy = yj - yi, dz = zj - zi;
-                            const float r2 = dx * dx + dy * dy + dz * dz;
-                            if (r2 >= thr[k]) {
-                                const float inv = rsqrt_sfu(r2);
-                                const float s = m * inv * inv * inv;
-                                tx += s * dx;
-                                ty += s * dy;
-                                tz += s * dz;
-                            } else {
-                                double qx, qy, qz;
-                                candidate_pair(A, ctl, ev_keys, ev_cap, i, (ll)perm[q], inv_ms, qx, qy, qz);
-                                fold64(shx[k], slx[k], qx);
-                                fold64(shy[k], sly[k], qy);
-                                fold64(shz[k], slz[k], qz);
+                            float dx = xj - xi, dy = yj - yi, dz = zj - zi;
+                            float r2 = dx * dx + dy * dy + dz * dz;
+                            if (r2 < thr[k]) {
+                                /* near pair: difference of the hi/lo positions
+                                 * (error ~2^-24 |dx|) */
+                                const float4 hj = jhi[q], lj = jlo[q];
+                                dx = (hj.x - hi_i.x) + (lj.x - lo_i.x);
+                                dy = (hj.y - hi_i.y) + (lj.y - lo_i.y);
+                                dz = (hj.z - hi_i.z) + (lj.z - lo_i.z);
+                                r2 = dx * dx + dy * dy + dz * dz;
+                                const float rs = lo_i.w + lj.w;
+                                /* an overlap, or a pair within 2^-10 of the
+                                 * overlap distance, is decided in FP64 */
+                                if (!(r2 > rs * rs * (1.0f + 0x1p-10f) && rs >= 0.f) || (lo_i.w < 0.f) ||
+                                    (lj.w < 0.f)) {
+                                    double qx, qy, qz;
+                                    candidate_pair(A, ctl, ev_keys, ev_cap, i, (ll)perm[q], inv_ms, qx, qy, qz);
+                                    fold64(shx[k], slx[k], qx);
+                                    fold64(shy[k], sly[k], qy);
+                                    fold64(shz[k], slz[k], qz);
+                                    continue;
+                                }
                             }
+                            const float inv = rsqrt_sfu(r2);
+                            const float s = m * inv * inv * inv;
+                            tx += s * dx;
+                            ty += s * dy;
+                            tz += s * dz;
                         }
                     }
                     ax[k] = make_float2(tx, 0.f);

@@ -84,7 +84,9 @@ def dense_cluster(n, seed, behaviors=(A.NONE, A.SUBSUME, A.ELASTIC, A.FRAGMENT))
     beh = np.array(behaviors, dtype=np.int32)
     b["collision"][:] = beh[np.floor(rng.uniform(n, 0, len(beh))).astype(int)]
     b["frag_factor"][:] = rng.uniform(n, 0.0, 2.0)
-    b["frag_step"][:] = rng.uniform(n, 0.0, 400.0)
+    # a few fragments per impact: a fragmenting body's pieces all overlap, so
+    # F fragments make O(F^2) collision events per cycle
+    b["frag_step"][:] = rng.uniform(n, 0.0, 6.0)
     return b
 
 
@@ -135,7 +137,7 @@ def test_fragment_impact_emits_fragments_over_cycles():
     b = body_set([
         dict(x=-2.0, vx=40.0, vy=1.0, mass=1e6, radius=1.0, collision=A.ELASTIC),
         dict(x=0.5, vx=-5.0, vy=0.3, vz=0.2, mass=5e6, radius=2.0, collision=A.FRAGMENT, frag_factor=0.1,
-             frag_step=150.0),
+             frag_step=4.0),
     ])
     sim, ora = run_both(b, 0.01, 1.0, 6)
     assert ora.count() > 2, "the impact should have fragmented the second body"
