@@ -223,6 +223,34 @@ int nbg_get_forces(nbg_ctx *ctx, double *fx, double *fy, double *fz, int64_t cap
  * that exist; a diagnostic, O(N^2) on the device. */
 int nbg_energy(nbg_ctx *ctx, double *kinetic, double *potential, double momentum[3]);
 
+/* ---- force pass without device allocation ------------------------------ */
+
+/*
+ * No counterpart in the reference: an entry point for callers that cannot
+ * allocate device memory (a host framework whose pool owns the device, a
+ * real-time loop that must not block in the allocator).  It runs the
+ * mixed-precision force pass of nbg_force_pass on caller-owned device arrays:
+ * x, y, z, mass, radius (FP64), flags (NBG_F_*; bodies that exist and are not
+ * fragmenting get a force), and writes fx, fy, fz of those bodies.  Every
+ * intermediate buffer lives in one static device array of NBG_NOALLOC_BYTES
+ * that each GPU loading the library holds until exit; no cudaMalloc or
+ * cudaFree is called.  Collision events are not reported.
+ *  - n may be at most NBG_NOALLOC_MAX_BODIES; larger n returns NBG_E_ARG.
+ *  - The work is queued on `stream` (a cudaStream_t; NULL is the default
+ *    stream) and the call returns without waiting.
+ *  - The first call on a device looks up the static array's device address;
+ *    make that first call before any stream capture.
+ *  - All calls on one device share the array: calls that may overlap on the
+ *    GPU (other streams, other host threads) race and must be serialised by
+ *    the caller.
+ * Errors are reported through nbg_last_error(NULL).
+ */
+#define NBG_NOALLOC_MAX_BODIES 65536
+#define NBG_NOALLOC_BYTES 9472256
+int nbg_forces_mixed_noalloc(const double *x, const double *y, const double *z, const double *mass,
+                             const double *radius, const uint32_t *flags, int64_t n, double *fx, double *fy,
+                             double *fz, void *stream);
+
 /* ---- measurement ------------------------------------------------------- */
 
 /* Device time of the kernels of the last nbg_step call, summed over its

@@ -177,6 +177,7 @@ def declare(lib):
         "nbg_get_timing": (C.c_int, [P, C.POINTER(NbgTiming)]),
         "nbg_set_option": (C.c_int, [P, C.c_int, C.c_int64]),
         "nbg_probe_peaks": (C.c_int, [C.c_int, _pd, _pd, _pd]),
+        "nbg_forces_mixed_noalloc": (C.c_int, [C.c_void_p] * 6 + [C.c_int64] + [C.c_void_p] * 4),
     }
     for name, (res, args) in sigs.items():
         fn = getattr(lib, name)

@@ -29,6 +29,7 @@ UNITS = {
     "k_sort.cu": [],
     "k_probe.cu": [],
     "nbg_api.cu": [],
+    "nbg_noalloc.cu": [],
 }
 HEADERS = ["nbg_internal.cuh", "nbg_math.h", "nbg_shared.h"]
 

@@ -48,6 +48,13 @@ struct nbg_ctx {
 
 static std::string g_last_error;
 
+/* error message of calls without a context (read by nbg_last_error(NULL)) */
+const char *nbg_set_global_error(const char *msg)
+{
+    g_last_error = msg ? msg : "";
+    return g_last_error.c_str();
+}
+
 #define CK(call)                                                                                     \
     do {                                                                                             \
         cudaError_t e_ = (call);                                                                     \

@@ -1,0 +1,136 @@
+/*
+ * nbg_noalloc.cu - the mixed-precision force pass for callers that cannot
+ * allocate device memory.
+ *
+ * Some callers of this library may not call cudaMalloc at all: a host
+ * framework whose memory pool already owns the device (and forbids
+ * allocations behind its back), a real-time loop that must never block in
+ * the driver's allocator, or code that runs where an allocation would
+ * disturb a memory budget fixed in advance.  nbg_forces_mixed_noalloc serves
+ * them.  The caller passes device pointers for the inputs and outputs; every
+ * intermediate buffer the force pass needs (sorted packed positions, Morton
+ * sort keys, tile origins, partial sums, the control block) lives in one
+ * file-scope __device__ array of NBG_NOALLOC_BYTES bytes.  Every GPU that
+ * loads the library holds that array until the process exits, which is why
+ * it is sized for at most NBG_NOALLOC_MAX_BODIES bodies.
+ *
+ * The kernels are the ones the context path runs (k_mixed.cu, k_sort.cu);
+ * only the buffers differ.
+ */
+#include <mutex>
+#include <string>
+
+#include "nbg_internal.cuh"
+
+#define NOALLOC_SPLITS 4
+
+static constexpr size_t align256(size_t v) { return (v + 255) / 256 * 256; }
+
+static constexpr size_t OFF_CTL = 0;
+static constexpr size_t OFF_JHI = align256(sizeof(DevCtl));
+static constexpr size_t OFF_JLO = OFF_JHI + align256((size_t)NBG_NOALLOC_MAX_BODIES * 16);
+static constexpr size_t OFF_TILE = OFF_JLO + align256((size_t)NBG_NOALLOC_MAX_BODIES * 16);
+static constexpr size_t OFF_PART =
+    OFF_TILE + align256((size_t)((NBG_NOALLOC_MAX_BODIES + NBG_MIX_ITILE - 1) / NBG_MIX_ITILE) * 16);
+static constexpr size_t OFF_PERM = OFF_PART + align256((size_t)NOALLOC_SPLITS * 3 * NBG_NOALLOC_MAX_BODIES * 8);
+static constexpr size_t OFF_SVAL = OFF_PERM + align256((size_t)NBG_NOALLOC_MAX_BODIES * 4);
+static constexpr size_t OFF_KEY0 = OFF_SVAL + align256((size_t)NBG_NOALLOC_MAX_BODIES * 4);
+static constexpr size_t OFF_KEY1 = OFF_KEY0 + align256((size_t)NBG_NOALLOC_MAX_BODIES * 4);
+static constexpr size_t OFF_HIST = OFF_KEY1 + align256((size_t)NBG_NOALLOC_MAX_BODIES * 4);
+/* radix-sort histogram: 256 digits per 4096-body block */
+static constexpr size_t HIST_BYTES = (size_t)((NBG_NOALLOC_MAX_BODIES + 4095) / 4096) * 256 * 8;
+static constexpr size_t TOTAL_BYTES = OFF_HIST + align256(HIST_BYTES);
+static_assert(TOTAL_BYTES == NBG_NOALLOC_BYTES, "NBG_NOALLOC_BYTES in nbgpu.h is out of date");
+
+/* The scratch of every call on this device.  In host code this name is only
+ * a stand-in: the device address comes from cudaGetSymbolAddress. */
+static __device__ __align__(256) unsigned char g_noalloc_scratch[TOTAL_BYTES];
+
+#define NOALLOC_MAX_DEVICES 64
+static unsigned char *g_scratch_addr[NOALLOC_MAX_DEVICES];
+static std::mutex g_setup_mutex;
+
+/* The control block's reductions and counters must start at zero. */
+__global__ void k_noalloc_init(DevCtl *ctl, ll n, float kappa)
+{
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    unsigned char *p = (unsigned char *)ctl;
+    for (size_t k = 0; k < sizeof(DevCtl); k++) p[k] = 0;
+    ctl->n = n;
+    ctl->near_kappa = kappa;
+}
+
+static int noalloc_fail(int code, const char *msg);
+
+extern "C" int nbg_forces_mixed_noalloc(const double *x, const double *y, const double *z, const double *mass,
+                                        const double *radius, const uint32_t *flags, int64_t n, double *fx,
+                                        double *fy, double *fz, void *stream)
+{
+    if (n < 0 || n > NBG_NOALLOC_MAX_BODIES)
+        return noalloc_fail(NBG_E_ARG, "nbg_forces_mixed_noalloc: n must be 0..NBG_NOALLOC_MAX_BODIES (65536)");
+    if (n > 0 && (!x || !y || !z || !mass || !radius || !flags || !fx || !fy || !fz))
+        return noalloc_fail(NBG_E_ARG, "nbg_forces_mixed_noalloc: a pointer is NULL");
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= NOALLOC_MAX_DEVICES)
+        return noalloc_fail(NBG_E_CUDA, "nbg_forces_mixed_noalloc: no current CUDA device");
+    unsigned char *base;
+    {
+        /* once per device, with that device current: the device address of
+         * the scratch array */
+        std::lock_guard<std::mutex> lock(g_setup_mutex);
+        if (!g_scratch_addr[dev]) {
+            void *ptr = nullptr;
+            cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+            if (e != cudaSuccess || !ptr)
+                return noalloc_fail(NBG_E_CUDA, "nbg_forces_mixed_noalloc: cudaGetSymbolAddress failed");
+            g_scratch_addr[dev] = (unsigned char *)ptr;
+        }
+        base = g_scratch_addr[dev];
+    }
+    if (n == 0) return NBG_OK;
+    cudaStream_t st = (cudaStream_t)stream;
+
+    CycleBufs cb;
+    memset(&cb, 0, sizeof cb);
+    cb.a.x = const_cast<double *>(x);
+    cb.a.y = const_cast<double *>(y);
+    cb.a.z = const_cast<double *>(z);
+    cb.a.m = const_cast<double *>(mass);
+    cb.a.rad = const_cast<double *>(radius);
+    cb.a.flags = const_cast<unsigned *>(flags);
+    cb.a.fx = fx;
+    cb.a.fy = fy;
+    cb.a.fz = fz;
+    cb.cap = NBG_NOALLOC_MAX_BODIES;
+    cb.jhi = (float4 *)(base + OFF_JHI);
+    cb.jlo = (float4 *)(base + OFF_JLO);
+    cb.tile_c = (float4 *)(base + OFF_TILE);
+    cb.part = (double *)(base + OFF_PART);
+    cb.perm = (unsigned *)(base + OFF_PERM);
+    cb.sval = (unsigned *)(base + OFF_SVAL);
+    cb.skey[0] = (unsigned *)(base + OFF_KEY0);
+    cb.skey[1] = (unsigned *)(base + OFF_KEY1);
+    cb.shist = (ll *)(base + OFF_HIST);
+    cb.ev_keys = nullptr; /* events are discarded */
+    cb.ev_cap = 0;
+    cb.split_cap = NOALLOC_SPLITS;
+    cb.slots = nbg_mixed_slots(dev);
+    DevCtl *ctl = (DevCtl *)(base + OFF_CTL);
+
+    k_noalloc_init<<<1, 1, 0, st>>>(ctl, (ll)n, 0.07f);
+    nbg_launch_mixed_prep(cb, ctl, st);
+    nbg_launch_mixed_pair(cb, ctl, st);
+    nbg_launch_mixed_out(cb, ctl, st);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return noalloc_fail(NBG_E_CUDA, cudaGetErrorString(e));
+    return NBG_OK;
+}
+
+/* the message is read through nbg_last_error(NULL) */
+const char *nbg_set_global_error(const char *msg);
+
+static int noalloc_fail(int code, const char *msg)
+{
+    nbg_set_global_error(msg);
+    return code;
+}
