@@ -1,27 +1,45 @@
 """Benchmark of the nbodygo compute cycle on GB300.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--workload plummer_disk|ensemble|uniform|plummer|disk]
 
-Workload (one "step" = one compute cycle: force + collision detection,
-resolution, integration, compaction): `plummer_disk`, N = 131,072 bodies
-(65,536 Plummer a=300 M=1e16 + 65,536 disk bodies, radii 0.1-0.5, subsume,
-dt = 0.01), mixed precision.  Metric: pair interactions/s (N(N-1) per cycle,
-N at the start of the cycle).
+A "step" is one compute cycle: force and collision detection, resolution,
+integration, compaction.  The metric is pair interactions/s: N(N-1) per cycle,
+with N taken at the start of the cycle (summed over the simulations of an
+ensemble).
 
-`value` is device time (CUDA events on the stream the library runs on) with
-the collection resident in HBM; L2 is flushed (a 512 MB write) before every
-timed cycle.  `e2e` is the same metric through the C ABI with host buffers:
-every cycle uploads the full body state from pinned host memory
-(nbg_set_bodies), runs nbg_step and reads the full state back
-(nbg_get_state), timed on the host clock.
+Default workload `plummer_disk`:
+
+- N = 131,072 bodies: 65,536 in a Plummer sphere (a = 300, M = 1e16) plus
+  65,536 disk bodies.
+- Radii 0.1-0.5, subsume collisions, dt = 0.01, mixed precision.
+
+Other workloads:
+
+- `ensemble`: 512 independent simulations of 256-32,768 bodies in one
+  context, 10 cycles per CUDA graph.
+- `uniform`: N = 1,048,576.
+- `plummer`: N = 16,384, FP64.
+- `disk`: N = 1,000, FP64.
+
+Timing:
+
+- `value` is device time, taken with CUDA events on the stream the library
+  runs on, with the collection resident in HBM.  L2 is flushed (a 512 MB
+  write) before every timed cycle, or before every graph of cycles for the
+  ensemble.
+- `e2e` is the same metric through the C ABI with host buffers.  Every cycle
+  (or graph) uploads the full body state from pinned host memory, runs it,
+  and reads the full state back, timed on the host clock.
 
 `--impl reference` times the CPU restatement of the reference's cycle
-(oracle/, with every host thread as the reference's worker pool would use)
-on a 32,768-body sample of the same distribution per step.
+(oracle/), with every host thread, as the reference's worker pool would use
+them.  It runs on a 32,768-body sample of the same distribution per step.
 
-Under torchrun (N > 1) each rank runs an independent replica on its own GPU
-(the direct sum of one collection is not sharded: replicas only); value is the
-sum over ranks of the work done divided by the slowest rank's time.
+Under torchrun (N > 1) each rank runs an independent replica on its own GPU.
+The direct sum of one collection is not sharded, so this is replicas only.
+`value` is the sum over ranks of the work done, divided by the slowest rank's
+time.
 """
 import argparse
 import json
@@ -38,9 +56,17 @@ sys.path.insert(0, ROOT)
 
 METRIC = "pair interactions/s, 1 GB300: mixed vs FP64 plain at <=1e-6 rel accel error"
 UNIT = "interactions/s"
-WORKLOAD = "plummer_disk"
-DT = 0.01
 FLOPS_PER_PAIR = 20  # Nyland, Harris & Prins (GPU Gems 3, ch. 31) convention
+
+# workload -> (precision, dt, description)
+WORKLOADS = {
+    "plummer_disk": ("mixed", 0.01, "Plummer a=300 M=1e16 + disk r 400-4000, radii 0.1-0.5, subsume"),
+    "ensemble": ("mixed", 0.01, "512 sims, N log-uniform 256-32768, {uniform ball, Plummer, disk}, "
+                                "none/elastic/subsume, 10 cycles per CUDA graph"),
+    "uniform": ("mixed", 0.01, "uniform ball R=20000, m=1e10, radius 0.05, v~N(0,1), no collisions"),
+    "plummer": ("fp64", 0.01, "Plummer a=200 M=1e16, radius 0.2, elastic"),
+    "disk": ("fp64", 0.005, "central body 5e15 + disk r 100-1000, elastic"),
+}
 
 
 def parse():
@@ -49,7 +75,8 @@ def parse():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--n-each", type=int, default=65536, help="bodies per component (default: the workload)")
+    ap.add_argument("--workload", default="plummer_disk", choices=sorted(WORKLOADS))
+    ap.add_argument("--n-each", type=int, default=65536, help="plummer_disk: bodies per component")
     ap.add_argument("--no-plain", action="store_true", help="skip the FP64 comparison run")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     return ap.parse_args()
@@ -63,11 +90,10 @@ def dist_env():
 
 
 class Dist:
-    """Barrier / max-reduction over ranks (torch.distributed) when WORLD_SIZE > 1."""
+    """Barrier / max / sum over ranks (torch.distributed) when WORLD_SIZE > 1."""
 
     def __init__(self, ws, local):
         self.ws = ws
-        self.pg = None
         if ws > 1:
             import torch
             import torch.distributed as td
@@ -80,19 +106,18 @@ class Dist:
         if self.ws > 1:
             self.td.barrier()
 
-    def max(self, v):
+    def _reduce(self, v, op):
         if self.ws == 1:
             return v
         t = self.torch.tensor([float(v)], device="cuda")
-        self.td.all_reduce(t, op=self.td.ReduceOp.MAX)
+        self.td.all_reduce(t, op=op)
         return float(t.item())
 
+    def max(self, v):
+        return v if self.ws == 1 else self._reduce(v, self.td.ReduceOp.MAX)
+
     def sum(self, v):
-        if self.ws == 1:
-            return v
-        t = self.torch.tensor([float(v)], device="cuda")
-        self.td.all_reduce(t, op=self.td.ReduceOp.SUM)
-        return float(t.item())
+        return v if self.ws == 1 else self._reduce(v, self.td.ReduceOp.SUM)
 
     def close(self):
         if self.ws > 1:
@@ -148,9 +173,9 @@ class Clocks:
                 "samples": len(sm)}
 
 
-def traffic_from_profiles():
-    """DRAM bytes per launch of the mixed pair kernel from the committed ncu summary."""
-    p = os.path.join(ROOT, "profiles", "pair_mixed_plummer_disk.md")
+def traffic_from_profiles(workload):
+    """DRAM bytes per launch of the pair kernel from the committed ncu summary."""
+    p = os.path.join(ROOT, "profiles", f"pair_mixed_{workload}.md")
     try:
         txt = open(p).read()
     except OSError:
@@ -166,20 +191,52 @@ def measured_hbm():
         return {}
 
 
-def cpu_baseline_sample(n_each_sample=16384, steps=1):
+def make_workload(name, n_each, rank):
+    """(list of body dicts, one per simulation) for a workload."""
+    from nbodygo_gb300 import workloads as W
+
+    seed_off = 1000 * rank
+    if name == "plummer_disk":
+        return [W.plummer_disk(n_each=n_each, seed=3 + seed_off)]
+    if name == "ensemble":
+        return W.ensemble(seed=5 + seed_off)
+    if name == "uniform":
+        return [W.uniform_ball(seed=4 + seed_off)]
+    if name == "plummer":
+        return [W.plummer(seed=2 + seed_off)]
+    return [W.disk(seed=1 + seed_off)]
+
+
+def load(sim, sims):
+    if len(sims) == 1:
+        sim.set_bodies(sims[0])
+    else:
+        sim.set_collections(sims)
+
+
+def cpu_baseline_sample(workload, dt):
     """CPU restatement of the reference cycle, all host threads, on a sample."""
     from nbodygo_gb300 import workloads as W
     from oracle.oracle import OracleSim
 
     cores = os.cpu_count() or 1
-    b = W.plummer_disk(n_each=n_each_sample, seed=3)
+    if workload in ("plummer_disk", "ensemble", "uniform"):
+        b = W.plummer_disk(n_each=16384, seed=3)
+        what = "plummer_disk with 32768 bodies"
+    elif workload == "plummer":
+        b = W.plummer(seed=2)
+        what = "plummer with 16384 bodies (the full workload)"
+    else:
+        b = W.disk(seed=1)
+        what = "disk with 1000 bodies (the full workload)"
     o = OracleSim(threads=cores)
     o.set_bodies(b)
+    steps = 1 if len(b["x"]) > 10000 else 20
     t0 = time.perf_counter()
-    info = o.step(DT, 1.0, steps)
+    info = o.step(dt, 1.0, steps)
     t = time.perf_counter() - t0
     return {"value": info["interactions"] / t, "unit": UNIT, "cores": cores, "kind": "port",
-            "sample": f"plummer_disk with {2 * n_each_sample} bodies, {steps} cycle(s), {t:.2f} s"}
+            "sample": f"{what}, {steps} cycle(s), {t:.2f} s; C restatement of the reference's Go cycle (oracle/)"}
 
 
 def run_reference(args, ws, rank):
@@ -189,17 +246,25 @@ def run_reference(args, ws, rank):
     from nbodygo_gb300 import workloads as W
     from oracle.oracle import OracleSim
 
+    prec, dt, desc = WORKLOADS[args.workload]
     cores = os.cpu_count() or 1
-    n_each = 16384
-    b = W.plummer_disk(n_each=n_each, seed=3)
+    if args.workload in ("plummer_disk", "ensemble", "uniform"):
+        b = W.plummer_disk(n_each=16384, seed=3)
+        sample = "plummer_disk with 32,768 bodies per cycle"
+    elif args.workload == "plummer":
+        b = W.plummer(seed=2)
+        sample = "the full plummer workload (16,384 bodies)"
+    else:
+        b = W.disk(seed=1)
+        sample = "the full disk workload (1,000 bodies)"
     o = OracleSim(threads=cores)
     o.set_bodies(b)
     for _ in range(args.warmup):
-        o.step(DT, 1.0, 1)
+        o.step(dt, 1.0, 1)
     total_int, total_t = 0, 0.0
     for _ in range(args.steps):
         t0 = time.perf_counter()
-        info = o.step(DT, 1.0, 1)
+        info = o.step(dt, 1.0, 1)
         total_t += time.perf_counter() - t0
         total_int += info["interactions"]
     v = total_int / total_t
@@ -207,14 +272,26 @@ def run_reference(args, ws, rank):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total_t / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic",
-            "config": {"workload": f"{WORKLOAD} sample: {2 * n_each} bodies (full workload: 131,072)",
-                       "n_bodies": 2 * n_each, "dt": DT, "collision": "subsume"},
+            "config": {"workload": f"{args.workload} sample: {len(b['x'])} bodies ({desc})",
+                       "n_bodies": int(len(b["x"])), "dt": dt},
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
-                             "sample": f"plummer_disk with {2 * n_each} bodies per cycle; the C restatement of "
-                                       "the reference's Go cycle (oracle/), worker-pool slicing"},
+                             "sample": f"{sample}; the C restatement of the reference's Go cycle (oracle/) "
+                                       "with the worker-pool slicing"},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     return 0
+
+
+def pinned_like(torch, st, extra):
+    out, keep = {}, []
+    for k, v in st.items():
+        tdt = torch.int32 if v.dtype == np.uint32 else getattr(torch, str(v.dtype))
+        t = torch.empty(len(v) + extra, dtype=tdt, pin_memory=True)
+        keep.append(t)
+        arr = t.numpy().view(v.dtype)
+        arr[: len(v)] = v
+        out[k] = arr
+    return out, keep
 
 
 def main():
@@ -229,9 +306,9 @@ def main():
     import torch
 
     from nbodygo_gb300 import _abi as A
-    from nbodygo_gb300 import workloads as W
     from nbodygo_gb300.api import Simulation, probe_peaks
 
+    prec, DT, desc = WORKLOADS[args.workload]
     dist = Dist(ws, local)
     torch.cuda.set_device(local)
     # a dedicated stream: the library's kernels, the L2 flush and the timing
@@ -239,34 +316,37 @@ def main():
     # stream, which nbg_set_stream does not take)
     stream = torch.cuda.Stream()
     torch.cuda.set_stream(stream)
-    bodies = W.plummer_disk(n_each=args.n_each, seed=3 + 1000 * rank)
-    n0 = len(bodies["x"])
+    sims = make_workload(args.workload, args.n_each, rank)
+    n0 = int(sum(len(b["x"]) for b in sims))
+    chunk = 10 if args.workload == "ensemble" else 1
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
 
-    sim = Simulation("mixed", device=local, capacity=n0 + 4096)
+    sim = Simulation(prec, device=local, capacity=n0 + 4096)
     sim.set_stream(stream.cuda_stream)
-    sim.set_bodies(bodies)
-    for _ in range(max(args.warmup, 3)):
-        sim.step(DT, 1.0, 1)
+    sim.set_option(A.OPT_GRAPH_CYCLES, chunk)
+    load(sim, sims)
+    sim.step(DT, 1.0, max(args.warmup, 3) * chunk)
 
-    # ---- timed: K cycles, L2 flushed before each, device time ----
+    # ---- timed: K cycles, L2 flushed before each chunk, device time ----
+    nchunks = max(1, args.steps // chunk)
     clocks = Clocks(local)
     clocks.start()
     dist.barrier()
     torch.cuda.synchronize()
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
-    interactions = 0
-    for k in range(args.steps):
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(nchunks)]
+    interactions, cycles = 0, 0
+    for k in range(nchunks):
         flush.fill_(float(k))
         ev[k][0].record(stream)
-        info = sim.step(DT, 1.0, 1)
+        info = sim.step(DT, 1.0, chunk)
         ev[k][1].record(stream)
         interactions += info["interactions"]
+        cycles += info["steps_done"]
     torch.cuda.synchronize()
     dist.barrier()
     clk = clocks.stop()
-    per_step = [a.elapsed_time(b) for a, b in ev]
-    t_ms = sum(per_step)
+    per_chunk = [a.elapsed_time(b) for a, b in ev]
+    t_ms = sum(per_chunk)
     t_max = dist.max(t_ms)
     work = dist.sum(interactions)
     value = work / (t_max * 1e-3)
@@ -274,49 +354,58 @@ def main():
     # ---- pair-kernel time (library timing mode, same stream) ----
     sim.enable_timing(True)
     flush.fill_(1.0)
-    info_t = sim.step(DT, 1.0, args.steps)
+    tsteps = min(cycles, 10)
+    info_t = sim.step(DT, 1.0, tsteps)
     tm = sim.timing()
     sim.enable_timing(False)
-    n_now = info_t["interactions"] / max(1, info_t["steps_done"])
+    inter_t = info_t["interactions"] / max(1, info_t["steps_done"])
     pair_ms = tm["pair_ms"] / max(1, tm["pair_launches"])
-    launches = tm["kernel_launches"]
+    launches = tm["kernel_launches"] / max(1, info_t["steps_done"]) * cycles
 
     # ---- e2e through the C ABI with host buffers ----
     st = sim.state()
-    pinned, keep = {}, []
-    for k, v in st.items():
-        tdt = torch.int32 if v.dtype == np.uint32 else getattr(torch, str(v.dtype))
-        t = torch.empty(len(v) + 4096, dtype=tdt, pin_memory=True)
-        keep.append(t)
-        arr = t.numpy().view(v.dtype)
-        arr[: len(v)] = v
-        pinned[k] = arr
-    host = {k: a[: len(st["x"])] for k, a in pinned.items()}
-    e2e_int, e2e_t, h2d, d2h, e2e_steps = 0, 0.0, 0, 0, max(1, min(args.steps, 5))
-    for k in range(e2e_steps):
+    counts = sim.sim_counts()
+    pinned, keep = pinned_like(torch, st, 4096)
+    n_h = len(st["x"])
+    e2e_int, e2e_t, h2d, d2h, e2e_chunks = 0, 0.0, 0, 0, max(1, min(nchunks, 5))
+    for k in range(e2e_chunks):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        sim.set_bodies(host)
-        info = sim.step(DT, 1.0, 1)
-        host = sim.state(out=pinned)
-        e2e_t += time.perf_counter() - t0
-        e2e_int += info["interactions"]
+        host = {f: a[:n_h] for f, a in pinned.items()}
+        if len(counts) == 1:
+            sim.set_bodies(host)
+        else:
+            parts, o = [], 0
+            for c in counts:
+                parts.append({f: a[o:o + c] for f, a in host.items()})
+                o += c
+            sim.set_collections(parts)
         h2d += sum(a.nbytes for a in host.values())
-        d2h += sum(a.nbytes for a in host.values())
-    e2e = {"value": dist.sum(e2e_int) / dist.max(e2e_t), "unit": UNIT, "h2d_bytes_per_step": int(h2d // e2e_steps),
-           "d2h_bytes_per_step": int(d2h // e2e_steps),
-           "path": "nbg_set_bodies (full state, pinned host) + nbg_step + nbg_get_state (full state)"}
+        info = sim.step(DT, 1.0, chunk)
+        out = sim.state(out=pinned)
+        counts = sim.sim_counts()
+        e2e_t += time.perf_counter() - t0
+        n_h = len(out["x"])
+        d2h += sum(a.nbytes for a in out.values())
+        e2e_int += info["interactions"]
+    e2e = {"value": dist.sum(e2e_int) / dist.max(e2e_t), "unit": UNIT,
+           "h2d_bytes_per_step": int(h2d // (e2e_chunks * chunk)),
+           "d2h_bytes_per_step": int(d2h // (e2e_chunks * chunk)),
+           "path": "nbg_set_bodies / nbg_set_collections (full state, pinned host) + nbg_step + nbg_get_state "
+                   "(full state)" + (f", {chunk} cycles per call" if chunk > 1 else "")}
 
     # ---- FP32 / FP64 peaks, plain FP64 comparison, accuracy ----
     f32, f64, mhz = probe_peaks(local)
     result_extra = {}
-    if not args.no_plain and rank == 0:
+    plain_ok = prec == "mixed" and args.workload != "uniform" and not args.no_plain and rank == 0
+    if plain_ok:
         plain = Simulation("fp64", device=local, capacity=n0 + 4096)
         plain.set_stream(stream.cuda_stream)
-        plain.set_bodies(bodies)
+        load(plain, sims)
         fp = plain.force_pass()
         mixed0 = Simulation("mixed", device=local, capacity=n0 + 4096)
-        mixed0.set_bodies(bodies)
+        mixed0.set_stream(stream.cuda_stream)
+        load(mixed0, sims)
         fm = mixed0.force_pass()
         num = np.sqrt(sum(np.sum((a - b) ** 2) for a, b in zip(fm, fp)))
         den = np.sqrt(sum(np.sum(b ** 2) for b in fp))
@@ -339,34 +428,39 @@ def main():
                                     "reference": "plain FP64 GPU forces (bit-identical to the oracle)"}
         plain.close()
         mixed0.close()
-        ke0, pe0, _ = sim.energy()
-        result_extra["energy"] = {"kinetic": ke0, "potential": pe0}
 
-    achieved = n_now * FLOPS_PER_PAIR / (pair_ms * 1e-3) / 1e12
-    peak = f32 / 1e12
-    traffic = traffic_from_profiles()
+    if prec == "mixed":
+        achieved = inter_t * FLOPS_PER_PAIR / (pair_ms * 1e-3) / 1e12
+        peak, kernel, bound = f32 / 1e12, "k_pair_mixed", "fp32_fma"
+        peak_src = f"FFMA-chain probe on this GPU at {mhz:.0f} MHz (MEASURED_PEAKS.json has no FP32 figure)"
+    else:
+        achieved = inter_t * FLOPS_PER_PAIR / (pair_ms * 1e-3) / 1e12
+        peak, kernel, bound = f64 / 1e12, "k_pair_fp64", "fp64_fma"
+        peak_src = f"DFMA-chain probe on this GPU at {mhz:.0f} MHz (MEASURED_PEAKS.json has no FP64 figure)"
     cpu = None
     if rank == 0 and not args.no_cpu:
-        cpu = cpu_baseline_sample()
+        cpu = cpu_baseline_sample(args.workload, DT)
     sim.close()
     if rank == 0:
         line = {
-            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": t_max / args.steps,
-            "ms_per_step_each": [round(v, 4) for v in per_step], "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "fp32 pair terms, fp64 state",
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": cycles,
+            "warmup": args.warmup, "ms_per_step": t_max / cycles,
+            "ms_per_chunk_each": [round(v, 4) for v in per_chunk], "cycles_per_chunk": chunk,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "fp32 pair terms, fp64 state" if prec == "mixed" else "f64",
             "data": "synthetic",
-            "config": {"workload": f"{WORKLOAD}: {n0} bodies (Plummer a=300 M=1e16 + disk r 400-4000), subsume, "
-                                   f"dt={DT}, mixed precision", "n_bodies": n0, "dt": DT,
-                       "l2": "flushed (512 MB write) before every timed cycle", "parallelism": f"replicas x{ws}"},
+            "config": {"workload": f"{args.workload}: {n0} bodies in {len(sims)} simulation(s) ({desc}), "
+                                   f"dt={DT}, {prec} precision",
+                       "n_bodies": n0, "n_sims": len(sims), "dt": DT,
+                       "l2": "flushed (512 MB write) before every timed cycle"
+                             + (" graph" if chunk > 1 else ""), "parallelism": f"replicas x{ws}"},
             "e2e": e2e,
             "gpu_launches": int(launches),
-            "roofline": {"bound": "fp32_fma", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                         "frac": achieved / peak if peak else None, "traffic": traffic,
-                         "kernel": "k_pair_mixed", "flops_per_pair": FLOPS_PER_PAIR,
-                         "pair_kernel_ms": pair_ms,
-                         "peak_source": f"FFMA-chain probe on this GPU at {mhz:.0f} MHz (MEASURED_PEAKS.json "
-                                        "has no FP32 figure)"},
+            "roofline": {"bound": bound, "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                         "frac": achieved / peak if peak else None,
+                         "traffic": traffic_from_profiles(args.workload) if prec == "mixed" else None,
+                         "kernel": kernel, "flops_per_pair": FLOPS_PER_PAIR, "pair_kernel_ms": pair_ms,
+                         "peak_source": peak_src},
             "peaks": {"fp32_tflops": f32 / 1e12, "fp64_tflops": f64 / 1e12, "probe_sm_mhz": mhz,
                       "hbm_gbs_measured": measured_hbm().get("hbm_gbs")},
             "clocks": clk,

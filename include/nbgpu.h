@@ -168,6 +168,17 @@ int nbg_set_cycle(nbg_ctx *ctx, uint64_t cycle);
 
 /* Replaces the whole collection (NewSimBodyCollection, body_collection.go:45-68). */
 int nbg_set_bodies(nbg_ctx *ctx, const nbg_soa *host, int64_t n);
+/* Replaces the contents with `nsims` independent collections (1..2048) stored
+ * one after another: counts[s] bodies each, concatenated in `host`.  Bodies
+ * of different collections never interact; every collection follows the
+ * cycle exactly as if it were alone (its own event order, compaction, adds),
+ * and one nbg_step advances all of them with the same dt and R.  This is
+ * the batched form: many small simulations share each kernel launch.  No
+ * counterpart in the reference, which runs one collection per process.
+ * nbg_add_bodies and nbg_remove_bodies need a single collection. */
+int nbg_set_collections(nbg_ctx *ctx, int64_t nsims, const int64_t *counts, const nbg_soa *host);
+/* Body count of each collection (up to cap entries); *nsims = collections. */
+int nbg_sim_counts(nbg_ctx *ctx, int64_t *counts, int64_t cap, int64_t *nsims);
 /* Number of bodies in the array (BodyCollection.Count, body_collection.go:203-207). */
 int nbg_count(nbg_ctx *ctx, int64_t *n);
 /* Copies up to `cap` bodies out; *n receives the count. */
@@ -246,7 +257,7 @@ int nbg_energy(nbg_ctx *ctx, double *kinetic, double *potential, double momentum
  * Errors are reported through nbg_last_error(NULL).
  */
 #define NBG_NOALLOC_MAX_BODIES 65536
-#define NBG_NOALLOC_BYTES 9472256
+#define NBG_NOALLOC_BYTES 9472768
 int nbg_forces_mixed_noalloc(const double *x, const double *y, const double *z, const double *mass,
                              const double *radius, const uint32_t *flags, int64_t n, double *fx, double *fy,
                              double *fz, void *stream);
@@ -270,6 +281,7 @@ int nbg_get_timing(nbg_ctx *ctx, nbg_timing *t);
 #define NBG_OPT_GRAPH 2      /* 0 = launch each cycle directly, 1 = CUDA graph */
 #define NBG_OPT_EV_CAP 3     /* event-list capacity (rounded up to a power of two) */
 #define NBG_OPT_FRAG_CAP 4   /* fragments one cycle may emit */
+#define NBG_OPT_GRAPH_CYCLES 6 /* cycles captured in one CUDA graph (default 1) */
 #define NBG_OPT_NEAR_PPM 5   /* mixed: pairs closer than (value * 1e-6) x the i-tile's
                                 extent around its origin are computed in FP64
                                 (default 70000) */

@@ -40,6 +40,7 @@ OPT_GRAPH = 2
 OPT_EV_CAP = 3
 OPT_FRAG_CAP = 4
 OPT_NEAR_PPM = 5
+OPT_GRAPH_CYCLES = 6
 
 _pd = C.POINTER(C.c_double)
 _pi64 = C.POINTER(C.c_int64)
@@ -162,6 +163,8 @@ def declare(lib):
         "nbg_set_cycle": (C.c_int, [P, C.c_uint64]),
         "nbg_set_bodies": (C.c_int, [P, C.POINTER(NbgSoa), C.c_int64]),
         "nbg_count": (C.c_int, [P, _pi64]),
+        "nbg_set_collections": (C.c_int, [P, C.c_int64, _pi64, C.POINTER(NbgSoa)]),
+        "nbg_sim_counts": (C.c_int, [P, _pi64, C.c_int64, _pi64]),
         "nbg_get_state": (C.c_int, [P, C.POINTER(NbgSoa), C.c_int64, _pi64]),
         "nbg_add_bodies": (C.c_int, [P, C.POINTER(NbgSoa), C.c_int64, _pi64]),
         "nbg_apply_edits": (C.c_int, [P, C.POINTER(NbgEdit), C.c_int64, _pi32]),

@@ -122,6 +122,27 @@ class Simulation:
         self._check(self.lib.nbg_set_bodies(self.ctx, C.byref(soa), n))
         del keep
 
+    def set_collections(self, sims):
+        """Several independent collections in one context (a list of body
+        dicts); one step advances all of them, and they never interact."""
+        counts = np.array([len(b["x"]) for b in sims], dtype=np.int64)
+        keys = set(sims[0])
+        for b in sims[1:]:
+            keys &= set(b)
+        cat = {k: np.concatenate([np.asarray(b[k]) for b in sims]) for k in keys}
+        soa, keep = A.soa_from_arrays(cat)
+        self._check(self.lib.nbg_set_collections(self.ctx, len(sims), counts.ctypes.data_as(C.POINTER(C.c_int64)),
+                                                 C.byref(soa)))
+        del keep
+
+    def sim_counts(self):
+        ns = C.c_int64()
+        self._check(self.lib.nbg_sim_counts(self.ctx, None, 0, C.byref(ns)))
+        out = np.zeros(max(1, ns.value), dtype=np.int64)
+        self._check(self.lib.nbg_sim_counts(self.ctx, out.ctypes.data_as(C.POINTER(C.c_int64)), ns.value,
+                                            C.byref(ns)))
+        return out[:ns.value]
+
     def count(self):
         v = C.c_int64()
         self._check(self.lib.nbg_count(self.ctx, C.byref(v)))

@@ -51,23 +51,73 @@ __device__ static ll block_excl_scan(ll v, ll *total)
     return excl;
 }
 
+/* Exclusive scan of f(0..ns-1) into out[0..ns-1], out[ns] = total, by one
+ * block of NBG_SCAN_BLOCK threads; returns the total to every thread. */
+template <typename F>
+__device__ static ll block_scan_array(int ns, F f, ll *out)
+{
+    ll carry = 0;
+    for (int s0 = 0; s0 < ns; s0 += NBG_SCAN_BLOCK) {
+        const int s = s0 + (int)threadIdx.x;
+        const ll v = s < ns ? f(s) : 0;
+        ll tot;
+        const ll ex = block_excl_scan(v, &tot);
+        if (s < ns) out[s] = carry + ex;
+        carry += tot;
+    }
+    if (threadIdx.x == 0) out[ns] = carry;
+    __syncthreads();
+    return carry;
+}
+
 /* ------------------------------------------------------------------------ */
 /* cycle start                                                              */
 /* ------------------------------------------------------------------------ */
 
-__global__ void k_begin(DevCtl *ctl)
+/* Per-cycle resets and the work layout of every sim: 64-body tiles of the
+ * plain kernel, 512-body i-tiles, j-range splits and work items of the
+ * mixed kernel, and the interaction count.  One block. */
+__global__ void __launch_bounds__(NBG_SCAN_BLOCK) k_begin(DevCtl *ctl, SimSegs seg, int split_cap, int slots)
 {
-    if (threadIdx.x != 0 || ctl->error) return;
-    ll n = ctl->n;
-    ctl->n_before = n;
-    ctl->ev_count = 0;
-    ctl->frag_total = 0;
-    ctl->n_keep = n;
-    ctl->rend_n = 0;
-    ctl->last_ev_n = 0;
-    ctl->rmax_bits = 0;
-    ctl->xmax_bits = 0;
-    ctl->m_scale = 0.0;
+    if (ctl->error) return;
+    const int ns = seg.nsims;
+    const ll *off = seg.off;
+    for (int s = threadIdx.x; s < ns; s += NBG_SCAN_BLOCK) {
+        seg.keep[s] = 0;
+        seg.frag[s] = 0;
+        seg.xmax_bits[s] = 0;
+    }
+    block_scan_array(ns, [&](int s) { return (off[s + 1] - off[s] + 63) / 64; }, seg.tile_off);
+    const ll mtiles = block_scan_array(
+        ns, [&](int s) { return (off[s + 1] - off[s] + NBG_MIX_ITILE - 1) / NBG_MIX_ITILE; }, seg.mtile_off);
+    ll S = mtiles > 0 ? (8ll * slots + mtiles - 1) / mtiles : 1;
+    if (S > split_cap) S = split_cap;
+    if (S < 1) S = 1;
+    for (int s = threadIdx.x; s < ns; s += NBG_SCAN_BLOCK) {
+        const ll jt = (off[s + 1] - off[s] + NBG_MIX_JT - 1) / NBG_MIX_JT;
+        seg.splits[s] = (int)(jt < S ? jt : S);
+    }
+    __syncthreads();
+    block_scan_array(
+        ns, [&](int s) { return (seg.mtile_off[s + 1] - seg.mtile_off[s]) * (ll)seg.splits[s]; }, seg.item_off);
+    /* interactions: sum of n_s (n_s - 1), reusing the keep_start array */
+    const ll inter = block_scan_array(
+        ns, [&](int s) { const ll m = off[s + 1] - off[s]; return m * (m > 0 ? m - 1 : 0); }, seg.keep_start);
+    if (threadIdx.x == 0) {
+        ll n = ctl->n;
+        ctl->n_before = n;
+        ctl->ev_count = 0;
+        ctl->frag_total = 0;
+        ctl->n_keep = n;
+        ctl->rend_n = 0;
+        ctl->last_ev_n = 0;
+        ctl->rmax_bits = 0;
+        ctl->xmax_bits = 0;
+        ctl->m_scale = 0.0;
+        ctl->splits = (int)S;
+        ctl->work_next = 0;
+        ctl->cycle_interactions = inter;
+    }
 }
 
 /* Fragments body k emits this cycle: Compute calls fragment() for a body that
@@ -82,7 +132,18 @@ __device__ static ll frag_emit_count(const BodyArrays &A, ll k)
     return c < NBG_MAX_FRAGS_PER_CYCLE + 1 ? c : NBG_MAX_FRAGS_PER_CYCLE + 1;
 }
 
-__global__ void __launch_bounds__(NBG_SCAN_BLOCK) k_frag_blocksum(BodyArrays A, DevCtl *ctl, ll *blk_sum)
+/* Adds `v` to counter[sim] once per group of lanes that share `sim` (sim < 0:
+ * nothing).  Every lane of the warp must call it. */
+__device__ static void warp_add_per_sim(ll *counter, int sim, unsigned v)
+{
+    const unsigned peers = __match_any_sync(FULL_MASK, sim);
+    const unsigned t = __reduce_add_sync(peers, v);
+    if (sim >= 0 && (int)(threadIdx.x & 31) == __ffs(peers) - 1 && t != 0)
+        atomicAdd((unsigned long long *)&counter[sim], (ull)t);
+}
+
+__global__ void __launch_bounds__(NBG_SCAN_BLOCK) k_frag_blocksum(BodyArrays A, DevCtl *ctl, SimSegs seg,
+                                                                  ll *blk_sum)
 {
     if (ctl->error) return;
     const ll n = ctl->n;
@@ -91,14 +152,19 @@ __global__ void __launch_bounds__(NBG_SCAN_BLOCK) k_frag_blocksum(BodyArrays A, 
     ll s = 0;
     for (int q = 0; q < NBG_SCAN_ITEMS; q++) {
         ll k = base + (ll)threadIdx.x * NBG_SCAN_ITEMS + q;
-        if (k < n) s += frag_emit_count(A, k);
+        if (k < n) {
+            const ll c = frag_emit_count(A, k);
+            s += c;
+            if (c > 0) atomicAdd((unsigned long long *)&seg.frag[nbg_sim_of(seg.off, seg.nsims, k)], (ull)c);
+        }
     }
     ll tot;
     block_excl_scan(s, &tot);
     if (threadIdx.x == 0) blk_sum[blockIdx.x] = tot;
 }
 
-__global__ void __launch_bounds__(NBG_SCAN_BLOCK) k_keep_blocksum(BodyArrays A, DevCtl *ctl, ll *blk_sum)
+__global__ void __launch_bounds__(NBG_SCAN_BLOCK) k_keep_blocksum(BodyArrays A, DevCtl *ctl, SimSegs seg,
+                                                                  ll *blk_sum)
 {
     if (ctl->error) return;
     const ll n = ctl->n;
@@ -106,18 +172,23 @@ __global__ void __launch_bounds__(NBG_SCAN_BLOCK) k_keep_blocksum(BodyArrays A, 
     if (base >= n) return;
     ll s = 0;
     for (int q = 0; q < NBG_SCAN_ITEMS; q++) {
-        ll k = base + (ll)threadIdx.x * NBG_SCAN_ITEMS + q;
-        if (k < n) s += (A.flags[k] & NBG_F_EXISTS) ? 1 : 0;
+        /* consecutive lanes take consecutive bodies so a warp mostly sees one sim */
+        const ll k = base + (ll)q * NBG_SCAN_BLOCK + threadIdx.x;
+        const bool keep = k < n && (A.flags[k] & NBG_F_EXISTS);
+        s += keep ? 1 : 0;
+        warp_add_per_sim(seg.keep, keep ? nbg_sim_of(seg.off, seg.nsims, k) : -1, keep ? 1 : 0);
     }
     ll tot;
     block_excl_scan(s, &tot);
     if (threadIdx.x == 0) blk_sum[blockIdx.x] = tot;
 }
 
-/* Single-block exclusive scan of the per-block sums.  mode 0: fragment
- * counts (checks capacities); mode 1: surviving bodies. */
-__global__ void __launch_bounds__(NBG_SCAN_BLOCK) k_scan_blocks(DevCtl *ctl, const ll *blk_sum, ll *blk_off, int mode,
-                                                                ll cap, ll frag_cap)
+/* Single-block exclusive scan of the per-block sums, then the per-sim
+ * layout.  mode 0: fragment counts, fragment and host-add starts per sim,
+ * capacity checks.  mode 1: surviving bodies, keep starts and the layout
+ * after Cycle: sim s gets [kept bodies][its fragments][its host adds]. */
+__global__ void __launch_bounds__(NBG_SCAN_BLOCK) k_scan_blocks(DevCtl *ctl, SimSegs seg, const ll *blk_sum,
+                                                                ll *blk_off, int mode, ll cap, ll frag_cap)
 {
     if (ctl->error) return;
     const ll n = ctl->n;
@@ -131,10 +202,14 @@ __global__ void __launch_bounds__(NBG_SCAN_BLOCK) k_scan_blocks(DevCtl *ctl, con
         if (b < nb) blk_off[b] = carry + ex;
         carry += tot;
     }
-    if (threadIdx.x == 0) {
-        if (mode == 0) {
+    const int ns = seg.nsims;
+    if (mode == 0) {
+        block_scan_array(ns, [&](int s) { return seg.frag[s]; }, seg.frag_start);
+        const ll hadds = block_scan_array(ns, [&](int s) { return seg.hadd[s]; }, seg.hadd_start);
+        if (threadIdx.x == 0) {
             ctl->frag_total = carry;
-            ll need = n + carry + ctl->n_host_adds;
+            ctl->n_host_adds = hadds;
+            ll need = n + carry + hadds;
             if (carry > frag_cap) {
                 ctl->error = NBG_E_OVERFLOW;
                 ctl->error_what = 3;
@@ -144,9 +219,11 @@ __global__ void __launch_bounds__(NBG_SCAN_BLOCK) k_scan_blocks(DevCtl *ctl, con
                 ctl->error_what = 1;
                 ctl->error_need = need;
             }
-        } else {
-            ctl->n_keep = carry;
         }
+    } else {
+        block_scan_array(ns, [&](int s) { return seg.keep[s]; }, seg.keep_start);
+        block_scan_array(ns, [&](int s) { return seg.keep[s] + seg.frag[s] + seg.hadd[s]; }, seg.new_off);
+        if (threadIdx.x == 0) ctl->n_keep = carry;
     }
 }
 
@@ -183,14 +260,18 @@ __device__ static void emit_event(DevCtl *ctl, ull *keys, ll cap, ll i, ll j, in
  * so the result is bit-identical to the sequential loop.  The same dist
  * decides Collided (body.go:192-208); hits are appended to the event list.
  */
-__global__ void __launch_bounds__(P64_BLOCK) k_pair_fp64(BodyArrays A, DevCtl *ctl, ull *ev_keys, ll ev_cap)
+__global__ void __launch_bounds__(P64_BLOCK) k_pair_fp64(BodyArrays A, DevCtl *ctl, SimSegs seg, ull *ev_keys,
+                                                          ll ev_cap)
 {
     __shared__ double sx[P64_BLOCK], sy[P64_BLOCK], sz[P64_BLOCK], sm[P64_BLOCK], sr[P64_BLOCK];
     __shared__ unsigned sf[P64_BLOCK];
     if (ctl->error) return;
-    const ll n = ctl->n;
-    for (ll i0 = (ll)blockIdx.x * P64_BLOCK; i0 < n; i0 += (ll)gridDim.x * P64_BLOCK) {
-        const ll i = i0 + threadIdx.x;
+    const ll ntiles = seg.tile_off[seg.nsims];
+    for (ll T = blockIdx.x; T < ntiles; T += gridDim.x) {
+        /* tile T of sim s: i in [s0 + 64 t, ...), j over the sim [s0, s1) */
+        const int sim = nbg_sim_of(seg.tile_off, seg.nsims, T);
+        const ll s0 = seg.off[sim], n = seg.off[sim + 1];
+        const ll i = s0 + (T - seg.tile_off[sim]) * P64_BLOCK + threadIdx.x;
         const bool valid = i < n;
         double xi = 0, yi = 0, zi = 0, mi = 0, ri = 0;
         unsigned fi = 0;
@@ -207,7 +288,7 @@ __global__ void __launch_bounds__(P64_BLOCK) k_pair_fp64(BodyArrays A, DevCtl *c
         const unsigned bi = NBG_BEHAVIOR(fi);
         const double gmi = NBG_G * mi;
         double fx = 0.0, fy = 0.0, fz = 0.0;
-        for (ll j0 = 0; j0 < n; j0 += P64_BLOCK) {
+        for (ll j0 = s0; j0 < n; j0 += P64_BLOCK) {
             __syncthreads();
             const ll jl = j0 + threadIdx.x;
             if (jl < n) {
@@ -649,7 +730,10 @@ __device__ static bool cycle_changes(const DevCtl *ctl)
     return ctl->n_keep != ctl->n || ctl->frag_total > 0 || ctl->n_host_adds > 0;
 }
 
-__global__ void __launch_bounds__(NBG_SCAN_BLOCK) k_compact(BodyArrays A, BodyArrays Bt, DevCtl *ctl, const ll *blk_off)
+/* Kept body k of sim s goes to new_off[s] + (its rank among kept bodies -
+ * keep_start[s]): the order inside each sim is preserved. */
+__global__ void __launch_bounds__(NBG_SCAN_BLOCK) k_compact(BodyArrays A, BodyArrays Bt, DevCtl *ctl, SimSegs seg,
+                                                            const ll *blk_off)
 {
     if (ctl->error || !cycle_changes(ctl)) return;
     const ll n = ctl->n;
@@ -663,47 +747,63 @@ __global__ void __launch_bounds__(NBG_SCAN_BLOCK) k_compact(BodyArrays A, BodyAr
         s += c[q];
     }
     ll tot;
-    ll off = block_excl_scan(s, &tot) + blk_off[blockIdx.x];
+    ll rank = block_excl_scan(s, &tot) + blk_off[blockIdx.x];
     for (int q = 0; q < NBG_SCAN_ITEMS; q++) {
         ll k = base + (ll)threadIdx.x * NBG_SCAN_ITEMS + q;
-        if (c[q]) copy_body(A, k, Bt, off++);
+        if (c[q]) {
+            const int sim = nbg_sim_of(seg.off, seg.nsims, k);
+            copy_body(A, k, Bt, seg.new_off[sim] + (rank - seg.keep_start[sim]));
+            rank++;
+        }
     }
 }
 
-/* Appends the adds newest first (fragments of this cycle, then host adds),
- * each with r = R. */
-__global__ void k_append_adds(BodyArrays Bt, BodyArrays F, BodyArrays H, DevCtl *ctl)
+/* Appends each sim's adds after its kept bodies, newest first (the sim's
+ * fragments of this cycle, then its host adds), each with r = R. */
+__global__ void k_append_adds(BodyArrays Bt, BodyArrays F, BodyArrays H, DevCtl *ctl, SimSegs seg)
 {
     if (ctl->error || !cycle_changes(ctl)) return;
-    const ll nk = ctl->n_keep, nf = ctl->frag_total, nh = ctl->n_host_adds;
+    const ll nf = ctl->frag_total, nh = ctl->n_host_adds;
     const double R = ctl->R;
+    const int ns = seg.nsims;
     for (ll k = (ll)blockIdx.x * blockDim.x + threadIdx.x; k < nf + nh; k += (ll)gridDim.x * blockDim.x) {
-        ll d = nk + k;
+        ll d;
         if (k < nf) {
-            copy_body(F, nf - 1 - k, Bt, d);
+            const int s = nbg_sim_of(seg.frag_start, ns, k);
+            d = seg.new_off[s] + seg.keep[s] + (seg.frag_start[s + 1] - 1 - k);
+            copy_body(F, k, Bt, d);
         } else {
-            ll h = k - nf;
-            copy_body(H, nh - 1 - h, Bt, d);
+            const ll h = k - nf;
+            const int s = nbg_sim_of(seg.hadd_start, ns, h);
+            d = seg.new_off[s] + seg.keep[s] + seg.frag[s] + (seg.hadd_start[s + 1] - 1 - h);
+            copy_body(H, h, Bt, d);
         }
         Bt.rest[d] = R;
     }
 }
 
-__global__ void k_copy_back(BodyArrays A, BodyArrays Bt, DevCtl *ctl)
+__global__ void k_copy_back(BodyArrays A, BodyArrays Bt, DevCtl *ctl, SimSegs seg)
 {
     if (ctl->error || !cycle_changes(ctl)) return;
-    const ll total = ctl->n_keep + ctl->frag_total + ctl->n_host_adds;
+    const ll total = seg.new_off[seg.nsims];
     for (ll k = (ll)blockIdx.x * blockDim.x + threadIdx.x; k < total; k += (ll)gridDim.x * blockDim.x)
         copy_body(Bt, k, A, k);
 }
 
-__global__ void k_end(DevCtl *ctl)
+__global__ void __launch_bounds__(NBG_SCAN_BLOCK) k_end(DevCtl *ctl, SimSegs seg)
 {
-    if (threadIdx.x != 0 || ctl->error) return;
+    if (ctl->error) return;
+    const int ns = seg.nsims;
+    const bool changed = cycle_changes(ctl);
+    for (int s = threadIdx.x; s <= ns; s += NBG_SCAN_BLOCK) {
+        if (changed) seg.off[s] = seg.new_off[s];
+        if (s < ns) seg.hadd[s] = 0;
+    }
+    if (threadIdx.x != 0) return;
     const ll n = ctl->n;
     ctl->rend_n = n;
     ctl->acc_removed += n - ctl->n_keep;
-    ctl->acc_interactions += n * (n > 0 ? n - 1 : 0);
+    ctl->acc_interactions += ctl->cycle_interactions;
     ctl->n = ctl->n_keep + ctl->frag_total + ctl->n_host_adds;
     ctl->n_host_adds = 0;
     ctl->cycle += 1;
@@ -838,15 +938,14 @@ static int flat_grid(ll cap)
 
 void nbg_launch_begin(const CycleBufs &cb, DevCtl *ctl, cudaStream_t st)
 {
-    (void)cb;
-    k_begin<<<1, 32, 0, st>>>(ctl);
+    k_begin<<<1, NBG_SCAN_BLOCK, 0, st>>>(ctl, cb.seg, cb.split_cap, cb.slots);
 }
 
 void nbg_launch_frag_count(const CycleBufs &cb, DevCtl *ctl, cudaStream_t st)
 {
     int g = scan_grid(cb.cap);
-    k_frag_blocksum<<<g, NBG_SCAN_BLOCK, 0, st>>>(cb.a, ctl, cb.blk_sum);
-    k_scan_blocks<<<1, NBG_SCAN_BLOCK, 0, st>>>(ctl, cb.blk_sum, cb.blk_off, 0, cb.cap, cb.frag_cap);
+    k_frag_blocksum<<<g, NBG_SCAN_BLOCK, 0, st>>>(cb.a, ctl, cb.seg, cb.blk_sum);
+    k_scan_blocks<<<1, NBG_SCAN_BLOCK, 0, st>>>(ctl, cb.seg, cb.blk_sum, cb.blk_off, 0, cb.cap, cb.frag_cap);
 }
 
 int nbg_pair_fp64_grid(ll cap)
@@ -857,7 +956,7 @@ int nbg_pair_fp64_grid(ll cap)
 
 void nbg_launch_pair_fp64(const CycleBufs &cb, DevCtl *ctl, cudaStream_t st)
 {
-    k_pair_fp64<<<nbg_pair_fp64_grid(cb.cap), P64_BLOCK, 0, st>>>(cb.a, ctl, cb.ev_keys, cb.ev_cap);
+    k_pair_fp64<<<nbg_pair_fp64_grid(cb.cap), P64_BLOCK, 0, st>>>(cb.a, ctl, cb.seg, cb.ev_keys, cb.ev_cap);
 }
 
 /* everything after the pair kernel: order events, emit fragments, resolve,
@@ -869,12 +968,12 @@ void nbg_launch_after_pair(const CycleBufs &cb, DevCtl *ctl, cudaStream_t st)
     k_frag_emit<<<sg, NBG_SCAN_BLOCK, 0, st>>>(cb.a, cb.frags, ctl, cb.blk_off);
     k_resolve<<<1, 32, 0, st>>>(cb.a, ctl, cb.ev_keys, cb.ev_out);
     k_integrate<<<flat_grid(cb.cap), 256, 0, st>>>(cb.a, ctl, cb.rend);
-    k_keep_blocksum<<<sg, NBG_SCAN_BLOCK, 0, st>>>(cb.a, ctl, cb.blk_sum);
-    k_scan_blocks<<<1, NBG_SCAN_BLOCK, 0, st>>>(ctl, cb.blk_sum, cb.blk_off, 1, cb.cap, cb.frag_cap);
-    k_compact<<<sg, NBG_SCAN_BLOCK, 0, st>>>(cb.a, cb.b, ctl, cb.blk_off);
-    k_append_adds<<<flat_grid(cb.frag_cap + cb.adds_cap), 256, 0, st>>>(cb.b, cb.frags, cb.adds, ctl);
-    k_copy_back<<<flat_grid(cb.cap), 256, 0, st>>>(cb.a, cb.b, ctl);
-    k_end<<<1, 32, 0, st>>>(ctl);
+    k_keep_blocksum<<<sg, NBG_SCAN_BLOCK, 0, st>>>(cb.a, ctl, cb.seg, cb.blk_sum);
+    k_scan_blocks<<<1, NBG_SCAN_BLOCK, 0, st>>>(ctl, cb.seg, cb.blk_sum, cb.blk_off, 1, cb.cap, cb.frag_cap);
+    k_compact<<<sg, NBG_SCAN_BLOCK, 0, st>>>(cb.a, cb.b, ctl, cb.seg, cb.blk_off);
+    k_append_adds<<<flat_grid(cb.frag_cap + cb.adds_cap), 256, 0, st>>>(cb.b, cb.frags, cb.adds, ctl, cb.seg);
+    k_copy_back<<<flat_grid(cb.cap), 256, 0, st>>>(cb.a, cb.b, ctl, cb.seg);
+    k_end<<<1, NBG_SCAN_BLOCK, 0, st>>>(ctl, cb.seg);
 }
 
 void nbg_launch_remove(const CycleBufs &cb, DevCtl *ctl, ll count, ll *removed_dev, cudaStream_t st)

@@ -62,18 +62,33 @@ __device__ __forceinline__ bool is_special(double x, double y, double z, double 
 
 /* ---- per-cycle reductions: r_max, |x|_max, m_scale, splits ---------------- */
 
-__global__ void k_mix_reduce(BodyArrays A, DevCtl *ctl, int split_cap, int slots)
+__global__ void k_mix_reduce(BodyArrays A, DevCtl *ctl, SimSegs seg)
 {
     if (ctl->error) return;
     const ll n = ctl->n;
     float rmax = 0.f, xmax = 0.f;
     double mmax = 0.0;
-    for (ll k = (ll)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (ll)gridDim.x * blockDim.x) {
-        const double x = A.x[k], y = A.y[k], z = A.z[k], r = A.rad[k];
-        if (is_special(x, y, z, r)) continue;
-        rmax = fmaxf(rmax, (float)fmax(r, 0.0));
-        xmax = fmaxf(xmax, (float)fmax(fabs(x), fmax(fabs(y), fabs(z))));
-        if ((A.flags[k] & NBG_LIVE_MASK) == NBG_F_EXISTS) mmax = fmax(mmax, fabs(A.m[k]));
+    const ll stride = (ll)gridDim.x * blockDim.x;
+    /* warp-uniform trip count: every lane takes part in the per-sim reduction */
+    for (ll base = (ll)blockIdx.x * blockDim.x; base < n; base += stride) {
+        const ll k = base + threadIdx.x;
+        float xk = 0.f;
+        int sim = -1;
+        if (k < n) {
+            const double x = A.x[k], y = A.y[k], z = A.z[k], r = A.rad[k];
+            if (!is_special(x, y, z, r)) {
+                rmax = fmaxf(rmax, (float)fmax(r, 0.0));
+                xk = (float)fmax(fabs(x), fmax(fabs(y), fabs(z)));
+                xmax = fmaxf(xmax, xk);
+                if ((A.flags[k] & NBG_LIVE_MASK) == NBG_F_EXISTS) mmax = fmax(mmax, fabs(A.m[k]));
+                sim = nbg_sim_of(seg.off, seg.nsims, k);
+            }
+        }
+        if (seg.nsims > 1) {
+            const unsigned peers = __match_any_sync(FULL_MASK, sim);
+            const unsigned mx = __reduce_max_sync(peers, __float_as_uint(xk * (1.0f + 0x1p-20f)));
+            if (sim >= 0 && (int)(threadIdx.x & 31) == __ffs(peers) - 1) atomicMax(&seg.xmax_bits[sim], mx);
+        }
     }
     for (int o = 16; o > 0; o >>= 1) {
         rmax = fmaxf(rmax, __shfl_xor_sync(FULL_MASK, rmax, o));
@@ -85,17 +100,7 @@ __global__ void k_mix_reduce(BodyArrays A, DevCtl *ctl, int split_cap, int slots
         atomicMax(&ctl->rmax_bits, __float_as_uint(rmax * (1.0f + 0x1p-20f)));
         atomicMax(&ctl->xmax_bits, __float_as_uint(xmax * (1.0f + 0x1p-20f)));
         atomicMax((unsigned long long *)&ctl->m_scale, (ull)__double_as_longlong(mmax));
-    }
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
-        /* j-range splits: enough items for ~8 per resident CTA */
-        const ll ntiles = (n + NBG_MIX_ITILE - 1) / NBG_MIX_ITILE;
-        const ll jtiles = (n + NBG_MIX_JT - 1) / NBG_MIX_JT;
-        ll s = ntiles > 0 ? (8ll * slots + ntiles - 1) / ntiles : 1;
-        if (s > split_cap) s = split_cap;
-        if (s > jtiles) s = jtiles;
-        if (s < 1) s = 1;
-        ctl->splits = (int)s;
-        ctl->work_next = 0;
+        if (seg.nsims == 1) atomicMax(&seg.xmax_bits[0], __float_as_uint(xmax * (1.0f + 0x1p-20f)));
     }
 }
 
@@ -129,14 +134,16 @@ __global__ void k_mix_pack(BodyArrays A, DevCtl *ctl, const unsigned *perm, floa
 __device__ __forceinline__ bool packed_special(const float4 &lo) { return lo.x != lo.x; }
 
 /* origin of each i-tile: centre of the bounding box of its bodies */
-__global__ void __launch_bounds__(NBG_MIX_BLOCK) k_mix_tiles(DevCtl *ctl, const float4 *jhi, const float4 *jlo, float4 *tile_c)
+__global__ void __launch_bounds__(NBG_MIX_BLOCK) k_mix_tiles(DevCtl *ctl, SimSegs seg, const float4 *jhi,
+                                                             const float4 *jlo, float4 *tile_c)
 {
     __shared__ float red[6][NBG_MIX_BLOCK / 32];
     if (ctl->error) return;
-    const ll n = ctl->n;
-    const ll tile = blockIdx.x;
-    const ll base = tile * NBG_MIX_ITILE;
-    if (base >= n) return;
+    const ll ntiles = seg.mtile_off[seg.nsims];
+    for (ll tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    const int sim = nbg_sim_of(seg.mtile_off, seg.nsims, tile);
+    const ll n = seg.off[sim + 1];
+    const ll base = seg.off[sim] + (tile - seg.mtile_off[sim]) * NBG_MIX_ITILE;
     float lo[3] = {3e38f, 3e38f, 3e38f}, hi[3] = {-3e38f, -3e38f, -3e38f};
     for (int k = 0; k < NBG_MIX_K; k++) {
         ll p = base + (ll)k * NBG_MIX_BLOCK + threadIdx.x;
@@ -173,6 +180,8 @@ __global__ void __launch_bounds__(NBG_MIX_BLOCK) k_mix_tiles(DevCtl *ctl, const 
             c3[c] = (l <= h) ? 0.5f * l + 0.5f * h : 0.f;
         }
         tile_c[tile] = make_float4(c3[0], c3[1], c3[2], 0.f);
+    }
+    __syncthreads(); /* red[] is rewritten by the next tile */
     }
 }
 
@@ -237,20 +246,17 @@ __device__ __forceinline__ void fold64(float &hi, float &lo, double v)
  * event keys. */
 template <int K>
 __global__ void __launch_bounds__(NBG_MIX_BLOCK, 3)
-k_pair_mixed(BodyArrays A, DevCtl *ctl, const float4 *__restrict__ jhi, const float4 *__restrict__ jlo,
+k_pair_mixed(BodyArrays A, DevCtl *ctl, SimSegs seg, const float4 *__restrict__ jhi, const float4 *__restrict__ jlo,
              const float4 *__restrict__ tile_c, const unsigned *__restrict__ perm, double *__restrict__ part,
              ll part_stride, ull *ev_keys, ll ev_cap)
 {
     constexpr int JP = NBG_MIX_JT / 2; /* j pairs per tile */
     constexpr int ITILE = NBG_MIX_BLOCK * K;
+    static_assert(ITILE == NBG_MIX_ITILE, "tile layout of k_begin");
     __shared__ float4 sA[JP], sB[JP];
     __shared__ ll s_item;
     if (ctl->error) return;
-    const ll n = ctl->n;
-    const int S = ctl->splits;
-    const ll ntiles = (n + ITILE - 1) / ITILE;
-    const ll items = ntiles * S;
-    const ll jc = (((n + S - 1) / S) + NBG_MIX_JT - 1) / NBG_MIX_JT * NBG_MIX_JT;
+    const ll items = seg.item_off[seg.nsims];
     double ms = ctl->m_scale;
     if (!(ms > 0.0)) ms = 1.0;
     const double inv_ms = 1.0 / ms;
@@ -265,16 +271,23 @@ k_pair_mixed(BodyArrays A, DevCtl *ctl, const float4 *__restrict__ jhi, const fl
         const ll item = s_item;
         __syncthreads();
         if (item >= items) break;
-        const ll tile = item / S;
-        const int split = (int)(item % S);
-        const float4 c = tile_c[tile];
+        /* item -> sim, i-tile within the sim, j-range split */
+        const int sim = nbg_sim_of(seg.item_off, seg.nsims, item);
+        const int S = seg.splits[sim];
+        const ll local = item - seg.item_off[sim];
+        const ll t = local / S;
+        const int split = (int)(local % S);
+        const ll s0 = seg.off[sim], n = seg.off[sim + 1];
+        const ll jc = (((n - s0 + S - 1) / S) + NBG_MIX_JT - 1) / NBG_MIX_JT * NBG_MIX_JT;
+        const ll ibase = s0 + t * ITILE;
+        const float4 c = tile_c[seg.mtile_off[sim] + t];
 
         float2 nx[K], ny[K], nz[K];
         float thr[K];
         float shx[K], slx[K], shy[K], sly[K], shz[K], slz[K];
 #pragma unroll
         for (int k = 0; k < K; k++) {
-            const ll p = tile * ITILE + (ll)k * NBG_MIX_BLOCK + tid;
+            const ll p = ibase + (ll)k * NBG_MIX_BLOCK + tid;
             float xr = 0.f, yr = 0.f, zr = 0.f, t = -1.f;
             if (p < n) {
                 const float4 h = jhi[p], l = jlo[p];
@@ -299,7 +312,7 @@ k_pair_mixed(BodyArrays A, DevCtl *ctl, const float4 *__restrict__ jhi, const fl
             shx[k] = slx[k] = shy[k] = sly[k] = shz[k] = slz[k] = 0.f;
         }
 
-        const ll jb = (ll)split * jc;
+        const ll jb = s0 + (ll)split * jc;
         const ll je = jb + jc < n ? jb + jc : n;
         for (ll jt = jb; jt < je; jt += NBG_MIX_JT) {
             __syncthreads();
@@ -362,7 +375,7 @@ k_pair_mixed(BodyArrays A, DevCtl *ctl, const float4 *__restrict__ jhi, const fl
             for (int k = 0; k < K; k++) {
                 if (mn[k] < thr[k]) {
                     /* slow path: this tile holds a near or overlapping pair for i */
-                    const ll p = tile * ITILE + (ll)k * NBG_MIX_BLOCK + tid;
+                    const ll p = ibase + (ll)k * NBG_MIX_BLOCK + tid;
                     const ll i = perm[p];
                     const float4 hi_i = jhi[p], lo_i = jlo[p];
                     float tx = 0.f, ty = 0.f, tz = 0.f;
@@ -416,7 +429,7 @@ k_pair_mixed(BodyArrays A, DevCtl *ctl, const float4 *__restrict__ jhi, const fl
         }
 #pragma unroll
         for (int k = 0; k < K; k++) {
-            const ll p = tile * ITILE + (ll)k * NBG_MIX_BLOCK + tid;
+            const ll p = ibase + (ll)k * NBG_MIX_BLOCK + tid;
             if (p < n) {
                 double *o = part + (ll)split * 3 * part_stride;
                 o[p] = (double)shx[k] + (double)slx[k];
@@ -429,14 +442,15 @@ k_pair_mixed(BodyArrays A, DevCtl *ctl, const float4 *__restrict__ jhi, const fl
 
 /* f = (G m_i m_scale) * sum over j-range slots, in slot order, written to
  * body perm[p]. */
-__global__ void k_mix_out(BodyArrays A, DevCtl *ctl, const unsigned *perm, const double *part, ll part_stride)
+__global__ void k_mix_out(BodyArrays A, DevCtl *ctl, SimSegs seg, const unsigned *perm, const double *part,
+                          ll part_stride)
 {
     if (ctl->error) return;
     const ll n = ctl->n;
-    const int S = ctl->splits;
     double ms = ctl->m_scale;
     if (!(ms > 0.0)) ms = 1.0;
     for (ll p = (ll)blockIdx.x * blockDim.x + threadIdx.x; p < n; p += (ll)gridDim.x * blockDim.x) {
+        const int S = seg.splits[nbg_sim_of(seg.off, seg.nsims, p)];
         const ll i = perm[p];
         const unsigned f = A.flags[i];
         if ((f & NBG_LIVE_MASK) != NBG_F_EXISTS) continue;
@@ -489,20 +503,21 @@ static int flat_grid(ll cap)
 void nbg_launch_mixed_prep(const CycleBufs &cb, DevCtl *ctl, cudaStream_t st)
 {
     const int fg = flat_grid(cb.cap);
-    k_mix_reduce<<<fg, 256, 0, st>>>(cb.a, ctl, cb.split_cap, cb.slots);
+    k_mix_reduce<<<fg, 256, 0, st>>>(cb.a, ctl, cb.seg);
     nbg_launch_spatial_sort(cb, ctl, st);
     k_mix_pack<<<fg, 256, 0, st>>>(cb.a, ctl, cb.perm, cb.jhi, cb.jlo);
-    const ll tiles = (cb.cap + NBG_MIX_ITILE - 1) / NBG_MIX_ITILE;
-    k_mix_tiles<<<(int)tiles, NBG_MIX_BLOCK, 0, st>>>(ctl, cb.jhi, cb.jlo, cb.tile_c);
+    ll tiles = (cb.cap + NBG_MIX_ITILE - 1) / NBG_MIX_ITILE + cb.seg.nsims;
+    if (tiles > 152 * 64) tiles = 152 * 64;
+    k_mix_tiles<<<(int)tiles, NBG_MIX_BLOCK, 0, st>>>(ctl, cb.seg, cb.jhi, cb.jlo, cb.tile_c);
 }
 
 void nbg_launch_mixed_pair(const CycleBufs &cb, DevCtl *ctl, cudaStream_t st)
 {
-    k_pair_mixed<NBG_MIX_K><<<cb.slots, NBG_MIX_BLOCK, 0, st>>>(cb.a, ctl, cb.jhi, cb.jlo, cb.tile_c, cb.perm,
-                                                               cb.part, cb.cap, cb.ev_keys, cb.ev_cap);
+    k_pair_mixed<NBG_MIX_K><<<cb.slots, NBG_MIX_BLOCK, 0, st>>>(cb.a, ctl, cb.seg, cb.jhi, cb.jlo, cb.tile_c,
+                                                               cb.perm, cb.part, cb.cap, cb.ev_keys, cb.ev_cap);
 }
 
 void nbg_launch_mixed_out(const CycleBufs &cb, DevCtl *ctl, cudaStream_t st)
 {
-    k_mix_out<<<flat_grid(cb.cap), 256, 0, st>>>(cb.a, ctl, cb.perm, cb.part, cb.cap);
+    k_mix_out<<<flat_grid(cb.cap), 256, 0, st>>>(cb.a, ctl, cb.seg, cb.perm, cb.part, cb.cap);
 }

@@ -37,21 +37,37 @@ __device__ __forceinline__ unsigned quant10(float x, float inv_span)
     return (unsigned)t;
 }
 
-/* keys of the bodies 0..n-1 and the identity permutation */
-__global__ void k_morton_keys(BodyArrays A, DevCtl *ctl, unsigned *keys, unsigned *vals)
+/* Keys of the bodies 0..n-1 and the identity permutation.  One sim: a 30-bit
+ * Morton key over [-x_max, x_max]^3.  Several sims: the sim index in the top
+ * 11 bits and a 21-bit Morton key over the sim's own box, so every sim keeps
+ * its range of positions and is ordered inside it. */
+__global__ void k_morton_keys(BodyArrays A, DevCtl *ctl, SimSegs seg, unsigned *keys, unsigned *vals)
 {
     if (ctl->error) return;
     const ll n = ctl->n;
-    const float xmax = __uint_as_float(ctl->xmax_bits);
-    const float inv_span = xmax > 0.f ? 0.5f / xmax : 0.f;
+    const bool multi = seg.nsims > 1;
     for (ll k = (ll)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (ll)gridDim.x * blockDim.x) {
         const double x = A.x[k], y = A.y[k], z = A.z[k], r = A.rad[k];
         const bool finite = fabs(x) <= 1.7976931348623157e308 && fabs(y) <= 1.7976931348623157e308 &&
                             fabs(z) <= 1.7976931348623157e308 && r == r;
-        unsigned key = 1u << 30;
-        if (finite)
-            key = spread10(quant10((float)x, inv_span)) | (spread10(quant10((float)y, inv_span)) << 1) |
-                  (spread10(quant10((float)z, inv_span)) << 2);
+        unsigned key;
+        if (!multi) {
+            const float xmax = __uint_as_float(ctl->xmax_bits);
+            const float inv_span = xmax > 0.f ? 0.5f / xmax : 0.f;
+            key = 1u << 30;
+            if (finite)
+                key = spread10(quant10((float)x, inv_span)) | (spread10(quant10((float)y, inv_span)) << 1) |
+                      (spread10(quant10((float)z, inv_span)) << 2);
+        } else {
+            const int sim = nbg_sim_of(seg.off, seg.nsims, k);
+            const float xmax = __uint_as_float(seg.xmax_bits[sim]);
+            const float inv_span = xmax > 0.f ? 0.5f / xmax : 0.f;
+            unsigned m = 0x1fffffu;
+            if (finite)
+                m = (spread10(quant10((float)x, inv_span) >> 3) | (spread10(quant10((float)y, inv_span) >> 3) << 1) |
+                     (spread10(quant10((float)z, inv_span) >> 3) << 2));
+            key = ((unsigned)sim << 21) | m;
+        }
         keys[k] = key;
         vals[k] = (unsigned)k;
     }
@@ -161,7 +177,7 @@ ll nbg_sort_scratch_hist(ll cap) { return ((cap + RS_TILE - 1) / RS_TILE) * RS_B
 void nbg_launch_spatial_sort(const CycleBufs &cb, DevCtl *ctl, cudaStream_t st)
 {
     const int g = (int)((cb.cap + 255) / 256 < 152 * 16 ? (cb.cap + 255) / 256 : 152 * 16);
-    k_morton_keys<<<g > 0 ? g : 1, 256, 0, st>>>(cb.a, ctl, cb.skey[0], cb.perm);
+    k_morton_keys<<<g > 0 ? g : 1, 256, 0, st>>>(cb.a, ctl, cb.seg, cb.skey[0], cb.perm);
     const int nb = (int)((cb.cap + RS_TILE - 1) / RS_TILE);
     unsigned *kin = cb.skey[0], *vin = cb.perm, *kout = cb.skey[1], *vout = cb.sval;
     for (int pass = 0; pass < 4; pass++) {

@@ -38,13 +38,44 @@ struct nbg_ctx {
     nbg_timing tacc{};
     std::vector<cudaEvent_t> evs;
     int use_graph = 1;
+    int graph_cycles = 1; /* cycles captured in one graph */
     cudaGraphExec_t graph = nullptr;
     bool graph_valid = false;
     int graph_precision = -1;
     void *scratch = nullptr;
     size_t scratch_bytes = 0;
     ll launches_per_cycle = 0;
+    void *seg_mem = nullptr; /* SimSegs arrays */
+    int seg_cap = 0;         /* sims the allocation holds */
 };
+
+/* (Re)allocates the per-sim arrays for nsims sims and uploads the offsets of
+ * the given counts (host array, nsims entries). */
+static int set_segments(nbg_ctx *ctx, int nsims, const ll *counts)
+{
+    if (nsims > ctx->seg_cap) {
+        cudaFree(ctx->seg_mem);
+        ctx->seg_mem = nullptr;
+        cudaError_t e = cudaMalloc(&ctx->seg_mem, NBG_SEG_BYTES(nsims));
+        if (e != cudaSuccess) {
+            ctx->err = std::string("segment allocation: ") + cudaGetErrorString(e);
+            return NBG_E_CUDA;
+        }
+        ctx->seg_cap = nsims;
+    }
+    ctx->cb.seg = nbg_seg_carve(ctx->seg_mem, nsims);
+    std::vector<ll> h((size_t)nsims + 1, 0);
+    for (int s = 0; s < nsims; s++) h[(size_t)s + 1] = h[(size_t)s] + counts[s];
+    cudaError_t e = cudaMemsetAsync(ctx->seg_mem, 0, NBG_SEG_BYTES(nsims), ctx->st);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(ctx->cb.seg.off, h.data(), h.size() * sizeof(ll), cudaMemcpyHostToDevice, ctx->st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->st);
+    if (e != cudaSuccess) {
+        ctx->err = std::string("segment upload: ") + cudaGetErrorString(e);
+        return NBG_E_CUDA;
+    }
+    return NBG_OK;
+}
 
 static std::string g_last_error;
 
@@ -413,6 +444,8 @@ int nbg_create(int device, int precision, int64_t capacity, nbg_ctx **out)
         if ((rc = ensure_frag_cap(ctx, 4096)) != NBG_OK) break;
         if ((rc = ensure_adds_cap(ctx, 1024)) != NBG_OK) break;
         if ((rc = ensure_ev_cap(ctx, 65536)) != NBG_OK) break;
+        const ll zero = 0;
+        if ((rc = set_segments(ctx, 1, &zero)) != NBG_OK) break;
     } while (0);
     if (rc != NBG_OK) {
         g_last_error = ctx->err;
@@ -436,6 +469,7 @@ void nbg_destroy(nbg_ctx *ctx)
     cudaFree(ctx->cb.ev_keys);
     cudaFree(ctx->cb.ev_out);
     free_cap_buffers(ctx->cb);
+    cudaFree(ctx->seg_mem);
     cudaFree(ctx->scratch);
     cudaFree(ctx->ctl);
     if (ctx->ctl_h) cudaFreeHost(ctx->ctl_h);
@@ -502,11 +536,19 @@ int nbg_set_cycle(nbg_ctx *ctx, uint64_t cycle)
     return ctl_put(ctx, offsetof(DevCtl, cycle), &c, sizeof c);
 }
 
-int nbg_set_bodies(nbg_ctx *ctx, const nbg_soa *host, int64_t n)
+int nbg_set_collections(nbg_ctx *ctx, int64_t nsims, const int64_t *counts, const nbg_soa *host)
 {
-    if (!ctx || n < 0 || (n > 0 && !host)) return fail(ctx, NBG_E_ARG, "bad arguments");
+    if (!ctx || nsims < 1 || nsims > NBG_MAX_SIMS || !counts) return fail(ctx, NBG_E_ARG, "bad arguments");
+    ll n = 0;
+    for (ll s = 0; s < nsims; s++) {
+        if (counts[s] < 0) return fail(ctx, NBG_E_ARG, "negative body count");
+        n += counts[s];
+    }
+    if (n > 0 && !host) return fail(ctx, NBG_E_ARG, "host is NULL");
     CK(cudaSetDevice(ctx->device));
-    int rc = ensure_cap(ctx, n + ctx->pending_adds, 0);
+    CK(cudaStreamSynchronize(ctx->st));
+    ctx->pending_adds = 0; /* a new collection drops staged adds */
+    int rc = ensure_cap(ctx, n, 0);
     if (rc != NBG_OK) return rc;
     if ((rc = upload_soa(ctx, ctx->cb.a, 0, host, n)) != NBG_OK) return rc;
     if (!host || !host->id) {
@@ -516,10 +558,34 @@ int nbg_set_bodies(nbg_ctx *ctx, const nbg_soa *host, int64_t n)
         if ((rc = put_field(ctx, ctx->cb.a.id, ids.data(), n)) != NBG_OK) return rc;
         CK(cudaStreamSynchronize(ctx->st));
     }
-    ll nn = n;
-    rc = ctl_put(ctx, offsetof(DevCtl, n), &nn, sizeof nn);
-    if (rc != NBG_OK) return rc;
+    if ((rc = set_segments(ctx, (int)nsims, (const ll *)counts)) != NBG_OK) return rc;
+    invalidate_graph(ctx); /* kernel arguments carry the segment arrays */
+    ll nn = n, zero = 0;
+    if ((rc = ctl_put(ctx, offsetof(DevCtl, n), &nn, sizeof nn)) != NBG_OK) return rc;
+    if ((rc = ctl_put(ctx, offsetof(DevCtl, n_host_adds), &zero, sizeof zero)) != NBG_OK) return rc;
     ctx->n_host = n;
+    return NBG_OK;
+}
+
+int nbg_set_bodies(nbg_ctx *ctx, const nbg_soa *host, int64_t n)
+{
+    if (!ctx || n < 0 || (n > 0 && !host)) return fail(ctx, NBG_E_ARG, "bad arguments");
+    const int64_t counts[1] = {n};
+    return nbg_set_collections(ctx, 1, counts, host);
+}
+
+int nbg_sim_counts(nbg_ctx *ctx, int64_t *counts, int64_t cap, int64_t *nsims)
+{
+    if (!ctx || cap < 0) return fail(ctx, NBG_E_ARG, "bad arguments");
+    CK(cudaSetDevice(ctx->device));
+    const int ns = ctx->cb.seg.nsims;
+    if (nsims) *nsims = ns;
+    if (counts && cap > 0) {
+        std::vector<ll> off((size_t)ns + 1);
+        CK(cudaMemcpyAsync(off.data(), ctx->cb.seg.off, off.size() * sizeof(ll), cudaMemcpyDeviceToHost, ctx->st));
+        CK(cudaStreamSynchronize(ctx->st));
+        for (ll s = 0; s < ns && s < cap; s++) counts[s] = off[(size_t)s + 1] - off[(size_t)s];
+    }
     return NBG_OK;
 }
 
@@ -585,6 +651,7 @@ int nbg_add_bodies(nbg_ctx *ctx, const nbg_soa *host, int64_t n, int64_t *ids_ou
 {
     if (!ctx || n < 0 || (n > 0 && !host)) return fail(ctx, NBG_E_ARG, "bad arguments");
     if (n == 0) return NBG_OK;
+    if (ctx->cb.seg.nsims != 1) return fail(ctx, NBG_E_STATE, "adds need a single-collection context");
     CK(cudaSetDevice(ctx->device));
     int rc = sync_ctl(ctx);
     if (rc != NBG_OK) return rc;
@@ -602,6 +669,8 @@ int nbg_add_bodies(nbg_ctx *ctx, const nbg_soa *host, int64_t n, int64_t *ids_ou
     ctx->pending_adds += n;
     ll pa = ctx->pending_adds;
     if ((rc = ctl_put(ctx, offsetof(DevCtl, n_host_adds), &pa, sizeof pa)) != NBG_OK) return rc;
+    CK(cudaMemcpyAsync(ctx->cb.seg.hadd, &pa, sizeof pa, cudaMemcpyHostToDevice, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
     if ((rc = ctl_put(ctx, offsetof(DevCtl, next_id), &next, sizeof next)) != NBG_OK) return rc;
     if (ids_out)
         for (ll k = 0; k < n; k++) ids_out[k] = ids[(size_t)k];
@@ -637,6 +706,7 @@ int nbg_remove_bodies(nbg_ctx *ctx, int64_t count, int64_t *removed)
 {
     if (!ctx) return NBG_E_ARG;
     if (count == 0 || count < -1) return fail(ctx, NBG_E_ARG, "count must be -1 or positive");
+    if (ctx->cb.seg.nsims != 1) return fail(ctx, NBG_E_STATE, "RemoveBodies needs a single-collection context");
     CK(cudaSetDevice(ctx->device));
     int rc = ensure_scratch(ctx, sizeof(ll));
     if (rc != NBG_OK) return rc;
@@ -740,13 +810,14 @@ static void launch_cycle(nbg_ctx *ctx, int precision, long ev_base)
     ctx->launches_per_cycle = precision == NBG_PRECISION_MIXED ? 31 : 14;
 }
 
+/* One CUDA graph of ctx->graph_cycles consecutive cycles. */
 static int build_graph(nbg_ctx *ctx)
 {
     if (ctx->graph_valid && ctx->graph_precision == ctx->precision) return NBG_OK;
     invalidate_graph(ctx);
     cudaGraph_t g;
     CK(cudaStreamBeginCapture(ctx->st, cudaStreamCaptureModeThreadLocal));
-    launch_cycle(ctx, ctx->precision, -1);
+    for (int c = 0; c < ctx->graph_cycles; c++) launch_cycle(ctx, ctx->precision, -1);
     CK(cudaStreamEndCapture(ctx->st, &g));
     cudaError_t e = cudaGraphInstantiate(&ctx->graph, g, 0);
     cudaGraphDestroy(g);
@@ -784,11 +855,14 @@ int nbg_step(nbg_ctx *ctx, double dt, double R, int nsteps, nbg_step_info *info)
         int rc = ensure_cap(ctx, ctx->n_host + ctx->pending_adds + 1, ctx->n_host);
         if (rc != NBG_OK) return rc;
         const int todo = nsteps - done;
-        if (ctx->timing || !ctx->use_graph || todo == 1) {
+        if (ctx->timing || !ctx->use_graph || todo < ctx->graph_cycles || todo == 1) {
             for (int s = 0; s < todo; s++) launch_cycle(ctx, ctx->precision, ctx->timing ? 4L * s : -1L);
         } else {
+            /* whole graphs of graph_cycles cycles, the remainder directly */
             if ((rc = build_graph(ctx)) != NBG_OK) return rc;
-            for (int s = 0; s < todo; s++) CK(cudaGraphLaunch(ctx->graph, ctx->st));
+            const int graphs = todo / ctx->graph_cycles;
+            for (int s = 0; s < graphs; s++) CK(cudaGraphLaunch(ctx->graph, ctx->st));
+            for (int s = graphs * ctx->graph_cycles; s < todo; s++) launch_cycle(ctx, ctx->precision, -1L);
         }
         CK(cudaGetLastError());
         if ((rc = sync_ctl(ctx)) != NBG_OK) return rc;
@@ -966,6 +1040,13 @@ int nbg_set_option(nbg_ctx *ctx, int key, int64_t value)
         return NBG_OK;
     case NBG_OPT_GRAPH:
         ctx->use_graph = value != 0;
+        return NBG_OK;
+    case NBG_OPT_GRAPH_CYCLES:
+        if (value < 1 || value > 1000) return fail(ctx, NBG_E_ARG, "cycles per graph must be 1..1000");
+        if (value != ctx->graph_cycles) {
+            ctx->graph_cycles = (int)value;
+            invalidate_graph(ctx);
+        }
         return NBG_OK;
     case NBG_OPT_NEAR_PPM: {
         if (value < 0 || value > 10000000) return fail(ctx, NBG_E_ARG, "near radius factor out of range");

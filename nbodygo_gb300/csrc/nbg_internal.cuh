@@ -35,6 +35,7 @@ typedef unsigned long long ull;
 #define NBG_EVT_SUB_JI 2u  /* subsume(j absorbs i) */
 
 #define NBG_MAX_BODIES ((ll)1 << 30) /* event keys pack i and j in 30 bits */
+#define NBG_MAX_SIMS 2048            /* Morton keys of several sims carry the sim in 11 bits */
 
 #define NBG_NF64 20
 struct BodyArrays {
@@ -57,7 +58,7 @@ struct DevCtl {
     int pad0;
     ll error_need;   /* for NBG_E_OVERFLOW: the size that would have fitted */
     int error_what;  /* 1 = bodies, 2 = events, 3 = fragments, 4 = partials */
-    int splits;      /* mixed: j-range splits per i-tile for this cycle */
+    int splits;      /* mixed: j-range splits per i-tile (a sim uses at most its j-tile count) */
     ll work_next;    /* mixed: next work item for the persistent CTAs */
     /* per-cycle values */
     ll ev_count;     /* detected events (may exceed capacity) */
@@ -76,9 +77,73 @@ struct DevCtl {
     ll acc_steps, acc_interactions, acc_events, acc_frags, acc_removed, acc_nan;
     ll rend_n;       /* renderables written by the last cycle */
     ll last_ev_n;    /* resolved events recorded by the last cycle */
+    ll cycle_interactions; /* sum over sims of n_s (n_s - 1) at the cycle start */
 };
 
+/* A collection may hold several independent simulations stored one after
+ * another: sim s occupies bodies [off[s], off[s+1]) and bodies of different
+ * sims never interact.  Events, fragments and adds stay inside their sim, so
+ * each sim follows the reference's cycle exactly as if it were alone. */
+struct SimSegs {
+    int nsims;
+    ll *off;         /* [nsims+1] */
+    ll *tile_off;    /* [nsims+1] plain kernel: 64-body i-tiles before sim s */
+    ll *mtile_off;   /* [nsims+1] mixed kernel: 512-body i-tiles before sim s */
+    ll *item_off;    /* [nsims+1] mixed kernel: work items before sim s */
+    int *splits;     /* [nsims]   mixed kernel: j-range splits of sim s */
+    ll *keep;        /* [nsims]   bodies of sim s that survive Cycle */
+    ll *frag;        /* [nsims]   fragments sim s emits this cycle */
+    ll *frag_start;  /* [nsims+1] */
+    ll *hadd;        /* [nsims]   host adds staged for sim s */
+    ll *hadd_start;  /* [nsims+1] */
+    ll *keep_start;  /* [nsims+1] */
+    ll *new_off;     /* [nsims+1] layout after Cycle */
+    unsigned *xmax_bits; /* [nsims] mixed: |x| max of sim s (Morton grid) */
+};
+
+/* bytes of the SimSegs arrays for nsims sims (one allocation, carved by
+ * nbg_seg_carve: 11 ll arrays and 2 32-bit arrays of nsims + 1) */
+#define NBG_SEG_BYTES(ns) ((size_t)((ns) + 1) * 8 * 11 + (size_t)((ns) + 1) * 4 * 2 + 256)
+
+static inline SimSegs nbg_seg_carve(void *base, int nsims)
+{
+    SimSegs s;
+    const size_t m = (size_t)nsims + 1;
+    ll *p = (ll *)base;
+    s.nsims = nsims;
+    s.off = p;
+    s.tile_off = p + m;
+    s.mtile_off = p + 2 * m;
+    s.item_off = p + 3 * m;
+    s.keep = p + 4 * m;
+    s.frag = p + 5 * m;
+    s.frag_start = p + 6 * m;
+    s.hadd = p + 7 * m;
+    s.hadd_start = p + 8 * m;
+    s.keep_start = p + 9 * m;
+    s.new_off = p + 10 * m;
+    s.splits = (int *)(p + 11 * m);
+    s.xmax_bits = (unsigned *)(s.splits + m);
+    return s;
+}
+
+/* sim holding position k of a segmented array: the largest s with
+ * off[s] <= k (empty sims are skipped) */
+__device__ __forceinline__ int nbg_sim_of(const ll *off, int nsims, ll k)
+{
+    int lo = 0, hi = nsims - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (off[mid] <= k)
+            lo = mid;
+        else
+            hi = mid - 1;
+    }
+    return lo;
+}
+
 struct CycleBufs {
+    SimSegs seg;
     BodyArrays a;       /* the collection */
     BodyArrays b;       /* compaction target */
     BodyArrays adds;    /* host adds staged for the next Cycle (arrival order) */

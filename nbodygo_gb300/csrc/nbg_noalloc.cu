@@ -39,7 +39,9 @@ static constexpr size_t OFF_KEY1 = OFF_KEY0 + align256((size_t)NBG_NOALLOC_MAX_B
 static constexpr size_t OFF_HIST = OFF_KEY1 + align256((size_t)NBG_NOALLOC_MAX_BODIES * 4);
 /* radix-sort histogram: 256 digits per 4096-body block */
 static constexpr size_t HIST_BYTES = (size_t)((NBG_NOALLOC_MAX_BODIES + 4095) / 4096) * 256 * 8;
-static constexpr size_t TOTAL_BYTES = OFF_HIST + align256(HIST_BYTES);
+/* the per-sim layout arrays of one collection */
+static constexpr size_t OFF_SEG = OFF_HIST + align256(HIST_BYTES);
+static constexpr size_t TOTAL_BYTES = OFF_SEG + align256(NBG_SEG_BYTES(1));
 static_assert(TOTAL_BYTES == NBG_NOALLOC_BYTES, "NBG_NOALLOC_BYTES in nbgpu.h is out of date");
 
 /* The scratch of every call on this device.  In host code this name is only
@@ -50,14 +52,18 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[TOTAL_BYTES];
 static unsigned char *g_scratch_addr[NOALLOC_MAX_DEVICES];
 static std::mutex g_setup_mutex;
 
-/* The control block's reductions and counters must start at zero. */
-__global__ void k_noalloc_init(DevCtl *ctl, ll n, float kappa)
+/* The control block's reductions and counters, and the per-sim arrays, must
+ * start at zero; the collection is one sim of n bodies. */
+__global__ void k_noalloc_init(DevCtl *ctl, SimSegs seg, ll n, float kappa)
 {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
     unsigned char *p = (unsigned char *)ctl;
     for (size_t k = 0; k < sizeof(DevCtl); k++) p[k] = 0;
+    unsigned char *q = (unsigned char *)seg.off;
+    for (size_t k = 0; k < NBG_SEG_BYTES(1); k++) q[k] = 0;
     ctl->n = n;
     ctl->near_kappa = kappa;
+    seg.off[1] = n;
 }
 
 static int noalloc_fail(int code, const char *msg);
@@ -115,9 +121,11 @@ extern "C" int nbg_forces_mixed_noalloc(const double *x, const double *y, const 
     cb.ev_cap = 0;
     cb.split_cap = NOALLOC_SPLITS;
     cb.slots = nbg_mixed_slots(dev);
+    cb.seg = nbg_seg_carve(base + OFF_SEG, 1);
     DevCtl *ctl = (DevCtl *)(base + OFF_CTL);
 
-    k_noalloc_init<<<1, 1, 0, st>>>(ctl, (ll)n, 0.07f);
+    k_noalloc_init<<<1, 1, 0, st>>>(ctl, cb.seg, (ll)n, 0.07f);
+    nbg_launch_begin(cb, ctl, st); /* work layout of the one collection */
     nbg_launch_mixed_prep(cb, ctl, st);
     nbg_launch_mixed_pair(cb, ctl, st);
     nbg_launch_mixed_out(cb, ctl, st);

@@ -1,0 +1,127 @@
+"""Batched form: many independent collections in one context
+(nbg_set_collections).  Each collection must evolve exactly as it would alone:
+bit-identical to its own oracle run in the plain form, and within the mixed
+tolerance of its own FP64 forces in the mixed form."""
+import numpy as np
+import pytest
+
+from nbodygo_gb300 import _abi as A
+from nbodygo_gb300 import workloads as W
+from nbodygo_gb300.api import Simulation
+from oracle.oracle import OracleSim
+
+from helpers import assert_states_identical, rel_l2
+from test_gpu_plain_parity import dense_cluster
+
+pytestmark = pytest.mark.gpu
+
+
+def small_ensemble():
+    sims = [
+        W.disk(n=300, seed=1),
+        dense_cluster(150, seed=2),                       # every behaviour, removals, fragments
+        W.plummer(n=257, seed=3, behavior=A.SUBSUME, radius_range=(0.5, 3.0)),
+        W.uniform_ball(n=64, seed=4, R=50.0, radius=1.0, behavior=A.ELASTIC),
+        dense_cluster(1, seed=5),                         # a single body
+        W.plummer(n=1000, seed=6),
+    ]
+    return sims
+
+
+def split_state(st, counts):
+    out, o = [], 0
+    for c in counts:
+        out.append({k: v[o:o + c] for k, v in st.items()})
+        o += c
+    return out
+
+
+def test_plain_batch_matches_each_sim_alone():
+    sims = small_ensemble()
+    first_new_id = 1_000_000
+    gpu = Simulation("fp64", seed=77)
+    gpu.set_collections(sims)
+    gpu.set_next_id(first_new_id)
+    oracles = []
+    for b in sims:
+        o = OracleSim(seed=77, threads=4)
+        o.set_bodies(b)
+        o.set_next_id(first_new_id)
+        oracles.append(o)
+    dt, R = 0.02, 0.9
+    for cycle in range(12):
+        info = gpu.step(dt, R, 1)
+        exp_inter = 0
+        for o in oracles:
+            n = o.count()
+            exp_inter += n * (n - 1)
+            o.step(dt, R, 1)
+        assert info["interactions"] == exp_inter
+        counts = gpu.sim_counts()
+        assert list(counts) == [o.count() for o in oracles], f"cycle {cycle}"
+        parts = split_state(gpu.state(), counts)
+        for s, (got, o) in enumerate(zip(parts, oracles)):
+            exp = o.state()
+            # fragment ids come from one counter shared by all sims; the rest
+            # of the state must be bit-identical
+            fields = [f for f in got if f != "id"]
+            assert_states_identical(got, exp, fields=fields, where=f"cycle {cycle} sim {s}")
+            orig = exp["id"] < first_new_id
+            assert np.array_equal(got["id"][orig], exp["id"][orig])
+            assert np.all(got["id"][~orig] >= first_new_id)
+
+
+def test_plain_batch_graph_replay():
+    sims = small_ensemble()
+    a = Simulation("fp64")
+    a.set_collections(sims)
+    a.step(0.02, 1.0, 10)
+    b = Simulation("fp64")
+    b.set_collections(sims)
+    for _ in range(10):
+        b.step(0.02, 1.0, 1)
+    assert_states_identical(a.state(), b.state(), where="graph vs direct")
+    assert list(a.sim_counts()) == list(b.sim_counts())
+
+
+def test_mixed_batch_forces_per_sim():
+    sims = [W.plummer(n=n, seed=10 + n) for n in (256, 700, 2048, 4096)] + [W.disk(n=999, seed=3)]
+    gpu = Simulation("mixed")
+    gpu.set_collections(sims)
+    f = gpu.force_pass()
+    o = 0
+    for s, b in enumerate(sims):
+        n = len(b["x"])
+        ora = OracleSim(threads=8)
+        ora.set_bodies(b)
+        g = ora.forces()
+        err = rel_l2([c[o:o + n] for c in f], g)
+        assert err <= 1e-6, f"sim {s}: rel L2 {err:.3e}"
+        o += n
+
+
+def test_mixed_batch_events_and_counts():
+    sims = [dense_cluster(200, seed=s) for s in (21, 22, 23)]
+    gpu = Simulation("mixed", seed=9)
+    gpu.set_collections(sims)
+    gpu.step(0.05, 1.0, 1)
+    ev = gpu.events()
+    total = 0
+    for b in sims:
+        o = OracleSim(seed=9, threads=4)
+        o.set_bodies(b)
+        o.step(0.05, 1.0, 1)
+        total += len(o.events())
+    assert len(ev) == total
+    counts = gpu.sim_counts()
+    assert len(counts) == 3 and counts.sum() == gpu.count()
+
+
+def test_batch_rejects_single_collection_operations():
+    gpu = Simulation("fp64")
+    gpu.set_collections([W.disk(n=50, seed=1), W.disk(n=60, seed=2)])
+    from nbodygo_gb300.api import NbgError
+    with pytest.raises(NbgError):
+        gpu.remove_bodies(3)
+    with pytest.raises(NbgError):
+        gpu.add_bodies(W.disk(n=2, seed=3))
