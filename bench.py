@@ -79,6 +79,7 @@ def parse():
     ap.add_argument("--n-each", type=int, default=65536, help="plummer_disk: bodies per component")
     ap.add_argument("--no-plain", action="store_true", help="skip the FP64 comparison run")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--no-autotune", action="store_true", help="keep the default kernel shape")
     return ap.parse_args()
 
 
@@ -325,6 +326,10 @@ def main():
     sim.set_stream(stream.cuda_stream)
     sim.set_option(A.OPT_GRAPH_CYCLES, chunk)
     load(sim, sims)
+    tuned = None
+    if prec == "mixed" and not args.no_autotune:
+        shape, tms = sim.autotune()
+        tuned = {"shape": shape, "pair_kernel_ms": tms, "candidates": A.MIX_SHAPES}
     sim.step(DT, 1.0, max(args.warmup, 3) * chunk)
 
     # ---- timed: K cycles, L2 flushed before each chunk, device time ----
@@ -465,6 +470,7 @@ def main():
                       "hbm_gbs_measured": measured_hbm().get("hbm_gbs")},
             "clocks": clk,
             "cpu_baseline": cpu,
+            "autotune": tuned,
         }
         line.update(result_extra)
         print(json.dumps(line), flush=True)

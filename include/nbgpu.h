@@ -282,10 +282,24 @@ int nbg_get_timing(nbg_ctx *ctx, nbg_timing *t);
 #define NBG_OPT_EV_CAP 3     /* event-list capacity (rounded up to a power of two) */
 #define NBG_OPT_FRAG_CAP 4   /* fragments one cycle may emit */
 #define NBG_OPT_GRAPH_CYCLES 6 /* cycles captured in one CUDA graph (default 1) */
+#define NBG_OPT_MIX_SHAPE 7    /* shape of the mixed pair kernel, 0..6 (see nbg_autotune) */
 #define NBG_OPT_NEAR_PPM 5   /* mixed: pairs closer than (value * 1e-6) x the i-tile's
                                 extent around its origin are computed in FP64
                                 (default 70000) */
 int nbg_set_option(nbg_ctx *ctx, int key, int64_t value);
+
+/* Autotuner of the mixed pair kernel.  Seven shapes are compiled (threads per
+ * CTA x i-bodies per thread x j per shared-memory tile x unroll):
+ *   0: 128x4, 256, 2 (default)   1: 128x4, 256, 1   2: 128x2, 256, 2
+ *   3: 256x2, 256, 2             4: 128x4, 512, 2   5: 64x4, 256, 2
+ *   6: 128x2, 128, 4
+ * nbg_autotune times the pair kernel of each on the context's current
+ * collection (the best of three force passes after one warm-up) and keeps the
+ * fastest.  cache_path (may be NULL) names a text file of earlier results
+ * keyed by GPU name, SM count, body-count bucket (power of two) and
+ * collection-count bucket: a matching entry is used without measuring, and a
+ * new measurement is appended. */
+int nbg_autotune(nbg_ctx *ctx, const char *cache_path, int *shape, double *best_ms);
 
 /* Peak probes: FFMA (FP32) and DFMA (FP64) throughput of the device in
  * FLOP/s (an FMA counts 2), measured with dependent-chain kernels. */

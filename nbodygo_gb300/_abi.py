@@ -41,6 +41,8 @@ OPT_EV_CAP = 3
 OPT_FRAG_CAP = 4
 OPT_NEAR_PPM = 5
 OPT_GRAPH_CYCLES = 6
+OPT_MIX_SHAPE = 7
+MIX_SHAPES = 7
 
 _pd = C.POINTER(C.c_double)
 _pi64 = C.POINTER(C.c_int64)
@@ -180,6 +182,7 @@ def declare(lib):
         "nbg_get_timing": (C.c_int, [P, C.POINTER(NbgTiming)]),
         "nbg_set_option": (C.c_int, [P, C.c_int, C.c_int64]),
         "nbg_probe_peaks": (C.c_int, [C.c_int, _pd, _pd, _pd]),
+        "nbg_autotune": (C.c_int, [P, C.c_char_p, _pi32, _pd]),
         "nbg_forces_mixed_noalloc": (C.c_int, [C.c_void_p] * 6 + [C.c_int64] + [C.c_void_p] * 4),
     }
     for name, (res, args) in sigs.items():

@@ -106,6 +106,14 @@ class Simulation:
     def set_option(self, key, value):
         self._check(self.lib.nbg_set_option(self.ctx, int(key), int(value)))
 
+    def autotune(self, cache_path=None):
+        """Times every compiled shape of the mixed pair kernel on the current
+        collection and keeps the fastest; returns (shape, ms)."""
+        v, ms = C.c_int32(), C.c_double()
+        path = cache_path.encode() if cache_path else None
+        self._check(self.lib.nbg_autotune(self.ctx, path, C.byref(v), C.byref(ms)))
+        return v.value, ms.value
+
     def enable_timing(self, on=True):
         self._check(self.lib.nbg_enable_timing(self.ctx, 1 if on else 0))
 

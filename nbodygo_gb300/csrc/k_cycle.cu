@@ -77,7 +77,8 @@ __device__ static ll block_scan_array(int ns, F f, ll *out)
 /* Per-cycle resets and the work layout of every sim: 64-body tiles of the
  * plain kernel, 512-body i-tiles, j-range splits and work items of the
  * mixed kernel, and the interaction count.  One block. */
-__global__ void __launch_bounds__(NBG_SCAN_BLOCK) k_begin(DevCtl *ctl, SimSegs seg, int split_cap, int slots)
+__global__ void __launch_bounds__(NBG_SCAN_BLOCK) k_begin(DevCtl *ctl, SimSegs seg, int split_cap, int slots,
+                                                          int itile)
 {
     if (ctl->error) return;
     const int ns = seg.nsims;
@@ -89,7 +90,7 @@ __global__ void __launch_bounds__(NBG_SCAN_BLOCK) k_begin(DevCtl *ctl, SimSegs s
     }
     block_scan_array(ns, [&](int s) { return (off[s + 1] - off[s] + 63) / 64; }, seg.tile_off);
     const ll mtiles = block_scan_array(
-        ns, [&](int s) { return (off[s + 1] - off[s] + NBG_MIX_ITILE - 1) / NBG_MIX_ITILE; }, seg.mtile_off);
+        ns, [&](int s) { return (off[s + 1] - off[s] + itile - 1) / itile; }, seg.mtile_off);
     ll S = mtiles > 0 ? (8ll * slots + mtiles - 1) / mtiles : 1;
     if (S > split_cap) S = split_cap;
     if (S < 1) S = 1;
@@ -302,6 +303,9 @@ __global__ void __launch_bounds__(P64_BLOCK) k_pair_fp64(BodyArrays A, DevCtl *c
             __syncthreads();
             if (!live_i) continue;
             const int cnt = (n - j0) < P64_BLOCK ? (int)(n - j0) : P64_BLOCK;
+            /* unrolled: the divisions and square roots of later j overlap;
+             * the sum still runs in j order */
+#pragma unroll 4
             for (int t = 0; t < cnt; t++) {
                 const ll j = j0 + t;
                 const double dx = sx[t] - xi;
@@ -604,35 +608,60 @@ __device__ static void resolve_subsume(BodyArrays &A, ll b, ll o)
     A.flags[o] &= ~NBG_F_EXISTS;
 }
 
-__global__ void k_resolve(BodyArrays A, DevCtl *ctl, const ull *keys, nbg_event *ev_out)
+/* first index of sorted keys[0..cnt) that is >= v */
+__device__ static ll lower_bound_u64(const ull *keys, ll cnt, ull v)
 {
-    if (threadIdx.x != 0 || blockIdx.x != 0 || ctl->error) return;
-    ctl->next_id += ctl->frag_total; /* fragments took ids next_id .. next_id+total-1 */
-    const ll cnt = ctl->ev_count;
-    for (ll k = cnt - 1; k >= 0; k--) {
-        const ull key = keys[k];
-        const ll i = (ll)(key >> 32);
-        const ll j = (ll)((key >> 2) & 0x3fffffffull);
-        const unsigned type = (unsigned)(key & 3ull);
-        ll b1 = i, b2 = j;
-        if (type == NBG_EVT_SUB_JI) {
-            b1 = j;
-            b2 = i;
-        }
-        nbg_event e;
-        e.id1 = A.id[b1];
-        e.id2 = A.id[b2];
-        e.type = type == NBG_EVT_COLL_IJ ? NBG_EV_COLLISION : NBG_EV_SUBSUME;
-        e.pad = 0;
-        ev_out[cnt - 1 - k] = e;
-        if (type == NBG_EVT_COLL_IJ)
-            resolve_collision(A, b1, b2);
+    ll lo = 0, hi = cnt;
+    while (lo < hi) {
+        const ll mid = (lo + hi) >> 1;
+        if (keys[mid] < v)
+            lo = mid + 1;
         else
-            resolve_subsume(A, b1, b2);
+            hi = mid;
     }
-    ctl->last_ev_n = cnt;
-    ctl->acc_events += cnt;
-    ctl->acc_frags += ctl->frag_total;
+    return lo;
+}
+
+/* ProcessMods: every sim walks its own events newest first, one thread per
+ * sim.  Events of one sim only touch that sim's bodies and the sorted keys
+ * are grouped by sim (i ranges), so this is the sequential order of each sim
+ * exactly.  ev_out holds the sims one after another, each in resolution
+ * order. */
+__global__ void k_resolve(BodyArrays A, DevCtl *ctl, SimSegs seg, const ull *keys, nbg_event *ev_out)
+{
+    if (ctl->error) return;
+    const ll cnt = ctl->ev_count;
+    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < seg.nsims; s += gridDim.x * blockDim.x) {
+        const ll lo = seg.nsims == 1 ? 0 : lower_bound_u64(keys, cnt, (ull)seg.off[s] << 32);
+        const ll hi = seg.nsims == 1 ? cnt : lower_bound_u64(keys, cnt, (ull)seg.off[s + 1] << 32);
+        for (ll k = hi - 1; k >= lo; k--) {
+            const ull key = keys[k];
+            const ll i = (ll)(key >> 32);
+            const ll j = (ll)((key >> 2) & 0x3fffffffull);
+            const unsigned type = (unsigned)(key & 3ull);
+            ll b1 = i, b2 = j;
+            if (type == NBG_EVT_SUB_JI) {
+                b1 = j;
+                b2 = i;
+            }
+            nbg_event e;
+            e.id1 = A.id[b1];
+            e.id2 = A.id[b2];
+            e.type = type == NBG_EVT_COLL_IJ ? NBG_EV_COLLISION : NBG_EV_SUBSUME;
+            e.pad = 0;
+            ev_out[lo + (hi - 1 - k)] = e;
+            if (type == NBG_EVT_COLL_IJ)
+                resolve_collision(A, b1, b2);
+            else
+                resolve_subsume(A, b1, b2);
+        }
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        ctl->next_id += ctl->frag_total; /* fragments took ids next_id .. next_id+total-1 */
+        ctl->last_ev_n = cnt;
+        ctl->acc_events += cnt;
+        ctl->acc_frags += ctl->frag_total;
+    }
 }
 
 /* ------------------------------------------------------------------------ */
@@ -938,7 +967,7 @@ static int flat_grid(ll cap)
 
 void nbg_launch_begin(const CycleBufs &cb, DevCtl *ctl, cudaStream_t st)
 {
-    k_begin<<<1, NBG_SCAN_BLOCK, 0, st>>>(ctl, cb.seg, cb.split_cap, cb.slots);
+    k_begin<<<1, NBG_SCAN_BLOCK, 0, st>>>(ctl, cb.seg, cb.split_cap, cb.slots, cb.itile > 0 ? cb.itile : 512);
 }
 
 void nbg_launch_frag_count(const CycleBufs &cb, DevCtl *ctl, cudaStream_t st)
@@ -966,7 +995,7 @@ void nbg_launch_after_pair(const CycleBufs &cb, DevCtl *ctl, cudaStream_t st)
     const int sg = scan_grid(cb.cap);
     k_sort_events<<<1, SORT_BLOCK, 0, st>>>(ctl, cb.ev_keys, cb.ev_cap);
     k_frag_emit<<<sg, NBG_SCAN_BLOCK, 0, st>>>(cb.a, cb.frags, ctl, cb.blk_off);
-    k_resolve<<<1, 32, 0, st>>>(cb.a, ctl, cb.ev_keys, cb.ev_out);
+    k_resolve<<<(cb.seg.nsims + 63) / 64, 64, 0, st>>>(cb.a, ctl, cb.seg, cb.ev_keys, cb.ev_out);
     k_integrate<<<flat_grid(cb.cap), 256, 0, st>>>(cb.a, ctl, cb.rend);
     k_keep_blocksum<<<sg, NBG_SCAN_BLOCK, 0, st>>>(cb.a, ctl, cb.seg, cb.blk_sum);
     k_scan_blocks<<<1, NBG_SCAN_BLOCK, 0, st>>>(ctl, cb.seg, cb.blk_sum, cb.blk_off, 1, cb.cap, cb.frag_cap);

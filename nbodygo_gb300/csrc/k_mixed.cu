@@ -134,20 +134,19 @@ __global__ void k_mix_pack(BodyArrays A, DevCtl *ctl, const unsigned *perm, floa
 __device__ __forceinline__ bool packed_special(const float4 &lo) { return lo.x != lo.x; }
 
 /* origin of each i-tile: centre of the bounding box of its bodies */
-__global__ void __launch_bounds__(NBG_MIX_BLOCK) k_mix_tiles(DevCtl *ctl, SimSegs seg, const float4 *jhi,
-                                                             const float4 *jlo, float4 *tile_c)
+#define TILES_BLOCK 128
+__global__ void __launch_bounds__(TILES_BLOCK) k_mix_tiles(DevCtl *ctl, SimSegs seg, const float4 *jhi,
+                                                           const float4 *jlo, float4 *tile_c, int itile)
 {
-    __shared__ float red[6][NBG_MIX_BLOCK / 32];
+    __shared__ float red[6][TILES_BLOCK / 32];
     if (ctl->error) return;
     const ll ntiles = seg.mtile_off[seg.nsims];
     for (ll tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
     const int sim = nbg_sim_of(seg.mtile_off, seg.nsims, tile);
-    const ll n = seg.off[sim + 1];
-    const ll base = seg.off[sim] + (tile - seg.mtile_off[sim]) * NBG_MIX_ITILE;
+    const ll base = seg.off[sim] + (tile - seg.mtile_off[sim]) * itile;
+    const ll n = seg.off[sim + 1] < base + itile ? seg.off[sim + 1] : base + itile;
     float lo[3] = {3e38f, 3e38f, 3e38f}, hi[3] = {-3e38f, -3e38f, -3e38f};
-    for (int k = 0; k < NBG_MIX_K; k++) {
-        ll p = base + (ll)k * NBG_MIX_BLOCK + threadIdx.x;
-        if (p >= n) continue;
+    for (ll p = base + threadIdx.x; p < n; p += TILES_BLOCK) {
         if (packed_special(jlo[p])) continue;
         float4 h = jhi[p];
         lo[0] = fminf(lo[0], h.x);
@@ -173,7 +172,7 @@ __global__ void __launch_bounds__(NBG_MIX_BLOCK) k_mix_tiles(DevCtl *ctl, SimSeg
         float c3[3];
         for (int c = 0; c < 3; c++) {
             float l = red[c][0], h = red[3 + c][0];
-            for (int q = 1; q < NBG_MIX_BLOCK / 32; q++) {
+            for (int q = 1; q < TILES_BLOCK / 32; q++) {
                 l = fminf(l, red[c][q]);
                 h = fmaxf(h, red[3 + c][q]);
             }
@@ -244,15 +243,15 @@ __device__ __forceinline__ void fold64(float &hi, float &lo, double v)
 /* Everything in this kernel is indexed by sorted position (p for i, q for
  * j); perm maps a position to the body index used by the FP64 arrays and the
  * event keys. */
-template <int K>
-__global__ void __launch_bounds__(NBG_MIX_BLOCK, 3)
+template <int BLOCK, int K, int JT, int UNROLL, int MINB>
+__global__ void __launch_bounds__(BLOCK, MINB)
 k_pair_mixed(BodyArrays A, DevCtl *ctl, SimSegs seg, const float4 *__restrict__ jhi, const float4 *__restrict__ jlo,
              const float4 *__restrict__ tile_c, const unsigned *__restrict__ perm, double *__restrict__ part,
              ll part_stride, ull *ev_keys, ll ev_cap)
 {
-    constexpr int JP = NBG_MIX_JT / 2; /* j pairs per tile */
-    constexpr int ITILE = NBG_MIX_BLOCK * K;
-    static_assert(ITILE == NBG_MIX_ITILE, "tile layout of k_begin");
+    constexpr int JP = JT / 2; /* j pairs per tile */
+    constexpr int ITILE = BLOCK * K;
+    static_assert(ITILE >= NBG_MIX_MIN_ITILE, "tile-origin buffer is sized for the smallest i-tile");
     __shared__ float4 sA[JP], sB[JP];
     __shared__ ll s_item;
     if (ctl->error) return;
@@ -278,7 +277,7 @@ k_pair_mixed(BodyArrays A, DevCtl *ctl, SimSegs seg, const float4 *__restrict__ 
         const ll t = local / S;
         const int split = (int)(local % S);
         const ll s0 = seg.off[sim], n = seg.off[sim + 1];
-        const ll jc = (((n - s0 + S - 1) / S) + NBG_MIX_JT - 1) / NBG_MIX_JT * NBG_MIX_JT;
+        const ll jc = (((n - s0 + S - 1) / S) + JT - 1) / JT * JT;
         const ll ibase = s0 + t * ITILE;
         const float4 c = tile_c[seg.mtile_off[sim] + t];
 
@@ -287,7 +286,7 @@ k_pair_mixed(BodyArrays A, DevCtl *ctl, SimSegs seg, const float4 *__restrict__ 
         float shx[K], slx[K], shy[K], sly[K], shz[K], slz[K];
 #pragma unroll
         for (int k = 0; k < K; k++) {
-            const ll p = ibase + (ll)k * NBG_MIX_BLOCK + tid;
+            const ll p = ibase + (ll)k * BLOCK + tid;
             float xr = 0.f, yr = 0.f, zr = 0.f, t = -1.f;
             if (p < n) {
                 const float4 h = jhi[p], l = jlo[p];
@@ -314,13 +313,13 @@ k_pair_mixed(BodyArrays A, DevCtl *ctl, SimSegs seg, const float4 *__restrict__ 
 
         const ll jb = s0 + (ll)split * jc;
         const ll je = jb + jc < n ? jb + jc : n;
-        for (ll jt = jb; jt < je; jt += NBG_MIX_JT) {
+        for (ll jt = jb; jt < je; jt += JT) {
             __syncthreads();
-            {
+            for (int sp = tid; sp < JP; sp += BLOCK) {
                 float v[2][4];
 #pragma unroll
                 for (int e = 0; e < 2; e++) {
-                    const ll q = jt + 2 * tid + e;
+                    const ll q = jt + 2 * sp + e;
                     if (q < je) {
                         const float4 h = jhi[q], l = jlo[q];
                         v[e][0] = (h.x - c.x) + l.x;
@@ -336,8 +335,8 @@ k_pair_mixed(BodyArrays A, DevCtl *ctl, SimSegs seg, const float4 *__restrict__ 
                         v[e][3] = 0.f;
                     }
                 }
-                sA[tid] = make_float4(v[0][0], v[1][0], v[0][1], v[1][1]);
-                sB[tid] = make_float4(v[0][2], v[1][2], v[0][3], v[1][3]);
+                sA[sp] = make_float4(v[0][0], v[1][0], v[0][1], v[1][1]);
+                sB[sp] = make_float4(v[0][2], v[1][2], v[0][3], v[1][3]);
             }
             __syncthreads();
 
@@ -348,7 +347,7 @@ k_pair_mixed(BodyArrays A, DevCtl *ctl, SimSegs seg, const float4 *__restrict__ 
                 ax[k] = ay[k] = az[k] = make_float2(0.f, 0.f);
                 mn[k] = 3.0e38f;
             }
-#pragma unroll 2
+#pragma unroll UNROLL
             for (int pp = 0; pp < JP; pp++) {
                 const float4 a = sA[pp], b = sB[pp];
                 const float2 xj = make_float2(a.x, a.y), yj = make_float2(a.z, a.w);
@@ -375,7 +374,7 @@ k_pair_mixed(BodyArrays A, DevCtl *ctl, SimSegs seg, const float4 *__restrict__ 
             for (int k = 0; k < K; k++) {
                 if (mn[k] < thr[k]) {
                     /* slow path: this tile holds a near or overlapping pair for i */
-                    const ll p = ibase + (ll)k * NBG_MIX_BLOCK + tid;
+                    const ll p = ibase + (ll)k * BLOCK + tid;
                     const ll i = perm[p];
                     const float4 hi_i = jhi[p], lo_i = jlo[p];
                     float tx = 0.f, ty = 0.f, tz = 0.f;
@@ -429,7 +428,7 @@ k_pair_mixed(BodyArrays A, DevCtl *ctl, SimSegs seg, const float4 *__restrict__ 
         }
 #pragma unroll
         for (int k = 0; k < K; k++) {
-            const ll p = ibase + (ll)k * NBG_MIX_BLOCK + tid;
+            const ll p = ibase + (ll)k * BLOCK + tid;
             if (p < n) {
                 double *o = part + (ll)split * 3 * part_stride;
                 o[p] = (double)shx[k] + (double)slx[k];
@@ -479,17 +478,48 @@ __global__ void k_mix_out(BodyArrays A, DevCtl *ctl, SimSegs seg, const unsigned
     }
 }
 
-static int g_mixed_slots_cache[64];
+/* ---- kernel shapes ---------------------------------------------------------
+ * (threads per CTA, i-bodies per thread, j per shared-memory tile, unroll of
+ * the j loop, CTAs per SM the register budget is set for).  Variant 0 is the
+ * default; the autotuner (nbg_autotune) measures the others. */
+#define MIX_VARIANTS(X)   \
+    X(0, 128, 4, 256, 2, 3) \
+    X(1, 128, 4, 256, 1, 3) \
+    X(2, 128, 2, 256, 2, 4) \
+    X(3, 256, 2, 256, 2, 2) \
+    X(4, 128, 4, 512, 2, 3) \
+    X(5, 64, 4, 256, 2, 6)  \
+    X(6, 128, 2, 128, 4, 4)
 
-int nbg_mixed_slots(int device)
+MixVariantInfo nbg_mix_variant_info(int variant)
 {
-    if (device >= 0 && device < 64 && g_mixed_slots_cache[device] > 0) return g_mixed_slots_cache[device];
+    switch (variant) {
+#define X(id, b, k, jt, u, mb) \
+    case id: return MixVariantInfo{b, k, jt, u};
+        MIX_VARIANTS(X)
+#undef X
+    default: return MixVariantInfo{0, 0, 0, 0};
+    }
+}
+
+static int g_mixed_slots_cache[64][NBG_MIX_VARIANTS];
+
+int nbg_mixed_slots(int device, int variant)
+{
+    if (variant < 0 || variant >= NBG_MIX_VARIANTS) variant = 0;
+    if (device >= 0 && device < 64 && g_mixed_slots_cache[device][variant] > 0)
+        return g_mixed_slots_cache[device][variant];
     int per_sm = 0, sms = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pair_mixed<NBG_MIX_K>, NBG_MIX_BLOCK, 0);
+    switch (variant) {
+#define X(id, b, k, jt, u, mb) \
+    case id: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pair_mixed<b, k, jt, u, mb>, b, 0); break;
+        MIX_VARIANTS(X)
+#undef X
+    }
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
     int slots = per_sm * sms;
     if (slots < 1) slots = 1;
-    if (device >= 0 && device < 64) g_mixed_slots_cache[device] = slots;
+    if (device >= 0 && device < 64) g_mixed_slots_cache[device][variant] = slots;
     return slots;
 }
 
@@ -506,15 +536,23 @@ void nbg_launch_mixed_prep(const CycleBufs &cb, DevCtl *ctl, cudaStream_t st)
     k_mix_reduce<<<fg, 256, 0, st>>>(cb.a, ctl, cb.seg);
     nbg_launch_spatial_sort(cb, ctl, st);
     k_mix_pack<<<fg, 256, 0, st>>>(cb.a, ctl, cb.perm, cb.jhi, cb.jlo);
-    ll tiles = (cb.cap + NBG_MIX_ITILE - 1) / NBG_MIX_ITILE + cb.seg.nsims;
+    const int itile = cb.itile > 0 ? cb.itile : NBG_MIX_ITILE;
+    ll tiles = (cb.cap + itile - 1) / itile + cb.seg.nsims;
     if (tiles > 152 * 64) tiles = 152 * 64;
-    k_mix_tiles<<<(int)tiles, NBG_MIX_BLOCK, 0, st>>>(ctl, cb.seg, cb.jhi, cb.jlo, cb.tile_c);
+    k_mix_tiles<<<(int)tiles, TILES_BLOCK, 0, st>>>(ctl, cb.seg, cb.jhi, cb.jlo, cb.tile_c, itile);
 }
 
 void nbg_launch_mixed_pair(const CycleBufs &cb, DevCtl *ctl, cudaStream_t st)
 {
-    k_pair_mixed<NBG_MIX_K><<<cb.slots, NBG_MIX_BLOCK, 0, st>>>(cb.a, ctl, cb.seg, cb.jhi, cb.jlo, cb.tile_c,
-                                                               cb.perm, cb.part, cb.cap, cb.ev_keys, cb.ev_cap);
+    switch (cb.mix_variant) {
+#define X(id, b, k, jt, u, mb)                                                                                   \
+    case id:                                                                                                     \
+        k_pair_mixed<b, k, jt, u, mb><<<cb.slots, b, 0, st>>>(cb.a, ctl, cb.seg, cb.jhi, cb.jlo, cb.tile_c, cb.perm, \
+                                                             cb.part, cb.cap, cb.ev_keys, cb.ev_cap);            \
+        break;
+        MIX_VARIANTS(X)
+#undef X
+    }
 }
 
 void nbg_launch_mixed_out(const CycleBufs &cb, DevCtl *ctl, cudaStream_t st)

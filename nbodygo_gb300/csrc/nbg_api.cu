@@ -227,7 +227,8 @@ static int ensure_cap(nbg_ctx *ctx, ll need, ll keep)
     ctx->cb.nblk_cap = nblk;
     CK(cudaMalloc((void **)&ctx->cb.jhi, (size_t)cap * sizeof(float4)));
     CK(cudaMalloc((void **)&ctx->cb.jlo, (size_t)cap * sizeof(float4)));
-    ll tiles = (cap + NBG_MIX_ITILE - 1) / NBG_MIX_ITILE;
+    /* every sim may end in a partial tile: at most cap / itile + nsims tiles */
+    ll tiles = (cap + NBG_MIX_MIN_ITILE - 1) / NBG_MIX_MIN_ITILE + NBG_MAX_SIMS + 1;
     CK(cudaMalloc((void **)&ctx->cb.tile_c, (size_t)tiles * sizeof(float4)));
     CK(cudaMalloc((void **)&ctx->cb.part, (size_t)ctx->cb.split_cap * 3 * (size_t)cap * sizeof(double)));
     CK(cudaMalloc((void **)&ctx->cb.perm, (size_t)cap * sizeof(unsigned)));
@@ -439,7 +440,9 @@ int nbg_create(int device, int precision, int64_t capacity, nbg_ctx **out)
             break;
         }
         ctx->cb.split_cap = 32;
-        ctx->cb.slots = nbg_mixed_slots(device);
+        ctx->cb.mix_variant = 0;
+        ctx->cb.itile = nbg_mix_variant_info(0).block * nbg_mix_variant_info(0).k;
+        ctx->cb.slots = nbg_mixed_slots(device, 0);
         if ((rc = ensure_cap(ctx, capacity > 0 ? capacity : 1024, 0)) != NBG_OK) break;
         if ((rc = ensure_frag_cap(ctx, 4096)) != NBG_OK) break;
         if ((rc = ensure_adds_cap(ctx, 1024)) != NBG_OK) break;
@@ -936,6 +939,106 @@ int nbg_force_pass(nbg_ctx *ctx)
     return NBG_OK;
 }
 
+static int select_variant(nbg_ctx *ctx, int v)
+{
+    if (v < 0 || v >= NBG_MIX_VARIANTS) return fail(ctx, NBG_E_ARG, "unknown kernel shape");
+    const MixVariantInfo vi = nbg_mix_variant_info(v);
+    ctx->cb.mix_variant = v;
+    ctx->cb.itile = vi.block * vi.k;
+    ctx->cb.slots = nbg_mixed_slots(ctx->device, v);
+    invalidate_graph(ctx);
+    return NBG_OK;
+}
+
+/* Device time of the mixed pair kernel in one force pass of the current
+ * collection (CUDA events around the kernel on the context's stream). */
+static int time_mixed_pair(nbg_ctx *ctx, float *ms)
+{
+    cudaEvent_t e0 = get_event(ctx, 0), e1 = get_event(ctx, 1);
+    int z = 0;
+    CK(cudaMemcpyAsync(&ctx->ctl->error, &z, sizeof z, cudaMemcpyHostToDevice, ctx->st));
+    nbg_launch_begin(ctx->cb, ctx->ctl, ctx->st);
+    nbg_launch_mixed_prep(ctx->cb, ctx->ctl, ctx->st);
+    CK(cudaEventRecord(e0, ctx->st));
+    nbg_launch_mixed_pair(ctx->cb, ctx->ctl, ctx->st);
+    CK(cudaEventRecord(e1, ctx->st));
+    nbg_launch_mixed_out(ctx->cb, ctx->ctl, ctx->st);
+    CK(cudaGetLastError());
+    CK(cudaEventSynchronize(e1));
+    CK(cudaEventElapsedTime(ms, e0, e1));
+    return NBG_OK;
+}
+
+static std::string tune_key(nbg_ctx *ctx, ll n)
+{
+    cudaDeviceProp p;
+    cudaGetDeviceProperties(&p, ctx->device);
+    int bucket = 0;
+    while (((ll)1 << (bucket + 1)) <= n) bucket++;
+    int sb = 0;
+    while ((1 << (sb + 1)) <= ctx->cb.seg.nsims) sb++;
+    std::string name(p.name);
+    for (char &c : name)
+        if (c == ' ') c = '_';
+    char buf[256];
+    snprintf(buf, sizeof buf, "%s|sm%d|n2^%d|sims2^%d", name.c_str(), p.multiProcessorCount, bucket, sb);
+    return buf;
+}
+
+int nbg_autotune(nbg_ctx *ctx, const char *cache_path, int *variant, double *best_ms)
+{
+    if (!ctx) return NBG_E_ARG;
+    CK(cudaSetDevice(ctx->device));
+    int rc = sync_ctl(ctx);
+    if (rc != NBG_OK) return rc;
+    const ll n = ctx->ctl_h->n;
+    if (n <= 0) return fail(ctx, NBG_E_STATE, "autotune needs a loaded collection");
+    const std::string key = tune_key(ctx, n);
+    int best = -1;
+    double best_t = 0;
+    if (cache_path) {
+        if (FILE *f = fopen(cache_path, "r")) {
+            char k[256];
+            int v;
+            double t;
+            while (fscanf(f, "%255s %d %lf", k, &v, &t) == 3)
+                if (key == k && v >= 0 && v < NBG_MIX_VARIANTS) {
+                    best = v;
+                    best_t = t;
+                }
+            fclose(f);
+        }
+    }
+    if (best < 0) {
+        const int prev = ctx->cb.mix_variant;
+        for (int v = 0; v < NBG_MIX_VARIANTS; v++) {
+            if ((rc = select_variant(ctx, v)) != NBG_OK) return rc;
+            float ms = 0, t = 1e30f;
+            for (int rep = 0; rep < 4; rep++) {
+                if ((rc = time_mixed_pair(ctx, &ms)) != NBG_OK) {
+                    select_variant(ctx, prev);
+                    return rc;
+                }
+                if (rep > 0 && ms < t) t = ms; /* the first run warms up */
+            }
+            if (best < 0 || t < best_t) {
+                best = v;
+                best_t = t;
+            }
+        }
+        if (cache_path) {
+            if (FILE *f = fopen(cache_path, "a")) {
+                fprintf(f, "%s %d %.6f\n", key.c_str(), best, best_t);
+                fclose(f);
+            }
+        }
+    }
+    if ((rc = select_variant(ctx, best)) != NBG_OK) return rc;
+    if (variant) *variant = best;
+    if (best_ms) *best_ms = best_t;
+    return NBG_OK;
+}
+
 int nbg_get_renderables(nbg_ctx *ctx, nbg_renderable *host, int64_t cap, int64_t *n)
 {
     if (!ctx || cap < 0) return fail(ctx, NBG_E_ARG, "bad arguments");
@@ -1041,6 +1144,8 @@ int nbg_set_option(nbg_ctx *ctx, int key, int64_t value)
     case NBG_OPT_GRAPH:
         ctx->use_graph = value != 0;
         return NBG_OK;
+    case NBG_OPT_MIX_SHAPE:
+        return select_variant(ctx, (int)value);
     case NBG_OPT_GRAPH_CYCLES:
         if (value < 1 || value > 1000) return fail(ctx, NBG_E_ARG, "cycles per graph must be 1..1000");
         if (value != ctx->graph_cycles) {

@@ -167,7 +167,16 @@ struct CycleBufs {
     ll *shist;          /* radix-sort digit histogram / offsets */
     int split_cap;
     int slots;          /* resident CTAs of the mixed kernel on this device */
+    int mix_variant;    /* shape of the mixed pair kernel (see nbg_mix_variant_info) */
+    int itile;          /* i-bodies per work item of that shape */
 };
+
+/* Shapes of the mixed pair kernel the autotuner chooses from. */
+struct MixVariantInfo {
+    int block, k, jt, unroll;
+};
+#define NBG_MIX_VARIANTS 7
+#define NBG_MIX_MIN_ITILE 256
 
 #define NBG_SCAN_BLOCK 1024
 #define NBG_SCAN_ITEMS 4
@@ -193,7 +202,8 @@ int nbg_pair_fp64_grid(ll cap);
 void nbg_launch_mixed_prep(const CycleBufs &cb, DevCtl *ctl, cudaStream_t st);
 void nbg_launch_mixed_pair(const CycleBufs &cb, DevCtl *ctl, cudaStream_t st);
 void nbg_launch_mixed_out(const CycleBufs &cb, DevCtl *ctl, cudaStream_t st);
-int nbg_mixed_slots(int device);
+int nbg_mixed_slots(int device, int variant);
+MixVariantInfo nbg_mix_variant_info(int variant);
 
 /* k_sort.cu */
 void nbg_launch_spatial_sort(const CycleBufs &cb, DevCtl *ctl, cudaStream_t st);

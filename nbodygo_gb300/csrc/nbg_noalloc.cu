@@ -120,7 +120,9 @@ extern "C" int nbg_forces_mixed_noalloc(const double *x, const double *y, const 
     cb.ev_keys = nullptr; /* events are discarded */
     cb.ev_cap = 0;
     cb.split_cap = NOALLOC_SPLITS;
-    cb.slots = nbg_mixed_slots(dev);
+    cb.mix_variant = 0; /* the default shape: 512-body i-tiles */
+    cb.itile = NBG_MIX_ITILE;
+    cb.slots = nbg_mixed_slots(dev, 0);
     cb.seg = nbg_seg_carve(base + OFF_SEG, 1);
     DevCtl *ctl = (DevCtl *)(base + OFF_CTL);
 

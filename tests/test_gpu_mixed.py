@@ -137,3 +137,27 @@ def test_near_pairs_in_fp64_keep_error_down():
         errs[ppm] = rel_l2(sim.force_pass(), g)
     assert errs[70000] <= TOL
     assert errs[70000] <= errs[0]
+
+
+def test_every_kernel_shape_gives_the_same_physics():
+    """All compiled shapes of the mixed pair kernel agree with FP64 within
+    the tolerance and detect the same events; the autotuner picks one."""
+    b = dense_cluster(300, seed=51)
+    ora = OracleSim(threads=8)
+    ora.set_bodies(b)
+    g = ora.forces()
+    for shape in range(A.MIX_SHAPES):
+        sim = Simulation("mixed")
+        sim.set_option(A.OPT_MIX_SHAPE, shape)
+        sim.set_bodies(b)
+        assert rel_l2(sim.force_pass(), g) <= TOL, f"shape {shape}"
+        sim.step(0.05, 1.0, 1)
+        assert len(sim.events()) > 0
+    big = W.plummer_disk(n_each=4096, seed=7)
+    sim = Simulation("mixed")
+    sim.set_bodies(big)
+    shape, ms = sim.autotune()
+    assert 0 <= shape < A.MIX_SHAPES and ms > 0
+    ora = OracleSim(threads=8)
+    ora.set_bodies(big)
+    assert rel_l2(sim.force_pass(), ora.forces()) <= TOL
