@@ -1,0 +1,264 @@
+/*
+ * The reference's own Go tests of the body collection, the body and the
+ * runner, restated against the C++ mirror (include/nbodygo.hpp) over
+ * libnbgpu.so:
+ *
+ *   TestMod                      cmd/body/body_test.go:9-47
+ *   TestInitSize                 cmd/body/body_collection_test.go:61-67
+ *   TestRemove                   cmd/body/body_collection_test.go:73-89
+ *   TestGetByID / ByName         cmd/body/body_collection_test.go:94-148
+ *   TestModByID / NoMatch /      cmd/body/body_collection_test.go:154-262
+ *     ByName / ByClass
+ *   TestAdds                     cmd/body/body_collection_test.go:268-282
+ *   TestRunnerSetters            cmd/runner/computation-runner_test.go:10-31
+ *
+ * The bodies are those of createTestBody (body_collection_test.go:26-54):
+ * every field equal to the id, Name = Class = string(rune(id)).  The Go
+ * tests call Cycle/ProcessMods alone; here the whole cycle runs, so bodies
+ * that must not collide are given collision=none (no events, body.go:175-178).
+ *
+ * Usage: test_mirror host   - parsing and ApplyMods, no GPU
+ *        test_mirror gpu    - everything, on device 0
+ * Prints one line per test and exits non-zero on the first failure.
+ */
+#include <cstdio>
+#include <string>
+#include <vector>
+
+#include "nbodygo.hpp"
+
+using namespace nbodygo;
+
+static int g_fail = 0;
+#define CHECK(cond, what)                                                                                        \
+    do {                                                                                                         \
+        if (!(cond)) {                                                                                           \
+            std::printf("FAIL %s: %s (line %d)\n", cur_test, what, __LINE__);                                    \
+            g_fail = 1;                                                                                          \
+            return;                                                                                              \
+        }                                                                                                        \
+    } while (0)
+static const char *cur_test = "";
+
+/* Go's string(int): the UTF-8 encoding of the code point */
+static std::string go_string(int cp)
+{
+    std::string s;
+    if (cp < 0x80) s += (char)cp;
+    else if (cp < 0x800) {
+        s += (char)(0xC0 | (cp >> 6));
+        s += (char)(0x80 | (cp & 0x3F));
+    } else if (cp < 0x10000) {
+        s += (char)(0xE0 | (cp >> 12));
+        s += (char)(0x80 | ((cp >> 6) & 0x3F));
+        s += (char)(0x80 | (cp & 0x3F));
+    } else {
+        s += (char)(0xF0 | (cp >> 18));
+        s += (char)(0x80 | ((cp >> 12) & 0x3F));
+        s += (char)(0x80 | ((cp >> 6) & 0x3F));
+        s += (char)(0x80 | (cp & 0x3F));
+    }
+    return s;
+}
+
+static Body createTestBody(int id, CollisionBehavior beh = Elastic)
+{
+    Body b;
+    b.Id = id;
+    b.Name = b.Class = go_string(id);
+    b.X = b.Y = b.Z = b.Vx = b.Vy = b.Vz = b.Radius = b.Mass = b.FragFactor = b.FragStep = (double)id;
+    b.Behavior = beh;
+    b.Color = Red;
+    return b;
+}
+
+static std::vector<Body> createTestBodies(int cnt, CollisionBehavior beh = Elastic)
+{
+    std::vector<Body> v;
+    v.reserve(cnt);
+    for (int i = 0; i < cnt; i++) v.push_back(createTestBody(i, beh));
+    return v;
+}
+
+static void TestMod()
+{
+    cur_test = "TestMod";
+    Body b = createTestBody(1);
+    b.ApplyMods({"x=41", "y=42", "z=43", "vx=44", "vy=45", "vz=46", "mass=47", "radius=48", "frag-factor=49",
+                 "frag-step=50", "collision=subsume", "color=green", "telemetry=true", "exists=false"});
+    CHECK(b.X == 41 && b.Y == 42 && b.Z == 43 && b.Vx == 44 && b.Vy == 45 && b.Vz == 46, "position/velocity");
+    CHECK(b.Mass == 47 && b.Radius == 48 && b.FragFactor == 49 && b.FragStep == 50, "mass/radius/frag");
+    CHECK(b.Behavior == Subsume && b.Color == Green && b.WithTelemetry && !b.Exists, "enums/bools");
+    std::printf("ok   %s\n", cur_test);
+}
+
+static void TestParse()
+{
+    cur_test = "TestParse";
+    CHECK(ParseCollisionBehavior("FRAGMENT") == Fragment && ParseCollisionBehavior("bogus") == Elastic,
+          "ParseCollisionBehavior");
+    CHECK(ParseBoolean("Yes") && ParseBoolean("1") && !ParseBoolean("on"), "ParseBoolean");
+    CHECK(ParseBodyColor("LightGray") == Lightgray && ParseBodyColor("teal") == Random, "ParseBodyColor");
+    CHECK(SafeParseFloat("2.5e3", 1) == 2500 && SafeParseFloat("12abc", 7) == 7 && SafeParseFloat("", 3) == 3 &&
+              SafeParseFloat(" 1", 4) == 4,
+          "SafeParseFloat");
+    Body b = createTestBody(3);
+    b.ApplyMods({"x=1=2", "mass=heavy", "nosuch=1", "RADIUS=9"});
+    CHECK(b.X == 3 && b.Mass == 3 && b.Radius == 9, "malformed mods are ignored");
+    Body sun = createTestBody(4);
+    sun.IsSun = true;
+    sun.Color = White;
+    sun.ApplyMods({"color=blue"});
+    CHECK(sun.Color == White, "suns keep their colour");
+    std::printf("ok   %s\n", cur_test);
+}
+
+static void TestInitSize()
+{
+    cur_test = "TestInitSize";
+    const int cnt = 1000000;
+    BodyCollection bc(createTestBodies(cnt));
+    CHECK(bc.Count() == cnt, "Incorrect body count");
+    std::printf("ok   %s\n", cur_test);
+}
+
+static void TestRemove()
+{
+    cur_test = "TestRemove";
+    const int cnt = 1000, idToDelete = 10;
+    BodyCollection bc(createTestBodies(cnt, None));
+    CHECK(bc.ModBody(idToDelete, "", "", {"exists=false"}) == ModAll, "mod");
+    ComputationRunner cr(1, 1e-9, false, bc);
+    cr.RunOneComputation();
+    CHECK(bc.Count() == cnt - 1, "Body was not removed");
+    for (const Body &b : bc.GetArray()) CHECK(b.Id != idToDelete, "Body should have been removed");
+    std::printf("ok   %s\n", cur_test);
+}
+
+static void TestGetByID()
+{
+    cur_test = "TestGetByID";
+    BodyCollection bc(createTestBodies(1000));
+    auto b = bc.GetBody(10, "");
+    CHECK(b != nullptr, "Got nil body");
+    CHECK(b->Id == 10, "Got wrong body");
+    std::printf("ok   %s\n", cur_test);
+}
+
+static void TestGetByName()
+{
+    cur_test = "TestGetByName";
+    BodyCollection bc(createTestBodies(2000));
+    auto b = bc.GetBody(-1, go_string(1999));
+    CHECK(b != nullptr, "Got nil body");
+    CHECK(b->Id == 1999, "Got wrong body");
+    std::printf("ok   %s\n", cur_test);
+}
+
+static void mod_test(const char *name, int id, const std::string &nm, const std::string &cls, int idToGet,
+                     ModBodyResult want)
+{
+    cur_test = name;
+    BodyCollection bc(createTestBodies(1000));
+    ModBodyResult r = bc.ModBody(id, nm, cls, {"color=blue"});
+    CHECK(r == want, "Mod body failed");
+    if (want == ModAll) {
+        std::vector<Body> arr = bc.GetArray();
+        CHECK(arr[idToGet].Color == Blue, "Body modification failed");
+    }
+    std::printf("ok   %s\n", cur_test);
+}
+
+static void TestModPhysical()
+{
+    cur_test = "TestModPhysical";
+    BodyCollection bc(createTestBodies(100));
+    CHECK(bc.ModBody(7, "", "", {"x=-5", "mass=123.5", "collision=fragment", "telemetry=yes"}) == ModAll, "mod");
+    auto b = bc.GetBody(7, "");
+    CHECK(b && b->X == -5 && b->Mass == 123.5 && b->Behavior == Fragment && b->WithTelemetry && b->Y == 7,
+          "numeric mods reach the device copy");
+    std::printf("ok   %s\n", cur_test);
+}
+
+static void TestAdds()
+{
+    cur_test = "TestAdds";
+    const int cnt = 500, idToAdd = 600;
+    BodyCollection bc(createTestBodies(cnt, None));
+    bc.EnqueueAdd(createTestBody(idToAdd, None));
+    ComputationRunner cr(1, 1e-9, false, bc);
+    cr.RunOneComputation();
+    bool found = false;
+    for (const Body &b : bc.GetArray()) found |= b.Id == idToAdd;
+    CHECK(found, "Body was not added");
+    CHECK(bc.Count() == cnt + 1, "count after add");
+    std::printf("ok   %s\n", cur_test);
+}
+
+static void TestRunnerSetters()
+{
+    cur_test = "TestRunnerSetters";
+    BodyCollection bc(std::vector<Body>{});
+    ComputationRunner cr(1, 1, false, bc);
+    cr.SetCoefficientOfRestitution(5);
+    cr.SetTimeScaling(5);
+    cr.SetWorkers(5);
+    cr.RunOneComputation(); /* the setters are picked up at the start of a cycle */
+    CHECK(cr.CoefficientOfRestitution() == 5 && cr.TimeScaling() == 5 && cr.WorkerCount() == 5, "Setters failed");
+    bool threw = false;
+    try {
+        ComputationRunner bh(1, 1, true, bc);
+    } catch (const Error &e) {
+        threw = e.code == NBG_E_ARG;
+    }
+    CHECK(threw, "Barnes-Hut is refused");
+    std::printf("ok   %s\n", cur_test);
+}
+
+static void TestRunnerCycle()
+{
+    cur_test = "TestRunnerCycle";
+    /* two bodies at rest attract: after one cycle each moved toward the other */
+    std::vector<Body> v;
+    v.push_back(NewBody(1, -1, 0, 0, 0, 0, 0, 1e10, 0.1, None, Random, 0, 0, false, "a", "", false));
+    v.push_back(NewBody(2, 1, 0, 0, 0, 0, 0, 1e10, 0.1, None, Random, 0, 0, false, "b", "", false));
+    BodyCollection bc(v);
+    ComputationRunner cr(4, 0.5, false, bc);
+    std::vector<nbg_renderable> rend = cr.RunOneComputation();
+    CHECK(rend.size() == 2, "renderables");
+    std::vector<Body> arr = bc.GetArray();
+    CHECK(arr.size() == 2 && arr[0].X > -1 && arr[1].X < 1 && arr[0].Vx > 0 && arr[1].Vx < 0, "attraction");
+    CHECK(arr[0].X == -arr[1].X && arr[0].Vx == -arr[1].Vx, "symmetry");
+    cr.RemoveBodies(-1);
+    cr.RunOneComputation();
+    CHECK(bc.Count() == 0, "RemoveBodies(-1) empties the collection");
+    std::printf("ok   %s\n", cur_test);
+}
+
+int main(int argc, char **argv)
+{
+    const std::string mode = argc > 1 ? argv[1] : "host";
+    TestMod();
+    TestParse();
+    if (mode == "gpu" && !g_fail) {
+        try {
+            TestInitSize();
+            TestRemove();
+            TestGetByID();
+            TestGetByName();
+            mod_test("TestModByID", 10, "", "", 10, ModAll);
+            mod_test("TestModByIDNoMatch", 2000, "", "", 0, NoMatch);
+            mod_test("TestModByName", -1, go_string(10), "", 10, ModAll);
+            mod_test("TestModByClass", -1, "", go_string(10), 10, ModAll);
+            TestModPhysical();
+            TestAdds();
+            TestRunnerSetters();
+            TestRunnerCycle();
+        } catch (const Error &e) {
+            std::printf("FAIL %s: nbg status %d: %s\n", cur_test, e.code, e.what());
+            g_fail = 1;
+        }
+    }
+    std::printf(g_fail ? "FAILED\n" : "PASSED\n");
+    return g_fail;
+}
