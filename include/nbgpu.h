@@ -277,7 +277,7 @@ int nbg_enable_timing(nbg_ctx *ctx, int on);
 int nbg_get_timing(nbg_ctx *ctx, nbg_timing *t);
 
 /* Tuning knobs of the pair kernels (0 = default). */
-#define NBG_OPT_SPLIT 1      /* mixed: j-range splits per i-tile */
+#define NBG_OPT_SPLIT 1      /* mixed: most CTAs the pair work is divided among (0 = all resident) */
 #define NBG_OPT_GRAPH 2      /* 0 = launch each cycle directly, 1 = CUDA graph */
 #define NBG_OPT_EV_CAP 3     /* event-list capacity (rounded up to a power of two) */
 #define NBG_OPT_FRAG_CAP 4   /* fragments one cycle may emit */

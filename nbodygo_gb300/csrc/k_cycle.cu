@@ -75,10 +75,12 @@ __device__ static ll block_scan_array(int ns, F f, ll *out)
 /* ------------------------------------------------------------------------ */
 
 /* Per-cycle resets and the work layout of every sim: 64-body tiles of the
- * plain kernel, 512-body i-tiles, j-range splits and work items of the
- * mixed kernel, and the interaction count.  One block. */
-__global__ void __launch_bounds__(NBG_SCAN_BLOCK) k_begin(DevCtl *ctl, SimSegs seg, int split_cap, int slots,
-                                                          int itile)
+ * plain kernel; i-tiles and the pair work of the mixed kernel, and how many
+ * CTAs share it (P: at most the resident CTAs or work_cap, at least
+ * NBG_MIX_MIN_WORK units each, and few enough that the partial-sum slots fit
+ * in part_doubles); the interaction count.  One block. */
+__global__ void __launch_bounds__(NBG_SCAN_BLOCK) k_begin(DevCtl *ctl, SimSegs seg, int slots, int work_cap, int itile,
+                                                          ll part_doubles)
 {
     if (ctl->error) return;
     const int ns = seg.nsims;
@@ -91,16 +93,15 @@ __global__ void __launch_bounds__(NBG_SCAN_BLOCK) k_begin(DevCtl *ctl, SimSegs s
     block_scan_array(ns, [&](int s) { return (off[s + 1] - off[s] + 63) / 64; }, seg.tile_off);
     const ll mtiles = block_scan_array(
         ns, [&](int s) { return (off[s + 1] - off[s] + itile - 1) / itile; }, seg.mtile_off);
-    ll S = mtiles > 0 ? (8ll * slots + mtiles - 1) / mtiles : 1;
-    if (S > split_cap) S = split_cap;
-    if (S < 1) S = 1;
-    for (int s = threadIdx.x; s < ns; s += NBG_SCAN_BLOCK) {
-        const ll jt = (off[s + 1] - off[s] + NBG_MIX_JT - 1) / NBG_MIX_JT;
-        seg.splits[s] = (int)(jt < S ? jt : S);
-    }
-    __syncthreads();
-    block_scan_array(
-        ns, [&](int s) { return (seg.mtile_off[s + 1] - seg.mtile_off[s]) * (ll)seg.splits[s]; }, seg.item_off);
+    const ll W = block_scan_array(
+        ns, [&](int s) { return (seg.mtile_off[s + 1] - seg.mtile_off[s]) * (off[s + 1] - off[s]); }, seg.item_off);
+    ll P = slots;
+    if (work_cap > 0 && P > work_cap) P = work_cap;
+    if (P > W / NBG_MIX_MIN_WORK) P = W / NBG_MIX_MIN_WORK;
+    const ll part_slots = part_doubles / (3ll * itile);
+    if (P > part_slots - mtiles + 1) P = part_slots - mtiles + 1;
+    if (P < 1) P = 1;
+    const bool part_short = mtiles + P - 1 > part_slots;
     /* interactions: sum of n_s (n_s - 1), reusing the keep_start array */
     const ll inter = block_scan_array(
         ns, [&](int s) { const ll m = off[s + 1] - off[s]; return m * (m > 0 ? m - 1 : 0); }, seg.keep_start);
@@ -115,9 +116,14 @@ __global__ void __launch_bounds__(NBG_SCAN_BLOCK) k_begin(DevCtl *ctl, SimSegs s
         ctl->rmax_bits = 0;
         ctl->xmax_bits = 0;
         ctl->m_scale = 0.0;
-        ctl->splits = (int)S;
-        ctl->work_next = 0;
+        ctl->splits = (int)P;
+        ctl->work_total = W;
         ctl->cycle_interactions = inter;
+        if (part_short) {
+            ctl->error = NBG_E_OVERFLOW;
+            ctl->error_what = 4;
+            ctl->error_need = (mtiles + P - 1) * 3ll * itile;
+        }
     }
 }
 
@@ -622,45 +628,119 @@ __device__ static ll lower_bound_u64(const ull *keys, ll cnt, ull v)
     return lo;
 }
 
-/* ProcessMods: every sim walks its own events newest first, one thread per
- * sim.  Events of one sim only touch that sim's bodies and the sorted keys
- * are grouped by sim (i ranges), so this is the sequential order of each sim
- * exactly.  ev_out holds the sims one after another, each in resolution
- * order. */
-__global__ void k_resolve(BodyArrays A, DevCtl *ctl, SimSegs seg, const ull *keys, nbg_event *ev_out)
+/* ProcessMods (body_collection.go:213-235): each sim resolves its own events
+ * newest first.  Events of one sim only touch that sim's bodies, and the
+ * sorted keys are grouped by sim (i ranges).
+ *
+ * One CTA per sim.  Resolving an event reads and writes only its two bodies,
+ * so the sequential order only matters between events that share a body:
+ * the CTA resolves in rounds, and in each round every pending event that is
+ * the oldest pending one (in processing order) on both of its bodies is
+ * resolved, all such events in parallel.  Every body sees its events in the
+ * sequential order, so the result is the sequential result bit for bit.
+ * owner[] (one word per body; any contents on entry) holds, per round, the
+ * smallest pending processing index that touches the body.  ev_out holds the
+ * sims one after another, each in processing order; its pad field marks
+ * pending events during the kernel and is 0 on return. */
+#define RESOLVE_BLOCK 256
+
+__device__ static void event_bodies(ull key, ll &b1, ll &b2, unsigned &type)
 {
+    const ll i = (ll)(key >> 32);
+    const ll j = (ll)((key >> 2) & 0x3fffffffull);
+    type = (unsigned)(key & 3ull);
+    b1 = i;
+    b2 = j;
+    if (type == NBG_EVT_SUB_JI) {
+        b1 = j;
+        b2 = i;
+    }
+}
+
+__device__ static void resolve_one(BodyArrays &A, ull key, nbg_event *out)
+{
+    ll b1, b2;
+    unsigned type;
+    event_bodies(key, b1, b2, type);
+    nbg_event e;
+    e.id1 = A.id[b1];
+    e.id2 = A.id[b2];
+    e.type = type == NBG_EVT_COLL_IJ ? NBG_EV_COLLISION : NBG_EV_SUBSUME;
+    e.pad = 0;
+    if (type == NBG_EVT_COLL_IJ)
+        resolve_collision(A, b1, b2);
+    else
+        resolve_subsume(A, b1, b2);
+    *out = e;
+}
+
+__global__ void __launch_bounds__(RESOLVE_BLOCK) k_resolve(BodyArrays A, DevCtl *ctl, SimSegs seg, const ull *keys,
+                                                           nbg_event *ev_out, unsigned *owner)
+{
+    __shared__ int s_left, s_done;
     if (ctl->error) return;
     const ll cnt = ctl->ev_count;
-    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < seg.nsims; s += gridDim.x * blockDim.x) {
-        const ll lo = seg.nsims == 1 ? 0 : lower_bound_u64(keys, cnt, (ull)seg.off[s] << 32);
-        const ll hi = seg.nsims == 1 ? cnt : lower_bound_u64(keys, cnt, (ull)seg.off[s + 1] << 32);
-        for (ll k = hi - 1; k >= lo; k--) {
-            const ull key = keys[k];
-            const ll i = (ll)(key >> 32);
-            const ll j = (ll)((key >> 2) & 0x3fffffffull);
-            const unsigned type = (unsigned)(key & 3ull);
-            ll b1 = i, b2 = j;
-            if (type == NBG_EVT_SUB_JI) {
-                b1 = j;
-                b2 = i;
-            }
-            nbg_event e;
-            e.id1 = A.id[b1];
-            e.id2 = A.id[b2];
-            e.type = type == NBG_EVT_COLL_IJ ? NBG_EV_COLLISION : NBG_EV_SUBSUME;
-            e.pad = 0;
-            ev_out[lo + (hi - 1 - k)] = e;
-            if (type == NBG_EVT_COLL_IJ)
-                resolve_collision(A, b1, b2);
-            else
-                resolve_subsume(A, b1, b2);
-        }
-    }
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
+    const int s = blockIdx.x;
+    const int tid = threadIdx.x;
+    if (s == 0 && tid == 0) {
         ctl->next_id += ctl->frag_total; /* fragments took ids next_id .. next_id+total-1 */
         ctl->last_ev_n = cnt;
         ctl->acc_events += cnt;
         ctl->acc_frags += ctl->frag_total;
+    }
+    if (s >= seg.nsims) return;
+    const ll lo = seg.nsims == 1 ? 0 : lower_bound_u64(keys, cnt, (ull)seg.off[s] << 32);
+    const ll hi = seg.nsims == 1 ? cnt : lower_bound_u64(keys, cnt, (ull)seg.off[s + 1] << 32);
+    const ll m = hi - lo;
+    if (m <= 0) return;
+    if (m == 1) {
+        if (tid == 0) resolve_one(A, keys[lo], &ev_out[lo]);
+        return;
+    }
+    /* processing index p is keys[hi - 1 - p], written to ev_out[lo + p] */
+    for (ll p = tid; p < m; p += RESOLVE_BLOCK) ev_out[lo + p].pad = 1;
+    if (tid == 0) s_left = (int)(m < 0x7fffffff ? m : 0x7fffffff);
+    __syncthreads();
+    for (ll round = 0; round < m; round++) {
+        for (ll p = tid; p < m; p += RESOLVE_BLOCK) {
+            if (ev_out[lo + p].pad) {
+                ll b1, b2;
+                unsigned ty;
+                event_bodies(keys[hi - 1 - p], b1, b2, ty);
+                owner[b1] = 0xffffffffu;
+                owner[b2] = 0xffffffffu;
+            }
+        }
+        __syncthreads();
+        for (ll p = tid; p < m; p += RESOLVE_BLOCK) {
+            if (ev_out[lo + p].pad) {
+                ll b1, b2;
+                unsigned ty;
+                event_bodies(keys[hi - 1 - p], b1, b2, ty);
+                atomicMin(&owner[b1], (unsigned)p);
+                atomicMin(&owner[b2], (unsigned)p);
+            }
+        }
+        if (tid == 0) s_done = 0;
+        __syncthreads();
+        int done = 0;
+        for (ll p = tid; p < m; p += RESOLVE_BLOCK) {
+            if (ev_out[lo + p].pad) {
+                const ull key = keys[hi - 1 - p];
+                ll b1, b2;
+                unsigned ty;
+                event_bodies(key, b1, b2, ty);
+                if (owner[b1] == (unsigned)p && owner[b2] == (unsigned)p) {
+                    resolve_one(A, key, &ev_out[lo + p]); /* clears pad */
+                    done++;
+                }
+            }
+        }
+        if (done) atomicAdd(&s_done, done);
+        __syncthreads();
+        if (tid == 0) s_left -= s_done;
+        __syncthreads();
+        if (s_left <= 0) break;
     }
 }
 
@@ -967,7 +1047,8 @@ static int flat_grid(ll cap)
 
 void nbg_launch_begin(const CycleBufs &cb, DevCtl *ctl, cudaStream_t st)
 {
-    k_begin<<<1, NBG_SCAN_BLOCK, 0, st>>>(ctl, cb.seg, cb.split_cap, cb.slots, cb.itile > 0 ? cb.itile : 512);
+    k_begin<<<1, NBG_SCAN_BLOCK, 0, st>>>(ctl, cb.seg, cb.slots, cb.work_cap, cb.itile > 0 ? cb.itile : NBG_MIX_ITILE,
+                                          cb.part_doubles);
 }
 
 void nbg_launch_frag_count(const CycleBufs &cb, DevCtl *ctl, cudaStream_t st)
@@ -995,7 +1076,8 @@ void nbg_launch_after_pair(const CycleBufs &cb, DevCtl *ctl, cudaStream_t st)
     const int sg = scan_grid(cb.cap);
     k_sort_events<<<1, SORT_BLOCK, 0, st>>>(ctl, cb.ev_keys, cb.ev_cap);
     k_frag_emit<<<sg, NBG_SCAN_BLOCK, 0, st>>>(cb.a, cb.frags, ctl, cb.blk_off);
-    k_resolve<<<(cb.seg.nsims + 63) / 64, 64, 0, st>>>(cb.a, ctl, cb.seg, cb.ev_keys, cb.ev_out);
+    /* the radix-sort key buffer is free after the pair pass: per-body owner words */
+    k_resolve<<<cb.seg.nsims, RESOLVE_BLOCK, 0, st>>>(cb.a, ctl, cb.seg, cb.ev_keys, cb.ev_out, cb.skey[1]);
     k_integrate<<<flat_grid(cb.cap), 256, 0, st>>>(cb.a, ctl, cb.rend);
     k_keep_blocksum<<<sg, NBG_SCAN_BLOCK, 0, st>>>(cb.a, ctl, cb.seg, cb.blk_sum);
     k_scan_blocks<<<1, NBG_SCAN_BLOCK, 0, st>>>(ctl, cb.seg, cb.blk_sum, cb.blk_off, 1, cb.cap, cb.frag_cap);

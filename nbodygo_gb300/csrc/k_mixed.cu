@@ -22,10 +22,12 @@
  *    dist decides the overlap skip and the collision test, so the event set
  *    is the reference's, and the force of every near pair is FP64.
  *
- * Work items are (i-tile, j-range) pairs; persistent CTAs take them from an
- * atomic counter.  Each item writes its partial sums to its own slot, and
- * k_mix_out adds the slots in a fixed order, so results do not depend on
- * scheduling.
+ * The pair work of a cycle, W units of (i-tile, one j-body), is cut into P
+ * equal runs, one per resident CTA, so every CTA finishes at the same time
+ * whatever the sizes of the sims and tiles; a run is a sequence of (i-tile,
+ * j-range) segments.  Each CTA writes its share of an i-tile to a slot of its
+ * own, and k_mix_out adds the shares in CTA order, so results do not depend
+ * on scheduling.
  */
 #include "nbg_internal.cuh"
 #include "nbg_math.h"
@@ -60,7 +62,7 @@ __device__ __forceinline__ bool is_special(double x, double y, double z, double 
     return !(fabs(x) <= NBG_DBL_MAX && fabs(y) <= NBG_DBL_MAX && fabs(z) <= NBG_DBL_MAX) || r != r;
 }
 
-/* ---- per-cycle reductions: r_max, |x|_max, m_scale, splits ---------------- */
+/* ---- per-cycle reductions: r_max, |x|_max, m_scale ------------------------ */
 
 __global__ void k_mix_reduce(BodyArrays A, DevCtl *ctl, SimSegs seg)
 {
@@ -247,15 +249,17 @@ template <int BLOCK, int K, int JT, int UNROLL, int MINB>
 __global__ void __launch_bounds__(BLOCK, MINB)
 k_pair_mixed(BodyArrays A, DevCtl *ctl, SimSegs seg, const float4 *__restrict__ jhi, const float4 *__restrict__ jlo,
              const float4 *__restrict__ tile_c, const unsigned *__restrict__ perm, double *__restrict__ part,
-             ll part_stride, ull *ev_keys, ll ev_cap)
+             ull *ev_keys, ll ev_cap)
 {
     constexpr int JP = JT / 2; /* j pairs per tile */
     constexpr int ITILE = BLOCK * K;
     static_assert(ITILE >= NBG_MIX_MIN_ITILE, "tile-origin buffer is sized for the smallest i-tile");
     __shared__ float4 sA[JP], sB[JP];
-    __shared__ ll s_item;
     if (ctl->error) return;
-    const ll items = seg.item_off[seg.nsims];
+    const int P = ctl->splits;
+    const int cta = blockIdx.x;
+    if (cta >= P) return;
+    const ll W = ctl->work_total;
     double ms = ctl->m_scale;
     if (!(ms > 0.0)) ms = 1.0;
     const double inv_ms = 1.0 / ms;
@@ -264,22 +268,21 @@ k_pair_mixed(BodyArrays A, DevCtl *ctl, SimSegs seg, const float4 *__restrict__ 
     const double kappa = (double)ctl->near_kappa;
     const int tid = threadIdx.x;
 
-    for (;;) {
-        if (tid == 0) s_item = (ll)atomicAdd((unsigned long long *)&ctl->work_next, 1ull);
-        __syncthreads();
-        const ll item = s_item;
-        __syncthreads();
-        if (item >= items) break;
-        /* item -> sim, i-tile within the sim, j-range split */
-        const int sim = nbg_sim_of(seg.item_off, seg.nsims, item);
-        const int S = seg.splits[sim];
-        const ll local = item - seg.item_off[sim];
-        const ll t = local / S;
-        const int split = (int)(local % S);
+    /* this CTA's units [U, U1): a run of (i-tile, j-range) segments */
+    ll U = (ll)cta * W / P;
+    const ll U1 = (ll)(cta + 1) * W / P;
+    int sim = U < W ? nbg_sim_of(seg.item_off, seg.nsims, U) : 0;
+    while (U < U1) {
+        while (seg.item_off[sim + 1] <= U) sim++; /* past the end of a sim (or an empty one) */
         const ll s0 = seg.off[sim], n = seg.off[sim + 1];
-        const ll jc = (((n - s0 + S - 1) / S) + JT - 1) / JT * JT;
+        const ll ns = n - s0;
+        const ll local = U - seg.item_off[sim];
+        const ll t = local / ns;
+        const ll j0 = local - t * ns;
+        const ll len = ns - j0 < U1 - U ? ns - j0 : U1 - U;
+        const ll g = seg.mtile_off[sim] + t;
         const ll ibase = s0 + t * ITILE;
-        const float4 c = tile_c[seg.mtile_off[sim] + t];
+        const float4 c = tile_c[g];
 
         float2 nx[K], ny[K], nz[K];
         float thr[K];
@@ -311,8 +314,8 @@ k_pair_mixed(BodyArrays A, DevCtl *ctl, SimSegs seg, const float4 *__restrict__ 
             shx[k] = slx[k] = shy[k] = sly[k] = shz[k] = slz[k] = 0.f;
         }
 
-        const ll jb = s0 + (ll)split * jc;
-        const ll je = jb + jc < n ? jb + jc : n;
+        const ll jb = s0 + j0;
+        const ll je = jb + len;
         for (ll jt = jb; jt < je; jt += JT) {
             __syncthreads();
             for (int sp = tid; sp < JP; sp += BLOCK) {
@@ -426,30 +429,31 @@ k_pair_mixed(BodyArrays A, DevCtl *ctl, SimSegs seg, const float4 *__restrict__ 
                 two_sum_add(shz[k], slz[k], az[k].x + az[k].y);
             }
         }
+        /* this CTA's share of i-tile g: slot g + cta */
+        double *o = part + (g + cta) * 3 * ITILE;
 #pragma unroll
         for (int k = 0; k < K; k++) {
-            const ll p = ibase + (ll)k * BLOCK + tid;
-            if (p < n) {
-                double *o = part + (ll)split * 3 * part_stride;
-                o[p] = (double)shx[k] + (double)slx[k];
-                o[part_stride + p] = (double)shy[k] + (double)sly[k];
-                o[2 * part_stride + p] = (double)shz[k] + (double)slz[k];
-            }
+            const int li = k * BLOCK + tid;
+            o[li] = (double)shx[k] + (double)slx[k];
+            o[ITILE + li] = (double)shy[k] + (double)sly[k];
+            o[2 * ITILE + li] = (double)shz[k] + (double)slz[k];
         }
+        U += len;
     }
 }
 
-/* f = (G m_i m_scale) * sum over j-range slots, in slot order, written to
- * body perm[p]. */
+/* f = (G m_i m_scale) * the sum of the CTAs' shares of body p's i-tile, in
+ * CTA order, written to body perm[p]. */
 __global__ void k_mix_out(BodyArrays A, DevCtl *ctl, SimSegs seg, const unsigned *perm, const double *part,
-                          ll part_stride)
+                          int itile)
 {
     if (ctl->error) return;
     const ll n = ctl->n;
+    const int P = ctl->splits;
+    const ll W = ctl->work_total;
     double ms = ctl->m_scale;
     if (!(ms > 0.0)) ms = 1.0;
     for (ll p = (ll)blockIdx.x * blockDim.x + threadIdx.x; p < n; p += (ll)gridDim.x * blockDim.x) {
-        const int S = seg.splits[nbg_sim_of(seg.off, seg.nsims, p)];
         const ll i = perm[p];
         const unsigned f = A.flags[i];
         if ((f & NBG_LIVE_MASK) != NBG_F_EXISTS) continue;
@@ -464,17 +468,24 @@ __global__ void k_mix_out(BodyArrays A, DevCtl *ctl, SimSegs seg, const unsigned
             A.fz[i] = v;
             continue;
         }
+        const int sim = nbg_sim_of(seg.off, seg.nsims, p);
+        const ll s0 = seg.off[sim], ns = seg.off[sim + 1] - s0;
+        const ll t = (p - s0) / itile;
+        const int li = (int)(p - s0 - t * itile);
+        const ll g = seg.mtile_off[sim] + t;
+        const ll tu = seg.item_off[sim] + t * ns; /* the tile's first unit */
+        const int c0 = nbg_work_cta(tu, P, W), c1 = nbg_work_cta(tu + ns - 1, P, W);
         double sx = 0, sy = 0, sz = 0;
-        for (int s = 0; s < S; s++) {
-            const double *o = part + (ll)s * 3 * part_stride;
-            sx += o[p];
-            sy += o[part_stride + p];
-            sz += o[2 * part_stride + p];
+        for (int c = c0; c <= c1; c++) {
+            const double *o = part + (g + c) * 3 * itile;
+            sx += o[li];
+            sy += o[itile + li];
+            sz += o[2 * itile + li];
         }
-        const double g = NBG_G * A.m[i] * ms;
-        A.fx[i] = g * sx;
-        A.fy[i] = g * sy;
-        A.fz[i] = g * sz;
+        const double gm = NBG_G * A.m[i] * ms;
+        A.fx[i] = gm * sx;
+        A.fy[i] = gm * sy;
+        A.fz[i] = gm * sz;
     }
 }
 
@@ -548,7 +559,7 @@ void nbg_launch_mixed_pair(const CycleBufs &cb, DevCtl *ctl, cudaStream_t st)
 #define X(id, b, k, jt, u, mb)                                                                                   \
     case id:                                                                                                     \
         k_pair_mixed<b, k, jt, u, mb><<<cb.slots, b, 0, st>>>(cb.a, ctl, cb.seg, cb.jhi, cb.jlo, cb.tile_c, cb.perm, \
-                                                             cb.part, cb.cap, cb.ev_keys, cb.ev_cap);            \
+                                                             cb.part, cb.ev_keys, cb.ev_cap);                     \
         break;
         MIX_VARIANTS(X)
 #undef X
@@ -557,5 +568,6 @@ void nbg_launch_mixed_pair(const CycleBufs &cb, DevCtl *ctl, cudaStream_t st)
 
 void nbg_launch_mixed_out(const CycleBufs &cb, DevCtl *ctl, cudaStream_t st)
 {
-    k_mix_out<<<flat_grid(cb.cap), 256, 0, st>>>(cb.a, ctl, cb.seg, cb.perm, cb.part, cb.cap);
+    k_mix_out<<<flat_grid(cb.cap), 256, 0, st>>>(cb.a, ctl, cb.seg, cb.perm, cb.part,
+                                                 cb.itile > 0 ? cb.itile : NBG_MIX_ITILE);
 }

@@ -202,6 +202,17 @@ static void free_cap_buffers(CycleBufs &cb);
 
 /* (re)allocates the body-capacity dependent buffers, keeping the first
  * `keep` bodies of the collection */
+/* resident CTAs of the widest shape of the mixed pair kernel */
+static int max_mixed_slots(int device)
+{
+    int m = 1;
+    for (int v = 0; v < NBG_MIX_VARIANTS; v++) {
+        const int s = nbg_mixed_slots(device, v);
+        if (s > m) m = s;
+    }
+    return m;
+}
+
 static int ensure_cap(nbg_ctx *ctx, ll need, ll keep)
 {
     if (need <= ctx->cb.cap) return NBG_OK;
@@ -230,13 +241,27 @@ static int ensure_cap(nbg_ctx *ctx, ll need, ll keep)
     /* every sim may end in a partial tile: at most cap / itile + nsims tiles */
     ll tiles = (cap + NBG_MIX_MIN_ITILE - 1) / NBG_MIX_MIN_ITILE + NBG_MAX_SIMS + 1;
     CK(cudaMalloc((void **)&ctx->cb.tile_c, (size_t)tiles * sizeof(float4)));
-    CK(cudaMalloc((void **)&ctx->cb.part, (size_t)ctx->cb.split_cap * 3 * (size_t)cap * sizeof(double)));
+    ctx->cb.part_doubles = NBG_PART_DOUBLES(cap, max_mixed_slots(ctx->device));
+    CK(cudaMalloc((void **)&ctx->cb.part, (size_t)ctx->cb.part_doubles * sizeof(double)));
     CK(cudaMalloc((void **)&ctx->cb.perm, (size_t)cap * sizeof(unsigned)));
     CK(cudaMalloc((void **)&ctx->cb.sval, (size_t)cap * sizeof(unsigned)));
     CK(cudaMalloc((void **)&ctx->cb.skey[0], (size_t)cap * sizeof(unsigned)));
     CK(cudaMalloc((void **)&ctx->cb.skey[1], (size_t)cap * sizeof(unsigned)));
     CK(cudaMalloc((void **)&ctx->cb.shist, (size_t)nbg_sort_scratch_hist(cap) * sizeof(ll)));
     ctx->cb.cap = cap;
+    invalidate_graph(ctx);
+    return NBG_OK;
+}
+
+/* the mixed kernel's partial sums: at least `need` doubles */
+static int ensure_part(nbg_ctx *ctx, ll need)
+{
+    if (need <= ctx->cb.part_doubles) return NBG_OK;
+    cudaFree(ctx->cb.part);
+    ctx->cb.part = nullptr;
+    ctx->cb.part_doubles = 0;
+    CK(cudaMalloc((void **)&ctx->cb.part, (size_t)need * sizeof(double)));
+    ctx->cb.part_doubles = need;
     invalidate_graph(ctx);
     return NBG_OK;
 }
@@ -439,7 +464,7 @@ int nbg_create(int device, int precision, int64_t capacity, nbg_ctx **out)
             rc = fail(ctx, NBG_E_CUDA, "control block upload failed");
             break;
         }
-        ctx->cb.split_cap = 32;
+        ctx->cb.work_cap = 0;
         ctx->cb.mix_variant = 0;
         ctx->cb.itile = nbg_mix_variant_info(0).block * nbg_mix_variant_info(0).k;
         ctx->cb.slots = nbg_mixed_slots(device, 0);
@@ -897,6 +922,8 @@ int nbg_step(nbg_ctx *ctx, double dt, double R, int nsteps, nbg_step_info *info)
             rc = ensure_cap(ctx, h->error_need, ctx->n_host);
         else if (h->error_what == 2)
             rc = ensure_ev_cap(ctx, h->error_need);
+        else if (h->error_what == 4)
+            rc = ensure_part(ctx, h->error_need);
         else
             rc = ensure_frag_cap(ctx, h->error_need);
         if (rc != NBG_OK) return rc;
@@ -1131,13 +1158,9 @@ int nbg_set_option(nbg_ctx *ctx, int key, int64_t value)
     if (!ctx) return NBG_E_ARG;
     switch (key) {
     case NBG_OPT_SPLIT:
-        if (value < 1 || value > 256) return fail(ctx, NBG_E_ARG, "split cap must be 1..256");
-        if (value != ctx->cb.split_cap) {
-            CK(cudaSetDevice(ctx->device));
-            cudaFree(ctx->cb.part);
-            ctx->cb.part = nullptr;
-            ctx->cb.split_cap = (int)value;
-            CK(cudaMalloc((void **)&ctx->cb.part, (size_t)value * 3 * (size_t)ctx->cb.cap * sizeof(double)));
+        if (value < 0 || value > (1 << 20)) return fail(ctx, NBG_E_ARG, "work CTA cap must be 0..2^20");
+        if (value != ctx->cb.work_cap) {
+            ctx->cb.work_cap = (int)value;
             invalidate_graph(ctx);
         }
         return NBG_OK;

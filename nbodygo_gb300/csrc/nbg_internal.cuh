@@ -58,8 +58,8 @@ struct DevCtl {
     int pad0;
     ll error_need;   /* for NBG_E_OVERFLOW: the size that would have fitted */
     int error_what;  /* 1 = bodies, 2 = events, 3 = fragments, 4 = partials */
-    int splits;      /* mixed: j-range splits per i-tile (a sim uses at most its j-tile count) */
-    ll work_next;    /* mixed: next work item for the persistent CTAs */
+    int splits;      /* mixed: CTAs the pair work is divided among (P) */
+    ll work_total;   /* mixed: pair work W in (i-tile, j-body) units */
     /* per-cycle values */
     ll ev_count;     /* detected events (may exceed capacity) */
     ll frag_total;   /* fragments emitted this cycle */
@@ -89,8 +89,8 @@ struct SimSegs {
     ll *off;         /* [nsims+1] */
     ll *tile_off;    /* [nsims+1] plain kernel: 64-body i-tiles before sim s */
     ll *mtile_off;   /* [nsims+1] mixed kernel: 512-body i-tiles before sim s */
-    ll *item_off;    /* [nsims+1] mixed kernel: work items before sim s */
-    int *splits;     /* [nsims]   mixed kernel: j-range splits of sim s */
+    ll *item_off;    /* [nsims+1] mixed kernel: pair work before sim s, in (i-tile, j-body)
+                      * units: sim s holds (its i-tiles) x n_s of them */
     ll *keep;        /* [nsims]   bodies of sim s that survive Cycle */
     ll *frag;        /* [nsims]   fragments sim s emits this cycle */
     ll *frag_start;  /* [nsims+1] */
@@ -122,8 +122,7 @@ static inline SimSegs nbg_seg_carve(void *base, int nsims)
     s.hadd_start = p + 8 * m;
     s.keep_start = p + 9 * m;
     s.new_off = p + 10 * m;
-    s.splits = (int *)(p + 11 * m);
-    s.xmax_bits = (unsigned *)(s.splits + m);
+    s.xmax_bits = (unsigned *)(p + 11 * m) + m; /* the first 32-bit array is spare */
     return s;
 }
 
@@ -165,7 +164,8 @@ struct CycleBufs {
     unsigned *skey[2];  /* radix-sort keys (ping-pong) */
     unsigned *sval;     /* radix-sort values (ping-pong partner of perm) */
     ll *shist;          /* radix-sort digit histogram / offsets */
-    int split_cap;
+    ll part_doubles;    /* size of part */
+    int work_cap;       /* most CTAs the mixed pair work is divided among (0 = slots) */
     int slots;          /* resident CTAs of the mixed kernel on this device */
     int mix_variant;    /* shape of the mixed pair kernel (see nbg_mix_variant_info) */
     int itile;          /* i-bodies per work item of that shape */
@@ -177,6 +177,23 @@ struct MixVariantInfo {
 };
 #define NBG_MIX_VARIANTS 7
 #define NBG_MIX_MIN_ITILE 256
+#define NBG_MIX_MAX_ITILE 512
+/* fewest (i-tile, j-body) units of pair work a CTA is given */
+#define NBG_MIX_MIN_WORK 2048
+
+/* The mixed pair work of a cycle is W units, (i-tile, j-body) pairs in sim,
+ * i-tile, j order; CTA c of P takes units [c W / P, (c + 1) W / P).  This is
+ * the CTA that holds unit u. */
+__host__ __device__ __forceinline__ int nbg_work_cta(ll u, int P, ll W)
+{
+    return (int)(((u + 1) * (ll)P + W - 1) / W - 1);
+}
+
+/* Partial sums of the mixed pair kernel: CTA c's share of i-tile g (global
+ * tile index) is slot g + c, 3 x itile doubles; no two (tile, CTA) pairs that
+ * both hold work share a slot, since CTAs take the tiles in order.  Slots
+ * needed: tiles + P - 1, tiles <= cap / itile + sims. */
+#define NBG_PART_DOUBLES(cap, pmax) (3 * ((ll)(cap) + (ll)NBG_MIX_MAX_ITILE * ((ll)(pmax) + NBG_MAX_SIMS + 2)))
 
 #define NBG_SCAN_BLOCK 1024
 #define NBG_SCAN_ITEMS 4

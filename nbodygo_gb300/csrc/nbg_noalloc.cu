@@ -22,7 +22,9 @@
 
 #include "nbg_internal.cuh"
 
-#define NOALLOC_SPLITS 4
+/* partial sums: 786,432 doubles, 512 slots of a 512-body i-tile; a 65,536-body
+ * collection has 128 i-tiles, which leaves room for 385 CTAs */
+#define NOALLOC_PART_DOUBLES (4 * 3 * NBG_NOALLOC_MAX_BODIES)
 
 static constexpr size_t align256(size_t v) { return (v + 255) / 256 * 256; }
 
@@ -32,7 +34,7 @@ static constexpr size_t OFF_JLO = OFF_JHI + align256((size_t)NBG_NOALLOC_MAX_BOD
 static constexpr size_t OFF_TILE = OFF_JLO + align256((size_t)NBG_NOALLOC_MAX_BODIES * 16);
 static constexpr size_t OFF_PART =
     OFF_TILE + align256((size_t)((NBG_NOALLOC_MAX_BODIES + NBG_MIX_ITILE - 1) / NBG_MIX_ITILE) * 16);
-static constexpr size_t OFF_PERM = OFF_PART + align256((size_t)NOALLOC_SPLITS * 3 * NBG_NOALLOC_MAX_BODIES * 8);
+static constexpr size_t OFF_PERM = OFF_PART + align256((size_t)NOALLOC_PART_DOUBLES * 8);
 static constexpr size_t OFF_SVAL = OFF_PERM + align256((size_t)NBG_NOALLOC_MAX_BODIES * 4);
 static constexpr size_t OFF_KEY0 = OFF_SVAL + align256((size_t)NBG_NOALLOC_MAX_BODIES * 4);
 static constexpr size_t OFF_KEY1 = OFF_KEY0 + align256((size_t)NBG_NOALLOC_MAX_BODIES * 4);
@@ -119,7 +121,8 @@ extern "C" int nbg_forces_mixed_noalloc(const double *x, const double *y, const 
     cb.shist = (ll *)(base + OFF_HIST);
     cb.ev_keys = nullptr; /* events are discarded */
     cb.ev_cap = 0;
-    cb.split_cap = NOALLOC_SPLITS;
+    cb.part_doubles = NOALLOC_PART_DOUBLES;
+    cb.work_cap = 0;
     cb.mix_variant = 0; /* the default shape: 512-body i-tiles */
     cb.itile = NBG_MIX_ITILE;
     cb.slots = nbg_mixed_slots(dev, 0);
