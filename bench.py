@@ -80,6 +80,7 @@ def parse():
     ap.add_argument("--no-plain", action="store_true", help="skip the FP64 comparison run")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default kernel shape")
+    ap.add_argument("--shape", type=int, default=None, help="use this shape of the mixed pair kernel (no autotune)")
     return ap.parse_args()
 
 
@@ -327,7 +328,10 @@ def main():
     sim.set_option(A.OPT_GRAPH_CYCLES, chunk)
     load(sim, sims)
     tuned = None
-    if prec == "mixed" and not args.no_autotune:
+    if prec == "mixed" and args.shape is not None:
+        sim.set_option(A.OPT_MIX_SHAPE, args.shape)
+        tuned = {"shape": args.shape, "pair_kernel_ms": None, "candidates": A.MIX_SHAPES, "fixed": True}
+    elif prec == "mixed" and not args.no_autotune:
         shape, tms = sim.autotune()
         tuned = {"shape": shape, "pair_kernel_ms": tms, "candidates": A.MIX_SHAPES}
     sim.step(DT, 1.0, max(args.warmup, 3) * chunk)

@@ -277,12 +277,13 @@ int nbg_enable_timing(nbg_ctx *ctx, int on);
 int nbg_get_timing(nbg_ctx *ctx, nbg_timing *t);
 
 /* Tuning knobs of the pair kernels (0 = default). */
-#define NBG_OPT_SPLIT 1      /* mixed: most CTAs the pair work is divided among (0 = all resident) */
+#define NBG_OPT_SPLIT 1      /* mixed: most chunks the pair work is cut into (0 = 32 per resident CTA) */
 #define NBG_OPT_GRAPH 2      /* 0 = launch each cycle directly, 1 = CUDA graph */
 #define NBG_OPT_EV_CAP 3     /* event-list capacity (rounded up to a power of two) */
 #define NBG_OPT_FRAG_CAP 4   /* fragments one cycle may emit */
 #define NBG_OPT_GRAPH_CYCLES 6 /* cycles captured in one CUDA graph (default 1) */
-#define NBG_OPT_MIX_SHAPE 7    /* shape of the mixed pair kernel, 0..6 (see nbg_autotune) */
+#define NBG_OPT_MIX_SHAPE 7    /* shape of the mixed pair kernel, 0..NBG_MIX_SHAPES-1 (see nbg_autotune) */
+#define NBG_MIX_SHAPES 11
 #define NBG_OPT_NEAR_PPM 5   /* mixed: pairs closer than (value * 1e-6) x the i-tile's
                                 extent around its origin are computed in FP64
                                 (default 70000) */

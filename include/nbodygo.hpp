@@ -15,6 +15,9 @@
  *   ComputationRunner (NewComputationRunner, cmd/runner/computation-runner.go:24-326
  *     SetTimeScaling, SetCoefficientOfRestitution, RemoveBodies, SetWorkers,
  *     RunOneComputation, TimeScaling, CoefficientOfRestitution, WorkerCount)
+ *   NextId, Body::SetSun                   cmd/body/body.go:101-104, 315-328
+ *   FromCsv                                cmd/sim/fromcsv.go:46-131
+ *   ToCsv (snapshot in FromCsv's format; no counterpart in the reference)
  *
  * The body array lives on the GPU; strings (Name, Class), colour and light
  * intensity stay here, keyed by id.  The setters of the runner take effect at
@@ -24,11 +27,14 @@
 #ifndef NBODYGO_HPP
 #define NBODYGO_HPP
 
+#include <atomic>
 #include <cctype>
 #include <cerrno>
 #include <cmath>
 #include <cstdint>
+#include <cstdio>
 #include <cstdlib>
+#include <fstream>
 #include <map>
 #include <memory>
 #include <stdexcept>
@@ -110,7 +116,14 @@ struct Body {
     CollisionBehavior Behavior = Elastic;
     BodyColor Color = Random;
     bool IsSun = false, Exists = true, WithTelemetry = false, Pinned = false;
-    double Intensity = 0;
+
+    double intensity = 0;
+    /* body.go:101-104 */
+    void SetSun(double i)
+    {
+        IsSun = true;
+        intensity = i;
+    }
 
     /* body.go:274-313: property=value strings; unknown properties and parse
      * errors are ignored; always returns true. */
@@ -141,6 +154,22 @@ struct Body {
     }
 };
 
+/* body.NextId (body.go:315-328): one counter for the process, shared with the
+ * ids the GPU gives fragments (ComputationRunner keeps the two in step). */
+inline std::atomic<int64_t> &next_id_counter()
+{
+    static std::atomic<int64_t> c{0};
+    return c;
+}
+inline int64_t NextId() { return next_id_counter().fetch_add(1); }
+/* raises the counter to at least v */
+inline void AdvanceNextId(int64_t v)
+{
+    int64_t cur = next_id_counter().load();
+    while (cur < v && !next_id_counter().compare_exchange_weak(cur, v)) {
+    }
+}
+
 /* body.NewBody (body.go:56-89) */
 inline Body NewBody(int64_t id, double x, double y, double z, double vx, double vy, double vz, double mass,
                     double radius, CollisionBehavior behavior, BodyColor color, double fragFactor,
@@ -162,6 +191,176 @@ inline Body NewBody(int64_t id, double x, double y, double z, double vx, double 
     b.WithTelemetry = withTelemetry;
     b.Pinned = pinned;
     return b;
+}
+
+/* strconv.ParseBool: true for 1 t T TRUE true True, false for 0 f F FALSE
+ * false False; anything else is an error (returns false in *ok) */
+inline bool GoParseBool(const std::string &s, bool *ok)
+{
+    static const char *t[] = {"1", "t", "T", "TRUE", "true", "True"};
+    static const char *f[] = {"0", "f", "F", "FALSE", "false", "False"};
+    *ok = true;
+    for (const char *v : t)
+        if (s == v) return true;
+    for (const char *v : f)
+        if (s == v) return false;
+    *ok = false;
+    return false;
+}
+
+/* strconv.ParseFloat(s, 64) on the whole string; *ok = false on any error */
+inline double GoParseFloat(const std::string &s, bool *ok)
+{
+    const double nan_marker = 0;
+    *ok = false;
+    if (s.empty() || std::isspace((unsigned char)s[0])) return nan_marker;
+    const char *b = s.c_str();
+    char *end = nullptr;
+    errno = 0;
+    const double v = std::strtod(b, &end);
+    if (end == b || *end != '\0' || (errno == ERANGE && std::isinf(v))) return nan_marker;
+    *ok = true;
+    return v;
+}
+
+inline std::string TrimSpace(const std::string &s)
+{
+    size_t a = 0, b = s.size();
+    while (a < b && std::isspace((unsigned char)s[a])) a++;
+    while (b > a && std::isspace((unsigned char)s[b - 1])) b--;
+    return s.substr(a, b - a);
+}
+
+/* One record of encoding/csv with Comment '#' and FieldsPerRecord -1: comma
+ * separated, RFC 4180 quotes ("" inside a quoted field; a quoted field may
+ * span lines), lines starting with '#' and empty lines skipped.  Returns
+ * false at end of input; a bare quote in an unquoted field is an error, as
+ * in Go (the reference then stops the process; here Error is thrown). */
+inline bool ReadCsvRecord(std::istream &in, std::vector<std::string> &fields)
+{
+    std::string line;
+    for (;;) {
+        if (!std::getline(in, line)) return false;
+        if (!line.empty() && line.back() == '\r') line.pop_back();
+        if (line.empty() || line[0] == '#') continue;
+        break;
+    }
+    fields.clear();
+    std::string cur;
+    size_t i = 0;
+    for (;;) {
+        if (i < line.size() && line[i] == '"') {
+            /* quoted field */
+            i++;
+            for (;;) {
+                if (i >= line.size()) {
+                    std::string next;
+                    if (!std::getline(in, next)) throw Error(NBG_E_ARG, "csv: extraneous or missing \" in quoted-field");
+                    if (!next.empty() && next.back() == '\r') next.pop_back();
+                    cur += '\n';
+                    line = next;
+                    i = 0;
+                    continue;
+                }
+                if (line[i] == '"') {
+                    if (i + 1 < line.size() && line[i + 1] == '"') {
+                        cur += '"';
+                        i += 2;
+                        continue;
+                    }
+                    i++;
+                    break;
+                }
+                cur += line[i++];
+            }
+            if (i < line.size() && line[i] != ',') throw Error(NBG_E_ARG, "csv: extraneous \" in field");
+        } else {
+            while (i < line.size() && line[i] != ',') {
+                if (line[i] == '"') throw Error(NBG_E_ARG, "csv: bare \" in non-quoted-field");
+                cur += line[i++];
+            }
+        }
+        fields.push_back(cur);
+        cur.clear();
+        if (i >= line.size()) break;
+        i++; /* the comma */
+        if (i >= line.size()) {
+            fields.push_back("");
+            break;
+        }
+    }
+    return true;
+}
+
+/* sim.FromCsv (cmd/sim/fromcsv.go:46-131): fields x, y, z, vx, vy, vz, mass,
+ * radius (required), is_sun, collision_behavior, color, fragmentation_factor,
+ * fragmentation_step (optional, in that order).  A record whose required
+ * fields are missing or whose present fields do not parse is skipped, as the
+ * reference's recovered panic does: an empty optional field that is parsed
+ * (is_sun, the two fragmentation values) does not parse, so such a record is
+ * skipped too.  At most bodyCount records are kept; each body gets NextId().
+ * An unreadable file gives an empty list. */
+inline std::vector<Body> FromCsv(const std::string &csvPath, int bodyCount, CollisionBehavior defaultCollisionBehavior,
+                                 BodyColor defaultBodyColor)
+{
+    std::vector<Body> bodies;
+    std::ifstream in(csvPath);
+    if (!in) return bodies;
+    std::vector<std::string> f;
+    for (int lines = 0; lines < bodyCount;) {
+        if (!ReadCsvRecord(in, f)) break;
+        if (f.size() < 8) continue;
+        bool ok = true, o;
+        double v[8];
+        for (int k = 0; k < 8 && ok; k++) {
+            v[k] = GoParseFloat(TrimSpace(f[k]), &o);
+            ok = o;
+        }
+        if (!ok) continue;
+        bool isSun = false;
+        if (f.size() >= 9) {
+            isSun = GoParseBool(TrimSpace(f[8]), &o);
+            if (!o) continue;
+        }
+        CollisionBehavior cb = defaultCollisionBehavior;
+        if (f.size() >= 10) cb = ParseCollisionBehavior(TrimSpace(f[9]));
+        BodyColor color = defaultBodyColor;
+        if (f.size() >= 11) color = ParseBodyColor(TrimSpace(f[10]));
+        double fragFactor = 0, fragStep = 0;
+        if (f.size() >= 12) {
+            fragFactor = GoParseFloat(TrimSpace(f[11]), &o);
+            if (!o) continue;
+        }
+        if (f.size() >= 13) {
+            fragStep = GoParseFloat(TrimSpace(f[12]), &o);
+            if (!o) continue;
+        }
+        Body b = NewBody(NextId(), v[0], v[1], v[2], v[3], v[4], v[5], v[6], v[7], cb, color, fragFactor, fragStep,
+                         false, "", "", false);
+        if (isSun) b.SetSun(100);
+        bodies.push_back(b);
+        lines++;
+    }
+    return bodies;
+}
+
+/* Snapshot of bodies in FromCsv's 13-field format, every number written with
+ * 17 significant digits, so FromCsv reads back the same values bit for bit
+ * (ids come from NextId again).  Returns false if the file cannot be written. */
+inline bool ToCsv(const std::string &path, const std::vector<Body> &bodies)
+{
+    static const char *beh[] = {"none", "subsume", "elastic", "fragment"};
+    static const char *col[] = {"random", "black", "white", "darkgray", "gray", "lightgray", "red", "green",
+                                "blue", "yellow", "magenta", "cyan", "orange", "brown", "pink"};
+    FILE *f = std::fopen(path.c_str(), "w");
+    if (!f) return false;
+    std::fprintf(f, "# x,y,z,vx,vy,vz,mass,radius,is_sun,collision_behavior,color,fragmentation_factor,"
+                    "fragmentation_step\n");
+    for (const Body &b : bodies)
+        std::fprintf(f, "%.17g,%.17g,%.17g,%.17g,%.17g,%.17g,%.17g,%.17g,%s,%s,%s,%.17g,%.17g\n", b.X, b.Y, b.Z, b.Vx,
+                     b.Vy, b.Vz, b.Mass, b.Radius, b.IsSun ? "true" : "false", beh[b.Behavior & 3],
+                     col[(unsigned)b.Color < 15 ? b.Color : 0], b.FragFactor, b.FragStep);
+    return std::fclose(f) == 0;
 }
 
 /* The numeric part of ApplyMods as an nbg_edit (the C ABI's ModBody). */
@@ -254,15 +453,17 @@ class BodyCollection {
         }
         nbg_soa s = b.soa();
         check(nbg_set_bodies(ctx_.get(), &s, (int64_t)bodies.size()));
-        check(nbg_set_next_id(ctx_.get(), max_id + 1));
+        AdvanceNextId(max_id + 1);
+        check(nbg_set_next_id(ctx_.get(), next_id_counter().load()));
     }
 
     nbg_ctx *ctx() const { return ctx_.get(); }
 
     /* Enqueue(NewAdd(b)) (body_collection.go:82-88): appended by the next
-     * Cycle, newest first.  Returns the id (a new one when b.Id < 0). */
+     * Cycle, newest first.  Returns the id (NextId() when b.Id < 0). */
     int64_t EnqueueAdd(Body b)
     {
+        if (b.Id < 0) b.Id = NextId();
         SoaBuffers s;
         s.resize(1);
         s.put(0, b);
@@ -384,8 +585,14 @@ class ComputationRunner {
             int64_t removed = 0;
             bc_.check(nbg_remove_bodies(bc_.ctx(), pending_del_, &removed));
         }
+        /* fragments take ids from the same counter as NextId */
+        int64_t dev_next = 0;
+        bc_.check(nbg_get_next_id(bc_.ctx(), &dev_next));
+        const int64_t host_next = next_id_counter().load();
+        if (host_next > dev_next) bc_.check(nbg_set_next_id(bc_.ctx(), host_next));
         nbg_step_info info{};
         bc_.check(nbg_step(bc_.ctx(), dt_, R_, 1, &info));
+        AdvanceNextId(info.next_id);
         int64_t n = 0;
         bc_.check(nbg_get_renderables(bc_.ctx(), nullptr, 0, &n));
         std::vector<nbg_renderable> out((size_t)n);

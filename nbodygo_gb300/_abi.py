@@ -42,7 +42,7 @@ OPT_FRAG_CAP = 4
 OPT_NEAR_PPM = 5
 OPT_GRAPH_CYCLES = 6
 OPT_MIX_SHAPE = 7
-MIX_SHAPES = 7
+MIX_SHAPES = 11
 
 _pd = C.POINTER(C.c_double)
 _pi64 = C.POINTER(C.c_int64)

@@ -75,10 +75,10 @@ __device__ static ll block_scan_array(int ns, F f, ll *out)
 /* ------------------------------------------------------------------------ */
 
 /* Per-cycle resets and the work layout of every sim: 64-body tiles of the
- * plain kernel; i-tiles and the pair work of the mixed kernel, and how many
- * CTAs share it (P: at most the resident CTAs or work_cap, at least
- * NBG_MIX_MIN_WORK units each, and few enough that the partial-sum slots fit
- * in part_doubles); the interaction count.  One block. */
+ * plain kernel; i-tiles and the pair work of the mixed kernel, and the chunks
+ * it is cut into (C: NBG_MIX_CHUNKS_PER_CTA per resident CTA, or work_cap,
+ * at least NBG_MIX_MIN_WORK units each, and few enough that the partial-sum
+ * slots fit in part_doubles); the interaction count.  One block. */
 __global__ void __launch_bounds__(NBG_SCAN_BLOCK) k_begin(DevCtl *ctl, SimSegs seg, int slots, int work_cap, int itile,
                                                           ll part_doubles)
 {
@@ -95,7 +95,7 @@ __global__ void __launch_bounds__(NBG_SCAN_BLOCK) k_begin(DevCtl *ctl, SimSegs s
         ns, [&](int s) { return (off[s + 1] - off[s] + itile - 1) / itile; }, seg.mtile_off);
     const ll W = block_scan_array(
         ns, [&](int s) { return (seg.mtile_off[s + 1] - seg.mtile_off[s]) * (off[s + 1] - off[s]); }, seg.item_off);
-    ll P = slots;
+    ll P = (ll)slots * NBG_MIX_CHUNKS_PER_CTA;
     if (work_cap > 0 && P > work_cap) P = work_cap;
     if (P > W / NBG_MIX_MIN_WORK) P = W / NBG_MIX_MIN_WORK;
     const ll part_slots = part_doubles / (3ll * itile);
@@ -118,6 +118,7 @@ __global__ void __launch_bounds__(NBG_SCAN_BLOCK) k_begin(DevCtl *ctl, SimSegs s
         ctl->m_scale = 0.0;
         ctl->splits = (int)P;
         ctl->work_total = W;
+        ctl->work_next = 0;
         ctl->cycle_interactions = inter;
         if (part_short) {
             ctl->error = NBG_E_OVERFLOW;
@@ -639,10 +640,13 @@ __device__ static ll lower_bound_u64(const ull *keys, ll cnt, ull v)
  * resolved, all such events in parallel.  Every body sees its events in the
  * sequential order, so the result is the sequential result bit for bit.
  * owner[] (one word per body; any contents on entry) holds, per round, the
- * smallest pending processing index that touches the body.  ev_out holds the
- * sims one after another, each in processing order; its pad field marks
- * pending events during the kernel and is 0 on return. */
+ * smallest pending processing index that touches the body.  Once a round
+ * resolves fewer than RESOLVE_MIN_ROUND events (a long chain through one
+ * body, as when a large body absorbs many), one thread finishes the rest in
+ * order.  ev_out holds the sims one after another, each in processing order;
+ * its pad field marks pending events during the kernel and is 0 on return. */
 #define RESOLVE_BLOCK 256
+#define RESOLVE_MIN_ROUND 8 /* fewer events resolved in a round: finish sequentially */
 
 __device__ static void event_bodies(ull key, ll &b1, ll &b2, unsigned &type)
 {
@@ -740,8 +744,15 @@ __global__ void __launch_bounds__(RESOLVE_BLOCK) k_resolve(BodyArrays A, DevCtl 
         __syncthreads();
         if (tid == 0) s_left -= s_done;
         __syncthreads();
-        if (s_left <= 0) break;
+        if (s_left <= 0) return;
+        /* a chain of events on shared bodies: a round no longer pays for itself */
+        if (s_done < RESOLVE_MIN_ROUND) break;
     }
+    /* the rest in processing order, one thread: every pending event's
+     * predecessors are resolved or come before it */
+    if (tid == 0)
+        for (ll p = 0; p < m; p++)
+            if (ev_out[lo + p].pad) resolve_one(A, keys[hi - 1 - p], &ev_out[lo + p]);
 }
 
 /* ------------------------------------------------------------------------ */
@@ -848,22 +859,19 @@ __global__ void __launch_bounds__(NBG_SCAN_BLOCK) k_compact(BodyArrays A, BodyAr
     const ll n = ctl->n;
     const ll base = (ll)blockIdx.x * NBG_SCAN_TILE;
     if (base >= n) return;
-    ll c[NBG_SCAN_ITEMS];
-    ll s = 0;
+    /* rows of NBG_SCAN_BLOCK consecutive bodies, so every field access of a
+     * warp is coalesced; kept bodies keep their order */
+    ll rank = blk_off[blockIdx.x];
     for (int q = 0; q < NBG_SCAN_ITEMS; q++) {
-        ll k = base + (ll)threadIdx.x * NBG_SCAN_ITEMS + q;
-        c[q] = (k < n && (A.flags[k] & NBG_F_EXISTS)) ? 1 : 0;
-        s += c[q];
-    }
-    ll tot;
-    ll rank = block_excl_scan(s, &tot) + blk_off[blockIdx.x];
-    for (int q = 0; q < NBG_SCAN_ITEMS; q++) {
-        ll k = base + (ll)threadIdx.x * NBG_SCAN_ITEMS + q;
-        if (c[q]) {
+        const ll k = base + (ll)q * NBG_SCAN_BLOCK + threadIdx.x;
+        const bool keep = k < n && (A.flags[k] & NBG_F_EXISTS);
+        ll tot;
+        const ll ex = block_excl_scan(keep ? 1 : 0, &tot);
+        if (keep) {
             const int sim = nbg_sim_of(seg.off, seg.nsims, k);
-            copy_body(A, k, Bt, seg.new_off[sim] + (rank - seg.keep_start[sim]));
-            rank++;
+            copy_body(A, k, Bt, seg.new_off[sim] + (rank + ex - seg.keep_start[sim]));
         }
+        rank += tot;
     }
 }
 

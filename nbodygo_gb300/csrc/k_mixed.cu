@@ -22,12 +22,13 @@
  *    dist decides the overlap skip and the collision test, so the event set
  *    is the reference's, and the force of every near pair is FP64.
  *
- * The pair work of a cycle, W units of (i-tile, one j-body), is cut into P
- * equal runs, one per resident CTA, so every CTA finishes at the same time
- * whatever the sizes of the sims and tiles; a run is a sequence of (i-tile,
- * j-range) segments.  Each CTA writes its share of an i-tile to a slot of its
- * own, and k_mix_out adds the shares in CTA order, so results do not depend
- * on scheduling.
+ * The pair work of a cycle, W units of (i-tile, one j-body), is cut into C
+ * equal chunks, about 32 per resident CTA, whatever the sizes of the sims and
+ * tiles; a chunk is a run of (i-tile, j-range) segments.  Persistent CTAs
+ * take chunks from an atomic counter, so a CTA that meets many near pairs
+ * simply takes fewer.  Each chunk writes its share of an i-tile to a slot of
+ * its own, and k_mix_out adds the shares in chunk order, so results do not
+ * depend on scheduling.
  */
 #include "nbg_internal.cuh"
 #include "nbg_math.h"
@@ -245,7 +246,7 @@ __device__ __forceinline__ void fold64(float &hi, float &lo, double v)
 /* Everything in this kernel is indexed by sorted position (p for i, q for
  * j); perm maps a position to the body index used by the FP64 arrays and the
  * event keys. */
-template <int BLOCK, int K, int JT, int UNROLL, int MINB>
+template <int BLOCK, int K, int JT, int UNROLL, int MINB, bool SF>
 __global__ void __launch_bounds__(BLOCK, MINB)
 k_pair_mixed(BodyArrays A, DevCtl *ctl, SimSegs seg, const float4 *__restrict__ jhi, const float4 *__restrict__ jlo,
              const float4 *__restrict__ tile_c, const unsigned *__restrict__ perm, double *__restrict__ part,
@@ -254,11 +255,18 @@ k_pair_mixed(BodyArrays A, DevCtl *ctl, SimSegs seg, const float4 *__restrict__ 
     constexpr int JP = JT / 2; /* j pairs per tile */
     constexpr int ITILE = BLOCK * K;
     static_assert(ITILE >= NBG_MIX_MIN_ITILE, "tile-origin buffer is sized for the smallest i-tile");
+    static_assert(ITILE <= NBG_MIX_MAX_ITILE, "partial-sum buffer is sized for the largest i-tile");
     __shared__ float4 sA[JP], sB[JP];
+    /* SF: each i-body's (hi, lo) sums and near-pair threshold live in shared
+     * memory (only this thread touches them; read once per j-tile), which
+     * frees seven registers per i-body for occupancy */
+    __shared__ float sfold[6][SF ? ITILE : 1], sthr[SF ? ITILE : 1];
+    float rfold[6][SF ? 1 : K], rthr[SF ? 1 : K];
+#define FOLD(c, k) (SF ? sfold[c][(k) * BLOCK + tid] : rfold[c][SF ? 0 : (k)])
+#define THR(k) (SF ? sthr[(k) * BLOCK + tid] : rthr[SF ? 0 : (k)])
+    __shared__ ll s_chunk;
     if (ctl->error) return;
-    const int P = ctl->splits;
-    const int cta = blockIdx.x;
-    if (cta >= P) return;
+    const int C = ctl->splits;
     const ll W = ctl->work_total;
     double ms = ctl->m_scale;
     if (!(ms > 0.0)) ms = 1.0;
@@ -268,9 +276,15 @@ k_pair_mixed(BodyArrays A, DevCtl *ctl, SimSegs seg, const float4 *__restrict__ 
     const double kappa = (double)ctl->near_kappa;
     const int tid = threadIdx.x;
 
-    /* this CTA's units [U, U1): a run of (i-tile, j-range) segments */
-    ll U = (ll)cta * W / P;
-    const ll U1 = (ll)(cta + 1) * W / P;
+    for (;;) {
+    if (tid == 0) s_chunk = (ll)atomicAdd((unsigned long long *)&ctl->work_next, 1ull);
+    __syncthreads();
+    const ll chunk = s_chunk;
+    __syncthreads();
+    if (chunk >= C) break;
+    /* this chunk's units [U, U1): a run of (i-tile, j-range) segments */
+    ll U = chunk * W / C;
+    const ll U1 = (chunk + 1) * W / C;
     int sim = U < W ? nbg_sim_of(seg.item_off, seg.nsims, U) : 0;
     while (U < U1) {
         while (seg.item_off[sim + 1] <= U) sim++; /* past the end of a sim (or an empty one) */
@@ -285,8 +299,6 @@ k_pair_mixed(BodyArrays A, DevCtl *ctl, SimSegs seg, const float4 *__restrict__ 
         const float4 c = tile_c[g];
 
         float2 nx[K], ny[K], nz[K];
-        float thr[K];
-        float shx[K], slx[K], shy[K], sly[K], shz[K], slz[K];
 #pragma unroll
         for (int k = 0; k < K; k++) {
             const ll p = ibase + (ll)k * BLOCK + tid;
@@ -310,8 +322,9 @@ k_pair_mixed(BodyArrays A, DevCtl *ctl, SimSegs seg, const float4 *__restrict__ 
             nx[k] = make_float2(-xr, -xr);
             ny[k] = make_float2(-yr, -yr);
             nz[k] = make_float2(-zr, -zr);
-            thr[k] = t;
-            shx[k] = slx[k] = shy[k] = sly[k] = shz[k] = slz[k] = 0.f;
+            THR(k) = t;
+#pragma unroll
+            for (int cc = 0; cc < 6; cc++) FOLD(cc, k) = 0.f;
         }
 
         const ll jb = s0 + j0;
@@ -375,7 +388,8 @@ k_pair_mixed(BodyArrays A, DevCtl *ctl, SimSegs seg, const float4 *__restrict__ 
             }
 #pragma unroll
             for (int k = 0; k < K; k++) {
-                if (mn[k] < thr[k]) {
+                const float thk = THR(k);
+                if (mn[k] < thk) {
                     /* slow path: this tile holds a near or overlapping pair for i */
                     const ll p = ibase + (ll)k * BLOCK + tid;
                     const ll i = perm[p];
@@ -392,7 +406,7 @@ k_pair_mixed(BodyArrays A, DevCtl *ctl, SimSegs seg, const float4 *__restrict__ 
                             const float zj = e ? b.y : b.x, m = e ? b.w : b.z;
                             float dx = xj - xi, dy = yj - yi, dz = zj - zi;
                             float r2 = dx * dx + dy * dy + dz * dz;
-                            if (r2 < thr[k]) {
+                            if (r2 < thk) {
                                 /* near pair: difference of the hi/lo positions
                                  * (error ~2^-24 |dx|) */
                                 const float4 hj = jhi[q], lj = jlo[q];
@@ -407,9 +421,9 @@ k_pair_mixed(BodyArrays A, DevCtl *ctl, SimSegs seg, const float4 *__restrict__ 
                                     (lj.w < 0.f)) {
                                     double qx, qy, qz;
                                     candidate_pair(A, ctl, ev_keys, ev_cap, i, (ll)perm[q], inv_ms, qx, qy, qz);
-                                    fold64(shx[k], slx[k], qx);
-                                    fold64(shy[k], sly[k], qy);
-                                    fold64(shz[k], slz[k], qz);
+                                    fold64(FOLD(0, k), FOLD(1, k), qx);
+                                    fold64(FOLD(2, k), FOLD(3, k), qy);
+                                    fold64(FOLD(4, k), FOLD(5, k), qz);
                                     continue;
                                 }
                             }
@@ -424,32 +438,35 @@ k_pair_mixed(BodyArrays A, DevCtl *ctl, SimSegs seg, const float4 *__restrict__ 
                     ay[k] = make_float2(ty, 0.f);
                     az[k] = make_float2(tz, 0.f);
                 }
-                two_sum_add(shx[k], slx[k], ax[k].x + ax[k].y);
-                two_sum_add(shy[k], sly[k], ay[k].x + ay[k].y);
-                two_sum_add(shz[k], slz[k], az[k].x + az[k].y);
+                two_sum_add(FOLD(0, k), FOLD(1, k), ax[k].x + ax[k].y);
+                two_sum_add(FOLD(2, k), FOLD(3, k), ay[k].x + ay[k].y);
+                two_sum_add(FOLD(4, k), FOLD(5, k), az[k].x + az[k].y);
             }
         }
-        /* this CTA's share of i-tile g: slot g + cta */
-        double *o = part + (g + cta) * 3 * ITILE;
+        /* this chunk's share of i-tile g: slot g + chunk */
+        double *o = part + (g + chunk) * 3 * ITILE;
 #pragma unroll
         for (int k = 0; k < K; k++) {
             const int li = k * BLOCK + tid;
-            o[li] = (double)shx[k] + (double)slx[k];
-            o[ITILE + li] = (double)shy[k] + (double)sly[k];
-            o[2 * ITILE + li] = (double)shz[k] + (double)slz[k];
+            o[li] = (double)FOLD(0, k) + (double)FOLD(1, k);
+            o[ITILE + li] = (double)FOLD(2, k) + (double)FOLD(3, k);
+            o[2 * ITILE + li] = (double)FOLD(4, k) + (double)FOLD(5, k);
         }
         U += len;
     }
+    }
+#undef FOLD
+#undef THR
 }
 
-/* f = (G m_i m_scale) * the sum of the CTAs' shares of body p's i-tile, in
- * CTA order, written to body perm[p]. */
+/* f = (G m_i m_scale) * the sum of the chunks' shares of body p's i-tile, in
+ * chunk order, written to body perm[p]. */
 __global__ void k_mix_out(BodyArrays A, DevCtl *ctl, SimSegs seg, const unsigned *perm, const double *part,
                           int itile)
 {
     if (ctl->error) return;
     const ll n = ctl->n;
-    const int P = ctl->splits;
+    const int C = ctl->splits;
     const ll W = ctl->work_total;
     double ms = ctl->m_scale;
     if (!(ms > 0.0)) ms = 1.0;
@@ -474,7 +491,7 @@ __global__ void k_mix_out(BodyArrays A, DevCtl *ctl, SimSegs seg, const unsigned
         const int li = (int)(p - s0 - t * itile);
         const ll g = seg.mtile_off[sim] + t;
         const ll tu = seg.item_off[sim] + t * ns; /* the tile's first unit */
-        const int c0 = nbg_work_cta(tu, P, W), c1 = nbg_work_cta(tu + ns - 1, P, W);
+        const int c0 = nbg_work_chunk(tu, C, W), c1 = nbg_work_chunk(tu + ns - 1, C, W);
         double sx = 0, sy = 0, sz = 0;
         for (int c = c0; c <= c1; c++) {
             const double *o = part + (g + c) * 3 * itile;
@@ -491,21 +508,26 @@ __global__ void k_mix_out(BodyArrays A, DevCtl *ctl, SimSegs seg, const unsigned
 
 /* ---- kernel shapes ---------------------------------------------------------
  * (threads per CTA, i-bodies per thread, j per shared-memory tile, unroll of
- * the j loop, CTAs per SM the register budget is set for).  Variant 0 is the
- * default; the autotuner (nbg_autotune) measures the others. */
-#define MIX_VARIANTS(X)   \
-    X(0, 128, 4, 256, 2, 3) \
-    X(1, 128, 4, 256, 1, 3) \
-    X(2, 128, 2, 256, 2, 4) \
-    X(3, 256, 2, 256, 2, 2) \
-    X(4, 128, 4, 512, 2, 3) \
-    X(5, 64, 4, 256, 2, 6)  \
-    X(6, 128, 2, 128, 4, 4)
+ * the j loop, CTAs per SM the register budget is set for, sums in shared
+ * memory).  Variant 0 is the default; the autotuner (nbg_autotune) measures
+ * the others. */
+#define MIX_VARIANTS(X)             \
+    X(0, 128, 4, 256, 2, 3, false)  \
+    X(1, 128, 4, 256, 1, 3, false)  \
+    X(2, 128, 2, 256, 2, 4, false)  \
+    X(3, 256, 2, 256, 2, 2, false)  \
+    X(4, 128, 4, 512, 2, 3, false)  \
+    X(5, 64, 4, 256, 2, 6, false)   \
+    X(6, 128, 2, 128, 4, 4, false)  \
+    X(7, 128, 2, 256, 2, 5, true)   \
+    X(8, 128, 3, 256, 2, 4, true)   \
+    X(9, 128, 4, 256, 2, 4, true)   \
+    X(10, 128, 4, 128, 4, 4, true)
 
 MixVariantInfo nbg_mix_variant_info(int variant)
 {
     switch (variant) {
-#define X(id, b, k, jt, u, mb) \
+#define X(id, b, k, jt, u, mb, sf) \
     case id: return MixVariantInfo{b, k, jt, u};
         MIX_VARIANTS(X)
 #undef X
@@ -522,8 +544,8 @@ int nbg_mixed_slots(int device, int variant)
         return g_mixed_slots_cache[device][variant];
     int per_sm = 0, sms = 0;
     switch (variant) {
-#define X(id, b, k, jt, u, mb) \
-    case id: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pair_mixed<b, k, jt, u, mb>, b, 0); break;
+#define X(id, b, k, jt, u, mb, sf) \
+    case id: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pair_mixed<b, k, jt, u, mb, sf>, b, 0); break;
         MIX_VARIANTS(X)
 #undef X
     }
@@ -556,10 +578,10 @@ void nbg_launch_mixed_prep(const CycleBufs &cb, DevCtl *ctl, cudaStream_t st)
 void nbg_launch_mixed_pair(const CycleBufs &cb, DevCtl *ctl, cudaStream_t st)
 {
     switch (cb.mix_variant) {
-#define X(id, b, k, jt, u, mb)                                                                                   \
-    case id:                                                                                                     \
-        k_pair_mixed<b, k, jt, u, mb><<<cb.slots, b, 0, st>>>(cb.a, ctl, cb.seg, cb.jhi, cb.jlo, cb.tile_c, cb.perm, \
-                                                             cb.part, cb.ev_keys, cb.ev_cap);                     \
+#define X(id, b, k, jt, u, mb, sf)                                                                        \
+    case id:                                                                                                  \
+        k_pair_mixed<b, k, jt, u, mb, sf><<<cb.slots, b, 0, st>>>(cb.a, ctl, cb.seg, cb.jhi, cb.jlo, cb.tile_c, \
+                                                                 cb.perm, cb.part, cb.ev_keys, cb.ev_cap);     \
         break;
         MIX_VARIANTS(X)
 #undef X

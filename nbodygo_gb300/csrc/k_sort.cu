@@ -93,7 +93,9 @@ __global__ void __launch_bounds__(RS_BLOCK) k_rs_hist(DevCtl *ctl, const unsigne
     for (int d = threadIdx.x; d < RS_BINS; d += RS_BLOCK) hist[(ll)d * nb + b] = cnt[d];
 }
 
-/* exclusive scan of the digit-major histogram (one block) */
+/* exclusive scan of the digit-major histogram (one block; each thread takes
+ * four consecutive entries per round) */
+#define RS_SCAN_ITEMS 4
 __global__ void __launch_bounds__(1024) k_rs_scan(DevCtl *ctl, ll *hist)
 {
     __shared__ ll warp_tot[32];
@@ -103,10 +105,16 @@ __global__ void __launch_bounds__(1024) k_rs_scan(DevCtl *ctl, ll *hist)
     const ll total = nb * RS_BINS;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     ll carry = 0;
-    for (ll c0 = 0; c0 < total; c0 += 1024) {
-        const ll c = c0 + threadIdx.x;
-        const ll v = c < total ? hist[c] : 0;
-        ll x = v;
+    for (ll c0 = 0; c0 < total; c0 += 1024 * RS_SCAN_ITEMS) {
+        const ll c = c0 + (ll)threadIdx.x * RS_SCAN_ITEMS;
+        ll v[RS_SCAN_ITEMS];
+        ll sum = 0;
+#pragma unroll
+        for (int q = 0; q < RS_SCAN_ITEMS; q++) {
+            v[q] = c + q < total ? hist[c + q] : 0;
+            sum += v[q];
+        }
+        ll x = sum;
         for (int o = 1; o < 32; o <<= 1) {
             ll y = __shfl_up_sync(0xffffffffu, x, o);
             if (lane >= o) x += y;
@@ -122,8 +130,12 @@ __global__ void __launch_bounds__(1024) k_rs_scan(DevCtl *ctl, ll *hist)
             warp_tot[lane] = t;
         }
         __syncthreads();
-        const ll ex = x - v + (w > 0 ? warp_tot[w - 1] : 0);
-        if (c < total) hist[c] = carry + ex;
+        ll ex = carry + x - sum + (w > 0 ? warp_tot[w - 1] : 0);
+#pragma unroll
+        for (int q = 0; q < RS_SCAN_ITEMS; q++) {
+            if (c + q < total) hist[c + q] = ex;
+            ex += v[q];
+        }
         carry += warp_tot[31];
         __syncthreads();
     }

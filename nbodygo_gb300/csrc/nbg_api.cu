@@ -202,15 +202,11 @@ static void free_cap_buffers(CycleBufs &cb);
 
 /* (re)allocates the body-capacity dependent buffers, keeping the first
  * `keep` bodies of the collection */
-/* resident CTAs of the widest shape of the mixed pair kernel */
-static int max_mixed_slots(int device)
+/* partial-sum doubles the mixed pair kernel of the current shape needs */
+static ll part_need(const nbg_ctx *ctx, ll cap)
 {
-    int m = 1;
-    for (int v = 0; v < NBG_MIX_VARIANTS; v++) {
-        const int s = nbg_mixed_slots(device, v);
-        if (s > m) m = s;
-    }
-    return m;
+    const int itile = ctx->cb.itile > 0 ? ctx->cb.itile : NBG_MIX_ITILE;
+    return NBG_PART_DOUBLES(cap, (ll)ctx->cb.slots * NBG_MIX_CHUNKS_PER_CTA, itile);
 }
 
 static int ensure_cap(nbg_ctx *ctx, ll need, ll keep)
@@ -241,7 +237,7 @@ static int ensure_cap(nbg_ctx *ctx, ll need, ll keep)
     /* every sim may end in a partial tile: at most cap / itile + nsims tiles */
     ll tiles = (cap + NBG_MIX_MIN_ITILE - 1) / NBG_MIX_MIN_ITILE + NBG_MAX_SIMS + 1;
     CK(cudaMalloc((void **)&ctx->cb.tile_c, (size_t)tiles * sizeof(float4)));
-    ctx->cb.part_doubles = NBG_PART_DOUBLES(cap, max_mixed_slots(ctx->device));
+    ctx->cb.part_doubles = part_need(ctx, cap);
     CK(cudaMalloc((void **)&ctx->cb.part, (size_t)ctx->cb.part_doubles * sizeof(double)));
     CK(cudaMalloc((void **)&ctx->cb.perm, (size_t)cap * sizeof(unsigned)));
     CK(cudaMalloc((void **)&ctx->cb.sval, (size_t)cap * sizeof(unsigned)));
@@ -974,7 +970,7 @@ static int select_variant(nbg_ctx *ctx, int v)
     ctx->cb.itile = vi.block * vi.k;
     ctx->cb.slots = nbg_mixed_slots(ctx->device, v);
     invalidate_graph(ctx);
-    return NBG_OK;
+    return ensure_part(ctx, part_need(ctx, ctx->cb.cap));
 }
 
 /* Device time of the mixed pair kernel in one force pass of the current
@@ -1158,7 +1154,7 @@ int nbg_set_option(nbg_ctx *ctx, int key, int64_t value)
     if (!ctx) return NBG_E_ARG;
     switch (key) {
     case NBG_OPT_SPLIT:
-        if (value < 0 || value > (1 << 20)) return fail(ctx, NBG_E_ARG, "work CTA cap must be 0..2^20");
+        if (value < 0 || value > (1 << 24)) return fail(ctx, NBG_E_ARG, "chunk cap must be 0..2^24");
         if (value != ctx->cb.work_cap) {
             ctx->cb.work_cap = (int)value;
             invalidate_graph(ctx);

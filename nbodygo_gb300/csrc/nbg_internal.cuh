@@ -58,7 +58,7 @@ struct DevCtl {
     int pad0;
     ll error_need;   /* for NBG_E_OVERFLOW: the size that would have fitted */
     int error_what;  /* 1 = bodies, 2 = events, 3 = fragments, 4 = partials */
-    int splits;      /* mixed: CTAs the pair work is divided among (P) */
+    int splits;      /* mixed: chunks the pair work is cut into (C) */
     ll work_total;   /* mixed: pair work W in (i-tile, j-body) units */
     /* per-cycle values */
     ll ev_count;     /* detected events (may exceed capacity) */
@@ -78,6 +78,7 @@ struct DevCtl {
     ll rend_n;       /* renderables written by the last cycle */
     ll last_ev_n;    /* resolved events recorded by the last cycle */
     ll cycle_interactions; /* sum over sims of n_s (n_s - 1) at the cycle start */
+    ll work_next;    /* mixed: next chunk for the persistent CTAs */
 };
 
 /* A collection may hold several independent simulations stored one after
@@ -175,25 +176,29 @@ struct CycleBufs {
 struct MixVariantInfo {
     int block, k, jt, unroll;
 };
-#define NBG_MIX_VARIANTS 7
+#define NBG_MIX_VARIANTS NBG_MIX_SHAPES
 #define NBG_MIX_MIN_ITILE 256
 #define NBG_MIX_MAX_ITILE 512
-/* fewest (i-tile, j-body) units of pair work a CTA is given */
+/* fewest (i-tile, j-body) units of pair work in a chunk, and chunks per
+ * resident CTA */
 #define NBG_MIX_MIN_WORK 2048
+#define NBG_MIX_CHUNKS_PER_CTA 32
 
 /* The mixed pair work of a cycle is W units, (i-tile, j-body) pairs in sim,
- * i-tile, j order; CTA c of P takes units [c W / P, (c + 1) W / P).  This is
- * the CTA that holds unit u. */
-__host__ __device__ __forceinline__ int nbg_work_cta(ll u, int P, ll W)
+ * i-tile, j order, cut into C equal chunks: chunk c is units
+ * [c W / C, (c + 1) W / C).  Persistent CTAs take chunks from an atomic
+ * counter.  This is the chunk that holds unit u. */
+__host__ __device__ __forceinline__ int nbg_work_chunk(ll u, int C, ll W)
 {
-    return (int)(((u + 1) * (ll)P + W - 1) / W - 1);
+    return (int)(((u + 1) * (ll)C + W - 1) / W - 1);
 }
 
-/* Partial sums of the mixed pair kernel: CTA c's share of i-tile g (global
- * tile index) is slot g + c, 3 x itile doubles; no two (tile, CTA) pairs that
- * both hold work share a slot, since CTAs take the tiles in order.  Slots
- * needed: tiles + P - 1, tiles <= cap / itile + sims. */
-#define NBG_PART_DOUBLES(cap, pmax) (3 * ((ll)(cap) + (ll)NBG_MIX_MAX_ITILE * ((ll)(pmax) + NBG_MAX_SIMS + 2)))
+/* Partial sums of the mixed pair kernel: chunk c's share of i-tile g (global
+ * tile index) is slot g + c, 3 x itile doubles; no two (tile, chunk) pairs
+ * that both hold work share a slot, since chunks are contiguous and ordered.
+ * Slots needed: tiles + C - 1, tiles <= cap / itile + sims. */
+#define NBG_PART_DOUBLES(cap, chunks, itile) \
+    (3 * ((ll)(cap) + (ll)(itile) * ((ll)(chunks) + NBG_MAX_SIMS + 2)))
 
 #define NBG_SCAN_BLOCK 1024
 #define NBG_SCAN_ITEMS 4

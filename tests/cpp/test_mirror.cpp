@@ -12,16 +12,22 @@
  *   TestAdds                     cmd/body/body_collection_test.go:268-282
  *   TestRunnerSetters            cmd/runner/computation-runner_test.go:10-31
  *
+ * and FromCsv (cmd/sim/fromcsv.go:46-131) on the format its header
+ * documents, with the ToCsv snapshot read back bit for bit.
+ *
  * The bodies are those of createTestBody (body_collection_test.go:26-54):
  * every field equal to the id, Name = Class = string(rune(id)).  The Go
  * tests call Cycle/ProcessMods alone; here the whole cycle runs, so bodies
- * that must not collide are given collision=none (no events, body.go:175-178).
+ * that must not collide are given collision=none (no events, body.go:175-178),
+ * and body 0, whose mass is 0, leaves the collection too: Update computes
+ * v += (dt * 0) / 0 = NaN, and a NaN position clears Exists (body.go:114-139).
  *
  * Usage: test_mirror host   - parsing and ApplyMods, no GPU
  *        test_mirror gpu    - everything, on device 0
- * Prints one line per test and exits non-zero on the first failure.
+ * Prints one line per test and exits non-zero if any failed.
  */
 #include <cstdio>
+#include <fstream>
 #include <string>
 #include <vector>
 
@@ -113,6 +119,65 @@ static void TestParse()
     std::printf("ok   %s\n", cur_test);
 }
 
+static void TestFromCsv()
+{
+    cur_test = "TestFromCsv";
+    const std::string path = "test_mirror_in.csv";
+    {
+        std::ofstream o(path);
+        o << "# a comment\n"
+          << "100,100,100,100,100,100,10,.5,,,blue\n"   /* empty is_sun does not parse: skipped */
+          << "1,1,1,1,1,1,10000,10,true,elastic\n"      /* a sun */
+          << "\n"
+          << " 2 , 3 ,4,5,6,7,8,9,F,SUBSUME,Green,1.5,2.5\n"
+          << "1,2,3,4,5,6,7\n"                         /* radius missing: skipped */
+          << "1,2,3,4,5,6,7,x\n"                       /* radius does not parse: skipped */
+          << "\"-1e3\",0,0,0,0,0,1,1,0,bogus,teal\n"    /* quoted field; unknown names take defaults */
+          << "9,9,9,9,9,9,9,9\n";
+    }
+    const int64_t id0 = next_id_counter().load();
+    std::vector<Body> b = FromCsv(path, 1000, Fragment, Cyan);
+    CHECK(b.size() == 4, "record count");
+    CHECK(b[0].IsSun && b[0].X == 1 && b[0].Mass == 10000 && b[0].Radius == 10 && b[0].Behavior == Elastic &&
+              b[0].Color == Cyan && b[0].intensity == 100,
+          "sun record");
+    CHECK(!b[1].IsSun && b[1].X == 2 && b[1].Y == 3 && b[1].Vz == 7 && b[1].Behavior == Subsume &&
+              b[1].Color == Green && b[1].FragFactor == 1.5 && b[1].FragStep == 2.5,
+          "full record");
+    CHECK(b[2].X == -1e3 && b[2].Behavior == Elastic && b[2].Color == Random, "quoted record, unknown names");
+    CHECK(b[3].Behavior == Fragment && b[3].Color == Cyan && b[3].FragFactor == 0, "defaults");
+    CHECK(b[0].Id == id0 && b[3].Id == id0 + 3, "ids from NextId");
+    CHECK(FromCsv(path, 2, Elastic, Random).size() == 2, "bodyCount limit");
+    CHECK(FromCsv("no_such_file.csv", 10, Elastic, Random).empty(), "missing file");
+    /* snapshot round trip */
+    b[1].X = 0.1 + 0.2;
+    b[1].Vy = -1.0 / 3.0;
+    CHECK(ToCsv("test_mirror_snap.csv", b), "write snapshot");
+    std::vector<Body> r = FromCsv("test_mirror_snap.csv", 1000, None, Random);
+    CHECK(r.size() == b.size(), "snapshot count");
+    for (size_t k = 0; k < r.size(); k++)
+        CHECK(r[k].X == b[k].X && r[k].Y == b[k].Y && r[k].Z == b[k].Z && r[k].Vx == b[k].Vx && r[k].Vy == b[k].Vy &&
+                  r[k].Vz == b[k].Vz && r[k].Mass == b[k].Mass && r[k].Radius == b[k].Radius &&
+                  r[k].IsSun == b[k].IsSun && r[k].Behavior == b[k].Behavior && r[k].Color == b[k].Color &&
+                  r[k].FragFactor == b[k].FragFactor && r[k].FragStep == b[k].FragStep,
+              "snapshot values");
+    {
+        std::ofstream o("test_mirror_bad.csv");
+        o << "1,2,3,4,5,6,7,8x\"y\n";
+    }
+    bool threw = false;
+    try {
+        FromCsv("test_mirror_bad.csv", 10, Elastic, Random);
+    } catch (const Error &) {
+        threw = true;
+    }
+    CHECK(threw, "bare quote is an error");
+    std::remove(path.c_str());
+    std::remove("test_mirror_snap.csv");
+    std::remove("test_mirror_bad.csv");
+    std::printf("ok   %s\n", cur_test);
+}
+
 static void TestInitSize()
 {
     cur_test = "TestInitSize";
@@ -130,8 +195,8 @@ static void TestRemove()
     CHECK(bc.ModBody(idToDelete, "", "", {"exists=false"}) == ModAll, "mod");
     ComputationRunner cr(1, 1e-9, false, bc);
     cr.RunOneComputation();
-    CHECK(bc.Count() == cnt - 1, "Body was not removed");
-    for (const Body &b : bc.GetArray()) CHECK(b.Id != idToDelete, "Body should have been removed");
+    CHECK(bc.Count() == cnt - 2, "Body was not removed (body 0 leaves by the NaN rule)");
+    for (const Body &b : bc.GetArray()) CHECK(b.Id != idToDelete && b.Id != 0, "Body should have been removed");
     std::printf("ok   %s\n", cur_test);
 }
 
@@ -191,7 +256,7 @@ static void TestAdds()
     bool found = false;
     for (const Body &b : bc.GetArray()) found |= b.Id == idToAdd;
     CHECK(found, "Body was not added");
-    CHECK(bc.Count() == cnt + 1, "count after add");
+    CHECK(bc.Count() == cnt, "count after add (body 0 leaves by the NaN rule)");
     std::printf("ok   %s\n", cur_test);
 }
 
@@ -240,6 +305,7 @@ int main(int argc, char **argv)
     const std::string mode = argc > 1 ? argv[1] : "host";
     TestMod();
     TestParse();
+    TestFromCsv();
     if (mode == "gpu" && !g_fail) {
         try {
             TestInitSize();

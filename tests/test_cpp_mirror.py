@@ -2,9 +2,9 @@
 tests of the body collection and the runner, restated in tests/cpp/test_mirror.cpp.
 
 The program is compiled with g++ and linked to libnbgpu.so.  Without a GPU
-only its host part runs (ApplyMods and the parsing helpers,
-cmd/body/body_test.go:9-47, cmd/globals/globals.go:41-102); on a GPU every
-test runs through the C ABI.
+only its host part runs (ApplyMods, the parsing helpers and the CSV loader,
+cmd/body/body_test.go:9-47, cmd/globals/globals.go:41-102,
+cmd/sim/fromcsv.go:46-131); on a GPU every test runs through the C ABI.
 """
 import os
 import shutil
@@ -29,14 +29,14 @@ def _compile(tmp_path):
 
 
 def _run(exe, mode, timeout):
-    r = subprocess.run([exe, mode], capture_output=True, text=True, timeout=timeout)
+    r = subprocess.run([exe, mode], capture_output=True, text=True, timeout=timeout, cwd=os.path.dirname(exe))
     assert r.returncode == 0 and r.stdout.strip().endswith("PASSED"), r.stdout + r.stderr
     return r.stdout
 
 
 def test_mirror_host_part(tmp_path):
     out = _run(_compile(tmp_path), "host", 60)
-    assert "ok   TestMod" in out and "ok   TestParse" in out
+    assert "ok   TestMod" in out and "ok   TestParse" in out and "ok   TestFromCsv" in out
 
 
 @pytest.mark.gpu
