@@ -421,9 +421,14 @@ def main():
         mag = np.sqrt(fp[0] ** 2 + fp[1] ** 2 + fp[2] ** 2)
         err = np.sqrt((fm[0] - fp[0]) ** 2 + (fm[1] - fp[1]) ** 2 + (fm[2] - fp[2]) ** 2)
         ok = mag > 0
+        # energy over the same cycles from the same state, both forms
+        e0 = sum(plain.energy()[:2])
         plain.enable_timing(True)
         pi = plain.step(DT, 1.0, 2)
         ptm = plain.timing()
+        plain.enable_timing(False)
+        mixed0.step(DT, 1.0, 2)
+        ep, em = sum(plain.energy()[:2]), sum(mixed0.energy()[:2])
         p_ms = (ptm["pair_ms"] + ptm["other_ms"]) / max(1, ptm["pair_launches"])
         plain_rate = pi["interactions"] / (1e-3 * (ptm["pair_ms"] + ptm["other_ms"]))
         result_extra["plain_fp64"] = {
@@ -434,7 +439,10 @@ def main():
         result_extra["mixed_over_plain"] = value / plain_rate / ws if plain_rate else None
         result_extra["accuracy"] = {"rel_l2_vs_fp64": float(num / den), "max_rel": float(np.max(err[ok] / mag[ok])),
                                     "median_rel": float(np.median(err[ok] / mag[ok])),
-                                    "reference": "plain FP64 GPU forces (bit-identical to the oracle)"}
+                                    "reference": "plain FP64 GPU forces (bit-identical to the oracle)",
+                                    "energy_drift_2_cycles": {"fp64": abs(ep - e0) / abs(e0),
+                                                              "mixed": abs(em - e0) / abs(e0),
+                                                              "mixed_vs_fp64": abs(em - ep) / abs(e0)}}
         plain.close()
         mixed0.close()
 

@@ -231,7 +231,8 @@ int nbg_get_events(nbg_ctx *ctx, nbg_event *host, int64_t cap, int64_t *n);
 int nbg_get_forces(nbg_ctx *ctx, double *fx, double *fy, double *fz, int64_t cap, int64_t *n);
 
 /* Total energy (kinetic + pairwise potential, FP64) and momentum of the bodies
- * that exist; a diagnostic, O(N^2) on the device. */
+ * that exist, summed over the collections (pairs within each collection); a
+ * diagnostic, O(N^2) on the device. */
 int nbg_energy(nbg_ctx *ctx, double *kinetic, double *potential, double momentum[3]);
 
 /* ---- force pass without device allocation ------------------------------ */

@@ -1005,7 +1005,7 @@ __global__ void k_find(BodyArrays A, DevCtl *ctl, ll id, ll *idx)
 /* Kinetic and pairwise potential energy plus momentum, per-block partials
  * (out[blockIdx*5 + 0..4]) summed on the host in block order. */
 #define EN_BLOCK 128
-__global__ void __launch_bounds__(EN_BLOCK) k_energy(BodyArrays A, DevCtl *ctl, double *out)
+__global__ void __launch_bounds__(EN_BLOCK) k_energy(BodyArrays A, DevCtl *ctl, SimSegs seg, double *out)
 {
     __shared__ double red[5][EN_BLOCK];
     const ll n = ctl->n;
@@ -1018,7 +1018,8 @@ __global__ void __launch_bounds__(EN_BLOCK) k_energy(BodyArrays A, DevCtl *ctl, 
         py = m * vy;
         pz = m * vz;
         const double xi = A.x[i], yi = A.y[i], zi = A.z[i];
-        for (ll j = i + 1; j < n; j++) {
+        const ll end = seg.off[nbg_sim_of(seg.off, seg.nsims, i) + 1]; /* pairs within i's sim */
+        for (ll j = i + 1; j < end; j++) {
             if (!(A.flags[j] & NBG_F_EXISTS)) continue;
             const double dx = A.x[j] - xi, dy = A.y[j] - yi, dz = A.z[j] - zi;
             const double r = sqrt(dx * dx + dy * dy + dz * dz);
@@ -1114,5 +1115,5 @@ void nbg_launch_find(const CycleBufs &cb, DevCtl *ctl, ll id, ll *idx_dev, cudaS
 void nbg_launch_energy(const CycleBufs &cb, DevCtl *ctl, double *out_dev, cudaStream_t st)
 {
     int g = (int)((cb.cap + EN_BLOCK - 1) / EN_BLOCK);
-    k_energy<<<g, EN_BLOCK, 0, st>>>(cb.a, ctl, out_dev);
+    k_energy<<<g, EN_BLOCK, 0, st>>>(cb.a, ctl, cb.seg, out_dev);
 }

@@ -243,6 +243,76 @@ __device__ __forceinline__ void fold64(float &hi, float &lo, double v)
     lo += vl;
 }
 
+/* i-body at sorted position p (p >= n: none) re-centred on the tile origin
+ * c, and its near-pair threshold t on r^2 (FP32, conservative): pairs closer
+ * than max(r_i + r_max + the FP32 error bound, kappa |x - c|_max) take the
+ * exact path.  A special body sits at the sentinel with t = -1. */
+__device__ __forceinline__ void i_body_setup(const float4 *__restrict__ jhi, const float4 *__restrict__ jlo, ll p, ll n,
+                                             const float4 &c, float rmax, float xmax, double kappa, float &xr,
+                                             float &yr, float &zr, float &t)
+{
+    xr = yr = zr = 0.f;
+    t = -1.f;
+    if (p >= n) return;
+    const float4 h = jhi[p], l = jlo[p];
+    if (packed_special(l)) {
+        xr = yr = zr = SENTINEL_POS;
+        return;
+    }
+    xr = (h.x - c.x) + l.x;
+    yr = (h.y - c.y) + l.y;
+    zr = (h.z - c.z) + l.z;
+    const double ri = (double)l.w + fabs((double)l.w) * 0x1p-22; /* rounded up */
+    const double D = fmax(0.0, ri + (double)rmax);
+    const double amax = (double)fmaxf(fabsf(xr), fmaxf(fabsf(yr), fabsf(zr)));
+    const double eps = 0x1p-19 * (amax + D) + 0x1p-44 * (double)xmax + 0x1p-100;
+    const double b = fmax(D + eps, kappa * amax) * (1.0 + 0x1p-18);
+    t = __double2float_ru(b * b);
+}
+
+/* One j of a near-pair pass for i-body p (raw i: hi_i, lo_i; re-centred
+ * i: xi..zi; threshold thk): adds the FP32 term to (tx, ty, tz), or, for a
+ * near pair, the term from the exact hi/lo difference, or, for a possible
+ * overlap, the FP64 term folded into the (hi, lo) sums with the event
+ * recorded.  xj..m are j's re-centred position and mass from the tile;
+ * hj, lj its raw hi/lo (read only for a near pair, through get_raw). */
+template <typename RAW>
+__device__ __forceinline__ void near_pass_j(const BodyArrays &A, DevCtl *ctl, ull *ev_keys, ll ev_cap,
+                                            const unsigned *__restrict__ perm, double inv_ms, ll i, ll q,
+                                            const float4 &hi_i, const float4 &lo_i, float xi, float yi, float zi,
+                                            float thk, float xj, float yj, float zj, float m, RAW get_raw, float &tx,
+                                            float &ty, float &tz, float &fhx, float &flx, float &fhy, float &fly,
+                                            float &fhz, float &flz)
+{
+    float dx = xj - xi, dy = yj - yi, dz = zj - zi;
+    float r2 = dx * dx + dy * dy + dz * dz;
+    if (r2 < thk) {
+        /* near pair: difference of the hi/lo positions (error ~2^-24 |dx|) */
+        float4 hj, lj;
+        get_raw(q, hj, lj);
+        dx = (hj.x - hi_i.x) + (lj.x - lo_i.x);
+        dy = (hj.y - hi_i.y) + (lj.y - lo_i.y);
+        dz = (hj.z - hi_i.z) + (lj.z - lo_i.z);
+        r2 = dx * dx + dy * dy + dz * dz;
+        const float rs = lo_i.w + lj.w;
+        /* an overlap, or a pair within 2^-10 of the overlap distance, is
+         * decided in FP64 */
+        if (!(r2 > rs * rs * (1.0f + 0x1p-10f) && rs >= 0.f) || (lo_i.w < 0.f) || (lj.w < 0.f)) {
+            double qx, qy, qz;
+            candidate_pair(A, ctl, ev_keys, ev_cap, i, (ll)perm[q], inv_ms, qx, qy, qz);
+            fold64(fhx, flx, qx);
+            fold64(fhy, fly, qy);
+            fold64(fhz, flz, qz);
+            return;
+        }
+    }
+    const float inv = rsqrt_sfu(r2);
+    const float s = m * inv * inv * inv;
+    tx += s * dx;
+    ty += s * dy;
+    tz += s * dz;
+}
+
 /* Everything in this kernel is indexed by sorted position (p for i, q for
  * j); perm maps a position to the body index used by the FP64 arrays and the
  * event keys. */
@@ -302,23 +372,8 @@ k_pair_mixed(BodyArrays A, DevCtl *ctl, SimSegs seg, const float4 *__restrict__ 
 #pragma unroll
         for (int k = 0; k < K; k++) {
             const ll p = ibase + (ll)k * BLOCK + tid;
-            float xr = 0.f, yr = 0.f, zr = 0.f, t = -1.f;
-            if (p < n) {
-                const float4 h = jhi[p], l = jlo[p];
-                if (!packed_special(l)) {
-                    xr = (h.x - c.x) + l.x;
-                    yr = (h.y - c.y) + l.y;
-                    zr = (h.z - c.z) + l.z;
-                    const double ri = (double)l.w + fabs((double)l.w) * 0x1p-22; /* rounded up */
-                    const double D = fmax(0.0, ri + (double)rmax);
-                    const double amax = (double)fmaxf(fabsf(xr), fmaxf(fabsf(yr), fabsf(zr)));
-                    const double eps = 0x1p-19 * (amax + D) + 0x1p-44 * (double)xmax + 0x1p-100;
-                    const double b = fmax(D + eps, kappa * amax) * (1.0 + 0x1p-18);
-                    t = __double2float_ru(b * b);
-                } else {
-                    xr = yr = zr = SENTINEL_POS;
-                }
-            }
+            float xr, yr, zr, t;
+            i_body_setup(jhi, jlo, p, n, c, rmax, xmax, kappa, xr, yr, zr, t);
             nx[k] = make_float2(-xr, -xr);
             ny[k] = make_float2(-yr, -yr);
             nz[k] = make_float2(-zr, -zr);
@@ -402,36 +457,14 @@ k_pair_mixed(BodyArrays A, DevCtl *ctl, SimSegs seg, const float4 *__restrict__ 
                         for (int e = 0; e < 2; e++) {
                             const ll q = jt + 2 * pp + e;
                             if (q >= je || q == p) continue;
-                            const float xj = e ? a.y : a.x, yj = e ? a.w : a.z;
-                            const float zj = e ? b.y : b.x, m = e ? b.w : b.z;
-                            float dx = xj - xi, dy = yj - yi, dz = zj - zi;
-                            float r2 = dx * dx + dy * dy + dz * dz;
-                            if (r2 < thk) {
-                                /* near pair: difference of the hi/lo positions
-                                 * (error ~2^-24 |dx|) */
-                                const float4 hj = jhi[q], lj = jlo[q];
-                                dx = (hj.x - hi_i.x) + (lj.x - lo_i.x);
-                                dy = (hj.y - hi_i.y) + (lj.y - lo_i.y);
-                                dz = (hj.z - hi_i.z) + (lj.z - lo_i.z);
-                                r2 = dx * dx + dy * dy + dz * dz;
-                                const float rs = lo_i.w + lj.w;
-                                /* an overlap, or a pair within 2^-10 of the
-                                 * overlap distance, is decided in FP64 */
-                                if (!(r2 > rs * rs * (1.0f + 0x1p-10f) && rs >= 0.f) || (lo_i.w < 0.f) ||
-                                    (lj.w < 0.f)) {
-                                    double qx, qy, qz;
-                                    candidate_pair(A, ctl, ev_keys, ev_cap, i, (ll)perm[q], inv_ms, qx, qy, qz);
-                                    fold64(FOLD(0, k), FOLD(1, k), qx);
-                                    fold64(FOLD(2, k), FOLD(3, k), qy);
-                                    fold64(FOLD(4, k), FOLD(5, k), qz);
-                                    continue;
-                                }
-                            }
-                            const float inv = rsqrt_sfu(r2);
-                            const float s = m * inv * inv * inv;
-                            tx += s * dx;
-                            ty += s * dy;
-                            tz += s * dz;
+                            near_pass_j(A, ctl, ev_keys, ev_cap, perm, inv_ms, i, q, hi_i, lo_i, xi, yi, zi, thk,
+                                        e ? a.y : a.x, e ? a.w : a.z, e ? b.y : b.x, e ? b.w : b.z,
+                                        [&](ll qq, float4 &hj, float4 &lj) {
+                                            hj = jhi[qq];
+                                            lj = jlo[qq];
+                                        },
+                                        tx, ty, tz, FOLD(0, k), FOLD(1, k), FOLD(2, k), FOLD(3, k), FOLD(4, k),
+                                        FOLD(5, k));
                         }
                     }
                     ax[k] = make_float2(tx, 0.f);
@@ -507,27 +540,30 @@ __global__ void k_mix_out(BodyArrays A, DevCtl *ctl, SimSegs seg, const unsigned
 }
 
 /* ---- kernel shapes ---------------------------------------------------------
- * (threads per CTA, i-bodies per thread, j per shared-memory tile, unroll of
- * the j loop, CTAs per SM the register budget is set for, sums in shared
- * memory).  Variant 0 is the default; the autotuner (nbg_autotune) measures
- * the others. */
-#define MIX_VARIANTS(X)             \
-    X(0, 128, 4, 256, 2, 3, false)  \
-    X(1, 128, 4, 256, 1, 3, false)  \
-    X(2, 128, 2, 256, 2, 4, false)  \
-    X(3, 256, 2, 256, 2, 2, false)  \
-    X(4, 128, 4, 512, 2, 3, false)  \
-    X(5, 64, 4, 256, 2, 6, false)   \
-    X(6, 128, 2, 128, 4, 4, false)  \
-    X(7, 128, 2, 256, 2, 5, true)   \
-    X(8, 128, 3, 256, 2, 4, true)   \
-    X(9, 128, 4, 256, 2, 4, true)   \
-    X(10, 128, 4, 128, 4, 4, true)
+ * (kind, threads per CTA, i-bodies per thread, j per shared-memory tile,
+ * unroll of the j loop, CTAs per SM the register budget is set for).  Kind 0:
+ * sums in registers; 1: sums in shared memory.  Variant 0 is the default; the
+ * autotuner (nbg_autotune) measures the others. */
+#define MIX_VARIANTS(X)              \
+    X(0, 0, 128, 4, 256, 2, 3)       \
+    X(1, 0, 128, 4, 256, 1, 3)       \
+    X(2, 0, 128, 2, 256, 2, 4)       \
+    X(3, 0, 256, 2, 256, 2, 2)       \
+    X(4, 0, 128, 4, 512, 2, 3)       \
+    X(5, 0, 64, 4, 256, 2, 6)        \
+    X(6, 0, 128, 2, 128, 4, 4)       \
+    X(7, 1, 128, 2, 256, 2, 5)       \
+    X(8, 1, 128, 3, 256, 2, 4)       \
+    X(9, 1, 128, 4, 256, 2, 4)       \
+    X(10, 1, 128, 4, 128, 4, 4)
+
+/* the kernel of a shape */
+#define MIX_KERNEL(kind, b, k, jt, u, mb) k_pair_mixed<b, k, jt, u, mb, (kind) == 1>
 
 MixVariantInfo nbg_mix_variant_info(int variant)
 {
     switch (variant) {
-#define X(id, b, k, jt, u, mb, sf) \
+#define X(id, kind, b, k, jt, u, mb) \
     case id: return MixVariantInfo{b, k, jt, u};
         MIX_VARIANTS(X)
 #undef X
@@ -544,8 +580,8 @@ int nbg_mixed_slots(int device, int variant)
         return g_mixed_slots_cache[device][variant];
     int per_sm = 0, sms = 0;
     switch (variant) {
-#define X(id, b, k, jt, u, mb, sf) \
-    case id: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pair_mixed<b, k, jt, u, mb, sf>, b, 0); break;
+#define X(id, kind, b, k, jt, u, mb) \
+    case id: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, MIX_KERNEL(kind, b, k, jt, u, mb), b, 0); break;
         MIX_VARIANTS(X)
 #undef X
     }
@@ -578,10 +614,10 @@ void nbg_launch_mixed_prep(const CycleBufs &cb, DevCtl *ctl, cudaStream_t st)
 void nbg_launch_mixed_pair(const CycleBufs &cb, DevCtl *ctl, cudaStream_t st)
 {
     switch (cb.mix_variant) {
-#define X(id, b, k, jt, u, mb, sf)                                                                        \
-    case id:                                                                                                  \
-        k_pair_mixed<b, k, jt, u, mb, sf><<<cb.slots, b, 0, st>>>(cb.a, ctl, cb.seg, cb.jhi, cb.jlo, cb.tile_c, \
-                                                                 cb.perm, cb.part, cb.ev_keys, cb.ev_cap);     \
+#define X(id, kind, b, k, jt, u, mb)                                                                       \
+    case id:                                                                                           \
+        MIX_KERNEL(kind, b, k, jt, u, mb)<<<cb.slots, b, 0, st>>>(cb.a, ctl, cb.seg, cb.jhi, cb.jlo, cb.tile_c, \
+                                                                  cb.perm, cb.part, cb.ev_keys, cb.ev_cap);   \
         break;
         MIX_VARIANTS(X)
 #undef X
