@@ -66,6 +66,8 @@ WORKLOADS = {
     "uniform": ("mixed", 0.01, "uniform ball R=20000, m=1e10, radius 0.05, v~N(0,1), no collisions"),
     "plummer": ("fp64", 0.01, "Plummer a=200 M=1e16, radius 0.2, elastic"),
     "disk": ("fp64", 0.005, "central body 5e15 + disk r 100-1000, elastic"),
+    "plummer_bh": ("fp64", 0.01, "Plummer a=200 M=1e16, 131072 bodies, radius 0.2, elastic; Barnes-Hut octree "
+                                 "forces (theta 0.3, softening 1e-4, FP64), exact collisions"),
 }
 
 
@@ -206,6 +208,8 @@ def make_workload(name, n_each, rank):
         return [W.uniform_ball(seed=4 + seed_off)]
     if name == "plummer":
         return [W.plummer(seed=2 + seed_off)]
+    if name == "plummer_bh":
+        return [W.plummer(131072, seed=2 + seed_off)]
     return [W.disk(seed=1 + seed_off)]
 
 
@@ -228,10 +232,15 @@ def cpu_baseline_sample(workload, dt):
     elif workload == "plummer":
         b = W.plummer(seed=2)
         what = "plummer with 16384 bodies (the full workload)"
+    elif workload == "plummer_bh":
+        b = W.plummer(32768, seed=2)
+        what = "plummer with 32768 bodies, Barnes-Hut (the reference's octree, built once per cycle)"
     else:
         b = W.disk(seed=1)
         what = "disk with 1000 bodies (the full workload)"
     o = OracleSim(threads=cores)
+    if workload.endswith("_bh"):
+        o.set_barnes_hut(True)
     o.set_bodies(b)
     steps = 1 if len(b["x"]) > 10000 else 20
     t0 = time.perf_counter()
@@ -256,10 +265,15 @@ def run_reference(args, ws, rank):
     elif args.workload == "plummer":
         b = W.plummer(seed=2)
         sample = "the full plummer workload (16,384 bodies)"
+    elif args.workload == "plummer_bh":
+        b = W.plummer(32768, seed=2)
+        sample = "plummer with 32,768 bodies per cycle, Barnes-Hut"
     else:
         b = W.disk(seed=1)
         sample = "the full disk workload (1,000 bodies)"
     o = OracleSim(threads=cores)
+    if args.workload.endswith("_bh"):
+        o.set_barnes_hut(True)
     o.set_bodies(b)
     for _ in range(args.warmup):
         o.step(dt, 1.0, 1)
@@ -323,9 +337,12 @@ def main():
     chunk = 10 if args.workload == "ensemble" else 1
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
 
+    bh = args.workload.endswith("_bh")
     sim = Simulation(prec, device=local, capacity=n0 + 4096)
     sim.set_stream(stream.cuda_stream)
     sim.set_option(A.OPT_GRAPH_CYCLES, chunk)
+    if bh:
+        sim.set_option(A.OPT_BARNES_HUT, 1)
     load(sim, sims)
     tuned = None
     if prec == "mixed" and args.shape is not None:
@@ -368,6 +385,7 @@ def main():
     tm = sim.timing()
     sim.enable_timing(False)
     inter_t = info_t["interactions"] / max(1, info_t["steps_done"])
+    bh_terms_t = info_t["bh_terms"] / max(1, info_t["steps_done"])
     pair_ms = tm["pair_ms"] / max(1, tm["pair_launches"])
     launches = tm["kernel_launches"] / max(1, info_t["steps_done"]) * cycles
 
@@ -446,7 +464,13 @@ def main():
         plain.close()
         mixed0.close()
 
-    if prec == "mixed":
+    if bh:
+        # the whole tree pass (build, walk, collision query) against the FP64
+        # peak, counting only the point-mass terms the walk summed
+        achieved = bh_terms_t * FLOPS_PER_PAIR / (pair_ms * 1e-3) / 1e12
+        peak, kernel, bound = f64 / 1e12, "k_bh_* (tree build + k_bh_force + k_bh_collide)", "fp64_fma"
+        peak_src = f"DFMA-chain probe on this GPU at {mhz:.0f} MHz (MEASURED_PEAKS.json has no FP64 figure)"
+    elif prec == "mixed":
         achieved = inter_t * FLOPS_PER_PAIR / (pair_ms * 1e-3) / 1e12
         peak, kernel, bound = f32 / 1e12, "k_pair_mixed", "fp32_fma"
         peak_src = f"FFMA-chain probe on this GPU at {mhz:.0f} MHz (MEASURED_PEAKS.json has no FP32 figure)"
@@ -484,6 +508,13 @@ def main():
             "cpu_baseline": cpu,
             "autotune": tuned,
         }
+        if bh:
+            line["barnes_hut"] = {
+                "point_mass_terms_per_cycle": bh_terms_t,
+                "terms_per_body": bh_terms_t / max(1, n0),
+                "tree_pass_ms": pair_ms,
+                "note": "value counts N(N-1) per cycle, the direct sum the tree replaces; the roofline counts "
+                        "the terms the walk summed"}
         line.update(result_extra)
         print(json.dumps(line), flush=True)
     dist.close()

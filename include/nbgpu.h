@@ -103,6 +103,7 @@ typedef struct nbg_step_info {
     int64_t removed;           /* bodies removed by Cycle */
     int64_t nan_removed;       /* bodies removed because x, y or z became NaN */
     int64_t next_id;           /* next id NextId() would return */
+    int64_t bh_terms;          /* Barnes-Hut: point-mass terms the force pass summed */
 } nbg_step_info;
 
 /* Renderable (cmd/body/renderable.go:9-17) minus host-side colour/intensity. */
@@ -258,7 +259,7 @@ int nbg_energy(nbg_ctx *ctx, double *kinetic, double *potential, double momentum
  * Errors are reported through nbg_last_error(NULL).
  */
 #define NBG_NOALLOC_MAX_BODIES 65536
-#define NBG_NOALLOC_BYTES 9472768
+#define NBG_NOALLOC_BYTES 9473024
 int nbg_forces_mixed_noalloc(const double *x, const double *y, const double *z, const double *mass,
                              const double *radius, const uint32_t *flags, int64_t n, double *fx, double *fy,
                              double *fz, void *stream);
@@ -285,6 +286,12 @@ int nbg_get_timing(nbg_ctx *ctx, nbg_timing *t);
 #define NBG_OPT_GRAPH_CYCLES 6 /* cycles captured in one CUDA graph (default 1) */
 #define NBG_OPT_MIX_SHAPE 7    /* shape of the mixed pair kernel, 0..NBG_MIX_SHAPES-1 (see nbg_autotune) */
 #define NBG_MIX_SHAPES 11
+/* 1: forces from the Barnes-Hut octree of cmd/body/octree.go (opening angle
+ * 0.3, softening 1e-4, suns summed directly) with the FP64 arithmetic of the
+ * plain form, in either precision; collisions stay exact.  This is the
+ * reference's --barnes-hut path with its missing Octree.Build call made
+ * (body_collection.go:298-300).  Needs a single collection. */
+#define NBG_OPT_BARNES_HUT 8
 #define NBG_OPT_NEAR_PPM 5   /* mixed: pairs closer than (value * 1e-6) x the i-tile's
                                 extent around its origin are computed in FP64
                                 (default 70000) */

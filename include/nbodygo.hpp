@@ -557,12 +557,13 @@ class BodyCollection {
 /* ComputationRunner (computation-runner.go:24-326) over the GPU cycle. */
 class ComputationRunner {
   public:
-    /* NewComputationRunner(workerCnt, timeScaling, barnesHut, rqh, bc): the
-     * GPU runs the direct sum; barnesHut must be false. */
+    /* NewComputationRunner(workerCnt, timeScaling, barnesHut, rqh, bc):
+     * barnesHut selects the octree force pass (with the tree built every
+     * cycle, which the reference's BuildTree omits). */
     ComputationRunner(int workerCnt, double timeScaling, bool barnesHut, BodyCollection &bc)
         : bc_(bc), workers_(workerCnt), dt_(timeScaling)
     {
-        if (barnesHut) throw Error(NBG_E_ARG, "the GPU cycle is the direct sum (--no-barnes-hut)");
+        bc_.check(nbg_set_option(bc_.ctx(), NBG_OPT_BARNES_HUT, barnesHut ? 1 : 0));
     }
 
     /* setters take effect at the start of the next cycle (1-slot channels) */

@@ -42,6 +42,7 @@ OPT_FRAG_CAP = 4
 OPT_NEAR_PPM = 5
 OPT_GRAPH_CYCLES = 6
 OPT_MIX_SHAPE = 7
+OPT_BARNES_HUT = 8
 MIX_SHAPES = 11
 
 _pd = C.POINTER(C.c_double)
@@ -86,7 +87,7 @@ class NbgSoa(C.Structure):
 class NbgStepInfo(C.Structure):
     _fields_ = [(f, C.c_int64) for f in (
         "steps_done", "n_bodies", "interactions", "events", "fragments_emitted", "removed", "nan_removed",
-        "next_id")]
+        "next_id", "bh_terms")]
 
 
 class NbgRenderable(C.Structure):

@@ -3,9 +3,10 @@
     python -m nbodygo_gb300.build            # build what is out of date
     python -m nbodygo_gb300.build --force    # rebuild everything
 
-The translation units compile in parallel.  k_cycle.cu is compiled with
---fmad=false: its FP64 arithmetic must round after every operation to match
-the reference's Go code (and the oracle, compiled with -ffp-contract=off).
+The translation units compile in parallel.  k_cycle.cu and k_bh.cu are
+compiled with --fmad=false: their FP64 arithmetic must round after every
+operation to match the reference's Go code (and the oracle, compiled with
+-ffp-contract=off).
 """
 import argparse
 import os
@@ -25,6 +26,7 @@ NVCC_COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompi
                "-Xcompiler", "-ffp-contract=off", "-I", CSRC, "-I", os.path.join(ROOT, "include")]
 UNITS = {
     "k_cycle.cu": ["--fmad=false", "-DNBG_NO_FMAD"],
+    "k_bh.cu": ["--fmad=false", "-DNBG_NO_FMAD"],
     "k_mixed.cu": [],
     "k_sort.cu": [],
     "k_probe.cu": [],

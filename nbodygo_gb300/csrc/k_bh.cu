@@ -1,0 +1,768 @@
+/*
+ * k_bh.cu - the Barnes-Hut force pass (cmd/body/octree.go) on the GPU.
+ *
+ * The reference builds a point-region octree by inserting the bodies that
+ * exist and are not fragmenting, in array order, into a cube centred on
+ * their bounding box (half = max extent / 2 * 1.05, octree.go:136-188); a
+ * leaf holds one body, and an occupied leaf that receives another splits
+ * into eight children.  Which node each body ends in depends only on the
+ * comparisons x >= cx, y >= cy, z >= cz down the tree (octantOf,
+ * octree.go:53-65), so the tree is built here without insertion:
+ *
+ *   1. every tree body descends BH_LEVELS levels with the reference's own
+ *      centre arithmetic (cx +- half / 2, half / 2) and records its octant
+ *      path, 3 bits a level, as a 63-bit key;
+ *   2. the keys are sorted (LSD radix, stable);
+ *   3. a node is a key prefix shared by at least one body whose parent holds
+ *      two or more: the nodes that start at sorted position p run from the
+ *      first level where key p differs from key p - 1 down to the level
+ *      where it parts from key p + 1, so their count comes from the two
+ *      neighbouring keys, and one scan numbers every node in depth-first
+ *      order (position, then level).  That order makes the first child of a
+ *      node the next node and the end of its subtree the first node starting
+ *      at the end of its body range (the skip pointer), so the force pass
+ *      walks the tree without a stack;
+ *   4. masses and centres of mass are summed bottom-up, level by level, over
+ *      the children in octant order.
+ *
+ * The force pass (accumForce, octree.go:265-305) walks the tree for every
+ * body with the reference's expressions, softening 1e-4 and opening angle
+ * 0.3; a sun sums every body directly (CalcForce, octree.go:236-263).  The
+ * collision pass (Compute's second loop, body.go:171-186) becomes a range
+ * query on the same tree: nodes whose cube lies farther than r_i + r_max are
+ * skipped, and every body that remains is tested with the reference's exact
+ * dist <= r_i + r_j, so the event set is the O(N^2) loop's.  Bodies outside
+ * the tree (not existing, fragmenting, or not finite) are tested one by one.
+ *
+ * Against the reference's tree:
+ *  - the tree and the opening decisions are the same; a node's centre of
+ *    mass is sum(m x) / sum(m) instead of the reference's running update,
+ *    which differs in the last bits (a one-body leaf is x * m / m, as in the
+ *    reference).  The reference's node whose first inserted body is massless
+ *    has a NaN centre (0 / 0) and is therefore always opened; that is kept;
+ *  - keys have 21 levels; bodies that share a node at that depth (closer
+ *    than 2^-20 of the root cube) stay together in one leaf and each acts as
+ *    a leaf of its own, where the reference keeps splitting (and recurses
+ *    without end for two bodies at one position);
+ *  - the sun's direct sum is a parallel reduction, not array order.
+ *
+ * One collection per context.
+ */
+#include "nbg_internal.cuh"
+#include "nbg_math.h"
+#include "nbg_shared.h"
+
+#define BH_THETA 0.3
+#define BH_SOFTENING 1e-4
+#define BH_LEVELS 21
+#define BH_BLOCK 256
+#define BH_RS_BLOCK 256
+#define BH_RS_ITEMS 16
+#define BH_RS_TILE (BH_RS_BLOCK * BH_RS_ITEMS)
+#define BH_RS_BINS 256
+#define BH_SCAN_BLOCK 1024
+#define BH_SCAN_ITEMS 4
+#define BH_SCAN_TILE (BH_SCAN_BLOCK * BH_SCAN_ITEMS)
+#define BH_F_LEAF 1u
+#define BH_F_NAN_CM 2u
+#define FULL_MASK 0xffffffffu
+
+/* order-preserving integer image of a double (for atomicMin / atomicMax) */
+__device__ __forceinline__ ull dbl_ord(double v)
+{
+    const ull b = (ull)__double_as_longlong(v);
+    return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
+}
+__device__ __forceinline__ double ord_dbl(ull o)
+{
+    const ull b = (o >> 63) ? (o & 0x7fffffffffffffffull) : ~o;
+    return __longlong_as_double((long long)b);
+}
+
+__device__ __forceinline__ bool tree_body(const BodyArrays &A, ll k)
+{
+    if ((A.flags[k] & NBG_LIVE_MASK) != NBG_F_EXISTS) return false;
+    const double x = A.x[k], y = A.y[k], z = A.z[k];
+    return fabs(x) <= NBG_DBL_MAX && fabs(y) <= NBG_DBL_MAX && fabs(z) <= NBG_DBL_MAX;
+}
+
+/* the root cube, octree.go:174-183 */
+__device__ __forceinline__ void bh_root(const DevCtl *ctl, double &cx, double &cy, double &cz, double &half)
+{
+    const double minX = ord_dbl(ctl->bh_lo[0]), minY = ord_dbl(ctl->bh_lo[1]), minZ = ord_dbl(ctl->bh_lo[2]);
+    const double maxX = ord_dbl(ctl->bh_hi[0]), maxY = ord_dbl(ctl->bh_hi[1]), maxZ = ord_dbl(ctl->bh_hi[2]);
+    cx = (minX + maxX) / 2;
+    cy = (minY + maxY) / 2;
+    cz = (minZ + maxZ) / 2;
+    half = nbg_go_max(maxX - minX, nbg_go_max(maxY - minY, maxZ - minZ)) / 2 * 1.05;
+}
+
+/* ---- 1. bounds, keys -------------------------------------------------------- */
+
+__global__ void __launch_bounds__(BH_BLOCK) k_bh_bounds(BodyArrays A, DevCtl *ctl)
+{
+    if (ctl->error) return;
+    const ll n = ctl->n;
+    double lo[3] = {NBG_DBL_MAX, NBG_DBL_MAX, NBG_DBL_MAX}, hi[3] = {-NBG_DBL_MAX, -NBG_DBL_MAX, -NBG_DBL_MAX};
+    double rmax = 0;
+    unsigned cnt = 0;
+    for (ll k = (ll)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (ll)gridDim.x * blockDim.x) {
+        const double r = A.rad[k];
+        if (r > rmax) rmax = r;
+        if (!tree_body(A, k)) continue;
+        const double v[3] = {A.x[k], A.y[k], A.z[k]};
+        for (int c = 0; c < 3; c++) {
+            lo[c] = fmin(lo[c], v[c]);
+            hi[c] = fmax(hi[c], v[c]);
+        }
+        cnt++;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        for (int c = 0; c < 3; c++) {
+            lo[c] = fmin(lo[c], __shfl_xor_sync(FULL_MASK, lo[c], o));
+            hi[c] = fmax(hi[c], __shfl_xor_sync(FULL_MASK, hi[c], o));
+        }
+        rmax = fmax(rmax, __shfl_xor_sync(FULL_MASK, rmax, o));
+        cnt += __shfl_xor_sync(FULL_MASK, cnt, o);
+    }
+    if ((threadIdx.x & 31) == 0 && cnt > 0) {
+        for (int c = 0; c < 3; c++) {
+            atomicMin((unsigned long long *)&ctl->bh_lo[c], (unsigned long long)dbl_ord(lo[c]));
+            atomicMax((unsigned long long *)&ctl->bh_hi[c], (unsigned long long)dbl_ord(hi[c]));
+        }
+        atomicAdd((unsigned long long *)&ctl->bh_count, (unsigned long long)cnt);
+    }
+    if ((threadIdx.x & 31) == 0) atomicMax((unsigned long long *)&ctl->bh_rmax, (unsigned long long)dbl_ord(rmax));
+}
+
+/* octant path of every tree body; other bodies get the largest key */
+__global__ void __launch_bounds__(BH_BLOCK) k_bh_keys(BodyArrays A, DevCtl *ctl, ull *keys, unsigned *vals)
+{
+    if (ctl->error) return;
+    const ll n = ctl->n;
+    double cx0, cy0, cz0, half0;
+    bh_root(ctl, cx0, cy0, cz0, half0);
+    for (ll k = (ll)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (ll)gridDim.x * blockDim.x) {
+        ull key = ~0ull;
+        if (ctl->bh_count > 0 && tree_body(A, k)) {
+            const double x = A.x[k], y = A.y[k], z = A.z[k];
+            double cx = cx0, cy = cy0, cz = cz0, half = half0;
+            key = 0;
+            for (int d = 0; d < BH_LEVELS; d++) {
+                const unsigned oct = (x >= cx ? 1u : 0u) | (y >= cy ? 2u : 0u) | (z >= cz ? 4u : 0u);
+                key = (key << 3) | oct;
+                const double q = half / 2;
+                cx = (oct & 1u) ? cx + q : cx - q;
+                cy = (oct & 2u) ? cy + q : cy - q;
+                cz = (oct & 4u) ? cz + q : cz - q;
+                half = half / 2;
+            }
+        }
+        keys[k] = key;
+        vals[k] = (unsigned)k;
+    }
+}
+
+/* ---- 2. 64-bit LSD radix sort (stable) ----------------------------------- */
+
+__global__ void __launch_bounds__(BH_RS_BLOCK) k_bh_rs_hist(DevCtl *ctl, const ull *keys, int shift, ll *hist)
+{
+    __shared__ unsigned cnt[BH_RS_BINS];
+    if (ctl->error) return;
+    const ll n = ctl->n;
+    const ll nb = (n + BH_RS_TILE - 1) / BH_RS_TILE;
+    const ll b = blockIdx.x;
+    if (b >= nb) return;
+    for (int d = threadIdx.x; d < BH_RS_BINS; d += BH_RS_BLOCK) cnt[d] = 0;
+    __syncthreads();
+    for (int q = 0; q < BH_RS_ITEMS; q++) {
+        const ll k = b * BH_RS_TILE + (ll)q * BH_RS_BLOCK + threadIdx.x;
+        if (k < n) atomicAdd(&cnt[(unsigned)(keys[k] >> shift) & 0xffu], 1u);
+    }
+    __syncthreads();
+    for (int d = threadIdx.x; d < BH_RS_BINS; d += BH_RS_BLOCK) hist[(ll)d * nb + b] = cnt[d];
+}
+
+/* exclusive scan of the digit-major histogram (one block, four entries per
+ * thread per round) */
+__global__ void __launch_bounds__(1024) k_bh_rs_scan(DevCtl *ctl, ll *hist)
+{
+    __shared__ ll warp_tot[32];
+    if (ctl->error) return;
+    const ll n = ctl->n;
+    const ll total = ((n + BH_RS_TILE - 1) / BH_RS_TILE) * BH_RS_BINS;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    ll carry = 0;
+    for (ll c0 = 0; c0 < total; c0 += 4096) {
+        const ll c = c0 + (ll)threadIdx.x * 4;
+        ll v[4], sum = 0;
+        for (int q = 0; q < 4; q++) {
+            v[q] = c + q < total ? hist[c + q] : 0;
+            sum += v[q];
+        }
+        ll x = sum;
+        for (int o = 1; o < 32; o <<= 1) {
+            const ll y = __shfl_up_sync(FULL_MASK, x, o);
+            if (lane >= o) x += y;
+        }
+        if (lane == 31) warp_tot[w] = x;
+        __syncthreads();
+        if (w == 0) {
+            ll t = warp_tot[lane];
+            for (int o = 1; o < 32; o <<= 1) {
+                const ll y = __shfl_up_sync(FULL_MASK, t, o);
+                if (lane >= o) t += y;
+            }
+            warp_tot[lane] = t;
+        }
+        __syncthreads();
+        ll ex = carry + x - sum + (w > 0 ? warp_tot[w - 1] : 0);
+        for (int q = 0; q < 4; q++) {
+            if (c + q < total) hist[c + q] = ex;
+            ex += v[q];
+        }
+        carry += warp_tot[31];
+        __syncthreads();
+    }
+}
+
+__global__ void __launch_bounds__(BH_RS_BLOCK) k_bh_rs_scatter(DevCtl *ctl, const ull *keys_in,
+                                                             const unsigned *vals_in, ull *keys_out,
+                                                             unsigned *vals_out, int shift, const ll *offs)
+{
+    __shared__ ll base[BH_RS_BINS];
+    __shared__ unsigned wcnt[BH_RS_BLOCK / 32][BH_RS_BINS];
+    if (ctl->error) return;
+    const ll n = ctl->n;
+    const ll nb = (n + BH_RS_TILE - 1) / BH_RS_TILE;
+    const ll b = blockIdx.x;
+    if (b >= nb) return;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (int d = threadIdx.x; d < BH_RS_BINS; d += BH_RS_BLOCK) base[d] = offs[(ll)d * nb + b];
+    const unsigned lt = (1u << lane) - 1u;
+    for (int q = 0; q < BH_RS_ITEMS; q++) {
+        for (int d = threadIdx.x; d < BH_RS_BINS * (BH_RS_BLOCK / 32); d += BH_RS_BLOCK) (&wcnt[0][0])[d] = 0;
+        __syncthreads();
+        const ll k = b * BH_RS_TILE + (ll)q * BH_RS_BLOCK + threadIdx.x;
+        const bool ok = k < n;
+        const ull key = ok ? keys_in[k] : 0ull;
+        const unsigned d = ok ? (unsigned)(key >> shift) & 0xffu : BH_RS_BINS;
+        const unsigned peers = __match_any_sync(FULL_MASK, d);
+        const unsigned rank = __popc(peers & lt);
+        if (ok && rank == 0) wcnt[w][d] = __popc(peers);
+        __syncthreads();
+        if (ok) {
+            ll pos = base[d] + rank;
+            for (int v = 0; v < w; v++) pos += wcnt[v][d];
+            keys_out[pos] = key;
+            vals_out[pos] = vals_in[k];
+        }
+        __syncthreads();
+        for (int dd = threadIdx.x; dd < BH_RS_BINS; dd += BH_RS_BLOCK) {
+            ll s = 0;
+            for (int v = 0; v < BH_RS_BLOCK / 32; v++) s += wcnt[v][dd];
+            base[dd] += s;
+        }
+        __syncthreads();
+    }
+}
+
+/* ---- 3. nodes -------------------------------------------------------------- */
+
+/* levels two keys have in common (BH_LEVELS when equal) */
+__device__ __forceinline__ int common_levels(ull a, ull b)
+{
+    const ull x = a ^ b;
+    if (x == 0) return BH_LEVELS;
+    return (__clzll((long long)x) - 1) / 3;
+}
+
+/* first and last level of the nodes that start at sorted position p (none
+ * when first > last) */
+__device__ __forceinline__ void node_levels(const ull *keys, ll p, ll M, int &d0, int &d1)
+{
+    const int cp = p == 0 ? -1 : common_levels(keys[p - 1], keys[p]);
+    const int cn = p == M - 1 ? -1 : common_levels(keys[p], keys[p + 1]);
+    d0 = p == 0 ? 0 : cp + 1;
+    const int e = cn + 1 > d0 ? cn + 1 : d0;
+    d1 = e < BH_LEVELS ? e : BH_LEVELS;
+}
+
+/* per-block sums of the node counts of sorted positions [0, M) */
+__global__ void __launch_bounds__(BH_SCAN_BLOCK) k_bh_count(DevCtl *ctl, const ull *keys, ll *base, ll *blk)
+{
+    __shared__ ll red[BH_SCAN_BLOCK / 32];
+    if (ctl->error) return;
+    const ll M = ctl->bh_count;
+    const ll b0 = (ll)blockIdx.x * BH_SCAN_TILE;
+    if (b0 > M) return;
+    ll s = 0;
+    for (int q = 0; q < BH_SCAN_ITEMS; q++) {
+        const ll p = b0 + (ll)q * BH_SCAN_BLOCK + threadIdx.x;
+        ll c = 0;
+        if (p < M) {
+            int d0, d1;
+            node_levels(keys, p, M, d0, d1);
+            c = d1 >= d0 ? d1 - d0 + 1 : 0;
+        }
+        if (p <= M) base[p] = c; /* base[M] = 0: the scan leaves the total there */
+        s += c;
+    }
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(FULL_MASK, s, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        ll t = 0;
+        for (int w = 0; w < BH_SCAN_BLOCK / 32; w++) t += red[w];
+        blk[blockIdx.x] = t;
+    }
+}
+
+/* exclusive scan of the block sums (one block) and the node total */
+__global__ void __launch_bounds__(1024) k_bh_count_top(DevCtl *ctl, ll *blk, ll node_cap)
+{
+    __shared__ ll warp_tot[32];
+    if (ctl->error) return;
+    const ll M = ctl->bh_count;
+    const ll nblk = M / BH_SCAN_TILE + 1;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    ll carry = 0;
+    for (ll c0 = 0; c0 < nblk; c0 += 1024) {
+        const ll c = c0 + threadIdx.x;
+        const ll v = c < nblk ? blk[c] : 0;
+        ll x = v;
+        for (int o = 1; o < 32; o <<= 1) {
+            const ll y = __shfl_up_sync(FULL_MASK, x, o);
+            if (lane >= o) x += y;
+        }
+        if (lane == 31) warp_tot[w] = x;
+        __syncthreads();
+        if (w == 0) {
+            ll t = warp_tot[lane];
+            for (int o = 1; o < 32; o <<= 1) {
+                const ll y = __shfl_up_sync(FULL_MASK, t, o);
+                if (lane >= o) t += y;
+            }
+            warp_tot[lane] = t;
+        }
+        __syncthreads();
+        if (c < nblk) blk[c] = carry + x - v + (w > 0 ? warp_tot[w - 1] : 0);
+        carry += warp_tot[31];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        ctl->bh_nodes = carry;
+        if (carry > node_cap) {
+            ctl->error = NBG_E_OVERFLOW;
+            ctl->error_what = 5;
+            ctl->error_need = carry;
+        }
+    }
+}
+
+/* exclusive scan of the node counts within each block, plus the block's
+ * offset: base[p] = first node starting at p, base[M] = node total */
+__global__ void __launch_bounds__(BH_SCAN_BLOCK) k_bh_count_scan(DevCtl *ctl, ll *base, const ll *blk)
+{
+    __shared__ ll warp_tot[32];
+    if (ctl->error) return;
+    const ll M = ctl->bh_count;
+    const ll b0 = (ll)blockIdx.x * BH_SCAN_TILE;
+    if (b0 > M) return;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    ll carry = blk[blockIdx.x];
+    for (int q = 0; q < BH_SCAN_ITEMS; q++) {
+        const ll p = b0 + (ll)q * BH_SCAN_BLOCK + threadIdx.x;
+        const ll v = p <= M ? base[p] : 0;
+        ll x = v;
+        for (int o = 1; o < 32; o <<= 1) {
+            const ll y = __shfl_up_sync(FULL_MASK, x, o);
+            if (lane >= o) x += y;
+        }
+        if (lane == 31) warp_tot[w] = x;
+        __syncthreads();
+        if (w == 0) {
+            ll t = warp_tot[lane];
+            for (int o = 1; o < 32; o <<= 1) {
+                const ll y = __shfl_up_sync(FULL_MASK, t, o);
+                if (lane >= o) t += y;
+            }
+            warp_tot[lane] = t;
+        }
+        __syncthreads();
+        if (p <= M) base[p] = carry + x - v + (w > 0 ? warp_tot[w - 1] : 0);
+        carry += warp_tot[31];
+        __syncthreads();
+    }
+}
+
+/* one thread per sorted position: every node that starts there */
+__global__ void __launch_bounds__(BH_BLOCK) k_bh_nodes(DevCtl *ctl, const ull *keys, const ll *base, BhTree t)
+{
+    if (ctl->error) return;
+    const ll M = ctl->bh_count;
+    const ll total = ctl->bh_nodes;
+    double cx0, cy0, cz0, half0;
+    bh_root(ctl, cx0, cy0, cz0, half0);
+    for (ll p = (ll)blockIdx.x * blockDim.x + threadIdx.x; p < M; p += (ll)gridDim.x * blockDim.x) {
+        int d0, d1;
+        node_levels(keys, p, M, d0, d1);
+        if (d1 < d0) continue;
+        const ull key = keys[p];
+        /* the cube of the level-d0 node: descend d0 levels along the key */
+        double cx = cx0, cy = cy0, cz = cz0, half = half0;
+        for (int d = 0; d < d0; d++) {
+            const unsigned oct = (unsigned)(key >> (3 * (BH_LEVELS - 1 - d))) & 7u;
+            const double q = half / 2;
+            cx = (oct & 1u) ? cx + q : cx - q;
+            cy = (oct & 2u) ? cy + q : cy - q;
+            cz = (oct & 4u) ? cz + q : cz - q;
+            half = half / 2;
+        }
+        for (int d = d0; d <= d1; d++) {
+            const ll id = base[p] + (d - d0);
+            /* end of the body range: the first key past this node's prefix */
+            ll end = M;
+            if (d > 0) {
+                const int sh = 3 * (BH_LEVELS - d);
+                const ull pre = key >> sh;
+                ll lo = p + 1, hi = M;
+                while (lo < hi) {
+                    const ll mid = (lo + hi) >> 1;
+                    if ((keys[mid] >> sh) <= pre)
+                        lo = mid + 1;
+                    else
+                        hi = mid;
+                }
+                end = lo;
+            }
+            t.start[id] = (int)p;
+            t.end[id] = (int)end;
+            t.skip[id] = (int)(end >= M ? total : base[end]);
+            t.level[id] = (unsigned char)d;
+            t.flags[id] = (end - p == 1 || d == BH_LEVELS) ? BH_F_LEAF : 0u;
+            t.cx[id] = cx;
+            t.cy[id] = cy;
+            t.cz[id] = cz;
+            t.half[id] = half;
+            if (d < d1) {
+                const unsigned oct = (unsigned)(key >> (3 * (BH_LEVELS - 1 - d))) & 7u;
+                const double q = half / 2;
+                cx = (oct & 1u) ? cx + q : cx - q;
+                cy = (oct & 2u) ? cy + q : cy - q;
+                cz = (oct & 4u) ? cz + q : cz - q;
+                half = half / 2;
+            }
+        }
+    }
+}
+
+/* ---- 4. mass and centre of mass, one level per launch, deepest first ------ */
+
+__global__ void __launch_bounds__(BH_BLOCK) k_bh_mass(BodyArrays A, DevCtl *ctl, const unsigned *vals, BhTree t,
+                                                      int level)
+{
+    if (ctl->error) return;
+    const ll total = ctl->bh_nodes;
+    for (ll id = (ll)blockIdx.x * blockDim.x + threadIdx.x; id < total; id += (ll)gridDim.x * blockDim.x) {
+        if (t.level[id] != level) continue;
+        double M = 0, mx = 0, my = 0, mz = 0;
+        int first = 0x7fffffff;
+        if (t.flags[id] & BH_F_LEAF) {
+            for (int q = t.start[id]; q < t.end[id]; q++) {
+                const unsigned k = vals[q];
+                const double m = A.m[k];
+                M = M + m;
+                mx = mx + A.x[k] * m;
+                my = my + A.y[k] * m;
+                mz = mz + A.z[k] * m;
+                if ((int)k < first) first = (int)k;
+            }
+        } else {
+            const int stop = t.skip[id];
+            for (int c = (int)id + 1; c < stop; c = t.skip[c]) {
+                M = M + t.mass[c];
+                mx = mx + t.mx[c];
+                my = my + t.my[c];
+                mz = mz + t.mz[c];
+                if (t.first[c] < first) first = t.first[c];
+            }
+        }
+        t.mass[id] = M;
+        t.mx[id] = mx;
+        t.my[id] = my;
+        t.mz[id] = mz;
+        t.first[id] = first;
+        if (M != 0) {
+            t.cmx[id] = mx / M;
+            t.cmy[id] = my / M;
+            t.cmz[id] = mz / M;
+        }
+        /* the reference's running centre is 0 / 0 when the node's first body
+         * (in array order) is massless, and stays NaN */
+        if (A.m[first] == 0) t.flags[id] |= BH_F_NAN_CM;
+    }
+}
+
+/* ---- 5. forces ------------------------------------------------------------- */
+
+/* accumForce's point-mass term, octree.go:286-292 */
+__device__ __forceinline__ void bh_term(double gm_i, double M, double dx, double dy, double dz, double &fx,
+                                        double &fy, double &fz)
+{
+    const double distSq = dx * dx + dy * dy + dz * dz + BH_SOFTENING * BH_SOFTENING;
+    const double dist = sqrt(distSq);
+    const double force = gm_i * M / distSq;
+    fx += force * dx / dist;
+    fy += force * dy / dist;
+    fz += force * dz / dist;
+}
+
+/* one thread per tree body (sorted order, so a warp walks nearby paths) */
+__global__ void __launch_bounds__(BH_BLOCK) k_bh_force(BodyArrays A, DevCtl *ctl, const unsigned *vals, BhTree t)
+{
+    if (ctl->error) return;
+    const ll M = ctl->bh_count;
+    const int total = (int)ctl->bh_nodes;
+    unsigned long long terms = 0;
+    /* every lane runs the same number of rounds, for the warp reduction */
+    for (ll base0 = (ll)blockIdx.x * blockDim.x; base0 < M; base0 += (ll)gridDim.x * blockDim.x) {
+        const ll p = base0 + threadIdx.x;
+        if (p >= M) continue;
+        const unsigned k = vals[p];
+        if (A.flags[k] & NBG_F_IS_SUN) continue; /* k_bh_sun */
+        const double x = A.x[k], y = A.y[k], z = A.z[k];
+        const double gm = NBG_G * A.m[k];
+        double fx = 0, fy = 0, fz = 0;
+        int id = 0;
+        while (id < total) {
+            const double Mn = t.mass[id];
+            if (Mn == 0) {
+                id = t.skip[id];
+                continue;
+            }
+            const unsigned fl = t.flags[id];
+            const bool leaf = (fl & BH_F_LEAF) != 0;
+            const double dx = t.cmx[id] - x;
+            const double dy = t.cmy[id] - y;
+            const double dz = t.cmz[id] - z;
+            const double distSq = dx * dx + dy * dy + dz * dz + BH_SOFTENING * BH_SOFTENING;
+            const double dist = sqrt(distSq);
+            if (leaf || (!(fl & BH_F_NAN_CM) && (2 * t.half[id] / dist) < BH_THETA)) {
+                const int s = t.start[id], e = t.end[id];
+                if (leaf && e - s > 1) {
+                    /* a leaf at the deepest level holding several bodies: each
+                     * acts as a leaf of its own */
+                    for (int q = s; q < e; q++) {
+                        const unsigned j = vals[q];
+                        const double mj = A.m[j];
+                        if (j == k || mj == 0) continue;
+                        bh_term(gm, mj, A.x[j] * mj / mj - x, A.y[j] * mj / mj - y, A.z[j] * mj / mj - z, fx, fy,
+                                fz);
+                        terms++;
+                    }
+                } else if (!(leaf && vals[s] == k)) {
+                    const double force = gm * Mn / distSq;
+                    fx += force * dx / dist;
+                    fy += force * dy / dist;
+                    fz += force * dz / dist;
+                    terms++;
+                }
+                id = t.skip[id];
+            } else {
+                id = id + 1;
+            }
+        }
+        A.fx[k] = fx;
+        A.fy[k] = fy;
+        A.fz[k] = fz;
+    }
+    /* point-mass terms summed, for the measured work */
+    for (int o = 16; o > 0; o >>= 1) terms += __shfl_xor_sync(FULL_MASK, terms, o);
+    if ((threadIdx.x & 31) == 0 && terms) atomicAdd((unsigned long long *)&ctl->acc_bh_terms, terms);
+}
+
+/* a sun sums every tree body directly (directForce, octree.go:310-325); one
+ * CTA per sun, a fixed-order block reduction */
+__global__ void __launch_bounds__(BH_BLOCK) k_bh_sun(BodyArrays A, DevCtl *ctl)
+{
+    __shared__ double red[3][BH_BLOCK];
+    if (ctl->error) return;
+    const ll n = ctl->n;
+    for (ll k = blockIdx.x; k < n; k += gridDim.x) {
+        if ((A.flags[k] & (NBG_LIVE_MASK | NBG_F_IS_SUN)) != (NBG_F_EXISTS | NBG_F_IS_SUN) || !tree_body(A, k)) continue;
+        const double x = A.x[k], y = A.y[k], z = A.z[k];
+        const double gm = NBG_G * A.m[k];
+        double fx = 0, fy = 0, fz = 0;
+        for (ll j = threadIdx.x; j < n; j += blockDim.x) {
+            if (j == k || (A.flags[j] & NBG_LIVE_MASK) != NBG_F_EXISTS) continue;
+            bh_term(gm, A.m[j], A.x[j] - x, A.y[j] - y, A.z[j] - z, fx, fy, fz);
+        }
+        red[0][threadIdx.x] = fx;
+        red[1][threadIdx.x] = fy;
+        red[2][threadIdx.x] = fz;
+        __syncthreads();
+        for (int s = BH_BLOCK / 2; s > 0; s >>= 1) {
+            if (threadIdx.x < s)
+                for (int c = 0; c < 3; c++) red[c][threadIdx.x] += red[c][threadIdx.x + s];
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) {
+            A.fx[k] = red[0][0];
+            A.fy[k] = red[1][0];
+            A.fz[k] = red[2][0];
+        }
+        __syncthreads();
+    }
+}
+
+/* ---- 6. collisions: Compute's second pass as a range query ----------------- */
+
+/* Collided + the event rules for tree body i against body j (j != i) */
+__device__ __forceinline__ void bh_test_pair(const BodyArrays &A, DevCtl *ctl, ull *ev_keys, ll ev_cap, ll i,
+                                             double xi, double yi, double zi, double ri, unsigned bi, ll j)
+{
+    const double dx = A.x[j] - xi;
+    const double dy = A.y[j] - yi;
+    const double dz = A.z[j] - zi;
+    const double dist = sqrt(dx * dx + dy * dy + dz * dz);
+    const double rj = A.rad[j];
+    if (dist <= ri + rj) {
+        const int type = nbg_detect_event(bi, NBG_BEHAVIOR(A.flags[j]), ri, rj, dist);
+        if (type >= 0) nbg_emit_event(ctl, ev_keys, ev_cap, i, j, type);
+    }
+}
+
+__global__ void __launch_bounds__(BH_BLOCK) k_bh_collide(BodyArrays A, DevCtl *ctl, const unsigned *vals, BhTree t,
+                                                         ull *ev_keys, ll ev_cap)
+{
+    if (ctl->error) return;
+    const ll n = ctl->n;
+    const ll M = ctl->bh_count;
+    const int total = (int)ctl->bh_nodes;
+    const double rmax = ord_dbl(ctl->bh_rmax);
+    double cx0, cy0, cz0, half0;
+    bh_root(ctl, cx0, cy0, cz0, half0);
+    const double slack = (fabs(cx0) + fabs(cy0) + fabs(cz0) + half0) * 0x1p-44;
+    for (ll p = (ll)blockIdx.x * blockDim.x + threadIdx.x; p < M; p += (ll)gridDim.x * blockDim.x) {
+        const unsigned i = vals[p];
+        const unsigned fi = A.flags[i];
+        if (fi & NBG_F_COLLIDED) continue; /* Collided's guard (always clear here) */
+        const double xi = A.x[i], yi = A.y[i], zi = A.z[i], ri = A.rad[i];
+        const unsigned bi = NBG_BEHAVIOR(fi);
+        /* reach: r_i + r_max, widened so the cube test never drops a pair the
+         * exact test would keep (a body sits in its node's cube up to a few
+         * ulps of the coordinates, the cube distance is good to ~2^-50) */
+        const double R = (ri + rmax) * (1.0 + 0x1p-40) + slack;
+        if (!(R >= 0)) continue; /* a NaN radius collides with nothing */
+        const double R2 = R * R;
+        int id = 0;
+        while (id < total) {
+            const double h = t.half[id];
+            const double ax = fmax(fabs(xi - t.cx[id]) - h, 0.0);
+            const double ay = fmax(fabs(yi - t.cy[id]) - h, 0.0);
+            const double az = fmax(fabs(zi - t.cz[id]) - h, 0.0);
+            if (ax * ax + ay * ay + az * az > R2) {
+                id = t.skip[id];
+                continue;
+            }
+            if (t.flags[id] & BH_F_LEAF) {
+                for (int q = t.start[id]; q < t.end[id]; q++) {
+                    const unsigned j = vals[q];
+                    if (j != i) bh_test_pair(A, ctl, ev_keys, ev_cap, i, xi, yi, zi, ri, bi, j);
+                }
+                id = t.skip[id];
+            } else {
+                id = id + 1;
+            }
+        }
+        /* bodies outside the tree */
+        for (ll q = M; q < n; q++) bh_test_pair(A, ctl, ev_keys, ev_cap, i, xi, yi, zi, ri, bi, vals[q]);
+    }
+}
+
+/* ---- host side -------------------------------------------------------------- */
+
+int nbg_bh_alloc(BhTree &t, ll cap, ll node_cap)
+{
+    nbg_bh_free(t);
+    const ll nb = (cap + BH_RS_TILE - 1) / BH_RS_TILE;
+    const ll nblk = cap / BH_SCAN_TILE + 2;
+    bool ok = true;
+#define ALLOC(p, cnt) ok = ok && cudaMalloc((void **)&(p), (size_t)(cnt) * sizeof(*(p))) == cudaSuccess
+    ALLOC(t.key[0], cap);
+    ALLOC(t.key[1], cap);
+    ALLOC(t.val[0], cap);
+    ALLOC(t.val[1], cap);
+    ALLOC(t.hist, nb * BH_RS_BINS);
+    ALLOC(t.base, cap + 1);
+    ALLOC(t.blk, nblk);
+    ALLOC(t.mass, node_cap);
+    ALLOC(t.mx, node_cap);
+    ALLOC(t.my, node_cap);
+    ALLOC(t.mz, node_cap);
+    ALLOC(t.cmx, node_cap);
+    ALLOC(t.cmy, node_cap);
+    ALLOC(t.cmz, node_cap);
+    ALLOC(t.cx, node_cap);
+    ALLOC(t.cy, node_cap);
+    ALLOC(t.cz, node_cap);
+    ALLOC(t.half, node_cap);
+    ALLOC(t.skip, node_cap);
+    ALLOC(t.start, node_cap);
+    ALLOC(t.end, node_cap);
+    ALLOC(t.first, node_cap);
+    ALLOC(t.level, node_cap);
+    ALLOC(t.flags, node_cap);
+#undef ALLOC
+    if (!ok) {
+        nbg_bh_free(t);
+        return NBG_E_CUDA;
+    }
+    t.node_cap = node_cap;
+    return NBG_OK;
+}
+
+void nbg_bh_free(BhTree &t)
+{
+    void *ps[] = {t.key[0], t.key[1], t.val[0], t.val[1], t.hist, t.base, t.blk, t.mass, t.mx, t.my,
+                  t.mz, t.cmx, t.cmy, t.cmz, t.cx, t.cy, t.cz, t.half, t.skip, t.start,
+                  t.end, t.first, t.level, t.flags};
+    for (void *p : ps) cudaFree(p);
+    memset(&t, 0, sizeof t);
+}
+
+/* The force and collision pass of one cycle (the replacement of the pair
+ * kernel): bounds, keys, sort, nodes, masses, forces, suns, collisions. */
+void nbg_launch_bh(const CycleBufs &cb, DevCtl *ctl, cudaStream_t st)
+{
+    const BhTree &t = cb.t;
+    const ll cap = cb.cap;
+    int g = (int)((cap + BH_BLOCK - 1) / BH_BLOCK);
+    if (g > 152 * 8) g = 152 * 8;
+    if (g < 1) g = 1;
+    k_bh_bounds<<<g, BH_BLOCK, 0, st>>>(cb.a, ctl);
+    k_bh_keys<<<g, BH_BLOCK, 0, st>>>(cb.a, ctl, t.key[0], t.val[0]);
+    const int nb = (int)((cap + BH_RS_TILE - 1) / BH_RS_TILE);
+    int in = 0;
+    for (int pass = 0; pass < 8; pass++) {
+        k_bh_rs_hist<<<nb, BH_RS_BLOCK, 0, st>>>(ctl, t.key[in], 8 * pass, t.hist);
+        k_bh_rs_scan<<<1, 1024, 0, st>>>(ctl, t.hist);
+        k_bh_rs_scatter<<<nb, BH_RS_BLOCK, 0, st>>>(ctl, t.key[in], t.val[in], t.key[in ^ 1], t.val[in ^ 1],
+                                                   8 * pass, t.hist);
+        in ^= 1;
+    }
+    /* eight passes: sorted keys and values are back in buffer 0 */
+    const int sb = (int)(cap / BH_SCAN_TILE + 1);
+    k_bh_count<<<sb, BH_SCAN_BLOCK, 0, st>>>(ctl, t.key[0], t.base, t.blk);
+    k_bh_count_top<<<1, 1024, 0, st>>>(ctl, t.blk, t.node_cap);
+    k_bh_count_scan<<<sb, BH_SCAN_BLOCK, 0, st>>>(ctl, t.base, t.blk);
+    k_bh_nodes<<<g, BH_BLOCK, 0, st>>>(ctl, t.key[0], t.base, t);
+    int ng = (int)((t.node_cap + BH_BLOCK - 1) / BH_BLOCK);
+    if (ng > 152 * 8) ng = 152 * 8;
+    for (int level = BH_LEVELS; level >= 0; level--)
+        k_bh_mass<<<ng, BH_BLOCK, 0, st>>>(cb.a, ctl, t.val[0], t, level);
+    k_bh_force<<<g, BH_BLOCK, 0, st>>>(cb.a, ctl, t.val[0], t);
+    k_bh_sun<<<64, BH_BLOCK, 0, st>>>(cb.a, ctl);
+    k_bh_collide<<<g, BH_BLOCK, 0, st>>>(cb.a, ctl, t.val[0], t, cb.ev_keys, cb.ev_cap);
+}

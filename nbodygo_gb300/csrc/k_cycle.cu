@@ -119,6 +119,13 @@ __global__ void __launch_bounds__(NBG_SCAN_BLOCK) k_begin(DevCtl *ctl, SimSegs s
         ctl->splits = (int)P;
         ctl->work_total = W;
         ctl->work_next = 0;
+        for (int c = 0; c < 3; c++) {
+            ctl->bh_lo[c] = ~0ull;
+            ctl->bh_hi[c] = 0ull;
+        }
+        ctl->bh_count = 0;
+        ctl->bh_nodes = 0;
+        ctl->bh_rmax = 0ull;
         ctl->cycle_interactions = inter;
         if (part_short) {
             ctl->error = NBG_E_OVERFLOW;
@@ -243,24 +250,6 @@ __global__ void __launch_bounds__(NBG_SCAN_BLOCK) k_scan_blocks(DevCtl *ctl, Sim
 
 /* Detection rule of Compute's second pass (body.go:172-186) for a pair with
  * Collided(i, j) true. Returns the event type or -1. */
-__device__ static int detect_event(unsigned bi, unsigned bj, double ri, double rj, double dist)
-{
-    bool ei = (bi == NBG_ELASTIC || bi == NBG_FRAGMENT);
-    bool ej = (bj == NBG_ELASTIC || bj == NBG_FRAGMENT);
-    if (ei && ej) return (int)NBG_EVT_COLL_IJ;
-    if (bi == NBG_SUBSUME || bj == NBG_SUBSUME) {
-        if (ri > rj && dist <= ri) return (int)NBG_EVT_SUB_IJ;
-        if (rj > ri && dist <= rj) return (int)NBG_EVT_SUB_JI;
-    }
-    return -1;
-}
-
-__device__ static void emit_event(DevCtl *ctl, ull *keys, ll cap, ll i, ll j, int type)
-{
-    ll slot = atomicAdd((unsigned long long *)&ctl->ev_count, 1ull);
-    if (slot < cap) keys[slot] = ((ull)i << 32) | ((ull)j << 2) | (ull)type;
-}
-
 /*
  * One thread per body i.  For each j in array order (tiles of P64_BLOCK staged
  * in shared memory) it evaluates exactly the reference's expressions
@@ -329,8 +318,8 @@ __global__ void __launch_bounds__(P64_BLOCK) k_pair_fp64(BodyArrays A, DevCtl *c
                     fz += force * dz / dist;
                 }
                 if (!coll_i && dist <= rr && j != i) {
-                    int type = detect_event(bi, NBG_BEHAVIOR(fj), ri, sr[t], dist);
-                    if (type >= 0) emit_event(ctl, ev_keys, ev_cap, i, j, type);
+                    int type = nbg_detect_event(bi, NBG_BEHAVIOR(fj), ri, sr[t], dist);
+                    if (type >= 0) nbg_emit_event(ctl, ev_keys, ev_cap, i, j, type);
                 }
             }
         }

@@ -45,6 +45,7 @@ struct nbg_ctx {
     void *scratch = nullptr;
     size_t scratch_bytes = 0;
     ll launches_per_cycle = 0;
+    ll bh_cap = 0; /* capacity the Barnes-Hut buffers were sized for */
     void *seg_mem = nullptr; /* SimSegs arrays */
     int seg_cap = 0;         /* sims the allocation holds */
 };
@@ -199,6 +200,7 @@ static void invalidate_graph(nbg_ctx *ctx)
 }
 
 static void free_cap_buffers(CycleBufs &cb);
+static int ensure_bh(nbg_ctx *ctx, ll nodes);
 
 /* (re)allocates the body-capacity dependent buffers, keeping the first
  * `keep` bodies of the collection */
@@ -246,6 +248,7 @@ static int ensure_cap(nbg_ctx *ctx, ll need, ll keep)
     CK(cudaMalloc((void **)&ctx->cb.shist, (size_t)nbg_sort_scratch_hist(cap) * sizeof(ll)));
     ctx->cb.cap = cap;
     invalidate_graph(ctx);
+    if (ctx->cb.bh) return ensure_bh(ctx, 0);
     return NBG_OK;
 }
 
@@ -258,6 +261,18 @@ static int ensure_part(nbg_ctx *ctx, ll need)
     ctx->cb.part_doubles = 0;
     CK(cudaMalloc((void **)&ctx->cb.part, (size_t)need * sizeof(double)));
     ctx->cb.part_doubles = need;
+    invalidate_graph(ctx);
+    return NBG_OK;
+}
+
+/* Barnes-Hut buffers for the current capacity and at least `nodes` nodes */
+static int ensure_bh(nbg_ctx *ctx, ll nodes)
+{
+    BhTree &t = ctx->cb.t;
+    const ll want = nodes > 2 * ctx->cb.cap + 64 ? nodes + nodes / 4 : 2 * ctx->cb.cap + 64;
+    if (t.key[0] && t.node_cap >= nodes && ctx->bh_cap == ctx->cb.cap) return NBG_OK;
+    if (nbg_bh_alloc(t, ctx->cb.cap, want) != NBG_OK) return fail(ctx, NBG_E_CUDA, "Barnes-Hut buffers");
+    ctx->bh_cap = ctx->cb.cap;
     invalidate_graph(ctx);
     return NBG_OK;
 }
@@ -493,6 +508,7 @@ void nbg_destroy(nbg_ctx *ctx)
     cudaFree(ctx->cb.ev_keys);
     cudaFree(ctx->cb.ev_out);
     free_cap_buffers(ctx->cb);
+    nbg_bh_free(ctx->cb.t);
     cudaFree(ctx->seg_mem);
     cudaFree(ctx->scratch);
     cudaFree(ctx->ctl);
@@ -816,7 +832,11 @@ static void launch_cycle(nbg_ctx *ctx, int precision, long ev_base)
     if (ev_base >= 0) cudaEventRecord(get_event(ctx, (size_t)ev_base), st);
     nbg_launch_begin(cb, ctx->ctl, st);
     nbg_launch_frag_count(cb, ctx->ctl, st);
-    if (precision == NBG_PRECISION_MIXED) {
+    if (cb.bh) {
+        if (ev_base >= 0) cudaEventRecord(get_event(ctx, (size_t)ev_base + 1), st);
+        nbg_launch_bh(cb, ctx->ctl, st);
+        if (ev_base >= 0) cudaEventRecord(get_event(ctx, (size_t)ev_base + 2), st);
+    } else if (precision == NBG_PRECISION_MIXED) {
         nbg_launch_mixed_prep(cb, ctx->ctl, st);
         if (ev_base >= 0) cudaEventRecord(get_event(ctx, (size_t)ev_base + 1), st);
         nbg_launch_mixed_pair(cb, ctx->ctl, st);
@@ -830,8 +850,9 @@ static void launch_cycle(nbg_ctx *ctx, int precision, long ev_base)
     nbg_launch_after_pair(cb, ctx->ctl, st);
     if (ev_base >= 0) cudaEventRecord(get_event(ctx, (size_t)ev_base + 3), st);
     /* begin, fragment count + scan, 10 after the pair kernel, and the pair
-     * kernel; mixed adds reduce, 13 sort, pack, tile origins and the output */
-    ctx->launches_per_cycle = precision == NBG_PRECISION_MIXED ? 31 : 14;
+     * kernel; mixed adds reduce, 13 sort, pack, tile origins and the output;
+     * Barnes-Hut replaces the pair kernel with 55 (k_bh.cu) */
+    ctx->launches_per_cycle = cb.bh ? 13 + 55 : precision == NBG_PRECISION_MIXED ? 31 : 14;
 }
 
 /* One CUDA graph of ctx->graph_cycles consecutive cycles. */
@@ -858,6 +879,7 @@ struct StepParams {
 int nbg_step(nbg_ctx *ctx, double dt, double R, int nsteps, nbg_step_info *info)
 {
     if (!ctx || nsteps < 0) return fail(ctx, NBG_E_ARG, "bad arguments");
+    if (ctx->cb.bh && ctx->cb.seg.nsims != 1) return fail(ctx, NBG_E_STATE, "Barnes-Hut needs a single collection");
     CK(cudaSetDevice(ctx->device));
     /* dt, R and the per-call accumulators */
     {
@@ -870,6 +892,7 @@ int nbg_step(nbg_ctx *ctx, double dt, double R, int nsteps, nbg_step_info *info)
         h->error_what = 0;
         h->error_need = 0;
         h->acc_steps = h->acc_interactions = h->acc_events = h->acc_frags = h->acc_removed = h->acc_nan = 0;
+        h->acc_bh_terms = 0;
         CK(cudaMemcpyAsync(ctx->ctl, h, sizeof(DevCtl), cudaMemcpyHostToDevice, ctx->st));
     }
     ctx->tacc = nbg_timing{};
@@ -920,6 +943,8 @@ int nbg_step(nbg_ctx *ctx, double dt, double R, int nsteps, nbg_step_info *info)
             rc = ensure_ev_cap(ctx, h->error_need);
         else if (h->error_what == 4)
             rc = ensure_part(ctx, h->error_need);
+        else if (h->error_what == 5)
+            rc = ensure_bh(ctx, h->error_need);
         else
             rc = ensure_frag_cap(ctx, h->error_need);
         if (rc != NBG_OK) return rc;
@@ -937,6 +962,7 @@ int nbg_step(nbg_ctx *ctx, double dt, double R, int nsteps, nbg_step_info *info)
         info->removed = h->acc_removed;
         info->nan_removed = h->acc_nan;
         info->next_id = h->next_id;
+        info->bh_terms = h->acc_bh_terms;
     }
     return NBG_OK;
 }
@@ -945,21 +971,31 @@ int nbg_force_pass(nbg_ctx *ctx)
 {
     if (!ctx) return NBG_E_ARG;
     CK(cudaSetDevice(ctx->device));
-    int z = 0;
-    CK(cudaMemcpyAsync(&ctx->ctl->error, &z, sizeof z, cudaMemcpyHostToDevice, ctx->st));
-    nbg_launch_begin(ctx->cb, ctx->ctl, ctx->st);
-    if (ctx->precision == NBG_PRECISION_MIXED) {
-        nbg_launch_mixed_prep(ctx->cb, ctx->ctl, ctx->st);
-        nbg_launch_mixed_pair(ctx->cb, ctx->ctl, ctx->st);
-        nbg_launch_mixed_out(ctx->cb, ctx->ctl, ctx->st);
-    } else {
-        nbg_launch_pair_fp64(ctx->cb, ctx->ctl, ctx->st);
+    if (ctx->cb.bh && ctx->cb.seg.nsims != 1) return fail(ctx, NBG_E_STATE, "Barnes-Hut needs a single collection");
+    for (int attempt = 0;; attempt++) {
+        int z = 0;
+        CK(cudaMemcpyAsync(&ctx->ctl->error, &z, sizeof z, cudaMemcpyHostToDevice, ctx->st));
+        nbg_launch_begin(ctx->cb, ctx->ctl, ctx->st);
+        if (ctx->cb.bh) {
+            nbg_launch_bh(ctx->cb, ctx->ctl, ctx->st);
+        } else if (ctx->precision == NBG_PRECISION_MIXED) {
+            nbg_launch_mixed_prep(ctx->cb, ctx->ctl, ctx->st);
+            nbg_launch_mixed_pair(ctx->cb, ctx->ctl, ctx->st);
+            nbg_launch_mixed_out(ctx->cb, ctx->ctl, ctx->st);
+        } else {
+            nbg_launch_pair_fp64(ctx->cb, ctx->ctl, ctx->st);
+        }
+        CK(cudaGetLastError());
+        int rc = sync_ctl(ctx);
+        if (rc != NBG_OK) return rc;
+        const DevCtl *h = ctx->ctl_h;
+        if (h->error == NBG_E_OVERFLOW && h->error_what == 5 && attempt < 4) {
+            if ((rc = ensure_bh(ctx, h->error_need)) != NBG_OK) return rc;
+            continue;
+        }
+        if (h->error) return fail(ctx, h->error, "force pass failed");
+        return NBG_OK;
     }
-    CK(cudaGetLastError());
-    int rc = sync_ctl(ctx);
-    if (rc != NBG_OK) return rc;
-    if (ctx->ctl_h->error) return fail(ctx, ctx->ctl_h->error, "force pass failed");
-    return NBG_OK;
 }
 
 static int select_variant(nbg_ctx *ctx, int v)
@@ -1165,6 +1201,17 @@ int nbg_set_option(nbg_ctx *ctx, int key, int64_t value)
         return NBG_OK;
     case NBG_OPT_MIX_SHAPE:
         return select_variant(ctx, (int)value);
+    case NBG_OPT_BARNES_HUT: {
+        CK(cudaSetDevice(ctx->device));
+        const int on = value != 0;
+        if (on == ctx->cb.bh) return NBG_OK;
+        ctx->cb.bh = on;
+        invalidate_graph(ctx);
+        if (on) return ensure_bh(ctx, 0);
+        nbg_bh_free(ctx->cb.t);
+        ctx->bh_cap = 0;
+        return NBG_OK;
+    }
     case NBG_OPT_GRAPH_CYCLES:
         if (value < 1 || value > 1000) return fail(ctx, NBG_E_ARG, "cycles per graph must be 1..1000");
         if (value != ctx->graph_cycles) {

@@ -74,11 +74,18 @@ struct DevCtl {
     float near_kappa;
     int pad1;
     /* accumulated over the cycles of one nbg_step call */
-    ll acc_steps, acc_interactions, acc_events, acc_frags, acc_removed, acc_nan;
+    ll acc_steps, acc_interactions, acc_events, acc_frags, acc_removed, acc_nan, acc_bh_terms;
     ll rend_n;       /* renderables written by the last cycle */
     ll last_ev_n;    /* resolved events recorded by the last cycle */
     ll cycle_interactions; /* sum over sims of n_s (n_s - 1) at the cycle start */
     ll work_next;    /* mixed: next chunk for the persistent CTAs */
+    /* Barnes-Hut (k_bh.cu): bounds of the tree bodies as order-preserving
+     * integer images of doubles, the tree body count, nodes built, and the
+     * largest radius of any body (for the collision query) */
+    ull bh_lo[3], bh_hi[3];
+    ll bh_count;
+    ll bh_nodes;
+    ull bh_rmax;
 };
 
 /* A collection may hold several independent simulations stored one after
@@ -142,6 +149,19 @@ __device__ __forceinline__ int nbg_sim_of(const ll *off, int nsims, ll k)
     return lo;
 }
 
+/* Barnes-Hut octree of one collection, nodes in depth-first order */
+struct BhTree {
+    ull *key[2];        /* octant-path keys (radix ping-pong) */
+    unsigned *val[2];   /* body index (ping-pong partner) */
+    ll *hist;           /* radix digit histogram */
+    ll *base;           /* nodes starting at each sorted position, then their scan */
+    ll *blk;            /* per-block sums of that scan */
+    double *mass, *mx, *my, *mz, *cmx, *cmy, *cmz, *cx, *cy, *cz, *half;
+    int *skip, *start, *end, *first;
+    unsigned char *level, *flags;
+    ll node_cap;
+};
+
 struct CycleBufs {
     SimSegs seg;
     BodyArrays a;       /* the collection */
@@ -170,6 +190,8 @@ struct CycleBufs {
     int slots;          /* resident CTAs of the mixed kernel on this device */
     int mix_variant;    /* shape of the mixed pair kernel (see nbg_mix_variant_info) */
     int itile;          /* i-bodies per work item of that shape */
+    int bh;             /* forces from the Barnes-Hut octree */
+    BhTree t;
 };
 
 /* Shapes of the mixed pair kernel the autotuner chooses from. */
@@ -208,6 +230,33 @@ __host__ __device__ __forceinline__ int nbg_work_chunk(ll u, int C, ll W)
 #define NBG_MIX_K 4
 #define NBG_MIX_ITILE (NBG_MIX_BLOCK * NBG_MIX_K)
 #define NBG_MIX_JT 256
+
+/* The reference's event rules (body.go:174-184): the event type for bodies
+ * i, j with behaviours bi, bj, radii ri, rj at distance dist, or -1. */
+__device__ static inline int nbg_detect_event(unsigned bi, unsigned bj, double ri, double rj, double dist)
+{
+    const bool ei = (bi == NBG_ELASTIC || bi == NBG_FRAGMENT);
+    const bool ej = (bj == NBG_ELASTIC || bj == NBG_FRAGMENT);
+    if (ei && ej) return (int)NBG_EVT_COLL_IJ;
+    if (bi == NBG_SUBSUME || bj == NBG_SUBSUME) {
+        if (ri > rj && dist <= ri) return (int)NBG_EVT_SUB_IJ;
+        if (rj > ri && dist <= rj) return (int)NBG_EVT_SUB_JI;
+    }
+    return -1;
+}
+
+/* appends event (i, j, type) to the list (the count may pass the capacity:
+ * the host grows the list and re-runs the cycle) */
+__device__ static inline void nbg_emit_event(DevCtl *ctl, ull *keys, ll cap, ll i, ll j, int type)
+{
+    const ll slot = (ll)atomicAdd((unsigned long long *)&ctl->ev_count, 1ull);
+    if (slot < cap) keys[slot] = ((ull)i << 32) | ((ull)j << 2) | (ull)type;
+}
+
+/* k_bh.cu (compiled with --fmad=false) */
+int nbg_bh_alloc(BhTree &t, ll cap, ll node_cap);
+void nbg_bh_free(BhTree &t);
+void nbg_launch_bh(const CycleBufs &cb, DevCtl *ctl, cudaStream_t st);
 
 /* k_cycle.cu (compiled with --fmad=false) */
 void nbg_launch_begin(const CycleBufs &cb, DevCtl *ctl, cudaStream_t st);

@@ -250,4 +250,12 @@ NBG_FN double nbg_go_min(double x, double y)
     return x < y ? x : y;
 }
 
+/* Go's math.Max: NaN if either is NaN, +0 beats -0. */
+NBG_FN double nbg_go_max(double x, double y)
+{
+    if (x != x || y != y) return nbg_nan();
+    if (x == 0.0 && y == 0.0) return nbg_signbit(x) ? y : x;
+    return x > y ? x : y;
+}
+
 #endif /* NBG_MATH_H */

@@ -86,9 +86,13 @@ static void ev_push(ev_vec *q, int type, ob_body *b1, ob_body *b2)
     q->n++;
 }
 
+typedef struct octree octree;
+
 struct nbo_sim {
     ob_body **arr;
     int64_t n;
+    int barnes_hut; /* forces from the octree (bc.Tree != nil) */
+    octree *tree;
     ev_vec queue; /* arrival order */
     int64_t next_id;
     uint64_t seed;
@@ -196,7 +200,251 @@ static void body_fragment(ob_body *b, const nbo_sim *s, slice_out *out)
     }
 }
 
-/* ---- Compute: body.go:148-187 (direct sum; bc.Tree == nil) --------------- */
+/* ---- Barnes-Hut: cmd/body/octree.go:97-325 --------------------------------
+ * The octree the reference builds when Barnes-Hut is on, with its wiring
+ * fixed: BuildTree (body_collection.go:298-300) creates the tree but never
+ * calls Build, so the reference applies no gravity at all in that mode; here
+ * Build runs at the start of every compute phase, as computation-runner.go:
+ * 294-296 intends.  Bodies are inserted in array order with the incremental
+ * centre-of-mass update, so the tree and every node value are the
+ * reference's.  One guard is added: the reference subdivides without end
+ * when two bodies share a position; here a leaf at depth BH_MAX_DEPTH keeps
+ * every further body it receives (a bucket), and the force pass takes each
+ * of its bodies with mass as a leaf. */
+#define BH_THETA 0.3
+#define BH_SOFTENING 1e-4
+#define BH_MAX_DEPTH 64
+
+typedef struct oct_node {
+    double cx, cy, cz, half;
+    double total_mass, cm_x, cm_y, cm_z;
+    const ob_body *body;
+    int64_t child[8]; /* -1: nil */
+    const ob_body **extra; /* bucket at BH_MAX_DEPTH */
+    int64_t nextra;
+} oct_node;
+
+struct octree {
+    oct_node *pool;
+    int64_t used, cap;
+    int64_t root; /* -1: no tree */
+};
+
+static octree *octree_new(void)
+{
+    octree *t = (octree *)calloc(1, sizeof(octree));
+    t->root = -1;
+    return t;
+}
+
+static void octree_reset(octree *t)
+{
+    for (int64_t k = 0; k < t->used; k++) free(t->pool[k].extra);
+    t->used = 0;
+    t->root = -1;
+}
+
+static void octree_free(octree *t)
+{
+    if (!t) return;
+    octree_reset(t);
+    free(t->pool);
+    free(t);
+}
+
+static int64_t oct_alloc(octree *t)
+{
+    if (t->used == t->cap) {
+        t->cap = t->cap ? 2 * t->cap : 16384;
+        t->pool = (oct_node *)realloc(t->pool, (size_t)t->cap * sizeof(oct_node));
+    }
+    oct_node *n = &t->pool[t->used];
+    memset(n, 0, sizeof *n);
+    for (int c = 0; c < 8; c++) n->child[c] = -1;
+    return t->used++;
+}
+
+/* octantOf, octree.go:53-65 */
+static int oct_octant(const oct_node *n, double x, double y, double z)
+{
+    int idx = 0;
+    if (x >= n->cx) idx |= 1;
+    if (y >= n->cy) idx |= 2;
+    if (z >= n->cz) idx |= 4;
+    return idx;
+}
+
+/* updateMass, octree.go:88-95 */
+static void oct_update_mass(oct_node *n, double mass, double x, double y, double z)
+{
+    double newTotal = n->total_mass + mass;
+    n->cm_x = (n->cm_x * n->total_mass + x * mass) / newTotal;
+    n->cm_y = (n->cm_y * n->total_mass + y * mass) / newTotal;
+    n->cm_z = (n->cm_z * n->total_mass + z * mass) / newTotal;
+    n->total_mass = newTotal;
+}
+
+/* subdivide, octree.go:213-225 (childCenter, octree.go:67-85) */
+static void oct_subdivide(octree *t, int64_t ni)
+{
+    for (int i = 0; i < 8; i++) {
+        int64_t c = oct_alloc(t);
+        oct_node *n = &t->pool[ni], *ch = &t->pool[c];
+        double q = n->half / 2;
+        ch->cx = (i & 1) ? n->cx + q : n->cx - q;
+        ch->cy = (i & 2) ? n->cy + q : n->cy - q;
+        ch->cz = (i & 4) ? n->cz + q : n->cz - q;
+        ch->half = n->half / 2;
+        n->child[i] = c;
+    }
+}
+
+static void oct_insert(octree *t, int64_t ni, const ob_body *b, int depth);
+
+/* insertIntoChild, octree.go:228-232 */
+static void oct_insert_into_child(octree *t, int64_t ni, const ob_body *b, int depth)
+{
+    const oct_node *n = &t->pool[ni];
+    oct_insert(t, n->child[oct_octant(n, b->x, b->y, b->z)], b, depth + 1);
+}
+
+/* insert, octree.go:191-211 */
+static void oct_insert(octree *t, int64_t ni, const ob_body *b, int depth)
+{
+    oct_node *n = &t->pool[ni];
+    oct_update_mass(n, b->mass, b->x, b->y, b->z);
+    if (n->child[0] < 0) {
+        if (n->body == NULL) {
+            n->body = b;
+            return;
+        }
+        if (depth >= BH_MAX_DEPTH) {
+            n->extra = (const ob_body **)realloc(n->extra, (size_t)(n->nextra + 1) * sizeof(ob_body *));
+            n->extra[n->nextra++] = b;
+            return;
+        }
+        const ob_body *existing = n->body;
+        n->body = NULL;
+        oct_subdivide(t, ni);
+        oct_insert_into_child(t, ni, existing, depth);
+        oct_insert_into_child(t, ni, b, depth);
+        return;
+    }
+    oct_insert_into_child(t, ni, b, depth);
+}
+
+/* Build, octree.go:136-188 */
+static void octree_build(octree *t, ob_body *const *bodies, int64_t nb)
+{
+    octree_reset(t);
+    if (nb == 0) return;
+    double minX = NBG_DBL_MAX, minY = NBG_DBL_MAX, minZ = NBG_DBL_MAX;
+    double maxX = -NBG_DBL_MAX, maxY = -NBG_DBL_MAX, maxZ = -NBG_DBL_MAX;
+    int64_t count = 0;
+    for (int64_t k = 0; k < nb; k++) {
+        const ob_body *b = bodies[k];
+        if (!b->exists || b->fragmenting) continue;
+        if (b->x < minX) minX = b->x;
+        if (b->y < minY) minY = b->y;
+        if (b->z < minZ) minZ = b->z;
+        if (b->x > maxX) maxX = b->x;
+        if (b->y > maxY) maxY = b->y;
+        if (b->z > maxZ) maxZ = b->z;
+        count++;
+    }
+    if (count == 0) return;
+    t->root = oct_alloc(t);
+    oct_node *r = &t->pool[t->root];
+    r->cx = (minX + maxX) / 2;
+    r->cy = (minY + maxY) / 2;
+    r->cz = (minZ + maxZ) / 2;
+    r->half = nbg_go_max(maxX - minX, nbg_go_max(maxY - minY, maxZ - minZ)) / 2 * 1.05;
+    for (int64_t k = 0; k < nb; k++)
+        if (bodies[k]->exists && !bodies[k]->fragmenting) oct_insert(t, t->root, bodies[k], 0);
+}
+
+/* the force of a point mass (m at x, y, z) on b, as accumForce applies it
+ * (octree.go:286-292) */
+static void bh_apply(const ob_body *b, double m, double x, double y, double z, double *fx, double *fy, double *fz)
+{
+    double dx = x - b->x;
+    double dy = y - b->y;
+    double dz = z - b->z;
+    double distSq = dx * dx + dy * dy + dz * dz + BH_SOFTENING * BH_SOFTENING;
+    double dist = sqrt(distSq);
+    double force = NBG_G * b->mass * m / distSq;
+    *fx += force * dx / dist;
+    *fy += force * dy / dist;
+    *fz += force * dz / dist;
+}
+
+/* accumForce, octree.go:265-305 */
+static void bh_accum(const octree *t, int64_t ni, const ob_body *b, double *fx, double *fy, double *fz)
+{
+    if (ni < 0) return;
+    const oct_node *n = &t->pool[ni];
+    if (n->total_mass == 0) return;
+    double dx = n->cm_x - b->x;
+    double dy = n->cm_y - b->y;
+    double dz = n->cm_z - b->z;
+    double distSq = dx * dx + dy * dy + dz * dz + BH_SOFTENING * BH_SOFTENING;
+    double dist = sqrt(distSq);
+    const int leaf = n->child[0] < 0;
+    if (leaf || (2 * n->half / dist) < BH_THETA) {
+        if (leaf && n->nextra > 0) {
+            /* bucket: every member as a leaf of its own */
+            const ob_body *o0 = n->body;
+            if (o0 != b && o0->mass != 0)
+                bh_apply(b, o0->mass, o0->x * o0->mass / o0->mass, o0->y * o0->mass / o0->mass,
+                         o0->z * o0->mass / o0->mass, fx, fy, fz);
+            for (int64_t k = 0; k < n->nextra; k++) {
+                const ob_body *o = n->extra[k];
+                if (o != b && o->mass != 0)
+                    bh_apply(b, o->mass, o->x * o->mass / o->mass, o->y * o->mass / o->mass,
+                             o->z * o->mass / o->mass, fx, fy, fz);
+            }
+            return;
+        }
+        if (leaf && n->body == b) return;
+        double force = NBG_G * b->mass * n->total_mass / distSq;
+        *fx += force * dx / dist;
+        *fy += force * dy / dist;
+        *fz += force * dz / dist;
+        return;
+    }
+    for (int c = 0; c < 8; c++) {
+        int64_t ci = n->child[c];
+        if (ci >= 0 && t->pool[ci].total_mass > 0) bh_accum(t, ci, b, fx, fy, fz);
+    }
+}
+
+/* CalcForce, octree.go:236-263: a sun sums every other body directly
+ * (directForce, octree.go:310-325), every other body walks the tree */
+static void bh_calc_force(const octree *t, const ob_body *b, ob_body *const *arr, int64_t n, double *fx, double *fy,
+                          double *fz)
+{
+    *fx = *fy = *fz = 0;
+    if (t->root < 0) return;
+    if (b->is_sun) {
+        for (int64_t k = 0; k < n; k++) {
+            const ob_body *o = arr[k];
+            if (o == b || !o->exists || o->fragmenting) continue;
+            double dx = o->x - b->x;
+            double dy = o->y - b->y;
+            double dz = o->z - b->z;
+            double distSq = dx * dx + dy * dy + dz * dz + BH_SOFTENING * BH_SOFTENING;
+            double dist = sqrt(distSq);
+            double force = NBG_G * b->mass * o->mass / distSq;
+            *fx += force * dx / dist;
+            *fy += force * dy / dist;
+            *fz += force * dz / dist;
+        }
+        return;
+    }
+    bh_accum(t, t->root, b, fx, fy, fz);
+}
+
+/* ---- Compute: body.go:148-187 (bc.Tree == nil: direct sum; else the tree) -- */
 
 static void body_compute(ob_body *b, const nbo_sim *s, slice_out *out)
 {
@@ -210,10 +458,14 @@ static void body_compute(ob_body *b, const nbo_sim *s, slice_out *out)
     b->fz = 0;
     ob_body **arr = s->arr;
     int64_t n = s->n;
-    for (int64_t k = 0; k < n; k++) {
-        const ob_body *o = arr[k];
-        if (!o->exists || b->fragmenting) continue;
-        if (b != o && o->exists && !o->fragmenting) calc_force_from(b, o);
+    if (s->barnes_hut) {
+        bh_calc_force(s->tree, b, arr, n, &b->fx, &b->fy, &b->fz);
+    } else {
+        for (int64_t k = 0; k < n; k++) {
+            const ob_body *o = arr[k];
+            if (!o->exists || b->fragmenting) continue;
+            if (b != o && o->exists && !o->fragmenting) calc_force_from(b, o);
+        }
     }
     for (int64_t k = 0; k < n; k++) {
         ob_body *o = arr[k];
@@ -467,6 +719,7 @@ static void free_bodies(nbo_sim *s)
 void nbo_destroy(nbo_sim *s)
 {
     if (!s) return;
+    octree_free(s->tree);
     free_bodies(s);
     free(s->queue.v);
     free(s->last_ev);
@@ -522,6 +775,12 @@ int nbo_set_bodies(nbo_sim *s, const nbg_soa *in, int64_t n)
 }
 
 int64_t nbo_count(const nbo_sim *s) { return s->n; }
+
+void nbo_set_barnes_hut(nbo_sim *s, int on)
+{
+    s->barnes_hut = on != 0;
+    if (s->barnes_hut && !s->tree) s->tree = octree_new();
+}
 void nbo_set_next_id(nbo_sim *s, int64_t id) { s->next_id = id; }
 int64_t nbo_get_next_id(const nbo_sim *s) { return s->next_id; }
 void nbo_set_cycle(nbo_sim *s, uint64_t cycle) { s->cycle = cycle; }
@@ -667,6 +926,7 @@ static void *compute_worker(void *p)
 void nbo_phase_compute(nbo_sim *s, int nthreads)
 {
     if (nthreads < 1) nthreads = 1;
+    if (s->barnes_hut) octree_build(s->tree, s->arr, s->n); /* computation-runner.go:294-296 */
     int64_t max = s->n;
     int64_t size = max / nthreads;
     if (max < 100) size = max;
@@ -841,7 +1101,10 @@ static void *force_worker(void *p)
     const nbo_sim *s = a->s;
     for (int64_t k = a->lo; k < a->hi; k++) {
         ob_body tmp = *s->arr[k];
-        if (tmp.exists && !tmp.fragmenting) {
+        if (s->barnes_hut) {
+            if (tmp.exists && !tmp.fragmenting)
+                bh_calc_force(s->tree, s->arr[k], s->arr, s->n, &tmp.fx, &tmp.fy, &tmp.fz);
+        } else if (tmp.exists && !tmp.fragmenting) {
             tmp.fx = tmp.fy = tmp.fz = 0;
             for (int64_t q = 0; q < s->n; q++) {
                 const ob_body *o = s->arr[q];
@@ -859,6 +1122,7 @@ static void *force_worker(void *p)
 int nbo_forces(const nbo_sim *s, double *fx, double *fy, double *fz, int nthreads)
 {
     if (nthreads < 1) nthreads = 1;
+    if (s->barnes_hut) octree_build(s->tree, s->arr, s->n);
     pthread_t *th = (pthread_t *)malloc((size_t)nthreads * sizeof(pthread_t));
     force_arg *fa = (force_arg *)malloc((size_t)nthreads * sizeof(force_arg));
     int64_t per = (s->n + nthreads - 1) / nthreads;

@@ -32,6 +32,10 @@ void nbo_set_next_id(nbo_sim *s, int64_t id);
 int64_t nbo_get_next_id(const nbo_sim *s);
 void nbo_set_cycle(nbo_sim *s, uint64_t cycle);
 
+/* Barnes-Hut forces (cmd/body/octree.go, with BuildTree's missing Build call
+ * made): the tree is rebuilt at the start of every compute phase. */
+void nbo_set_barnes_hut(nbo_sim *s, int on);
+
 /* Enqueue(NewAdd(b)); ids taken from the counter when id is NULL or < 0. */
 int nbo_add_bodies(nbo_sim *s, const nbg_soa *in, int64_t n, int64_t *ids_out);
 /* processDeletes (computation-runner.go:176-216). */

@@ -31,6 +31,7 @@ def load():
         "nbo_destroy": (None, [P]),
         "nbo_set_bodies": (C.c_int, [P, C.POINTER(A.NbgSoa), C.c_int64]),
         "nbo_count": (C.c_int64, [P]),
+        "nbo_set_barnes_hut": (None, [P, C.c_int]),
         "nbo_get_state": (C.c_int, [P, C.POINTER(A.NbgSoa), C.c_int64]),
         "nbo_set_next_id": (None, [P, C.c_int64]),
         "nbo_get_next_id": (C.c_int64, [P]),
@@ -85,6 +86,10 @@ class OracleSim:
         rc = self.lib.nbo_set_bodies(self.s, C.byref(soa), n)
         assert rc == 0
         del keep
+
+    def set_barnes_hut(self, on=True):
+        """Forces from the reference's octree (cmd/body/octree.go) instead of the direct sum."""
+        self.lib.nbo_set_barnes_hut(self.s, 1 if on else 0)
 
     def count(self):
         return self.lib.nbo_count(self.s)

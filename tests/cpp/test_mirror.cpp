@@ -264,19 +264,31 @@ static void TestRunnerSetters()
 {
     cur_test = "TestRunnerSetters";
     BodyCollection bc(std::vector<Body>{});
-    ComputationRunner cr(1, 1, false, bc);
+    ComputationRunner cr(1, 1, true, bc); /* Barnes-Hut, as the reference test */
     cr.SetCoefficientOfRestitution(5);
     cr.SetTimeScaling(5);
     cr.SetWorkers(5);
     cr.RunOneComputation(); /* the setters are picked up at the start of a cycle */
     CHECK(cr.CoefficientOfRestitution() == 5 && cr.TimeScaling() == 5 && cr.WorkerCount() == 5, "Setters failed");
-    bool threw = false;
-    try {
-        ComputationRunner bh(1, 1, true, bc);
-    } catch (const Error &e) {
-        threw = e.code == NBG_E_ARG;
-    }
-    CHECK(threw, "Barnes-Hut is refused");
+    std::printf("ok   %s\n", cur_test);
+}
+
+static void TestRunnerBarnesHut()
+{
+    cur_test = "TestRunnerBarnesHut";
+    /* with the tree built, Barnes-Hut applies gravity (the reference's
+     * BuildTree alone would leave every force at zero) */
+    std::vector<Body> v;
+    for (int k = 0; k < 64; k++)
+        v.push_back(NewBody(k, (k % 4) * 10.0, (k / 4 % 4) * 10.0, (k / 16) * 10.0, 0, 0, 0, 1e12, 0.1, Elastic, Random,
+                            0, 0, false, "", "", false));
+    BodyCollection bc(v);
+    ComputationRunner cr(4, 0.01, true, bc);
+    cr.RunOneComputation();
+    std::vector<Body> arr = bc.GetArray();
+    CHECK(arr.size() == 64, "count");
+    CHECK(arr[0].Vx > 0 && arr[0].Vy > 0 && arr[0].Vz > 0, "the corner body falls inward");
+    CHECK(arr[63].Vx < 0 && arr[63].Vy < 0 && arr[63].Vz < 0, "the far corner too");
     std::printf("ok   %s\n", cur_test);
 }
 
@@ -319,6 +331,7 @@ int main(int argc, char **argv)
             TestModPhysical();
             TestAdds();
             TestRunnerSetters();
+            TestRunnerBarnesHut();
             TestRunnerCycle();
         } catch (const Error &e) {
             std::printf("FAIL %s: nbg status %d: %s\n", cur_test, e.code, e.what());

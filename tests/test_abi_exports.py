@@ -41,6 +41,6 @@ def test_struct_sizes_match_header_layout():
     # nbg_soa: 24 pointers; nbg_edit: 8 + 4 + 4 + 10 doubles + 2 ints
     assert ctypes.sizeof(_abi.NbgSoa) == 24 * ctypes.sizeof(ctypes.c_void_p)
     assert ctypes.sizeof(_abi.NbgEdit) == 8 + 4 + 4 + 80 + 8
-    assert ctypes.sizeof(_abi.NbgStepInfo) == 8 * 8
+    assert ctypes.sizeof(_abi.NbgStepInfo) == 9 * 8
     assert ctypes.sizeof(_abi.NbgRenderable) == 32
     assert ctypes.sizeof(_abi.NbgEvent) == 24

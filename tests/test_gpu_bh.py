@@ -1,0 +1,129 @@
+"""Barnes-Hut force pass (cmd/body/octree.go, with BuildTree's missing Build
+call made) on the GPU against the oracle's restatement, through the C ABI.
+
+The GPU builds the reference's tree (same nodes, same opening decisions) but
+sums each node's centre of mass as sum(m x) / sum(m) rather than by the
+reference's running update, and a sun's direct sum as a parallel reduction;
+both differ in the last bits only, so forces agree to 1e-12 relative and
+whole cycles keep identical event lists."""
+import numpy as np
+import pytest
+
+from nbodygo_gb300 import _abi as A
+from nbodygo_gb300 import workloads as W
+from nbodygo_gb300.api import NbgError, Simulation
+from oracle.oracle import OracleSim
+
+from helpers import assert_events_identical
+from test_gpu_plain_parity import dense_cluster
+
+pytestmark = pytest.mark.gpu
+FORCE_RTOL = 1e-12
+
+
+def bh_pair(bodies, precision="fp64", seed=123):
+    sim = Simulation(precision, seed=seed)
+    sim.set_option(A.OPT_BARNES_HUT, 1)
+    sim.set_bodies(bodies)
+    ora = OracleSim(seed=seed, threads=8)
+    ora.set_barnes_hut(True)
+    ora.set_bodies(bodies)
+    return sim, ora
+
+
+def force_error(got, exp):
+    g, e = np.stack(got, 1), np.stack(exp, 1)
+    mag = np.linalg.norm(e, axis=1)
+    err = np.linalg.norm(g - e, axis=1)
+    ok = mag > 0
+    assert np.all(err[~ok] == 0)
+    return float(np.max(err[ok] / mag[ok])) if ok.any() else 0.0
+
+
+def with_sun(b, k=0):
+    b = {f: np.array(v) for f, v in b.items()}
+    b["flags"][k] |= A.F_IS_SUN
+    return b
+
+
+@pytest.mark.parametrize("name,bodies", [
+    ("plummer", lambda: W.plummer(3000, seed=7)),
+    ("disk_with_sun", lambda: with_sun(W.disk(1500))),
+    ("uniform", lambda: W.uniform_ball(2000, R=200.0)),
+])
+def test_bh_forces_match_oracle(name, bodies):
+    b = bodies()
+    sim, ora = bh_pair(b)
+    got = sim.force_pass()
+    exp = ora.forces()
+    assert force_error(got, exp) <= FORCE_RTOL, name
+
+
+def test_bh_forces_differ_from_direct_sum_by_the_approximation_only():
+    b = W.plummer(3000, seed=8)
+    sim, _ = bh_pair(b)
+    bh = np.stack(sim.force_pass(), 1)
+    direct = Simulation("fp64")
+    direct.set_bodies(b)
+    ds = np.stack(direct.force_pass(), 1)
+    rel = np.linalg.norm(bh - ds) / np.linalg.norm(ds)
+    assert 1e-6 < rel < 5e-3  # theta = 0.3 plus softening, not zero gravity
+
+
+def test_bh_massless_bodies_keep_the_reference_nan_centre_rule():
+    """A node whose first body (array order) is massless has the reference's
+    NaN running centre and is always opened."""
+    b = W.plummer(800, seed=9)
+    b["mass"][0] = 0.0
+    b["mass"][5] = 0.0
+    b["mass"][100:110] = 0.0
+    sim, ora = bh_pair(b)
+    assert force_error(sim.force_pass(), ora.forces()) <= FORCE_RTOL
+
+
+def test_bh_cycles_track_the_oracle_with_collisions():
+    """Dense cluster, every behaviour: the tree query finds exactly the
+    collisions of the O(N^2) pass, cycle after cycle."""
+    b = dense_cluster(400, seed=31)
+    sim, ora = bh_pair(b)
+    sim.apply_edits([dict(id=int(b["id"][3]), mask=A.M_EXISTS, exists=0)])
+    ora.apply_edits([dict(id=int(b["id"][3]), mask=A.M_EXISTS, exists=0)])
+    for c in range(12):
+        gi = sim.step(0.05, 0.9, 1)
+        oi = ora.step(0.05, 0.9, 1)
+        assert_events_identical(sim.events(), ora.events(), f"cycle {c}")
+        for k in ("n_bodies", "events", "fragments_emitted", "removed", "next_id"):
+            assert gi[k] == oi[k], f"cycle {c}: {k} {gi[k]} != {oi[k]}"
+        gs, os_ = sim.state(), ora.state()
+        assert np.array_equal(gs["id"], os_["id"])
+        assert np.array_equal(gs["flags"], os_["flags"])
+        for f in ("x", "y", "z", "vx", "vy", "vz", "mass"):
+            d = np.abs(gs[f] - os_[f])
+            scale = np.maximum(np.abs(os_[f]), 1e-300)
+            assert np.all((d <= 1e-9 * scale) | (d <= 1e-12)), f"cycle {c}: {f}"
+
+
+def test_bh_step_with_a_graph_equals_single_cycles():
+    b = W.plummer(2048, seed=11)
+    s1 = Simulation("fp64")
+    s1.set_option(A.OPT_BARNES_HUT, 1)
+    s1.set_bodies(b)
+    s1.step(0.01, 1.0, 6)
+    s2 = Simulation("fp64")
+    s2.set_option(A.OPT_BARNES_HUT, 1)
+    s2.set_option(A.OPT_GRAPH, 0)
+    s2.set_bodies(b)
+    for _ in range(6):
+        s2.step(0.01, 1.0, 1)
+    a, c = s1.state(), s2.state()
+    for f in ("x", "y", "z", "vx", "vy", "vz"):
+        assert np.array_equal(a[f].view(np.uint64), c[f].view(np.uint64)), f
+
+
+def test_bh_needs_a_single_collection():
+    sim = Simulation("fp64")
+    sim.set_option(A.OPT_BARNES_HUT, 1)
+    sim.set_collections([W.plummer(300, seed=1), W.plummer(200, seed=2)])
+    with pytest.raises(NbgError) as e:
+        sim.step(0.01, 1.0, 1)
+    assert e.value.code == A.NBG_E_STATE
