@@ -259,7 +259,7 @@ int nbg_energy(nbg_ctx *ctx, double *kinetic, double *potential, double momentum
  * Errors are reported through nbg_last_error(NULL).
  */
 #define NBG_NOALLOC_MAX_BODIES 65536
-#define NBG_NOALLOC_BYTES 9473024
+#define NBG_NOALLOC_BYTES 9473280
 int nbg_forces_mixed_noalloc(const double *x, const double *y, const double *z, const double *mass,
                              const double *radius, const uint32_t *flags, int64_t n, double *fx, double *fy,
                              double *fz, void *stream);

@@ -93,51 +93,99 @@ __global__ void __launch_bounds__(RS_BLOCK) k_rs_hist(DevCtl *ctl, const unsigne
     for (int d = threadIdx.x; d < RS_BINS; d += RS_BLOCK) hist[(ll)d * nb + b] = cnt[d];
 }
 
-/* exclusive scan of the digit-major histogram (one block; each thread takes
- * four consecutive entries per round) */
-#define RS_SCAN_ITEMS 4
-__global__ void __launch_bounds__(1024) k_rs_scan(DevCtl *ctl, ll *hist)
+/* Exclusive scan of the digit-major histogram in three launches: per-chunk
+ * sums, a scan of those sums (one block), and the scan of each chunk from its
+ * offset.  A chunk is RS_SCAN_CHUNK entries; the chunk sums sit after the
+ * histogram in the same buffer. */
+#define RS_SCAN_ITEMS 8
+#define RS_SCAN_CHUNK (1024 * RS_SCAN_ITEMS)
+
+__device__ __forceinline__ ll rs_hist_total(const DevCtl *ctl)
+{
+    return ((ctl->n + RS_TILE - 1) / RS_TILE) * RS_BINS;
+}
+
+/* block-wide inclusive scan of one value per thread (1024 threads) */
+__device__ __forceinline__ ll rs_block_incl(ll x, ll *warp_tot, ll *block_total)
+{
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (int o = 1; o < 32; o <<= 1) {
+        const ll y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) warp_tot[w] = x;
+    __syncthreads();
+    if (w == 0) {
+        ll t = warp_tot[lane];
+        for (int o = 1; o < 32; o <<= 1) {
+            const ll y = __shfl_up_sync(0xffffffffu, t, o);
+            if (lane >= o) t += y;
+        }
+        warp_tot[lane] = t;
+    }
+    __syncthreads();
+    const ll r = x + (w > 0 ? warp_tot[w - 1] : 0);
+    *block_total = warp_tot[31];
+    __syncthreads();
+    return r;
+}
+
+__global__ void __launch_bounds__(1024) k_rs_scan_part(DevCtl *ctl, ll *hist)
 {
     __shared__ ll warp_tot[32];
     if (ctl->error) return;
-    const ll n = ctl->n;
-    const ll nb = (n + RS_TILE - 1) / RS_TILE;
-    const ll total = nb * RS_BINS;
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const ll total = rs_hist_total(ctl);
+    const ll c0 = (ll)blockIdx.x * RS_SCAN_CHUNK;
+    if (c0 >= total) return;
+    ll s = 0;
+    for (int q = 0; q < RS_SCAN_ITEMS; q++) {
+        const ll c = c0 + (ll)q * 1024 + threadIdx.x;
+        if (c < total) s += hist[c];
+    }
+    ll tot;
+    rs_block_incl(s, warp_tot, &tot);
+    if (threadIdx.x == 0) hist[total + blockIdx.x] = tot;
+}
+
+__global__ void __launch_bounds__(1024) k_rs_scan_top(DevCtl *ctl, ll *hist)
+{
+    __shared__ ll warp_tot[32];
+    if (ctl->error) return;
+    const ll total = rs_hist_total(ctl);
+    const ll nchunk = (total + RS_SCAN_CHUNK - 1) / RS_SCAN_CHUNK;
+    ll *sums = hist + total;
     ll carry = 0;
-    for (ll c0 = 0; c0 < total; c0 += 1024 * RS_SCAN_ITEMS) {
-        const ll c = c0 + (ll)threadIdx.x * RS_SCAN_ITEMS;
-        ll v[RS_SCAN_ITEMS];
-        ll sum = 0;
+    for (ll b0 = 0; b0 < nchunk; b0 += 1024) {
+        const ll b = b0 + threadIdx.x;
+        const ll v = b < nchunk ? sums[b] : 0;
+        ll tot;
+        const ll inc = rs_block_incl(v, warp_tot, &tot);
+        if (b < nchunk) sums[b] = carry + inc - v;
+        carry += tot;
+    }
+}
+
+__global__ void __launch_bounds__(1024) k_rs_scan_fin(DevCtl *ctl, ll *hist)
+{
+    __shared__ ll warp_tot[32];
+    if (ctl->error) return;
+    const ll total = rs_hist_total(ctl);
+    const ll c0 = (ll)blockIdx.x * RS_SCAN_CHUNK;
+    if (c0 >= total) return;
+    /* thread t takes RS_SCAN_ITEMS consecutive entries */
+    const ll c = c0 + (ll)threadIdx.x * RS_SCAN_ITEMS;
+    ll v[RS_SCAN_ITEMS], s = 0;
 #pragma unroll
-        for (int q = 0; q < RS_SCAN_ITEMS; q++) {
-            v[q] = c + q < total ? hist[c + q] : 0;
-            sum += v[q];
-        }
-        ll x = sum;
-        for (int o = 1; o < 32; o <<= 1) {
-            ll y = __shfl_up_sync(0xffffffffu, x, o);
-            if (lane >= o) x += y;
-        }
-        if (lane == 31) warp_tot[w] = x;
-        __syncthreads();
-        if (w == 0) {
-            ll t = warp_tot[lane];
-            for (int o = 1; o < 32; o <<= 1) {
-                ll y = __shfl_up_sync(0xffffffffu, t, o);
-                if (lane >= o) t += y;
-            }
-            warp_tot[lane] = t;
-        }
-        __syncthreads();
-        ll ex = carry + x - sum + (w > 0 ? warp_tot[w - 1] : 0);
+    for (int q = 0; q < RS_SCAN_ITEMS; q++) {
+        v[q] = c + q < total ? hist[c + q] : 0;
+        s += v[q];
+    }
+    ll tot;
+    ll ex = rs_block_incl(s, warp_tot, &tot) - s + hist[total + blockIdx.x];
 #pragma unroll
-        for (int q = 0; q < RS_SCAN_ITEMS; q++) {
-            if (c + q < total) hist[c + q] = ex;
-            ex += v[q];
-        }
-        carry += warp_tot[31];
-        __syncthreads();
+    for (int q = 0; q < RS_SCAN_ITEMS; q++) {
+        if (c + q < total) hist[c + q] = ex;
+        ex += v[q];
     }
 }
 
@@ -183,7 +231,12 @@ __global__ void __launch_bounds__(RS_BLOCK) k_rs_scatter(DevCtl *ctl, const unsi
     }
 }
 
-ll nbg_sort_scratch_hist(ll cap) { return ((cap + RS_TILE - 1) / RS_TILE) * RS_BINS; }
+/* the histogram plus its chunk sums */
+ll nbg_sort_scratch_hist(ll cap)
+{
+    const ll h = ((cap + RS_TILE - 1) / RS_TILE) * RS_BINS;
+    return h + (h + RS_SCAN_CHUNK - 1) / RS_SCAN_CHUNK;
+}
 
 /* Leaves the sorted permutation in cb.perm. */
 void nbg_launch_spatial_sort(const CycleBufs &cb, DevCtl *ctl, cudaStream_t st)
@@ -191,11 +244,14 @@ void nbg_launch_spatial_sort(const CycleBufs &cb, DevCtl *ctl, cudaStream_t st)
     const int g = (int)((cb.cap + 255) / 256 < 152 * 16 ? (cb.cap + 255) / 256 : 152 * 16);
     k_morton_keys<<<g > 0 ? g : 1, 256, 0, st>>>(cb.a, ctl, cb.seg, cb.skey[0], cb.perm);
     const int nb = (int)((cb.cap + RS_TILE - 1) / RS_TILE);
+    const int nchunk = (int)(((ll)nb * RS_BINS + RS_SCAN_CHUNK - 1) / RS_SCAN_CHUNK);
     unsigned *kin = cb.skey[0], *vin = cb.perm, *kout = cb.skey[1], *vout = cb.sval;
     for (int pass = 0; pass < 4; pass++) {
         const int shift = 8 * pass;
         k_rs_hist<<<nb, RS_BLOCK, 0, st>>>(ctl, kin, shift, cb.shist);
-        k_rs_scan<<<1, 1024, 0, st>>>(ctl, cb.shist);
+        k_rs_scan_part<<<nchunk, 1024, 0, st>>>(ctl, cb.shist);
+        k_rs_scan_top<<<1, 1024, 0, st>>>(ctl, cb.shist);
+        k_rs_scan_fin<<<nchunk, 1024, 0, st>>>(ctl, cb.shist);
         k_rs_scatter<<<nb, RS_BLOCK, 0, st>>>(ctl, kin, vin, kout, vout, shift, cb.shist);
         unsigned *t = kin;
         kin = kout;

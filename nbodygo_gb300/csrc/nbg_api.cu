@@ -850,9 +850,9 @@ static void launch_cycle(nbg_ctx *ctx, int precision, long ev_base)
     nbg_launch_after_pair(cb, ctx->ctl, st);
     if (ev_base >= 0) cudaEventRecord(get_event(ctx, (size_t)ev_base + 3), st);
     /* begin, fragment count + scan, 10 after the pair kernel, and the pair
-     * kernel; mixed adds reduce, 13 sort, pack, tile origins and the output;
+     * kernel; mixed adds reduce, 21 sort, pack, tile origins and the output;
      * Barnes-Hut replaces the pair kernel with 55 (k_bh.cu) */
-    ctx->launches_per_cycle = cb.bh ? 13 + 55 : precision == NBG_PRECISION_MIXED ? 31 : 14;
+    ctx->launches_per_cycle = cb.bh ? 13 + 55 : precision == NBG_PRECISION_MIXED ? 39 : 14;
 }
 
 /* One CUDA graph of ctx->graph_cycles consecutive cycles. */

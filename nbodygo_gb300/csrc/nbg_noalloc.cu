@@ -39,8 +39,10 @@ static constexpr size_t OFF_SVAL = OFF_PERM + align256((size_t)NBG_NOALLOC_MAX_B
 static constexpr size_t OFF_KEY0 = OFF_SVAL + align256((size_t)NBG_NOALLOC_MAX_BODIES * 4);
 static constexpr size_t OFF_KEY1 = OFF_KEY0 + align256((size_t)NBG_NOALLOC_MAX_BODIES * 4);
 static constexpr size_t OFF_HIST = OFF_KEY1 + align256((size_t)NBG_NOALLOC_MAX_BODIES * 4);
-/* radix-sort histogram: 256 digits per 4096-body block */
-static constexpr size_t HIST_BYTES = (size_t)((NBG_NOALLOC_MAX_BODIES + 4095) / 4096) * 256 * 8;
+/* radix-sort histogram: 256 digits per 4096-body block, then one sum per
+ * 8192-entry chunk of it */
+static constexpr size_t HIST_ENTRIES = (size_t)((NBG_NOALLOC_MAX_BODIES + 4095) / 4096) * 256;
+static constexpr size_t HIST_BYTES = (HIST_ENTRIES + (HIST_ENTRIES + 8191) / 8192) * 8;
 /* the per-sim layout arrays of one collection */
 static constexpr size_t OFF_SEG = OFF_HIST + align256(HIST_BYTES);
 static constexpr size_t TOTAL_BYTES = OFF_SEG + align256(NBG_SEG_BYTES(1));
