@@ -68,6 +68,10 @@ WORKLOADS = {
     "disk": ("fp64", 0.005, "central body 5e15 + disk r 100-1000, elastic"),
     "plummer_bh": ("fp64", 0.01, "Plummer a=200 M=1e16, 131072 bodies, radius 0.2, elastic; Barnes-Hut octree "
                                  "forces (theta 0.3, softening 1e-4, FP64), exact collisions"),
+    "plummer_bh_mixed": ("mixed", 0.01, "Plummer a=200 M=1e16, 131072 bodies, radius 0.2, elastic; Barnes-Hut "
+                                        "octree, mixed walk (FP32 terms), exact collisions"),
+    "uniform_bh_mixed": ("mixed", 0.01, "uniform ball R=20000, m=1e10, radius 0.05, 1048576 bodies, no collisions; "
+                                        "Barnes-Hut octree, mixed walk"),
 }
 
 
@@ -208,8 +212,10 @@ def make_workload(name, n_each, rank):
         return [W.uniform_ball(seed=4 + seed_off)]
     if name == "plummer":
         return [W.plummer(seed=2 + seed_off)]
-    if name == "plummer_bh":
+    if name in ("plummer_bh", "plummer_bh_mixed"):
         return [W.plummer(131072, seed=2 + seed_off)]
+    if name == "uniform_bh_mixed":
+        return [W.uniform_ball(seed=4 + seed_off)]
     return [W.disk(seed=1 + seed_off)]
 
 
@@ -232,14 +238,14 @@ def cpu_baseline_sample(workload, dt):
     elif workload == "plummer":
         b = W.plummer(seed=2)
         what = "plummer with 16384 bodies (the full workload)"
-    elif workload == "plummer_bh":
+    elif workload.endswith("_bh") or workload.endswith("_bh_mixed"):
         b = W.plummer(32768, seed=2)
         what = "plummer with 32768 bodies, Barnes-Hut (the reference's octree, built once per cycle)"
     else:
         b = W.disk(seed=1)
         what = "disk with 1000 bodies (the full workload)"
     o = OracleSim(threads=cores)
-    if workload.endswith("_bh"):
+    if "_bh" in workload:
         o.set_barnes_hut(True)
     o.set_bodies(b)
     steps = 1 if len(b["x"]) > 10000 else 20
@@ -265,14 +271,14 @@ def run_reference(args, ws, rank):
     elif args.workload == "plummer":
         b = W.plummer(seed=2)
         sample = "the full plummer workload (16,384 bodies)"
-    elif args.workload == "plummer_bh":
+    elif "_bh" in args.workload:
         b = W.plummer(32768, seed=2)
         sample = "plummer with 32,768 bodies per cycle, Barnes-Hut"
     else:
         b = W.disk(seed=1)
         sample = "the full disk workload (1,000 bodies)"
     o = OracleSim(threads=cores)
-    if args.workload.endswith("_bh"):
+    if "_bh" in args.workload:
         o.set_barnes_hut(True)
     o.set_bodies(b)
     for _ in range(args.warmup):
@@ -337,7 +343,7 @@ def main():
     chunk = 10 if args.workload == "ensemble" else 1
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
 
-    bh = args.workload.endswith("_bh")
+    bh = "_bh" in args.workload
     sim = Simulation(prec, device=local, capacity=n0 + 4096)
     sim.set_stream(stream.cuda_stream)
     sim.set_option(A.OPT_GRAPH_CYCLES, chunk)
@@ -348,7 +354,7 @@ def main():
     if prec == "mixed" and args.shape is not None:
         sim.set_option(A.OPT_MIX_SHAPE, args.shape)
         tuned = {"shape": args.shape, "pair_kernel_ms": None, "candidates": A.MIX_SHAPES, "fixed": True}
-    elif prec == "mixed" and not args.no_autotune:
+    elif prec == "mixed" and not args.no_autotune and not bh:
         shape, tms = sim.autotune()
         tuned = {"shape": shape, "pair_kernel_ms": tms, "candidates": A.MIX_SHAPES}
     sim.step(DT, 1.0, max(args.warmup, 3) * chunk)
@@ -424,7 +430,7 @@ def main():
     # ---- FP32 / FP64 peaks, plain FP64 comparison, accuracy ----
     f32, f64, mhz = probe_peaks(local)
     result_extra = {}
-    plain_ok = prec == "mixed" and args.workload != "uniform" and not args.no_plain and rank == 0
+    plain_ok = prec == "mixed" and args.workload != "uniform" and not bh and not args.no_plain and rank == 0
     if plain_ok:
         plain = Simulation("fp64", device=local, capacity=n0 + 4096)
         plain.set_stream(stream.cuda_stream)
@@ -468,8 +474,12 @@ def main():
         # the whole tree pass (build, walk, collision query) against the FP64
         # peak, counting only the point-mass terms the walk summed
         achieved = bh_terms_t * FLOPS_PER_PAIR / (pair_ms * 1e-3) / 1e12
-        peak, kernel, bound = f64 / 1e12, "k_bh_* (tree build + k_bh_force + k_bh_collide)", "fp64_fma"
-        peak_src = f"DFMA-chain probe on this GPU at {mhz:.0f} MHz (MEASURED_PEAKS.json has no FP64 figure)"
+        if prec == "mixed":
+            peak, kernel, bound = f32 / 1e12, "k_bh_* (tree build + k_bh_force_mixed + k_bh_collide)", "fp32_fma"
+            peak_src = f"FFMA-chain probe on this GPU at {mhz:.0f} MHz (MEASURED_PEAKS.json has no FP32 figure)"
+        else:
+            peak, kernel, bound = f64 / 1e12, "k_bh_* (tree build + k_bh_force + k_bh_collide)", "fp64_fma"
+            peak_src = f"DFMA-chain probe on this GPU at {mhz:.0f} MHz (MEASURED_PEAKS.json has no FP64 figure)"
     elif prec == "mixed":
         achieved = inter_t * FLOPS_PER_PAIR / (pair_ms * 1e-3) / 1e12
         peak, kernel, bound = f32 / 1e12, "k_pair_mixed", "fp32_fma"

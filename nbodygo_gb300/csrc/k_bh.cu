@@ -582,6 +582,155 @@ __global__ void __launch_bounds__(BH_BLOCK) k_bh_force(BodyArrays A, DevCtl *ctl
     if ((threadIdx.x & 31) == 0 && terms) atomicAdd((unsigned long long *)&ctl->acc_bh_terms, terms);
 }
 
+/* ---- 5b. the mixed-precision walk --------------------------------------------
+ * The same tree and the same acceptance rule in FP32: centres of mass as
+ * hi/lo float pairs (so dx = (cm_hi - x_hi) + (cm_lo - x_lo) keeps ~2^-24 of
+ * |dx|), masses relative to the root's, the opening test as
+ * r^2 > (2 half / theta)^2 on the softened r^2, and the reciprocal square
+ * root of the SFU.  The 32 bodies of a warp (neighbours in key order) walk
+ * one node sequence together: a lane that accepts a node waits until the
+ * warp leaves that node's subtree (its skip pointer), and the warp descends
+ * when any lane opens, so every node load is a broadcast and no lane
+ * diverges.  Each lane sums its terms in FP32 and folds them into FP64 every
+ * 64 terms. */
+__global__ void __launch_bounds__(BH_BLOCK) k_bh_prep_mixed(DevCtl *ctl, BhTree t)
+{
+    if (ctl->error) return;
+    const ll total = ctl->bh_nodes;
+    if (total <= 0) return;
+    const double mroot = t.mass[0];
+    const double inv_root = mroot != 0 ? 1.0 / mroot : 0.0;
+    for (ll id = (ll)blockIdx.x * blockDim.x + threadIdx.x; id < total; id += (ll)gridDim.x * blockDim.x) {
+        const double M = t.mass[id];
+        float4 a = make_float4(0.f, 0.f, 0.f, 0.f), b = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (M != 0) {
+            const double cx = t.cmx[id], cy = t.cmy[id], cz = t.cmz[id];
+            a.x = (float)cx;
+            a.y = (float)cy;
+            a.z = (float)cz;
+            b.x = (float)(cx - (double)a.x);
+            b.y = (float)(cy - (double)a.y);
+            b.z = (float)(cz - (double)a.z);
+            a.w = (float)(M * inv_root);
+            const double o = 2 * t.half[id] / BH_THETA;
+            b.w = (float)(o * o);
+        }
+        t.fa[id] = a;
+        t.fb[id] = b;
+    }
+}
+
+__device__ __forceinline__ float bh_rsqrt(float x)
+{
+    float y;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
+__global__ void __launch_bounds__(BH_BLOCK) k_bh_force_mixed(BodyArrays A, DevCtl *ctl, const unsigned *vals,
+                                                             BhTree t)
+{
+    if (ctl->error) return;
+    const ll M = ctl->bh_count;
+    const int total = (int)ctl->bh_nodes;
+    if (total <= 0) return;
+    const double mroot = t.mass[0];
+    const float soft2 = (float)(BH_SOFTENING * BH_SOFTENING);
+    unsigned long long terms = 0;
+    for (ll base0 = (ll)blockIdx.x * blockDim.x; base0 < M; base0 += (ll)gridDim.x * blockDim.x) {
+        const ll p = base0 + threadIdx.x;
+        unsigned k = 0;
+        bool have = p < M;
+        if (have) {
+            k = vals[p];
+            have = !(A.flags[k] & NBG_F_IS_SUN); /* k_bh_sun */
+        }
+        float xh = 0.f, yh = 0.f, zh = 0.f, xl = 0.f, yl = 0.f, zl = 0.f;
+        if (have) {
+            const double x = A.x[k], y = A.y[k], z = A.z[k];
+            xh = (float)x;
+            yh = (float)y;
+            zh = (float)z;
+            xl = (float)(x - (double)xh);
+            yl = (float)(y - (double)yh);
+            zl = (float)(z - (double)zh);
+        }
+        int wait = have ? 0 : 0x7fffffff;
+        float ax = 0.f, ay = 0.f, az = 0.f;
+        double sx = 0, sy = 0, sz = 0;
+        int nacc = 0;
+        int id = 0;
+        if (!__any_sync(FULL_MASK, have)) continue;
+        while (id < total) {
+            const float4 a = t.fa[id];
+            const int sk = t.skip[id];
+            if (a.w == 0.f) {
+                /* nothing with mass below: no lane waits inside this subtree */
+                id = sk;
+                continue;
+            }
+            const float4 b = t.fb[id];
+            const unsigned fl = t.flags[id];
+            const bool leaf = (fl & BH_F_LEAF) != 0;
+            const bool active = id >= wait;
+            const float dx = (a.x - xh) + (b.x - xl);
+            const float dy = (a.y - yh) + (b.y - yl);
+            const float dz = (a.z - zh) + (b.z - zl);
+            const float r2 = dx * dx + dy * dy + dz * dz + soft2;
+            const bool accept = leaf || (!(fl & BH_F_NAN_CM) && r2 > b.w);
+            if (active && accept) {
+                const int s = t.start[id], e = t.end[id];
+                if (leaf && e - s > 1) {
+                    for (int q = s; q < e; q++) {
+                        const unsigned j = vals[q];
+                        const double mj = A.m[j];
+                        if (j == k || mj == 0) continue;
+                        const float ex = (float)(A.x[j] - (double)xh - (double)xl);
+                        const float ey = (float)(A.y[j] - (double)yh - (double)yl);
+                        const float ez = (float)(A.z[j] - (double)zh - (double)zl);
+                        const float q2 = ex * ex + ey * ey + ez * ez + soft2;
+                        const float inv = bh_rsqrt(q2);
+                        const float w = (float)(mj / mroot) * inv * inv * inv;
+                        ax += w * ex;
+                        ay += w * ey;
+                        az += w * ez;
+                        nacc++;
+                    }
+                } else if (!(leaf && vals[s] == k)) {
+                    const float inv = bh_rsqrt(r2);
+                    const float w = a.w * inv * inv * inv;
+                    ax += w * dx;
+                    ay += w * dy;
+                    az += w * dz;
+                    nacc++;
+                }
+                if (nacc >= 64) {
+                    sx += ax;
+                    sy += ay;
+                    sz += az;
+                    terms += nacc;
+                    ax = ay = az = 0.f;
+                    nacc = 0;
+                }
+                wait = sk;
+            }
+            if (__any_sync(FULL_MASK, active && !accept))
+                id = id + 1;
+            else
+                id = (int)__reduce_min_sync(FULL_MASK, (unsigned)wait);
+        }
+        if (have) {
+            terms += nacc;
+            const double gm = NBG_G * A.m[k] * mroot;
+            A.fx[k] = gm * (sx + ax);
+            A.fy[k] = gm * (sy + ay);
+            A.fz[k] = gm * (sz + az);
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) terms += __shfl_xor_sync(FULL_MASK, terms, o);
+    if ((threadIdx.x & 31) == 0 && terms) atomicAdd((unsigned long long *)&ctl->acc_bh_terms, terms);
+}
+
 /* a sun sums every tree body directly (directForce, octree.go:310-325); one
  * CTA per sun, a fixed-order block reduction */
 __global__ void __launch_bounds__(BH_BLOCK) k_bh_sun(BodyArrays A, DevCtl *ctl)
@@ -714,6 +863,8 @@ int nbg_bh_alloc(BhTree &t, ll cap, ll node_cap)
     ALLOC(t.first, node_cap);
     ALLOC(t.level, node_cap);
     ALLOC(t.flags, node_cap);
+    ALLOC(t.fa, node_cap);
+    ALLOC(t.fb, node_cap);
 #undef ALLOC
     if (!ok) {
         nbg_bh_free(t);
@@ -727,14 +878,15 @@ void nbg_bh_free(BhTree &t)
 {
     void *ps[] = {t.key[0], t.key[1], t.val[0], t.val[1], t.hist, t.base, t.blk, t.mass, t.mx, t.my,
                   t.mz, t.cmx, t.cmy, t.cmz, t.cx, t.cy, t.cz, t.half, t.skip, t.start,
-                  t.end, t.first, t.level, t.flags};
+                  t.end, t.first, t.level, t.flags, t.fa, t.fb};
     for (void *p : ps) cudaFree(p);
     memset(&t, 0, sizeof t);
 }
 
 /* The force and collision pass of one cycle (the replacement of the pair
- * kernel): bounds, keys, sort, nodes, masses, forces, suns, collisions. */
-void nbg_launch_bh(const CycleBufs &cb, DevCtl *ctl, cudaStream_t st)
+ * kernel): bounds, keys, sort, nodes, masses, forces (FP64, or the mixed
+ * walk), suns, collisions. */
+void nbg_launch_bh(const CycleBufs &cb, DevCtl *ctl, cudaStream_t st, bool mixed)
 {
     const BhTree &t = cb.t;
     const ll cap = cb.cap;
@@ -762,7 +914,12 @@ void nbg_launch_bh(const CycleBufs &cb, DevCtl *ctl, cudaStream_t st)
     if (ng > 152 * 8) ng = 152 * 8;
     for (int level = BH_LEVELS; level >= 0; level--)
         k_bh_mass<<<ng, BH_BLOCK, 0, st>>>(cb.a, ctl, t.val[0], t, level);
-    k_bh_force<<<g, BH_BLOCK, 0, st>>>(cb.a, ctl, t.val[0], t);
+    if (mixed) {
+        k_bh_prep_mixed<<<ng, BH_BLOCK, 0, st>>>(ctl, t);
+        k_bh_force_mixed<<<g, BH_BLOCK, 0, st>>>(cb.a, ctl, t.val[0], t);
+    } else {
+        k_bh_force<<<g, BH_BLOCK, 0, st>>>(cb.a, ctl, t.val[0], t);
+    }
     k_bh_sun<<<64, BH_BLOCK, 0, st>>>(cb.a, ctl);
     k_bh_collide<<<g, BH_BLOCK, 0, st>>>(cb.a, ctl, t.val[0], t, cb.ev_keys, cb.ev_cap);
 }

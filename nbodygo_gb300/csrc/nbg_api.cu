@@ -834,7 +834,7 @@ static void launch_cycle(nbg_ctx *ctx, int precision, long ev_base)
     nbg_launch_frag_count(cb, ctx->ctl, st);
     if (cb.bh) {
         if (ev_base >= 0) cudaEventRecord(get_event(ctx, (size_t)ev_base + 1), st);
-        nbg_launch_bh(cb, ctx->ctl, st);
+        nbg_launch_bh(cb, ctx->ctl, st, precision == NBG_PRECISION_MIXED);
         if (ev_base >= 0) cudaEventRecord(get_event(ctx, (size_t)ev_base + 2), st);
     } else if (precision == NBG_PRECISION_MIXED) {
         nbg_launch_mixed_prep(cb, ctx->ctl, st);
@@ -852,7 +852,8 @@ static void launch_cycle(nbg_ctx *ctx, int precision, long ev_base)
     /* begin, fragment count + scan, 10 after the pair kernel, and the pair
      * kernel; mixed adds reduce, 21 sort, pack, tile origins and the output;
      * Barnes-Hut replaces the pair kernel with 55 (k_bh.cu) */
-    ctx->launches_per_cycle = cb.bh ? 13 + 55 : precision == NBG_PRECISION_MIXED ? 39 : 14;
+    ctx->launches_per_cycle = cb.bh ? 13 + 55 + (precision == NBG_PRECISION_MIXED ? 1 : 0)
+                                    : precision == NBG_PRECISION_MIXED ? 39 : 14;
 }
 
 /* One CUDA graph of ctx->graph_cycles consecutive cycles. */
@@ -977,7 +978,7 @@ int nbg_force_pass(nbg_ctx *ctx)
         CK(cudaMemcpyAsync(&ctx->ctl->error, &z, sizeof z, cudaMemcpyHostToDevice, ctx->st));
         nbg_launch_begin(ctx->cb, ctx->ctl, ctx->st);
         if (ctx->cb.bh) {
-            nbg_launch_bh(ctx->cb, ctx->ctl, ctx->st);
+            nbg_launch_bh(ctx->cb, ctx->ctl, ctx->st, ctx->precision == NBG_PRECISION_MIXED);
         } else if (ctx->precision == NBG_PRECISION_MIXED) {
             nbg_launch_mixed_prep(ctx->cb, ctx->ctl, ctx->st);
             nbg_launch_mixed_pair(ctx->cb, ctx->ctl, ctx->st);

@@ -157,6 +157,7 @@ struct BhTree {
     ll *base;           /* nodes starting at each sorted position, then their scan */
     ll *blk;            /* per-block sums of that scan */
     double *mass, *mx, *my, *mz, *cmx, *cmy, *cmz, *cx, *cy, *cz, *half;
+    float4 *fa, *fb;    /* mixed walk: (cm hi xyz, mass / root mass), (cm lo xyz, opening r^2) */
     int *skip, *start, *end, *first;
     unsigned char *level, *flags;
     ll node_cap;
@@ -256,7 +257,7 @@ __device__ static inline void nbg_emit_event(DevCtl *ctl, ull *keys, ll cap, ll 
 /* k_bh.cu (compiled with --fmad=false) */
 int nbg_bh_alloc(BhTree &t, ll cap, ll node_cap);
 void nbg_bh_free(BhTree &t);
-void nbg_launch_bh(const CycleBufs &cb, DevCtl *ctl, cudaStream_t st);
+void nbg_launch_bh(const CycleBufs &cb, DevCtl *ctl, cudaStream_t st, bool mixed);
 
 /* k_cycle.cu (compiled with --fmad=false) */
 void nbg_launch_begin(const CycleBufs &cb, DevCtl *ctl, cudaStream_t st);

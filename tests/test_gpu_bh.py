@@ -127,3 +127,33 @@ def test_bh_needs_a_single_collection():
     with pytest.raises(NbgError) as e:
         sim.step(0.01, 1.0, 1)
     assert e.value.code == A.NBG_E_STATE
+
+
+@pytest.mark.parametrize("name,bodies", [
+    ("plummer", lambda: W.plummer(3000, seed=7)),
+    ("disk_with_sun", lambda: with_sun(W.disk(1500))),
+    ("uniform", lambda: W.uniform_ball(2000, R=200.0)),
+])
+def test_mixed_bh_walk_stays_close_to_the_fp64_tree(name, bodies):
+    """The mixed walk: FP32 terms on the same tree.  Its error against the
+    FP64 tree is far below the tree's own approximation (~1e-3); a body
+    whose opening test flips at theta may differ by that approximation."""
+    b = bodies()
+    sim, ora = bh_pair(b, precision="mixed")
+    g = np.stack(sim.force_pass(), 1)
+    e = np.stack(ora.forces(), 1)
+    rel = np.linalg.norm(g - e) / np.linalg.norm(e)
+    mag = np.linalg.norm(e, axis=1)
+    per = np.linalg.norm(g - e, axis=1)[mag > 0] / mag[mag > 0]
+    assert rel <= 1e-5, (name, rel)
+    assert np.median(per) <= 1e-6, name
+    assert np.max(per) <= 1e-2, name
+
+
+def test_mixed_bh_first_cycle_events_are_exact():
+    """Collisions come from the FP64 range query in both precisions."""
+    b = dense_cluster(400, seed=33)
+    sim, ora = bh_pair(b, precision="mixed")
+    sim.step(0.05, 0.9, 1)
+    ora.step(0.05, 0.9, 1)
+    assert_events_identical(sim.events(), ora.events(), "cycle 0")
