@@ -617,6 +617,7 @@ __global__ void __launch_bounds__(BH_BLOCK) k_bh_prep_mixed(DevCtl *ctl, BhTree 
         }
         t.fa[id] = a;
         t.fb[id] = b;
+        t.fc[id] = make_int4(t.skip[id], t.start[id], t.end[id], (int)t.flags[id]);
     }
 }
 
@@ -627,8 +628,8 @@ __device__ __forceinline__ float bh_rsqrt(float x)
     return y;
 }
 
-__global__ void __launch_bounds__(BH_BLOCK) k_bh_force_mixed(BodyArrays A, DevCtl *ctl, const unsigned *vals,
-                                                             BhTree t)
+__global__ void __launch_bounds__(BH_BLOCK, 3) k_bh_force_mixed(BodyArrays A, DevCtl *ctl, const unsigned *vals,
+                                                                BhTree t)
 {
     if (ctl->error) return;
     const ll M = ctl->bh_count;
@@ -662,15 +663,17 @@ __global__ void __launch_bounds__(BH_BLOCK) k_bh_force_mixed(BodyArrays A, DevCt
         int id = 0;
         if (!__any_sync(FULL_MASK, have)) continue;
         while (id < total) {
+            /* one round trip: the node's three records are independent loads */
             const float4 a = t.fa[id];
-            const int sk = t.skip[id];
+            const float4 b = t.fb[id];
+            const int4 c = t.fc[id];
+            const int sk = c.x;
             if (a.w == 0.f) {
                 /* nothing with mass below: no lane waits inside this subtree */
                 id = sk;
                 continue;
             }
-            const float4 b = t.fb[id];
-            const unsigned fl = t.flags[id];
+            const unsigned fl = (unsigned)c.w;
             const bool leaf = (fl & BH_F_LEAF) != 0;
             const bool active = id >= wait;
             const float dx = (a.x - xh) + (b.x - xl);
@@ -679,7 +682,7 @@ __global__ void __launch_bounds__(BH_BLOCK) k_bh_force_mixed(BodyArrays A, DevCt
             const float r2 = dx * dx + dy * dy + dz * dz + soft2;
             const bool accept = leaf || (!(fl & BH_F_NAN_CM) && r2 > b.w);
             if (active && accept) {
-                const int s = t.start[id], e = t.end[id];
+                const int s = c.y, e = c.z;
                 if (leaf && e - s > 1) {
                     for (int q = s; q < e; q++) {
                         const unsigned j = vals[q];
@@ -696,7 +699,7 @@ __global__ void __launch_bounds__(BH_BLOCK) k_bh_force_mixed(BodyArrays A, DevCt
                         az += w * ez;
                         nacc++;
                     }
-                } else if (!(leaf && vals[s] == k)) {
+                } else if (!(leaf && (ll)s == p)) { /* a one-body leaf holds sorted position s */
                     const float inv = bh_rsqrt(r2);
                     const float w = a.w * inv * inv * inv;
                     ax += w * dx;
@@ -865,6 +868,7 @@ int nbg_bh_alloc(BhTree &t, ll cap, ll node_cap)
     ALLOC(t.flags, node_cap);
     ALLOC(t.fa, node_cap);
     ALLOC(t.fb, node_cap);
+    ALLOC(t.fc, node_cap);
 #undef ALLOC
     if (!ok) {
         nbg_bh_free(t);
@@ -878,7 +882,7 @@ void nbg_bh_free(BhTree &t)
 {
     void *ps[] = {t.key[0], t.key[1], t.val[0], t.val[1], t.hist, t.base, t.blk, t.mass, t.mx, t.my,
                   t.mz, t.cmx, t.cmy, t.cmz, t.cx, t.cy, t.cz, t.half, t.skip, t.start,
-                  t.end, t.first, t.level, t.flags, t.fa, t.fb};
+                  t.end, t.first, t.level, t.flags, t.fa, t.fb, t.fc};
     for (void *p : ps) cudaFree(p);
     memset(&t, 0, sizeof t);
 }

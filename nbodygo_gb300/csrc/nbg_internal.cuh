@@ -158,6 +158,7 @@ struct BhTree {
     ll *blk;            /* per-block sums of that scan */
     double *mass, *mx, *my, *mz, *cmx, *cmy, *cmz, *cx, *cy, *cz, *half;
     float4 *fa, *fb;    /* mixed walk: (cm hi xyz, mass / root mass), (cm lo xyz, opening r^2) */
+    int4 *fc;           /* mixed walk: (skip, start, end, flags) */
     int *skip, *start, *end, *first;
     unsigned char *level, *flags;
     ll node_cap;
