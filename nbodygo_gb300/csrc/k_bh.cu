@@ -445,6 +445,7 @@ __global__ void __launch_bounds__(BH_BLOCK) k_bh_nodes(DevCtl *ctl, const ull *k
             t.cy[id] = cy;
             t.cz[id] = cz;
             t.half[id] = half;
+            t.fd[id] = make_float4((float)cx, (float)cy, (float)cz, (float)half);
             if (d < d1) {
                 const unsigned oct = (unsigned)(key >> (3 * (BH_LEVELS - 1 - d))) & 7u;
                 const double q = half / 2;
@@ -591,7 +592,7 @@ __global__ void __launch_bounds__(BH_BLOCK) k_bh_force(BodyArrays A, DevCtl *ctl
  * one node sequence together: a lane that accepts a node waits until the
  * warp leaves that node's subtree (its skip pointer), and the warp descends
  * when any lane opens, so every node load is a broadcast and no lane
- * diverges.  Each lane sums its terms in FP32 and folds them into FP64 every
+ * diverges.  A node with no mass below it is skipped by every lane.  Each lane sums its terms in FP32 and folds them into FP64 every
  * 64 terms. */
 __global__ void __launch_bounds__(BH_BLOCK) k_bh_prep_mixed(DevCtl *ctl, BhTree t)
 {
@@ -628,7 +629,32 @@ __device__ __forceinline__ float bh_rsqrt(float x)
     return y;
 }
 
-__global__ void __launch_bounds__(BH_BLOCK, 3) k_bh_force_mixed(BodyArrays A, DevCtl *ctl, const unsigned *vals,
+/* the terms of a leaf at the deepest level holding bodies [s, e) (rare; kept
+ * out of the walk's registers) */
+__device__ __noinline__ int bucket_terms(const BodyArrays &A, const unsigned *vals, int s, int e, unsigned k, float xh,
+                                         float yh, float zh, float xl, float yl, float zl, float soft2, double mroot,
+                                         float &ax, float &ay, float &az)
+{
+    int cnt = 0;
+    for (int q = s; q < e; q++) {
+        const unsigned j = vals[q];
+        const double mj = A.m[j];
+        if (j == k || mj == 0) continue;
+        const float ex = (float)(A.x[j] - (double)xh - (double)xl);
+        const float ey = (float)(A.y[j] - (double)yh - (double)yl);
+        const float ez = (float)(A.z[j] - (double)zh - (double)zl);
+        const float q2 = ex * ex + ey * ey + ez * ez + soft2;
+        const float inv = bh_rsqrt(q2);
+        const float w = (float)(mj / mroot) * inv * inv * inv;
+        ax += w * ex;
+        ay += w * ey;
+        az += w * ez;
+        cnt++;
+    }
+    return cnt;
+}
+
+__global__ void __launch_bounds__(BH_BLOCK, 4) k_bh_force_mixed(BodyArrays A, DevCtl *ctl, const unsigned *vals,
                                                                 BhTree t)
 {
     if (ctl->error) return;
@@ -660,48 +686,40 @@ __global__ void __launch_bounds__(BH_BLOCK, 3) k_bh_force_mixed(BodyArrays A, De
         float ax = 0.f, ay = 0.f, az = 0.f;
         double sx = 0, sy = 0, sz = 0;
         int nacc = 0;
-        int id = 0;
         if (!__any_sync(FULL_MASK, have)) continue;
+        /* The next node is the first child when any lane opens this one, and
+         * otherwise this node's skip pointer: every lane that waits at this
+         * node accepted an ancestor, whose subtree ends at or after this
+         * node's.  So the next address is known right after the vote, and its
+         * loads are in flight while the lanes add their terms. */
+        int id = 0;
+        float4 a = t.fa[0], b = t.fb[0];
+        int4 c = t.fc[0];
         while (id < total) {
-            /* one round trip: the node's three records are independent loads */
-            const float4 a = t.fa[id];
-            const float4 b = t.fb[id];
-            const int4 c = t.fc[id];
             const int sk = c.x;
-            if (a.w == 0.f) {
-                /* nothing with mass below: no lane waits inside this subtree */
-                id = sk;
-                continue;
-            }
             const unsigned fl = (unsigned)c.w;
             const bool leaf = (fl & BH_F_LEAF) != 0;
-            const bool active = id >= wait;
+            const bool live = a.w != 0.f; /* nothing with mass below: skipped by every lane */
+            const bool active = live && id >= wait;
             const float dx = (a.x - xh) + (b.x - xl);
             const float dy = (a.y - yh) + (b.y - yl);
             const float dz = (a.z - zh) + (b.z - zl);
             const float r2 = dx * dx + dy * dy + dz * dz + soft2;
             const bool accept = leaf || (!(fl & BH_F_NAN_CM) && r2 > b.w);
+            const int next = __any_sync(FULL_MASK, active && !accept) ? id + 1 : sk;
+            const int s = c.y, e = c.z;
+            const float mw = a.w;
+            if (next < total) {
+                a = t.fa[next];
+                b = t.fb[next];
+                c = t.fc[next];
+            }
             if (active && accept) {
-                const int s = c.y, e = c.z;
                 if (leaf && e - s > 1) {
-                    for (int q = s; q < e; q++) {
-                        const unsigned j = vals[q];
-                        const double mj = A.m[j];
-                        if (j == k || mj == 0) continue;
-                        const float ex = (float)(A.x[j] - (double)xh - (double)xl);
-                        const float ey = (float)(A.y[j] - (double)yh - (double)yl);
-                        const float ez = (float)(A.z[j] - (double)zh - (double)zl);
-                        const float q2 = ex * ex + ey * ey + ez * ez + soft2;
-                        const float inv = bh_rsqrt(q2);
-                        const float w = (float)(mj / mroot) * inv * inv * inv;
-                        ax += w * ex;
-                        ay += w * ey;
-                        az += w * ez;
-                        nacc++;
-                    }
+                    nacc += bucket_terms(A, vals, s, e, k, xh, yh, zh, xl, yl, zl, soft2, mroot, ax, ay, az);
                 } else if (!(leaf && (ll)s == p)) { /* a one-body leaf holds sorted position s */
                     const float inv = bh_rsqrt(r2);
-                    const float w = a.w * inv * inv * inv;
+                    const float w = mw * inv * inv * inv;
                     ax += w * dx;
                     ay += w * dy;
                     az += w * dz;
@@ -717,10 +735,7 @@ __global__ void __launch_bounds__(BH_BLOCK, 3) k_bh_force_mixed(BodyArrays A, De
                 }
                 wait = sk;
             }
-            if (__any_sync(FULL_MASK, active && !accept))
-                id = id + 1;
-            else
-                id = (int)__reduce_min_sync(FULL_MASK, (unsigned)wait);
+            id = next;
         }
         if (have) {
             terms += nacc;
@@ -734,37 +749,54 @@ __global__ void __launch_bounds__(BH_BLOCK, 3) k_bh_force_mixed(BodyArrays A, De
     if ((threadIdx.x & 31) == 0 && terms) atomicAdd((unsigned long long *)&ctl->acc_bh_terms, terms);
 }
 
-/* a sun sums every tree body directly (directForce, octree.go:310-325); one
- * CTA per sun, a fixed-order block reduction */
+/* a sun sums every tree body directly (directForce, octree.go:310-325): each
+ * CTA scans a run of bodies for suns, and sums every sun it finds with all
+ * its threads, in a fixed-order block reduction */
 __global__ void __launch_bounds__(BH_BLOCK) k_bh_sun(BodyArrays A, DevCtl *ctl)
 {
     __shared__ double red[3][BH_BLOCK];
+    __shared__ unsigned s_mask[BH_BLOCK / 32];
     if (ctl->error) return;
     const ll n = ctl->n;
-    for (ll k = blockIdx.x; k < n; k += gridDim.x) {
-        if ((A.flags[k] & (NBG_LIVE_MASK | NBG_F_IS_SUN)) != (NBG_F_EXISTS | NBG_F_IS_SUN) || !tree_body(A, k)) continue;
-        const double x = A.x[k], y = A.y[k], z = A.z[k];
-        const double gm = NBG_G * A.m[k];
-        double fx = 0, fy = 0, fz = 0;
-        for (ll j = threadIdx.x; j < n; j += blockDim.x) {
-            if (j == k || (A.flags[j] & NBG_LIVE_MASK) != NBG_F_EXISTS) continue;
-            bh_term(gm, A.m[j], A.x[j] - x, A.y[j] - y, A.z[j] - z, fx, fy, fz);
-        }
-        red[0][threadIdx.x] = fx;
-        red[1][threadIdx.x] = fy;
-        red[2][threadIdx.x] = fz;
+    for (ll base = (ll)blockIdx.x * BH_BLOCK; base < n; base += (ll)gridDim.x * BH_BLOCK) {
+        const ll mine = base + threadIdx.x;
+        const bool sun = mine < n &&
+                         (A.flags[mine] & (NBG_LIVE_MASK | NBG_F_IS_SUN)) == (NBG_F_EXISTS | NBG_F_IS_SUN) &&
+                         tree_body(A, mine);
+        const unsigned m = __ballot_sync(FULL_MASK, sun);
+        if ((threadIdx.x & 31) == 0) s_mask[threadIdx.x >> 5] = m;
         __syncthreads();
-        for (int s = BH_BLOCK / 2; s > 0; s >>= 1) {
-            if (threadIdx.x < s)
-                for (int c = 0; c < 3; c++) red[c][threadIdx.x] += red[c][threadIdx.x + s];
-            __syncthreads();
+        for (int w = 0; w < BH_BLOCK / 32; w++) {
+            unsigned bits = s_mask[w];
+            while (bits) {
+                const int lane = __ffs(bits) - 1;
+                bits &= bits - 1;
+                const ll k = base + w * 32 + lane;
+                const double x = A.x[k], y = A.y[k], z = A.z[k];
+                const double gm = NBG_G * A.m[k];
+                double fx = 0, fy = 0, fz = 0;
+                for (ll j = threadIdx.x; j < n; j += blockDim.x) {
+                    if (j == k || (A.flags[j] & NBG_LIVE_MASK) != NBG_F_EXISTS) continue;
+                    bh_term(gm, A.m[j], A.x[j] - x, A.y[j] - y, A.z[j] - z, fx, fy, fz);
+                }
+                red[0][threadIdx.x] = fx;
+                red[1][threadIdx.x] = fy;
+                red[2][threadIdx.x] = fz;
+                __syncthreads();
+                for (int st = BH_BLOCK / 2; st > 0; st >>= 1) {
+                    if (threadIdx.x < st)
+                        for (int q = 0; q < 3; q++) red[q][threadIdx.x] += red[q][threadIdx.x + st];
+                    __syncthreads();
+                }
+                if (threadIdx.x == 0) {
+                    A.fx[k] = red[0][0];
+                    A.fy[k] = red[1][0];
+                    A.fz[k] = red[2][0];
+                }
+                __syncthreads();
+            }
         }
-        if (threadIdx.x == 0) {
-            A.fx[k] = red[0][0];
-            A.fy[k] = red[1][0];
-            A.fz[k] = red[2][0];
-        }
-        __syncthreads();
+        __syncthreads(); /* s_mask is rewritten for the next run */
     }
 }
 
@@ -795,32 +827,37 @@ __global__ void __launch_bounds__(BH_BLOCK) k_bh_collide(BodyArrays A, DevCtl *c
     const double rmax = ord_dbl(ctl->bh_rmax);
     double cx0, cy0, cz0, half0;
     bh_root(ctl, cx0, cy0, cz0, half0);
-    const double slack = (fabs(cx0) + fabs(cy0) + fabs(cz0) + half0) * 0x1p-44;
+    /* every coordinate, centre and half in the tree is at most this large */
+    const float span = (float)((fabs(cx0) + fabs(cy0) + fabs(cz0) + 3 * half0) * (1.0 + 0x1p-20));
     for (ll p = (ll)blockIdx.x * blockDim.x + threadIdx.x; p < M; p += (ll)gridDim.x * blockDim.x) {
         const unsigned i = vals[p];
         const unsigned fi = A.flags[i];
         if (fi & NBG_F_COLLIDED) continue; /* Collided's guard (always clear here) */
         const double xi = A.x[i], yi = A.y[i], zi = A.z[i], ri = A.rad[i];
         const unsigned bi = NBG_BEHAVIOR(fi);
-        /* reach: r_i + r_max, widened so the cube test never drops a pair the
-         * exact test would keep (a body sits in its node's cube up to a few
-         * ulps of the coordinates, the cube distance is good to ~2^-50) */
-        const double R = (ri + rmax) * (1.0 + 0x1p-40) + slack;
-        if (!(R >= 0)) continue; /* a NaN radius collides with nothing */
-        const double R2 = R * R;
+        /* The cube test runs in FP32 and only prunes: a node is skipped when
+         * its cube lies farther than r_i + r_max plus a bound on every FP32
+         * rounding of the coordinates, centres, halves and the test itself
+         * (2^-18 of the tree's span); the pairs that remain get the exact
+         * FP64 test. */
+        const double Rd = ri + rmax;
+        if (!(Rd >= 0)) continue; /* a NaN radius collides with nothing */
+        const float R = (float)(Rd * (1.0 + 0x1p-20)) + span * 0x1p-18f;
+        const float R2 = R * R * (1.0f + 0x1p-18f);
+        const float xf = (float)xi, yf = (float)yi, zf = (float)zi;
         int id = 0;
         while (id < total) {
-            const double h = t.half[id];
-            const double ax = fmax(fabs(xi - t.cx[id]) - h, 0.0);
-            const double ay = fmax(fabs(yi - t.cy[id]) - h, 0.0);
-            const double az = fmax(fabs(zi - t.cz[id]) - h, 0.0);
+            const float4 q = t.fd[id];
+            const float ax = fmaxf(fabsf(xf - q.x) - q.w, 0.f);
+            const float ay = fmaxf(fabsf(yf - q.y) - q.w, 0.f);
+            const float az = fmaxf(fabsf(zf - q.z) - q.w, 0.f);
             if (ax * ax + ay * ay + az * az > R2) {
                 id = t.skip[id];
                 continue;
             }
             if (t.flags[id] & BH_F_LEAF) {
-                for (int q = t.start[id]; q < t.end[id]; q++) {
-                    const unsigned j = vals[q];
+                for (int qq = t.start[id]; qq < t.end[id]; qq++) {
+                    const unsigned j = vals[qq];
                     if (j != i) bh_test_pair(A, ctl, ev_keys, ev_cap, i, xi, yi, zi, ri, bi, j);
                 }
                 id = t.skip[id];
@@ -869,6 +906,7 @@ int nbg_bh_alloc(BhTree &t, ll cap, ll node_cap)
     ALLOC(t.fa, node_cap);
     ALLOC(t.fb, node_cap);
     ALLOC(t.fc, node_cap);
+    ALLOC(t.fd, node_cap);
 #undef ALLOC
     if (!ok) {
         nbg_bh_free(t);
@@ -882,7 +920,7 @@ void nbg_bh_free(BhTree &t)
 {
     void *ps[] = {t.key[0], t.key[1], t.val[0], t.val[1], t.hist, t.base, t.blk, t.mass, t.mx, t.my,
                   t.mz, t.cmx, t.cmy, t.cmz, t.cx, t.cy, t.cz, t.half, t.skip, t.start,
-                  t.end, t.first, t.level, t.flags, t.fa, t.fb, t.fc};
+                  t.end, t.first, t.level, t.flags, t.fa, t.fb, t.fc, t.fd};
     for (void *p : ps) cudaFree(p);
     memset(&t, 0, sizeof t);
 }

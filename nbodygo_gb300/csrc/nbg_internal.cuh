@@ -159,6 +159,7 @@ struct BhTree {
     double *mass, *mx, *my, *mz, *cmx, *cmy, *cmz, *cx, *cy, *cz, *half;
     float4 *fa, *fb;    /* mixed walk: (cm hi xyz, mass / root mass), (cm lo xyz, opening r^2) */
     int4 *fc;           /* mixed walk: (skip, start, end, flags) */
+    float4 *fd;         /* collision query: the node's cube (centre xyz, half) in FP32 */
     int *skip, *start, *end, *first;
     unsigned char *level, *flags;
     ll node_cap;
