@@ -43,6 +43,7 @@ OPT_NEAR_PPM = 5
 OPT_GRAPH_CYCLES = 6
 OPT_MIX_SHAPE = 7
 OPT_BARNES_HUT = 8
+OPT_BH_SHAPE = 9
 MIX_SHAPES = 11
 
 _pd = C.POINTER(C.c_double)

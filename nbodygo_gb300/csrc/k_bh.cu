@@ -654,7 +654,8 @@ __device__ __noinline__ int bucket_terms(const BodyArrays &A, const unsigned *va
     return cnt;
 }
 
-__global__ void __launch_bounds__(BH_BLOCK, 4) k_bh_force_mixed(BodyArrays A, DevCtl *ctl, const unsigned *vals,
+template <int MINB>
+__global__ void __launch_bounds__(BH_BLOCK, MINB) k_bh_force_mixed(BodyArrays A, DevCtl *ctl, const unsigned *vals,
                                                                 BhTree t)
 {
     if (ctl->error) return;
@@ -958,7 +959,13 @@ void nbg_launch_bh(const CycleBufs &cb, DevCtl *ctl, cudaStream_t st, bool mixed
         k_bh_mass<<<ng, BH_BLOCK, 0, st>>>(cb.a, ctl, t.val[0], t, level);
     if (mixed) {
         k_bh_prep_mixed<<<ng, BH_BLOCK, 0, st>>>(ctl, t);
-        k_bh_force_mixed<<<g, BH_BLOCK, 0, st>>>(cb.a, ctl, t.val[0], t);
+        /* CTAs per SM the walk's registers are capped for: the walk is bound
+         * by the latency of its node loads, so occupancy is what counts */
+        switch (cb.bh_shape) {
+        case 1: k_bh_force_mixed<5><<<g, BH_BLOCK, 0, st>>>(cb.a, ctl, t.val[0], t); break;
+        case 2: k_bh_force_mixed<6><<<g, BH_BLOCK, 0, st>>>(cb.a, ctl, t.val[0], t); break;
+        default: k_bh_force_mixed<4><<<g, BH_BLOCK, 0, st>>>(cb.a, ctl, t.val[0], t); break;
+        }
     } else {
         k_bh_force<<<g, BH_BLOCK, 0, st>>>(cb.a, ctl, t.val[0], t);
     }

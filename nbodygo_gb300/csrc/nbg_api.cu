@@ -1202,6 +1202,11 @@ int nbg_set_option(nbg_ctx *ctx, int key, int64_t value)
         return NBG_OK;
     case NBG_OPT_MIX_SHAPE:
         return select_variant(ctx, (int)value);
+    case NBG_OPT_BH_SHAPE:
+        if (value < 0 || value > 2) return fail(ctx, NBG_E_ARG, "Barnes-Hut walk shape must be 0..2");
+        ctx->cb.bh_shape = (int)value;
+        invalidate_graph(ctx);
+        return NBG_OK;
     case NBG_OPT_BARNES_HUT: {
         CK(cudaSetDevice(ctx->device));
         const int on = value != 0;

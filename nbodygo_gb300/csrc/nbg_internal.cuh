@@ -194,6 +194,7 @@ struct CycleBufs {
     int mix_variant;    /* shape of the mixed pair kernel (see nbg_mix_variant_info) */
     int itile;          /* i-bodies per work item of that shape */
     int bh;             /* forces from the Barnes-Hut octree */
+    int bh_shape;       /* register cap of the mixed walk: 0, 1, 2 = 4, 5, 6 CTAs per SM */
     BhTree t;
 };
 
