@@ -222,6 +222,30 @@ int nbg_force_pass(nbg_ctx *ctx);
  * before compaction; renderable.go:22-40). */
 int nbg_get_renderables(nbg_ctx *ctx, nbg_renderable *host, int64_t cap, int64_t *n);
 
+/* Header of one slot of a render ring. */
+typedef struct nbg_ring_slot {
+    int64_t cycle;   /* cycle whose renderables the slot holds (-1: none yet) */
+    int64_t count;   /* renderables of that cycle */
+    int64_t written; /* of them in the slot: min(count, slot capacity) */
+    int64_t pad;
+} nbg_ring_slot;
+
+/* Bytes of a render ring of `slots` slots of `slot_cap` renderables: the
+ * slots' headers, then each slot's renderables. */
+#define NBG_RING_BYTES(slots, slot_cap) \
+    ((int64_t)(slots) * (int64_t)sizeof(nbg_ring_slot) + \
+     (int64_t)(slots) * (int64_t)(slot_cap) * (int64_t)sizeof(nbg_renderable))
+
+/* Renderables written straight into host memory by every cycle's Update, the
+ * path of the reference's result queue (computation-runner.go:316-321,
+ * resultqueue.go:97-129) without a copy call.  `ring` (NBG_RING_BYTES of
+ * memory the caller owns) is pinned and mapped here; cycle c writes slot
+ * c mod slots: its renderables first, then the header's count and written,
+ * then its cycle, each after a system-wide fence, so a reader that sees a
+ * slot's cycle change finds the slot complete.  A reader must copy a slot
+ * out before `slots` more cycles overwrite it.  NULL detaches (and unpins). */
+int nbg_set_render_ring(nbg_ctx *ctx, void *ring, int64_t slot_cap, int slots);
+
 /* Events resolved by the last cycle, in resolution order.  Self-collisions
  * (b1 == b2), which the reference enqueues and then resolves as no-ops
  * (collisioncalc.go:89-92), are not reported. */
@@ -259,7 +283,7 @@ int nbg_energy(nbg_ctx *ctx, double *kinetic, double *potential, double momentum
  * Errors are reported through nbg_last_error(NULL).
  */
 #define NBG_NOALLOC_MAX_BODIES 65536
-#define NBG_NOALLOC_BYTES 9473280
+#define NBG_NOALLOC_BYTES 10521856
 int nbg_forces_mixed_noalloc(const double *x, const double *y, const double *z, const double *mass,
                              const double *radius, const uint32_t *flags, int64_t n, double *fx, double *fy,
                              double *fz, void *stream);

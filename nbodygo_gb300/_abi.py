@@ -117,6 +117,7 @@ class NbgTiming(C.Structure):
 RENDERABLE_DTYPE = np.dtype([("id", np.int64), ("x", np.float32), ("y", np.float32), ("z", np.float32),
                              ("flags", np.uint32), ("radius", np.float64)])
 EVENT_DTYPE = np.dtype([("id1", np.int64), ("id2", np.int64), ("type", np.int32), ("pad", np.int32)])
+RING_SLOT_DTYPE = np.dtype([("cycle", np.int64), ("count", np.int64), ("written", np.int64), ("pad", np.int64)])
 assert RENDERABLE_DTYPE.itemsize == C.sizeof(NbgRenderable)
 assert EVENT_DTYPE.itemsize == C.sizeof(NbgEvent)
 
@@ -178,6 +179,7 @@ def declare(lib):
         "nbg_force_pass": (C.c_int, [P]),
         "nbg_get_renderables": (C.c_int, [P, C.c_void_p, C.c_int64, _pi64]),
         "nbg_get_events": (C.c_int, [P, C.c_void_p, C.c_int64, _pi64]),
+        "nbg_set_render_ring": (C.c_int, [P, C.c_void_p, C.c_int64, C.c_int]),
         "nbg_get_forces": (C.c_int, [P, _pd, _pd, _pd, C.c_int64, _pi64]),
         "nbg_energy": (C.c_int, [P, _pd, _pd, _pd]),
         "nbg_enable_timing": (C.c_int, [P, C.c_int]),

@@ -66,6 +66,7 @@ class Simulation:
         if getattr(self, "ctx", None):
             self.lib.nbg_destroy(self.ctx)
             self.ctx = None
+        self._ring = None
 
     def __del__(self):
         try:
@@ -219,6 +220,22 @@ class Simulation:
         out = np.zeros(n.value, dtype=A.RENDERABLE_DTYPE)
         self._check(self.lib.nbg_get_renderables(self.ctx, out.ctypes.data_as(C.c_void_p), n.value, C.byref(n)))
         return out
+
+    def set_render_ring(self, slots, slot_cap):
+        """Attaches a render ring of `slots` slots of `slot_cap` renderables in
+        host memory owned here; returns (headers, renderables) numpy views:
+        headers[s] describes slot s, renderables[s, :written] its bodies."""
+        nbytes = slots * A.RING_SLOT_DTYPE.itemsize + slots * slot_cap * A.RENDERABLE_DTYPE.itemsize
+        buf = np.zeros(nbytes, dtype=np.uint8)
+        self._check(self.lib.nbg_set_render_ring(self.ctx, buf.ctypes.data_as(C.c_void_p), int(slot_cap), int(slots)))
+        self._ring = buf
+        head = buf[:slots * A.RING_SLOT_DTYPE.itemsize].view(A.RING_SLOT_DTYPE)
+        rend = buf[slots * A.RING_SLOT_DTYPE.itemsize:].view(A.RENDERABLE_DTYPE).reshape(slots, slot_cap)
+        return head, rend
+
+    def clear_render_ring(self):
+        self._check(self.lib.nbg_set_render_ring(self.ctx, None, 0, 0))
+        self._ring = None
 
     def events(self):
         n = C.c_int64()

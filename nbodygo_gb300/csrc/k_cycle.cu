@@ -748,12 +748,15 @@ __global__ void __launch_bounds__(RESOLVE_BLOCK) k_resolve(BodyArrays A, DevCtl 
 /* K6: integration (Update, body.go:114-139) + renderables                 */
 /* ------------------------------------------------------------------------ */
 
-__global__ void k_integrate(BodyArrays A, DevCtl *ctl, nbg_renderable *rend)
+__global__ void k_integrate(BodyArrays A, DevCtl *ctl, nbg_renderable *rend, nbg_renderable *ring_rend, ll ring_cap,
+                            int ring_slots)
 {
     if (ctl->error) return;
     const ll n = ctl->n;
     const double dt = ctl->dt, R = ctl->R;
     ll nan_local = 0;
+    /* this cycle's slot of the render ring, if one is attached */
+    nbg_renderable *ring = ring_rend ? ring_rend + (ll)(ctl->cycle % (ull)ring_slots) * ring_cap : nullptr;
     for (ll k = (ll)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (ll)gridDim.x * blockDim.x) {
         unsigned f = A.flags[k];
         nbg_renderable r;
@@ -763,6 +766,7 @@ __global__ void k_integrate(BodyArrays A, DevCtl *ctl, nbg_renderable *rend)
             r.flags = 0;
             r.radius = 0.0;
             rend[k] = r;
+            if (ring && k < ring_cap) ring[k] = r;
             continue;
         }
         double vx = A.vx[k], vy = A.vy[k], vz = A.vz[k];
@@ -799,8 +803,26 @@ __global__ void k_integrate(BodyArrays A, DevCtl *ctl, nbg_renderable *rend)
             r.radius = 0.0;
         }
         rend[k] = r;
+        if (ring && k < ring_cap) ring[k] = r;
     }
+    if (ring) __threadfence_system(); /* the slot's renderables before its header */
     if (nan_local) atomicAdd((unsigned long long *)&ctl->acc_nan, (ull)nan_local);
+}
+
+/* the header of this cycle's ring slot, after its renderables: count and
+ * written, a system-wide fence, then the cycle */
+__global__ void k_ring_header(DevCtl *ctl, nbg_ring_slot *head, ll ring_cap, int ring_slots)
+{
+    if (ctl->error) return;
+    const ull cycle = ctl->cycle;
+    const ll n = ctl->n;
+    volatile nbg_ring_slot *h = head + cycle % (ull)ring_slots;
+    __threadfence_system();
+    h->count = n;
+    h->written = n < ring_cap ? n : ring_cap;
+    __threadfence_system();
+    h->cycle = (ll)cycle;
+    __threadfence_system();
 }
 
 /* ------------------------------------------------------------------------ */
@@ -1076,7 +1098,8 @@ void nbg_launch_after_pair(const CycleBufs &cb, DevCtl *ctl, cudaStream_t st)
     k_frag_emit<<<sg, NBG_SCAN_BLOCK, 0, st>>>(cb.a, cb.frags, ctl, cb.blk_off);
     /* the radix-sort key buffer is free after the pair pass: per-body owner words */
     k_resolve<<<cb.seg.nsims, RESOLVE_BLOCK, 0, st>>>(cb.a, ctl, cb.seg, cb.ev_keys, cb.ev_out, cb.skey[1]);
-    k_integrate<<<flat_grid(cb.cap), 256, 0, st>>>(cb.a, ctl, cb.rend);
+    k_integrate<<<flat_grid(cb.cap), 256, 0, st>>>(cb.a, ctl, cb.rend, cb.ring_rend, cb.ring_cap, cb.ring_slots);
+    if (cb.ring_head) k_ring_header<<<1, 1, 0, st>>>(ctl, cb.ring_head, cb.ring_cap, cb.ring_slots);
     k_keep_blocksum<<<sg, NBG_SCAN_BLOCK, 0, st>>>(cb.a, ctl, cb.seg, cb.blk_sum);
     k_scan_blocks<<<1, NBG_SCAN_BLOCK, 0, st>>>(ctl, cb.seg, cb.blk_sum, cb.blk_off, 1, cb.cap, cb.frag_cap);
     k_compact<<<sg, NBG_SCAN_BLOCK, 0, st>>>(cb.a, cb.b, ctl, cb.seg, cb.blk_off);

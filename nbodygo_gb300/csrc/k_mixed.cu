@@ -270,6 +270,27 @@ __device__ __forceinline__ void i_body_setup(const float4 *__restrict__ jhi, con
     t = __double2float_ru(b * b);
 }
 
+/* every i-body's re-centred position and near-pair threshold, once per
+ * cycle; the pair kernel reads them for each chunk that covers the body */
+__global__ void k_mix_iprep(DevCtl *ctl, SimSegs seg, const float4 *__restrict__ jhi,
+                            const float4 *__restrict__ jlo, const float4 *__restrict__ tile_c, float4 *iprep,
+                            int itile)
+{
+    if (ctl->error) return;
+    const ll n = ctl->n;
+    const float rmax = __uint_as_float(ctl->rmax_bits);
+    const float xmax = __uint_as_float(ctl->xmax_bits);
+    const double kappa = (double)ctl->near_kappa;
+    for (ll p = (ll)blockIdx.x * blockDim.x + threadIdx.x; p < n; p += (ll)gridDim.x * blockDim.x) {
+        const int sim = nbg_sim_of(seg.off, seg.nsims, p);
+        const ll s0 = seg.off[sim];
+        const float4 c = tile_c[seg.mtile_off[sim] + (p - s0) / itile];
+        float xr, yr, zr, t;
+        i_body_setup(jhi, jlo, p, seg.off[sim + 1], c, rmax, xmax, kappa, xr, yr, zr, t);
+        iprep[p] = make_float4(xr, yr, zr, t);
+    }
+}
+
 /* One j of a near-pair pass for i-body p (raw i: hi_i, lo_i; re-centred
  * i: xi..zi; threshold thk): adds the FP32 term to (tx, ty, tz), or, for a
  * near pair, the term from the exact hi/lo difference, or, for a possible
@@ -319,8 +340,8 @@ __device__ __forceinline__ void near_pass_j(const BodyArrays &A, DevCtl *ctl, ul
 template <int BLOCK, int K, int JT, int UNROLL, int MINB, bool SF>
 __global__ void __launch_bounds__(BLOCK, MINB)
 k_pair_mixed(BodyArrays A, DevCtl *ctl, SimSegs seg, const float4 *__restrict__ jhi, const float4 *__restrict__ jlo,
-             const float4 *__restrict__ tile_c, const unsigned *__restrict__ perm, double *__restrict__ part,
-             ull *ev_keys, ll ev_cap)
+             const float4 *__restrict__ tile_c, const float4 *__restrict__ iprep, const unsigned *__restrict__ perm,
+             double *__restrict__ part, ull *ev_keys, ll ev_cap)
 {
     constexpr int JP = JT / 2; /* j pairs per tile */
     constexpr int ITILE = BLOCK * K;
@@ -372,8 +393,14 @@ k_pair_mixed(BodyArrays A, DevCtl *ctl, SimSegs seg, const float4 *__restrict__ 
 #pragma unroll
         for (int k = 0; k < K; k++) {
             const ll p = ibase + (ll)k * BLOCK + tid;
-            float xr, yr, zr, t;
-            i_body_setup(jhi, jlo, p, n, c, rmax, xmax, kappa, xr, yr, zr, t);
+            float xr = 0.f, yr = 0.f, zr = 0.f, t = -1.f;
+            if (p < n) {
+                const float4 v = iprep[p];
+                xr = v.x;
+                yr = v.y;
+                zr = v.z;
+                t = v.w;
+            }
             nx[k] = make_float2(-xr, -xr);
             ny[k] = make_float2(-yr, -yr);
             nz[k] = make_float2(-zr, -zr);
@@ -609,6 +636,7 @@ void nbg_launch_mixed_prep(const CycleBufs &cb, DevCtl *ctl, cudaStream_t st)
     ll tiles = (cb.cap + itile - 1) / itile + cb.seg.nsims;
     if (tiles > 152 * 64) tiles = 152 * 64;
     k_mix_tiles<<<(int)tiles, TILES_BLOCK, 0, st>>>(ctl, cb.seg, cb.jhi, cb.jlo, cb.tile_c, itile);
+    k_mix_iprep<<<fg, 256, 0, st>>>(ctl, cb.seg, cb.jhi, cb.jlo, cb.tile_c, cb.iprep, itile);
 }
 
 void nbg_launch_mixed_pair(const CycleBufs &cb, DevCtl *ctl, cudaStream_t st)
@@ -617,7 +645,8 @@ void nbg_launch_mixed_pair(const CycleBufs &cb, DevCtl *ctl, cudaStream_t st)
 #define X(id, kind, b, k, jt, u, mb)                                                                       \
     case id:                                                                                           \
         MIX_KERNEL(kind, b, k, jt, u, mb)<<<cb.slots, b, 0, st>>>(cb.a, ctl, cb.seg, cb.jhi, cb.jlo, cb.tile_c, \
-                                                                  cb.perm, cb.part, cb.ev_keys, cb.ev_cap);   \
+                                                                  cb.iprep, cb.perm, cb.part, cb.ev_keys,   \
+                                                                  cb.ev_cap);                                \
         break;
         MIX_VARIANTS(X)
 #undef X

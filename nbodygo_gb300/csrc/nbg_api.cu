@@ -46,6 +46,7 @@ struct nbg_ctx {
     size_t scratch_bytes = 0;
     ll launches_per_cycle = 0;
     ll bh_cap = 0; /* capacity the Barnes-Hut buffers were sized for */
+    void *ring_host = nullptr; /* the caller's render ring, registered here */
     void *seg_mem = nullptr; /* SimSegs arrays */
     int seg_cap = 0;         /* sims the allocation holds */
 };
@@ -239,6 +240,7 @@ static int ensure_cap(nbg_ctx *ctx, ll need, ll keep)
     /* every sim may end in a partial tile: at most cap / itile + nsims tiles */
     ll tiles = (cap + NBG_MIX_MIN_ITILE - 1) / NBG_MIX_MIN_ITILE + NBG_MAX_SIMS + 1;
     CK(cudaMalloc((void **)&ctx->cb.tile_c, (size_t)tiles * sizeof(float4)));
+    CK(cudaMalloc((void **)&ctx->cb.iprep, (size_t)cap * sizeof(float4)));
     ctx->cb.part_doubles = part_need(ctx, cap);
     CK(cudaMalloc((void **)&ctx->cb.part, (size_t)ctx->cb.part_doubles * sizeof(double)));
     CK(cudaMalloc((void **)&ctx->cb.perm, (size_t)cap * sizeof(unsigned)));
@@ -285,6 +287,7 @@ static void free_cap_buffers(CycleBufs &cb)
     cudaFree(cb.jhi);
     cudaFree(cb.jlo);
     cudaFree(cb.tile_c);
+    cudaFree(cb.iprep);
     cudaFree(cb.part);
     cudaFree(cb.perm);
     cudaFree(cb.sval);
@@ -509,6 +512,7 @@ void nbg_destroy(nbg_ctx *ctx)
     cudaFree(ctx->cb.ev_out);
     free_cap_buffers(ctx->cb);
     nbg_bh_free(ctx->cb.t);
+    if (ctx->ring_host) cudaHostUnregister(ctx->ring_host);
     cudaFree(ctx->seg_mem);
     cudaFree(ctx->scratch);
     cudaFree(ctx->ctl);
@@ -850,10 +854,12 @@ static void launch_cycle(nbg_ctx *ctx, int precision, long ev_base)
     nbg_launch_after_pair(cb, ctx->ctl, st);
     if (ev_base >= 0) cudaEventRecord(get_event(ctx, (size_t)ev_base + 3), st);
     /* begin, fragment count + scan, 10 after the pair kernel, and the pair
-     * kernel; mixed adds reduce, 21 sort, pack, tile origins and the output;
+     * kernel; mixed adds reduce, 21 sort, pack, tile origins, i-body set-up
+     * and the output;
      * Barnes-Hut replaces the pair kernel with 55 (k_bh.cu) */
-    ctx->launches_per_cycle = cb.bh ? 13 + 55 + (precision == NBG_PRECISION_MIXED ? 1 : 0)
-                                    : precision == NBG_PRECISION_MIXED ? 39 : 14;
+    ctx->launches_per_cycle = (cb.bh ? 13 + 55 + (precision == NBG_PRECISION_MIXED ? 1 : 0)
+                                     : precision == NBG_PRECISION_MIXED ? 40 : 14) +
+                              (cb.ring_head ? 1 : 0);
 }
 
 /* One CUDA graph of ctx->graph_cycles consecutive cycles. */
@@ -1111,6 +1117,41 @@ int nbg_get_renderables(nbg_ctx *ctx, nbg_renderable *host, int64_t cap, int64_t
         if ((rc = get_field(ctx, host, ctx->cb.rend, m < cap ? m : cap)) != NBG_OK) return rc;
         CK(cudaStreamSynchronize(ctx->st));
     }
+    return NBG_OK;
+}
+
+int nbg_set_render_ring(nbg_ctx *ctx, void *ring, int64_t slot_cap, int slots)
+{
+    if (!ctx) return NBG_E_ARG;
+    if (ring && (slot_cap < 1 || slots < 1)) return fail(ctx, NBG_E_ARG, "ring needs slot_cap >= 1 and slots >= 1");
+    CK(cudaSetDevice(ctx->device));
+    CK(cudaStreamSynchronize(ctx->st)); /* no cycle in flight writes the old ring */
+    if (ctx->ring_host) {
+        cudaHostUnregister(ctx->ring_host);
+        ctx->ring_host = nullptr;
+    }
+    ctx->cb.ring_head = nullptr;
+    ctx->cb.ring_rend = nullptr;
+    ctx->cb.ring_cap = 0;
+    ctx->cb.ring_slots = 0;
+    invalidate_graph(ctx);
+    if (!ring) return NBG_OK;
+    nbg_ring_slot *h = (nbg_ring_slot *)ring;
+    for (int s = 0; s < slots; s++) h[s] = nbg_ring_slot{-1, 0, 0, 0};
+    const size_t bytes = (size_t)NBG_RING_BYTES(slots, slot_cap);
+    cudaError_t e = cudaHostRegister(ring, bytes, cudaHostRegisterMapped);
+    if (e != cudaSuccess) return fail(ctx, NBG_E_CUDA, std::string("cudaHostRegister: ") + cudaGetErrorString(e));
+    void *dev = nullptr;
+    e = cudaHostGetDevicePointer(&dev, ring, 0);
+    if (e != cudaSuccess) {
+        cudaHostUnregister(ring);
+        return fail(ctx, NBG_E_CUDA, std::string("cudaHostGetDevicePointer: ") + cudaGetErrorString(e));
+    }
+    ctx->ring_host = ring;
+    ctx->cb.ring_head = (nbg_ring_slot *)dev;
+    ctx->cb.ring_rend = (nbg_renderable *)((char *)dev + (size_t)slots * sizeof(nbg_ring_slot));
+    ctx->cb.ring_cap = slot_cap;
+    ctx->cb.ring_slots = slots;
     return NBG_OK;
 }
 

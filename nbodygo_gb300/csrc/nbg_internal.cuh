@@ -183,6 +183,7 @@ struct CycleBufs {
     /* mixed form (indexed by sorted position) */
     float4 *jhi, *jlo;
     float4 *tile_c;
+    float4 *iprep;      /* per sorted position: re-centred x, y, z and near-pair threshold */
     double *part;
     unsigned *perm;     /* sorted position -> body index */
     unsigned *skey[2];  /* radix-sort keys (ping-pong) */
@@ -193,6 +194,11 @@ struct CycleBufs {
     int slots;          /* resident CTAs of the mixed kernel on this device */
     int mix_variant;    /* shape of the mixed pair kernel (see nbg_mix_variant_info) */
     int itile;          /* i-bodies per work item of that shape */
+    /* render ring in mapped host memory (device addresses; NULL: none) */
+    nbg_ring_slot *ring_head;
+    nbg_renderable *ring_rend;
+    ll ring_cap;
+    int ring_slots;
     int bh;             /* forces from the Barnes-Hut octree */
     int bh_shape;       /* register cap of the mixed walk: 0, 1, 2 = 4, 5, 6 CTAs per SM */
     BhTree t;

@@ -32,8 +32,9 @@ static constexpr size_t OFF_CTL = 0;
 static constexpr size_t OFF_JHI = align256(sizeof(DevCtl));
 static constexpr size_t OFF_JLO = OFF_JHI + align256((size_t)NBG_NOALLOC_MAX_BODIES * 16);
 static constexpr size_t OFF_TILE = OFF_JLO + align256((size_t)NBG_NOALLOC_MAX_BODIES * 16);
-static constexpr size_t OFF_PART =
+static constexpr size_t OFF_IPREP =
     OFF_TILE + align256((size_t)((NBG_NOALLOC_MAX_BODIES + NBG_MIX_ITILE - 1) / NBG_MIX_ITILE) * 16);
+static constexpr size_t OFF_PART = OFF_IPREP + align256((size_t)NBG_NOALLOC_MAX_BODIES * 16);
 static constexpr size_t OFF_PERM = OFF_PART + align256((size_t)NOALLOC_PART_DOUBLES * 8);
 static constexpr size_t OFF_SVAL = OFF_PERM + align256((size_t)NBG_NOALLOC_MAX_BODIES * 4);
 static constexpr size_t OFF_KEY0 = OFF_SVAL + align256((size_t)NBG_NOALLOC_MAX_BODIES * 4);
@@ -115,6 +116,7 @@ extern "C" int nbg_forces_mixed_noalloc(const double *x, const double *y, const 
     cb.jhi = (float4 *)(base + OFF_JHI);
     cb.jlo = (float4 *)(base + OFF_JLO);
     cb.tile_c = (float4 *)(base + OFF_TILE);
+    cb.iprep = (float4 *)(base + OFF_IPREP);
     cb.part = (double *)(base + OFF_PART);
     cb.perm = (unsigned *)(base + OFF_PERM);
     cb.sval = (unsigned *)(base + OFF_SVAL);
