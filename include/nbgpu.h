@@ -318,9 +318,10 @@ int nbg_get_timing(nbg_ctx *ctx, nbg_timing *t);
 #define NBG_OPT_BARNES_HUT 8
 /* mixed Barnes-Hut walk: registers capped for 4, 5 or 6 CTAs per SM (0..2) */
 #define NBG_OPT_BH_SHAPE 9
-#define NBG_OPT_NEAR_PPM 5   /* mixed: pairs closer than (value * 1e-6) x the i-tile's
-                                extent around its origin are computed in FP64
-                                (default 70000) */
+#define NBG_OPT_NEAR_PPM 5   /* mixed: pairs closer than (value * 1e-6) x the i-body's
+                                distance from its tile origin take the near-pair
+                                pass: the exact hi/lo difference, FP64 for a
+                                possible overlap (default 70000) */
 int nbg_set_option(nbg_ctx *ctx, int key, int64_t value);
 
 /* Autotuner of the mixed pair kernel.  Seven shapes are compiled (threads per
