@@ -98,16 +98,19 @@ def dist_env():
 
 
 class Dist:
-    """Barrier / max / sum over ranks (torch.distributed) when WORLD_SIZE > 1."""
+    """Barrier / max / sum over ranks (torch.distributed) when WORLD_SIZE > 1:
+    NCCL between GPUs, gloo when asked (the CPU tests of the replica path)."""
 
-    def __init__(self, ws, local):
+    def __init__(self, ws, local, backend="nccl"):
         self.ws = ws
+        self.backend = backend
         if ws > 1:
             import torch
             import torch.distributed as td
 
-            torch.cuda.set_device(local)
-            td.init_process_group("nccl")
+            if backend == "nccl":
+                torch.cuda.set_device(local)
+            td.init_process_group(backend)
             self.td, self.torch = td, torch
 
     def barrier(self):
@@ -117,7 +120,8 @@ class Dist:
     def _reduce(self, v, op):
         if self.ws == 1:
             return v
-        t = self.torch.tensor([float(v)], device="cuda")
+        dev = "cuda" if self.backend == "nccl" else "cpu"
+        t = self.torch.tensor([float(v)], dtype=self.torch.float64, device=dev)
         self.td.all_reduce(t, op=op)
         return float(t.item())
 
@@ -130,6 +134,14 @@ class Dist:
     def close(self):
         if self.ws > 1:
             self.td.destroy_process_group()
+
+
+def aggregate(dist, interactions, t_ms):
+    """Whole-job rate of N replicas: the work of all ranks over the slowest
+    rank's time.  Returns (value per second, slowest ms, total work)."""
+    t_max = dist.max(t_ms)
+    work = dist.sum(interactions)
+    return work / (t_max * 1e-3), t_max, work
 
 
 class Clocks:
@@ -379,9 +391,7 @@ def main():
     clk = clocks.stop()
     per_chunk = [a.elapsed_time(b) for a, b in ev]
     t_ms = sum(per_chunk)
-    t_max = dist.max(t_ms)
-    work = dist.sum(interactions)
-    value = work / (t_max * 1e-3)
+    value, t_max, work = aggregate(dist, interactions, t_ms)
 
     # ---- pair-kernel time (library timing mode, same stream) ----
     sim.enable_timing(True)
