@@ -17,6 +17,7 @@
  */
 #include <cstdio>
 #include <cstdlib>
+#include <algorithm>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -49,12 +50,19 @@ struct nbg_ctx {
     void *ring_host = nullptr; /* the caller's render ring, registered here */
     void *seg_mem = nullptr; /* SimSegs arrays */
     int seg_cap = 0;         /* sims the allocation holds */
+    ll *seg_h = nullptr;     /* pinned staging of the segment offsets */
+    unsigned *flags_h = nullptr; /* pinned staging for the packed flag words */
+    ll flags_cap = 0;
 };
 
 /* (Re)allocates the per-sim arrays for nsims sims and uploads the offsets of
- * the given counts (host array, nsims entries). */
-static int set_segments(nbg_ctx *ctx, int nsims, const ll *counts)
+ * the given counts (host array, nsims entries), stream-ordered through a
+ * pinned staging array (whose previous copy the caller has synchronised).
+ * *reshaped tells whether the arrays moved or the sim count changed: the
+ * kernels of a captured graph carry both. */
+static int set_segments(nbg_ctx *ctx, int nsims, const ll *counts, bool *reshaped)
 {
+    *reshaped = nsims != ctx->cb.seg.nsims;
     if (nsims > ctx->seg_cap) {
         cudaFree(ctx->seg_mem);
         ctx->seg_mem = nullptr;
@@ -64,14 +72,22 @@ static int set_segments(nbg_ctx *ctx, int nsims, const ll *counts)
             return NBG_E_CUDA;
         }
         ctx->seg_cap = nsims;
+        *reshaped = true;
+    }
+    if (!ctx->seg_h) {
+        cudaError_t e = cudaMallocHost((void **)&ctx->seg_h, (size_t)(NBG_MAX_SIMS + 1) * sizeof(ll));
+        if (e != cudaSuccess) {
+            ctx->err = std::string("segment staging: ") + cudaGetErrorString(e);
+            return NBG_E_CUDA;
+        }
     }
     ctx->cb.seg = nbg_seg_carve(ctx->seg_mem, nsims);
-    std::vector<ll> h((size_t)nsims + 1, 0);
-    for (int s = 0; s < nsims; s++) h[(size_t)s + 1] = h[(size_t)s] + counts[s];
+    ll *h = ctx->seg_h;
+    h[0] = 0;
+    for (int s = 0; s < nsims; s++) h[s + 1] = h[s] + counts[s];
     cudaError_t e = cudaMemsetAsync(ctx->seg_mem, 0, NBG_SEG_BYTES(nsims), ctx->st);
     if (e == cudaSuccess)
-        e = cudaMemcpyAsync(ctx->cb.seg.off, h.data(), h.size() * sizeof(ll), cudaMemcpyHostToDevice, ctx->st);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->st);
+        e = cudaMemcpyAsync(ctx->cb.seg.off, h, (size_t)(nsims + 1) * sizeof(ll), cudaMemcpyHostToDevice, ctx->st);
     if (e != cudaSuccess) {
         ctx->err = std::string("segment upload: ") + cudaGetErrorString(e);
         return NBG_E_CUDA;
@@ -112,6 +128,13 @@ static int fail(nbg_ctx *ctx, int code, const std::string &m)
 }
 
 /* ---- small utility kernels --------------------------------------------- */
+
+/* the body count of a freshly loaded collection (stream-ordered, no sync) */
+__global__ void k_set_loaded(DevCtl *ctl, ll n)
+{
+    ctl->n = n;
+    ctl->n_host_adds = 0;
+}
 
 __global__ void k_fill_f64(double *p, ll n, double v)
 {
@@ -377,6 +400,20 @@ static int get_field(nbg_ctx *ctx, T *dst, const T *src, ll n)
     return NBG_OK;
 }
 
+/* pinned host staging of at least n flag words (the previous copy out of it
+ * must be complete: every user syncs the stream before reuse) */
+static int ensure_flags_h(nbg_ctx *ctx, ll n)
+{
+    if (n <= ctx->flags_cap) return NBG_OK;
+    CK(cudaStreamSynchronize(ctx->st));
+    if (ctx->flags_h) cudaFreeHost(ctx->flags_h);
+    ctx->flags_h = nullptr;
+    ctx->flags_cap = 0;
+    CK(cudaMallocHost((void **)&ctx->flags_h, (size_t)n * sizeof(unsigned)));
+    ctx->flags_cap = n;
+    return NBG_OK;
+}
+
 /* Uploads n bodies from a host SoA into D at offset `off`; NULL optional
  * fields get NewBody defaults. */
 static int upload_soa(nbg_ctx *ctx, BodyArrays &D, ll off, const nbg_soa *h, ll n)
@@ -384,12 +421,15 @@ static int upload_soa(nbg_ctx *ctx, BodyArrays &D, ll off, const nbg_soa *h, ll 
     if (n <= 0) return NBG_OK;
     if (!h->x || !h->y || !h->z || !h->vx || !h->vy || !h->vz || !h->radius || !h->mass)
         return fail(ctx, NBG_E_ARG, "x, y, z, vx, vy, vz, radius and mass are required");
-    std::vector<unsigned> flags((size_t)n);
+    int rc0 = ensure_flags_h(ctx, n);
+    if (rc0 != NBG_OK) return rc0;
+    CK(cudaStreamSynchronize(ctx->st)); /* the staging's last copy is done */
+    unsigned *flags = ctx->flags_h;
     for (ll k = 0; k < n; k++) {
         int32_t c = h->collision ? h->collision[k] : NBG_ELASTIC;
         if (c < NBG_NONE || c > NBG_FRAGMENT) return fail(ctx, NBG_E_ARG, "collision behaviour out of range");
         uint32_t f = h->flags ? h->flags[k] : NBG_F_EXISTS;
-        flags[(size_t)k] = (f & 0xffu) | ((unsigned)c << NBG_BEHAVIOR_SHIFT);
+        flags[k] = (f & 0xffu) | ((unsigned)c << NBG_BEHAVIOR_SHIFT);
     }
     int rc;
 #define PUTD(fld, src)                                                                      \
@@ -427,10 +467,8 @@ static int upload_soa(nbg_ctx *ctx, BodyArrays &D, ll off, const nbg_soa *h, ll 
     if (h->id) {
         if ((rc = put_field(ctx, D.id + off, (const ll *)h->id, n)) != NBG_OK) return rc;
     }
-    if ((rc = put_field(ctx, D.flags + off, flags.data(), n)) != NBG_OK) return rc;
+    if ((rc = put_field(ctx, D.flags + off, flags, n)) != NBG_OK) return rc;
     CK(cudaGetLastError());
-    /* the flag vector is a host temporary */
-    CK(cudaStreamSynchronize(ctx->st));
     return NBG_OK;
 }
 
@@ -487,7 +525,8 @@ int nbg_create(int device, int precision, int64_t capacity, nbg_ctx **out)
         if ((rc = ensure_adds_cap(ctx, 1024)) != NBG_OK) break;
         if ((rc = ensure_ev_cap(ctx, 65536)) != NBG_OK) break;
         const ll zero = 0;
-        if ((rc = set_segments(ctx, 1, &zero)) != NBG_OK) break;
+        bool reshaped;
+        if ((rc = set_segments(ctx, 1, &zero, &reshaped)) != NBG_OK) break;
     } while (0);
     if (rc != NBG_OK) {
         g_last_error = ctx->err;
@@ -513,6 +552,8 @@ void nbg_destroy(nbg_ctx *ctx)
     free_cap_buffers(ctx->cb);
     nbg_bh_free(ctx->cb.t);
     if (ctx->ring_host) cudaHostUnregister(ctx->ring_host);
+    if (ctx->flags_h) cudaFreeHost(ctx->flags_h);
+    if (ctx->seg_h) cudaFreeHost(ctx->seg_h);
     cudaFree(ctx->seg_mem);
     cudaFree(ctx->scratch);
     cudaFree(ctx->ctl);
@@ -602,11 +643,11 @@ int nbg_set_collections(nbg_ctx *ctx, int64_t nsims, const int64_t *counts, cons
         if ((rc = put_field(ctx, ctx->cb.a.id, ids.data(), n)) != NBG_OK) return rc;
         CK(cudaStreamSynchronize(ctx->st));
     }
-    if ((rc = set_segments(ctx, (int)nsims, (const ll *)counts)) != NBG_OK) return rc;
-    invalidate_graph(ctx); /* kernel arguments carry the segment arrays */
-    ll nn = n, zero = 0;
-    if ((rc = ctl_put(ctx, offsetof(DevCtl, n), &nn, sizeof nn)) != NBG_OK) return rc;
-    if ((rc = ctl_put(ctx, offsetof(DevCtl, n_host_adds), &zero, sizeof zero)) != NBG_OK) return rc;
+    bool reshaped = false;
+    if ((rc = set_segments(ctx, (int)nsims, (const ll *)counts, &reshaped)) != NBG_OK) return rc;
+    if (reshaped) invalidate_graph(ctx);
+    k_set_loaded<<<1, 1, 0, ctx->st>>>(ctx->ctl, n);
+    CK(cudaGetLastError());
     ctx->n_host = n;
     return NBG_OK;
 }
@@ -678,15 +719,15 @@ int nbg_get_state(nbg_ctx *ctx, nbg_soa *h, int64_t cap, int64_t *n_out)
 #undef GETD
     if ((rc = get_field(ctx, (ll *)h->id, A.id, n)) != NBG_OK) return rc;
     if ((rc = get_field(ctx, (ll *)h->frag_fragments, A.fr_cnt, n)) != NBG_OK) return rc;
-    std::vector<unsigned> fl;
     if (h->flags || h->collision) {
-        fl.resize((size_t)(n > 0 ? n : 1));
-        if ((rc = get_field(ctx, fl.data(), A.flags, n)) != NBG_OK) return rc;
+        if ((rc = ensure_flags_h(ctx, n)) != NBG_OK) return rc;
+        if ((rc = get_field(ctx, ctx->flags_h, A.flags, n)) != NBG_OK) return rc;
     }
     CK(cudaStreamSynchronize(ctx->st));
+    const unsigned *fl = ctx->flags_h;
     for (ll k = 0; k < n && (h->flags || h->collision); k++) {
-        if (h->flags) h->flags[k] = fl[(size_t)k] & 0xffu;
-        if (h->collision) h->collision[k] = (int32_t)NBG_BEHAVIOR(fl[(size_t)k]);
+        if (h->flags) h->flags[k] = fl[k] & 0xffu;
+        if (h->collision) h->collision[k] = (int32_t)NBG_BEHAVIOR(fl[k]);
     }
     return NBG_OK;
 }
