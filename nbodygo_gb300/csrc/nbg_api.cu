@@ -400,6 +400,88 @@ static int get_field(nbg_ctx *ctx, T *dst, const T *src, ll n)
     return NBG_OK;
 }
 
+/* Copies between device arrays and host arrays in one kernel when the host
+ * side is pinned (page-locked memory is mapped into the device's address
+ * space): the SMs read or write it over the host link in one launch, where
+ * one DMA copy per field would pay a fixed cost each.  Pageable host memory
+ * takes cudaMemcpyAsync. */
+#define NBG_COPY_BATCH 32
+struct CopyBatch {
+    void *dst[NBG_COPY_BATCH];
+    const void *src[NBG_COPY_BATCH];
+    ll bytes[NBG_COPY_BATCH];
+    int n;
+};
+
+__global__ void k_copy_batch(CopyBatch b)
+{
+    const int e = blockIdx.y;
+    if (e >= b.n) return;
+    const ll bytes = b.bytes[e];
+    const ll stride = (ll)gridDim.x * blockDim.x;
+    const ll t0 = (ll)blockIdx.x * blockDim.x + threadIdx.x;
+    const uintptr_t d = (uintptr_t)b.dst[e], s = (uintptr_t)b.src[e];
+    if (((d | s) & 15) == 0) {
+        const ll u = bytes >> 4;
+        for (ll k = t0; k < u; k += stride) ((uint4 *)d)[k] = ((const uint4 *)s)[k];
+        for (ll k = (u << 4) + t0; k < bytes; k += stride) ((char *)d)[k] = ((const char *)s)[k];
+    } else if (((d | s) & 7) == 0) {
+        const ll u = bytes >> 3;
+        for (ll k = t0; k < u; k += stride) ((ull *)d)[k] = ((const ull *)s)[k];
+        for (ll k = (u << 3) + t0; k < bytes; k += stride) ((char *)d)[k] = ((const char *)s)[k];
+    } else {
+        for (ll k = t0; k < bytes; k += stride) ((char *)d)[k] = ((const char *)s)[k];
+    }
+}
+
+/* the device address of pinned host memory, or NULL (pageable) */
+static const void *mapped_host(const void *p)
+{
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
+static int batch_flush(nbg_ctx *ctx, CopyBatch &b)
+{
+    if (b.n == 0) return NBG_OK;
+    ll most = 0;
+    for (int k = 0; k < b.n; k++) most = b.bytes[k] > most ? b.bytes[k] : most;
+    ll blocks = (most / 16 + 255) / 256;
+    if (blocks > 64) blocks = 64;
+    if (blocks < 1) blocks = 1;
+    k_copy_batch<<<dim3((unsigned)blocks, (unsigned)b.n), 256, 0, ctx->st>>>(b);
+    CK(cudaGetLastError());
+    b.n = 0;
+    return NBG_OK;
+}
+
+/* host -> device (dir 0) or device -> host (dir 1) copy of n elements */
+template <typename T>
+static int batch_copy(nbg_ctx *ctx, CopyBatch &b, T *dst, const T *src, ll n, int dir)
+{
+    if (n <= 0 || !dst || !src) return NBG_OK;
+    const void *host = dir == 0 ? (const void *)src : (const void *)dst;
+    const void *mapped = mapped_host(host);
+    if (!mapped) {
+        CK(cudaMemcpyAsync(dst, src, (size_t)n * sizeof(T), dir == 0 ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToHost,
+                           ctx->st));
+        return NBG_OK;
+    }
+    if (b.n == NBG_COPY_BATCH) {
+        int rc = batch_flush(ctx, b);
+        if (rc != NBG_OK) return rc;
+    }
+    b.dst[b.n] = dir == 0 ? (void *)dst : const_cast<void *>(mapped);
+    b.src[b.n] = dir == 0 ? mapped : (const void *)src;
+    b.bytes[b.n] = n * (ll)sizeof(T);
+    b.n++;
+    return NBG_OK;
+}
+
 /* pinned host staging of at least n flag words (the previous copy out of it
  * must be complete: every user syncs the stream before reuse) */
 static int ensure_flags_h(nbg_ctx *ctx, ll n)
@@ -432,9 +514,11 @@ static int upload_soa(nbg_ctx *ctx, BodyArrays &D, ll off, const nbg_soa *h, ll 
         flags[k] = (f & 0xffu) | ((unsigned)c << NBG_BEHAVIOR_SHIFT);
     }
     int rc;
-#define PUTD(fld, src)                                                                      \
-    if ((src) != nullptr) {                                                                 \
-        if ((rc = put_field(ctx, D.fld + off, (const double *)(src), n)) != NBG_OK) return rc; \
+    CopyBatch cb;
+    cb.n = 0;
+#define PUTD(fld, src)                                                                                 \
+    if ((src) != nullptr) {                                                                            \
+        if ((rc = batch_copy(ctx, cb, D.fld + off, (const double *)(src), n, 0)) != NBG_OK) return rc; \
     }
 #define FILLD(fld, v) k_fill_f64<<<grid_for(n), 256, 0, ctx->st>>>(D.fld + off, n, v)
     PUTD(x, h->x);
@@ -460,15 +544,19 @@ static int upload_soa(nbg_ctx *ctx, BodyArrays &D, ll off, const nbg_soa *h, ll 
 #undef PUTD
 #undef FILLD
     if (h->frag_fragments) {
-        if ((rc = put_field(ctx, D.fr_cnt + off, (const ll *)h->frag_fragments, n)) != NBG_OK) return rc;
+        if ((rc = batch_copy(ctx, cb, D.fr_cnt + off, (const ll *)h->frag_fragments, n, 0)) != NBG_OK) return rc;
     } else {
         k_fill_i64<<<grid_for(n), 256, 0, ctx->st>>>(D.fr_cnt + off, n, 0);
     }
     if (h->id) {
-        if ((rc = put_field(ctx, D.id + off, (const ll *)h->id, n)) != NBG_OK) return rc;
+        if ((rc = batch_copy(ctx, cb, D.id + off, (const ll *)h->id, n, 0)) != NBG_OK) return rc;
     }
-    if ((rc = put_field(ctx, D.flags + off, flags, n)) != NBG_OK) return rc;
+    if ((rc = batch_copy(ctx, cb, D.flags + off, (const unsigned *)flags, n, 0)) != NBG_OK) return rc;
+    if ((rc = batch_flush(ctx, cb)) != NBG_OK) return rc;
     CK(cudaGetLastError());
+    /* the caller's arrays are read before this returns (they may be reused
+     * at once, cgo memory included) */
+    CK(cudaStreamSynchronize(ctx->st));
     return NBG_OK;
 }
 
@@ -694,8 +782,10 @@ int nbg_get_state(nbg_ctx *ctx, nbg_soa *h, int64_t cap, int64_t *n_out)
     const ll n = n0 < cap ? n0 : cap;
     if (n_out) *n_out = n0;
     BodyArrays &A = ctx->cb.a;
+    CopyBatch cb;
+    cb.n = 0;
 #define GETD(hf, df) \
-    if ((rc = get_field(ctx, h->hf, (const double *)A.df, n)) != NBG_OK) return rc;
+    if ((rc = batch_copy(ctx, cb, h->hf, (const double *)A.df, n, 1)) != NBG_OK) return rc;
     GETD(x, x);
     GETD(y, y);
     GETD(z, z);
@@ -717,12 +807,13 @@ int nbg_get_state(nbg_ctx *ctx, nbg_soa *h, int64_t cap, int64_t *n_out)
     GETD(frag_cy, fr_cy);
     GETD(frag_cz, fr_cz);
 #undef GETD
-    if ((rc = get_field(ctx, (ll *)h->id, A.id, n)) != NBG_OK) return rc;
-    if ((rc = get_field(ctx, (ll *)h->frag_fragments, A.fr_cnt, n)) != NBG_OK) return rc;
+    if ((rc = batch_copy(ctx, cb, (ll *)h->id, (const ll *)A.id, n, 1)) != NBG_OK) return rc;
+    if ((rc = batch_copy(ctx, cb, (ll *)h->frag_fragments, (const ll *)A.fr_cnt, n, 1)) != NBG_OK) return rc;
     if (h->flags || h->collision) {
         if ((rc = ensure_flags_h(ctx, n)) != NBG_OK) return rc;
-        if ((rc = get_field(ctx, ctx->flags_h, A.flags, n)) != NBG_OK) return rc;
+        if ((rc = batch_copy(ctx, cb, ctx->flags_h, (const unsigned *)A.flags, n, 1)) != NBG_OK) return rc;
     }
+    if ((rc = batch_flush(ctx, cb)) != NBG_OK) return rc;
     CK(cudaStreamSynchronize(ctx->st));
     const unsigned *fl = ctx->flags_h;
     for (ll k = 0; k < n && (h->flags || h->collision); k++) {
