@@ -592,8 +592,10 @@ __global__ void __launch_bounds__(BH_BLOCK) k_bh_force(BodyArrays A, DevCtl *ctl
  * one node sequence together: a lane that accepts a node waits until the
  * warp leaves that node's subtree (its skip pointer), and the warp descends
  * when any lane opens, so every node load is a broadcast and no lane
- * diverges.  A node with no mass below it is skipped by every lane.  Each lane sums its terms in FP32 and folds them into FP64 every
- * 64 terms. */
+ * diverges.  A node with no mass below it is skipped by every lane.  Each
+ * lane sums its terms in FP32 and, every 64 nodes, the warp folds them into
+ * (hi, lo) FP32 pairs: the GB300 FP64 pipe is 1/64 of the FP32 rate, and a
+ * few FP64 folds per node kept it saturated. */
 __global__ void __launch_bounds__(BH_BLOCK) k_bh_prep_mixed(DevCtl *ctl, BhTree t)
 {
     if (ctl->error) return;
@@ -620,6 +622,16 @@ __global__ void __launch_bounds__(BH_BLOCK) k_bh_prep_mixed(DevCtl *ctl, BhTree 
         t.fb[id] = b;
         t.fc[id] = make_int4(t.skip[id], t.start[id], t.end[id], (int)t.flags[id]);
     }
+}
+
+/* (hi, lo) += v with the rounding error of hi + v kept in lo (TwoSum) */
+__device__ __forceinline__ void fold2(float &hi, float &lo, float v)
+{
+    const float s = hi + v;
+    const float bb = s - hi;
+    const float e = (hi - (s - bb)) + (v - bb);
+    hi = s;
+    lo += e;
 }
 
 __device__ __forceinline__ float bh_rsqrt(float x)
@@ -685,8 +697,10 @@ __global__ void __launch_bounds__(BH_BLOCK, MINB) k_bh_force_mixed(BodyArrays A,
         }
         int wait = have ? 0 : 0x7fffffff;
         float ax = 0.f, ay = 0.f, az = 0.f;
-        double sx = 0, sy = 0, sz = 0;
-        int nacc = 0;
+        /* every 64 nodes the warp folds the FP32 partial sums into (hi, lo)
+         * FP32 pairs (TwoSum): all lanes together, and no FP64 in the walk */
+        float hx = 0.f, lx = 0.f, hy = 0.f, ly = 0.f, hz = 0.f, lz = 0.f;
+        int nacc = 0, steps = 0;
         if (!__any_sync(FULL_MASK, have)) continue;
         /* The next node is the first child when any lane opens this one, and
          * otherwise this node's skip pointer: every lane that waits at this
@@ -726,24 +740,23 @@ __global__ void __launch_bounds__(BH_BLOCK, MINB) k_bh_force_mixed(BodyArrays A,
                     az += w * dz;
                     nacc++;
                 }
-                if (nacc >= 64) {
-                    sx += ax;
-                    sy += ay;
-                    sz += az;
-                    terms += nacc;
-                    ax = ay = az = 0.f;
-                    nacc = 0;
-                }
                 wait = sk;
+            }
+            if (++steps == 64) {
+                fold2(hx, lx, ax);
+                fold2(hy, ly, ay);
+                fold2(hz, lz, az);
+                ax = ay = az = 0.f;
+                steps = 0;
             }
             id = next;
         }
         if (have) {
             terms += nacc;
             const double gm = NBG_G * A.m[k] * mroot;
-            A.fx[k] = gm * (sx + ax);
-            A.fy[k] = gm * (sy + ay);
-            A.fz[k] = gm * (sz + az);
+            A.fx[k] = gm * (((double)hx + (double)lx) + (double)ax);
+            A.fy[k] = gm * (((double)hy + (double)ly) + (double)ay);
+            A.fz[k] = gm * (((double)hz + (double)lz) + (double)az);
         }
     }
     for (int o = 16; o > 0; o >>= 1) terms += __shfl_xor_sync(FULL_MASK, terms, o);
@@ -962,8 +975,8 @@ void nbg_launch_bh(const CycleBufs &cb, DevCtl *ctl, cudaStream_t st, bool mixed
         /* CTAs per SM the walk's registers are capped for: the walk is bound
          * by the latency of its node loads, so occupancy is what counts */
         switch (cb.bh_shape) {
-        case 1: k_bh_force_mixed<5><<<g, BH_BLOCK, 0, st>>>(cb.a, ctl, t.val[0], t); break;
-        case 2: k_bh_force_mixed<6><<<g, BH_BLOCK, 0, st>>>(cb.a, ctl, t.val[0], t); break;
+        case 1: k_bh_force_mixed<3><<<g, BH_BLOCK, 0, st>>>(cb.a, ctl, t.val[0], t); break;
+        case 2: k_bh_force_mixed<5><<<g, BH_BLOCK, 0, st>>>(cb.a, ctl, t.val[0], t); break;
         default: k_bh_force_mixed<4><<<g, BH_BLOCK, 0, st>>>(cb.a, ctl, t.val[0], t); break;
         }
     } else {

@@ -200,7 +200,7 @@ struct CycleBufs {
     ll ring_cap;
     int ring_slots;
     int bh;             /* forces from the Barnes-Hut octree */
-    int bh_shape;       /* register cap of the mixed walk: 0, 1, 2 = 4, 5, 6 CTAs per SM */
+    int bh_shape;       /* register cap of the mixed walk: 0, 1, 2 = 4, 3, 5 CTAs per SM */
     BhTree t;
 };
 
