@@ -316,7 +316,7 @@ int nbg_get_timing(nbg_ctx *ctx, nbg_timing *t);
  * reference's --barnes-hut path with its missing Octree.Build call made
  * (body_collection.go:298-300).  Needs a single collection. */
 #define NBG_OPT_BARNES_HUT 8
-/* mixed Barnes-Hut walk: registers capped for 4, 3 or 5 CTAs per SM (0..2) */
+/* mixed Barnes-Hut walk: registers capped for 3, 4 or 5 CTAs per SM (0..2) */
 #define NBG_OPT_BH_SHAPE 9
 #define NBG_OPT_NEAR_PPM 5   /* mixed: pairs closer than (value * 1e-6) x the i-body's
                                 distance from its tile origin take the near-pair

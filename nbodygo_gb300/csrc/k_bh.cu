@@ -975,9 +975,9 @@ void nbg_launch_bh(const CycleBufs &cb, DevCtl *ctl, cudaStream_t st, bool mixed
         /* CTAs per SM the walk's registers are capped for: the walk is bound
          * by the latency of its node loads, so occupancy is what counts */
         switch (cb.bh_shape) {
-        case 1: k_bh_force_mixed<3><<<g, BH_BLOCK, 0, st>>>(cb.a, ctl, t.val[0], t); break;
+        case 1: k_bh_force_mixed<4><<<g, BH_BLOCK, 0, st>>>(cb.a, ctl, t.val[0], t); break;
         case 2: k_bh_force_mixed<5><<<g, BH_BLOCK, 0, st>>>(cb.a, ctl, t.val[0], t); break;
-        default: k_bh_force_mixed<4><<<g, BH_BLOCK, 0, st>>>(cb.a, ctl, t.val[0], t); break;
+        default: k_bh_force_mixed<3><<<g, BH_BLOCK, 0, st>>>(cb.a, ctl, t.val[0], t); break;
         }
     } else {
         k_bh_force<<<g, BH_BLOCK, 0, st>>>(cb.a, ctl, t.val[0], t);

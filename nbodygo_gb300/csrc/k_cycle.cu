@@ -331,6 +331,104 @@ __global__ void __launch_bounds__(P64_BLOCK) k_pair_fp64(BodyArrays A, DevCtl *c
     }
 }
 
+/* Small collections: one thread per body leaves most of the GPU idle (1,000
+ * bodies fill 16 SMs), and FP64 runs at 1/64 of the FP32 rate.  So the pair
+ * terms are computed for all (i, j) at once and stored, then each body adds
+ * its terms in j order: the same expressions, the same additions in the same
+ * order, so the result is bit-identical to k_pair_fp64.  A term that the
+ * reference skips is stored as +0.0, and adding +0.0 changes no sum here
+ * (the sum starts at +0.0 and can never be -0.0).  j runs in passes of jc;
+ * the sums are carried between passes in acc.  One collection. */
+#define P64_JS 16 /* j per block of k_p64_terms: more blocks for the few bodies */
+__global__ void __launch_bounds__(P64_BLOCK) k_p64_terms(BodyArrays A, DevCtl *ctl, double *T, ll cap, ll jc,
+                                                         ll jbase, ull *ev_keys, ll ev_cap)
+{
+    __shared__ double sx[P64_JS], sy[P64_JS], sz[P64_JS], sm[P64_JS], sr[P64_JS];
+    __shared__ unsigned sf[P64_JS];
+    if (ctl->error) return;
+    const ll n = ctl->n;
+    const ll j0 = jbase + (ll)blockIdx.y * P64_JS;
+    if (j0 >= n || (ll)blockIdx.x * P64_BLOCK >= n) return;
+    const ll i = (ll)blockIdx.x * P64_BLOCK + threadIdx.x;
+    const ll jl = j0 + threadIdx.x;
+    if (threadIdx.x < P64_JS && jl < n) {
+        sx[threadIdx.x] = A.x[jl];
+        sy[threadIdx.x] = A.y[jl];
+        sz[threadIdx.x] = A.z[jl];
+        sm[threadIdx.x] = A.m[jl];
+        sr[threadIdx.x] = A.rad[jl];
+        sf[threadIdx.x] = A.flags[jl];
+    }
+    __syncthreads();
+    if (i >= n) return;
+    const double xi = A.x[i], yi = A.y[i], zi = A.z[i], mi = A.m[i], ri = A.rad[i];
+    const unsigned fi = A.flags[i];
+    const bool live_i = (fi & NBG_LIVE_MASK) == NBG_F_EXISTS;
+    const bool coll_i = (fi & NBG_F_COLLIDED) != 0;
+    const unsigned bi = NBG_BEHAVIOR(fi);
+    const double gmi = NBG_G * mi;
+    const int cnt = (n - j0) < P64_JS ? (int)(n - j0) : P64_JS;
+    double *tx = T, *ty = T + jc * cap, *tz = T + 2 * jc * cap;
+    for (int t = 0; t < cnt; t++) {
+        const ll j = j0 + t;
+        const ll slot = (j - jbase) * cap + i;
+        double ex = 0.0, ey = 0.0, ez = 0.0;
+        if (live_i) {
+            const double dx = sx[t] - xi;
+            const double dy = sy[t] - yi;
+            const double dz = sz[t] - zi;
+            const double dist = sqrt(dx * dx + dy * dy + dz * dz);
+            const double rr = ri + sr[t];
+            const unsigned fj = sf[t];
+            const bool live_j = (fj & NBG_LIVE_MASK) == NBG_F_EXISTS;
+            if (live_j && j != i && (coll_i || dist > rr)) {
+                const double force = gmi * sm[t] / (dist * dist);
+                ex = force * dx / dist;
+                ey = force * dy / dist;
+                ez = force * dz / dist;
+            }
+            if (!coll_i && dist <= rr && j != i) {
+                const int type = nbg_detect_event(bi, NBG_BEHAVIOR(fj), ri, sr[t], dist);
+                if (type >= 0) nbg_emit_event(ctl, ev_keys, ev_cap, i, j, type);
+            }
+        }
+        tx[slot] = ex;
+        ty[slot] = ey;
+        tz[slot] = ez;
+    }
+}
+
+__global__ void k_p64_sum(BodyArrays A, DevCtl *ctl, const double *T, double *acc, ll cap, ll jc, ll jbase)
+{
+    if (ctl->error) return;
+    const ll n = ctl->n;
+    if (jbase >= n && jbase > 0) return;
+    const ll i = (ll)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double fx = jbase == 0 ? 0.0 : acc[i];
+    double fy = jbase == 0 ? 0.0 : acc[cap + i];
+    double fz = jbase == 0 ? 0.0 : acc[2 * cap + i];
+    const ll je = jbase + jc < n ? jbase + jc : n;
+    const double *tx = T, *ty = T + jc * cap, *tz = T + 2 * jc * cap;
+    for (ll j = jbase; j < je; j++) {
+        const ll slot = (j - jbase) * cap + i;
+        fx += tx[slot];
+        fy += ty[slot];
+        fz += tz[slot];
+    }
+    if (je >= n) {
+        if ((A.flags[i] & NBG_LIVE_MASK) == NBG_F_EXISTS) {
+            A.fx[i] = fx;
+            A.fy[i] = fy;
+            A.fz[i] = fz;
+        }
+    } else {
+        acc[i] = fx;
+        acc[cap + i] = fy;
+        acc[2 * cap + i] = fz;
+    }
+}
+
 /* ------------------------------------------------------------------------ */
 /* K4: order the events (i ascending, then j)                               */
 /* ------------------------------------------------------------------------ */
@@ -1086,7 +1184,24 @@ int nbg_pair_fp64_grid(ll cap)
 
 void nbg_launch_pair_fp64(const CycleBufs &cb, DevCtl *ctl, cudaStream_t st)
 {
+    if (cb.p64_terms && cb.seg.nsims == 1) {
+        const ll jc = cb.p64_jc;
+        const unsigned gi = (unsigned)((cb.cap + P64_BLOCK - 1) / P64_BLOCK);
+        const unsigned gj = (unsigned)(jc / P64_JS);
+        for (ll jbase = 0; jbase < cb.cap; jbase += jc) {
+            k_p64_terms<<<dim3(gi, gj), P64_BLOCK, 0, st>>>(cb.a, ctl, cb.p64_terms, cb.cap, jc, jbase, cb.ev_keys,
+                                                             cb.ev_cap);
+            k_p64_sum<<<(unsigned)((cb.cap + 255) / 256), 256, 0, st>>>(cb.a, ctl, cb.p64_terms, cb.p64_acc, cb.cap,
+                                                                        jc, jbase);
+        }
+        return;
+    }
     k_pair_fp64<<<nbg_pair_fp64_grid(cb.cap), P64_BLOCK, 0, st>>>(cb.a, ctl, cb.seg, cb.ev_keys, cb.ev_cap);
+}
+
+int nbg_pair_fp64_launches(const CycleBufs &cb)
+{
+    return cb.p64_terms && cb.seg.nsims == 1 ? (int)(2 * ((cb.cap + cb.p64_jc - 1) / cb.p64_jc)) : 1;
 }
 
 /* everything after the pair kernel: order events, emit fragments, resolve,

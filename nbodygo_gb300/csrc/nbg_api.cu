@@ -264,6 +264,11 @@ static int ensure_cap(nbg_ctx *ctx, ll need, ll keep)
     ll tiles = (cap + NBG_MIX_MIN_ITILE - 1) / NBG_MIX_MIN_ITILE + NBG_MAX_SIMS + 1;
     CK(cudaMalloc((void **)&ctx->cb.tile_c, (size_t)tiles * sizeof(float4)));
     CK(cudaMalloc((void **)&ctx->cb.iprep, (size_t)cap * sizeof(float4)));
+    if (cap <= NBG_P64_SPLIT_MAX_CAP) {
+        ctx->cb.p64_jc = cap < NBG_P64_SPLIT_JC ? cap : NBG_P64_SPLIT_JC;
+        CK(cudaMalloc((void **)&ctx->cb.p64_terms, (size_t)3 * ctx->cb.p64_jc * cap * sizeof(double)));
+        CK(cudaMalloc((void **)&ctx->cb.p64_acc, (size_t)3 * cap * sizeof(double)));
+    }
     ctx->cb.part_doubles = part_need(ctx, cap);
     CK(cudaMalloc((void **)&ctx->cb.part, (size_t)ctx->cb.part_doubles * sizeof(double)));
     CK(cudaMalloc((void **)&ctx->cb.perm, (size_t)cap * sizeof(unsigned)));
@@ -311,6 +316,10 @@ static void free_cap_buffers(CycleBufs &cb)
     cudaFree(cb.jlo);
     cudaFree(cb.tile_c);
     cudaFree(cb.iprep);
+    cudaFree(cb.p64_terms);
+    cudaFree(cb.p64_acc);
+    cb.p64_terms = cb.p64_acc = nullptr;
+    cb.p64_jc = 0;
     cudaFree(cb.part);
     cudaFree(cb.perm);
     cudaFree(cb.sval);
@@ -990,7 +999,7 @@ static void launch_cycle(nbg_ctx *ctx, int precision, long ev_base)
      * and the output;
      * Barnes-Hut replaces the pair kernel with 55 (k_bh.cu) */
     ctx->launches_per_cycle = (cb.bh ? 13 + 55 + (precision == NBG_PRECISION_MIXED ? 1 : 0)
-                                     : precision == NBG_PRECISION_MIXED ? 40 : 14) +
+                                     : precision == NBG_PRECISION_MIXED ? 40 : 13 + nbg_pair_fp64_launches(cb)) +
                               (cb.ring_head ? 1 : 0);
 }
 

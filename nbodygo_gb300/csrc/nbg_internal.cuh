@@ -199,8 +199,12 @@ struct CycleBufs {
     nbg_renderable *ring_rend;
     ll ring_cap;
     int ring_slots;
+    /* plain form, small collections: pair terms (3 x p64_jc x cap) and the
+     * sums carried between passes (3 x cap); NULL when cap is too large */
+    double *p64_terms, *p64_acc;
+    ll p64_jc;
     int bh;             /* forces from the Barnes-Hut octree */
-    int bh_shape;       /* register cap of the mixed walk: 0, 1, 2 = 4, 3, 5 CTAs per SM */
+    int bh_shape;       /* register cap of the mixed walk: 0, 1, 2 = 3, 4, 5 CTAs per SM */
     BhTree t;
 };
 
@@ -278,6 +282,10 @@ void nbg_launch_edits(const CycleBufs &cb, DevCtl *ctl, const nbg_edit *edits_de
 void nbg_launch_energy(const CycleBufs &cb, DevCtl *ctl, double *out_dev, cudaStream_t st);
 void nbg_launch_find(const CycleBufs &cb, DevCtl *ctl, ll id, ll *idx_dev, cudaStream_t st);
 int nbg_pair_fp64_grid(ll cap);
+int nbg_pair_fp64_launches(const CycleBufs &cb);
+/* largest capacity the plain form stores its pair terms for */
+#define NBG_P64_SPLIT_MAX_CAP 8192
+#define NBG_P64_SPLIT_JC 2048
 
 /* k_mixed.cu */
 void nbg_launch_mixed_prep(const CycleBufs &cb, DevCtl *ctl, cudaStream_t st);
