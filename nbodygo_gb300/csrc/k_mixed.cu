@@ -445,8 +445,10 @@ k_pair_mixed(BodyArrays A, DevCtl *ctl, SimSegs seg, const float4 *__restrict__ 
                 ax[k] = ay[k] = az[k] = make_float2(0.f, 0.f);
                 mn[k] = 3.0e38f;
             }
+            /* the j pairs this tile holds (a segment's last tile is short) */
+            const int jpv = je - jt >= JT ? JP : (int)((je - jt + 1) / 2);
 #pragma unroll UNROLL
-            for (int pp = 0; pp < JP; pp++) {
+            for (int pp = 0; pp < jpv; pp++) {
                 const float4 a = sA[pp], b = sB[pp];
                 const float2 xj = make_float2(a.x, a.y), yj = make_float2(a.z, a.w);
                 const float2 zj = make_float2(b.x, b.y), mj = make_float2(b.z, b.w);
@@ -478,7 +480,7 @@ k_pair_mixed(BodyArrays A, DevCtl *ctl, SimSegs seg, const float4 *__restrict__ 
                     const float4 hi_i = jhi[p], lo_i = jlo[p];
                     float tx = 0.f, ty = 0.f, tz = 0.f;
                     const float xi = -nx[k].x, yi = -ny[k].x, zi = -nz[k].x;
-                    for (int pp = 0; pp < JP; pp++) {
+                    for (int pp = 0; pp < jpv; pp++) {
                         const float4 a = sA[pp], b = sB[pp];
 #pragma unroll
                         for (int e = 0; e < 2; e++) {
