@@ -337,7 +337,7 @@ __device__ __forceinline__ void near_pass_j(const BodyArrays &A, DevCtl *ctl, ul
 /* Everything in this kernel is indexed by sorted position (p for i, q for
  * j); perm maps a position to the body index used by the FP64 arrays and the
  * event keys. */
-template <int BLOCK, int K, int JT, int UNROLL, int MINB, bool SF>
+template <int BLOCK, int K, int JT, int UNROLL, int MINB, bool SF, bool DB>
 __global__ void __launch_bounds__(BLOCK, MINB)
 k_pair_mixed(BodyArrays A, DevCtl *ctl, SimSegs seg, const float4 *__restrict__ jhi, const float4 *__restrict__ jlo,
              const float4 *__restrict__ tile_c, const float4 *__restrict__ iprep, const unsigned *__restrict__ perm,
@@ -347,7 +347,12 @@ k_pair_mixed(BodyArrays A, DevCtl *ctl, SimSegs seg, const float4 *__restrict__ 
     constexpr int ITILE = BLOCK * K;
     static_assert(ITILE >= NBG_MIX_MIN_ITILE, "tile-origin buffer is sized for the smallest i-tile");
     static_assert(ITILE <= NBG_MIX_MAX_ITILE, "partial-sum buffer is sized for the largest i-tile");
-    __shared__ float4 sA[JP], sB[JP];
+    /* DB: two tile buffers; the next tile's raw j is loaded into registers
+     * while this tile is computed, and stored to the other buffer after it,
+     * so a tile costs one barrier and its global loads are hidden */
+    __shared__ float4 sAb[DB ? 2 : 1][JP], sBb[DB ? 2 : 1][JP];
+    constexpr int PPT = (JP + BLOCK - 1) / BLOCK; /* j pairs a thread fills */
+    float4 pre[DB ? PPT : 1][2][2];
     /* SF: each i-body's (hi, lo) sums and near-pair threshold live in shared
      * memory (only this thread touches them; read once per j-tile), which
      * frees seven registers per i-body for occupancy */
@@ -411,32 +416,74 @@ k_pair_mixed(BodyArrays A, DevCtl *ctl, SimSegs seg, const float4 *__restrict__ 
 
         const ll jb = s0 + j0;
         const ll je = jb + len;
-        for (ll jt = jb; jt < je; jt += JT) {
-            __syncthreads();
-            for (int sp = tid; sp < JP; sp += BLOCK) {
-                float v[2][4];
+        /* re-centred j pair (q, q + 1) of a tile: sentinels past je or for a
+         * special body */
+        auto pack = [&](const float4 (&h)[2], const float4 (&l)[2], ll q, float4 &oa, float4 &ob) {
+            float v[2][4];
+#pragma unroll
+            for (int e = 0; e < 2; e++) {
+                if (q + e < je && !packed_special(l[e])) {
+                    v[e][0] = (h[e].x - c.x) + l[e].x;
+                    v[e][1] = (h[e].y - c.y) + l[e].y;
+                    v[e][2] = (h[e].z - c.z) + l[e].z;
+                    v[e][3] = h[e].w;
+                } else {
+                    v[e][0] = v[e][1] = v[e][2] = SENTINEL_POS;
+                    v[e][3] = 0.f;
+                }
+            }
+            oa = make_float4(v[0][0], v[1][0], v[0][1], v[1][1]);
+            ob = make_float4(v[0][2], v[1][2], v[0][3], v[1][3]);
+        };
+        auto load_raw = [&](ll jt2) {
+#pragma unroll
+            for (int r = 0; r < (DB ? PPT : 1); r++) {
+                const int sp = tid + r * BLOCK;
 #pragma unroll
                 for (int e = 0; e < 2; e++) {
-                    const ll q = jt + 2 * sp + e;
-                    if (q < je) {
-                        const float4 h = jhi[q], l = jlo[q];
-                        v[e][0] = (h.x - c.x) + l.x;
-                        v[e][1] = (h.y - c.y) + l.y;
-                        v[e][2] = (h.z - c.z) + l.z;
-                        v[e][3] = h.w;
-                        if (packed_special(l)) {
-                            v[e][0] = v[e][1] = v[e][2] = SENTINEL_POS;
-                            v[e][3] = 0.f;
-                        }
-                    } else {
-                        v[e][0] = v[e][1] = v[e][2] = SENTINEL_POS;
-                        v[e][3] = 0.f;
+                    const ll q = jt2 + 2 * sp + e;
+                    if (sp < JP && q < je) {
+                        pre[r][e][0] = jhi[q];
+                        pre[r][e][1] = jlo[q];
                     }
                 }
-                sA[sp] = make_float4(v[0][0], v[1][0], v[0][1], v[1][1]);
-                sB[sp] = make_float4(v[0][2], v[1][2], v[0][3], v[1][3]);
             }
-            __syncthreads();
+        };
+        auto store_raw = [&](int buf, ll jt2) {
+#pragma unroll
+            for (int r = 0; r < (DB ? PPT : 1); r++) {
+                const int sp = tid + r * BLOCK;
+                if (sp < JP) {
+                    const float4 h[2] = {pre[r][0][0], pre[r][1][0]}, l[2] = {pre[r][0][1], pre[r][1][1]};
+                    pack(h, l, jt2 + 2 * sp, sAb[buf][sp], sBb[buf][sp]);
+                }
+            }
+        };
+        int buf = 0;
+        if (DB) {
+            load_raw(jb);
+            __syncthreads(); /* the previous segment's readers are done */
+            store_raw(0, jb);
+        }
+        for (ll jt = jb; jt < je; jt += JT) {
+            const float4 *sA = sAb[DB ? buf : 0], *sB = sBb[DB ? buf : 0];
+            if (DB) {
+                __syncthreads(); /* this tile is stored */
+                if (jt + JT < je) load_raw(jt + JT);
+            } else {
+                __syncthreads();
+                for (int sp = tid; sp < JP; sp += BLOCK) {
+                    float4 h[2], l[2];
+#pragma unroll
+                    for (int e = 0; e < 2; e++) {
+                        const ll q = jt + 2 * sp + e;
+                        h[e] = q < je ? jhi[q] : make_float4(0.f, 0.f, 0.f, 0.f);
+                        l[e] = q < je ? jlo[q] : make_float4(0.f, 0.f, 0.f, 0.f);
+                    }
+                    pack(h, l, jt + 2 * sp, sAb[0][sp], sBb[0][sp]);
+                }
+                __syncthreads();
+            }
 
             float2 ax[K], ay[K], az[K];
             float mn[K];
@@ -503,6 +550,12 @@ k_pair_mixed(BodyArrays A, DevCtl *ctl, SimSegs seg, const float4 *__restrict__ 
                 two_sum_add(FOLD(0, k), FOLD(1, k), ax[k].x + ax[k].y);
                 two_sum_add(FOLD(2, k), FOLD(3, k), ay[k].x + ay[k].y);
                 two_sum_add(FOLD(4, k), FOLD(5, k), az[k].x + az[k].y);
+            }
+            if (DB) {
+                /* the other buffer's last readers finished the previous tile
+                 * before this tile's barrier */
+                if (jt + JT < je) store_raw(buf ^ 1, jt + JT);
+                buf ^= 1;
             }
         }
         /* this chunk's share of i-tile g: slot g + chunk */
@@ -571,8 +624,9 @@ __global__ void k_mix_out(BodyArrays A, DevCtl *ctl, SimSegs seg, const unsigned
 /* ---- kernel shapes ---------------------------------------------------------
  * (kind, threads per CTA, i-bodies per thread, j per shared-memory tile,
  * unroll of the j loop, CTAs per SM the register budget is set for).  Kind 0:
- * sums in registers; 1: sums in shared memory.  Variant 0 is the default; the
- * autotuner (nbg_autotune) measures the others. */
+ * sums in registers; 1: sums in shared memory; 2: sums in shared memory and
+ * two tile buffers filled from registers loaded a tile ahead.  Variant 0 is
+ * the default; the autotuner (nbg_autotune) measures the others. */
 #define MIX_VARIANTS(X)              \
     X(0, 0, 128, 4, 256, 2, 3)       \
     X(1, 0, 128, 4, 256, 1, 3)       \
@@ -584,10 +638,14 @@ __global__ void k_mix_out(BodyArrays A, DevCtl *ctl, SimSegs seg, const unsigned
     X(7, 1, 128, 2, 256, 2, 5)       \
     X(8, 1, 128, 3, 256, 2, 4)       \
     X(9, 1, 128, 4, 256, 2, 4)       \
-    X(10, 1, 128, 4, 128, 4, 4)
+    X(10, 1, 128, 4, 128, 4, 4)      \
+    X(11, 2, 128, 2, 128, 4, 4)      \
+    X(12, 2, 128, 2, 256, 2, 4)      \
+    X(13, 2, 128, 2, 128, 2, 4)      \
+    X(14, 2, 128, 4, 128, 2, 3)
 
 /* the kernel of a shape */
-#define MIX_KERNEL(kind, b, k, jt, u, mb) k_pair_mixed<b, k, jt, u, mb, (kind) == 1>
+#define MIX_KERNEL(kind, b, k, jt, u, mb) k_pair_mixed<b, k, jt, u, mb, (kind) >= 1, (kind) == 2>
 
 MixVariantInfo nbg_mix_variant_info(int variant)
 {
