@@ -84,9 +84,15 @@ def parse():
     ap.add_argument("--workload", default="plummer_disk", choices=sorted(WORKLOADS))
     ap.add_argument("--n-each", type=int, default=65536, help="plummer_disk: bodies per component")
     ap.add_argument("--no-plain", action="store_true", help="skip the FP64 comparison run")
+    ap.add_argument("--with-plain", action="store_true",
+                    help="run the FP64 comparison on the uniform ball too (one FP64 force pass, ~2 min at 1M bodies)")
+    ap.add_argument("--drift-cycles", type=int, default=0,
+                    help="after the timed run, step a fresh copy of the workload this many cycles and report the "
+                         "relative energy and momentum drift (untimed)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default kernel shape")
-    ap.add_argument("--shape", type=int, default=None, help="use this shape of the mixed pair kernel (no autotune)")
+    ap.add_argument("--shape", type=int, default=None,
+                    help="use this shape of the mixed pair kernel, or of the mixed Barnes-Hut walk (no autotune)")
     return ap.parse_args()
 
 
@@ -364,8 +370,10 @@ def main():
     load(sim, sims)
     tuned = None
     if prec == "mixed" and args.shape is not None:
-        sim.set_option(A.OPT_MIX_SHAPE, args.shape)
-        tuned = {"shape": args.shape, "pair_kernel_ms": None, "candidates": A.MIX_SHAPES, "fixed": True}
+        # Barnes-Hut: the shape of the mixed walk (CTAs per SM it is built for)
+        sim.set_option(A.OPT_BH_SHAPE if bh else A.OPT_MIX_SHAPE, args.shape)
+        tuned = {"shape": args.shape, "pair_kernel_ms": None, "candidates": 3 if bh else A.MIX_SHAPES,
+                 "fixed": True, "kernel": "k_bh_force_mixed" if bh else "k_pair_mixed"}
     elif prec == "mixed" and not args.no_autotune and not bh:
         shape, tms = sim.autotune()
         tuned = {"shape": shape, "pair_kernel_ms": tms, "candidates": A.MIX_SHAPES}
@@ -440,12 +448,21 @@ def main():
     # ---- FP32 / FP64 peaks, plain FP64 comparison, accuracy ----
     f32, f64, mhz = probe_peaks(local)
     result_extra = {}
-    plain_ok = prec == "mixed" and args.workload != "uniform" and not bh and not args.no_plain and rank == 0
+    plain_ok = (prec == "mixed" and (args.workload != "uniform" or args.with_plain) and not bh
+                and not args.no_plain and rank == 0)
     if plain_ok:
+        # above this size the plain comparison is one timed FP64 force pass
+        # (no stepping, no O(N^2) FP64 energy sums)
+        big = n0 > 262144
         plain = Simulation("fp64", device=local, capacity=n0 + 4096)
         plain.set_stream(stream.cuda_stream)
         load(plain, sims)
+        pe0, pe1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        pe0.record(stream)
         fp = plain.force_pass()
+        pe1.record(stream)
+        torch.cuda.synchronize()
+        force_ms = pe0.elapsed_time(pe1)
         mixed0 = Simulation("mixed", device=local, capacity=n0 + 4096)
         mixed0.set_stream(stream.cuda_stream)
         load(mixed0, sims)
@@ -455,30 +472,67 @@ def main():
         mag = np.sqrt(fp[0] ** 2 + fp[1] ** 2 + fp[2] ** 2)
         err = np.sqrt((fm[0] - fp[0]) ** 2 + (fm[1] - fp[1]) ** 2 + (fm[2] - fp[2]) ** 2)
         ok = mag > 0
-        # energy over the same cycles from the same state, both forms
-        e0 = sum(plain.energy()[:2])
-        plain.enable_timing(True)
-        pi = plain.step(DT, 1.0, 2)
-        ptm = plain.timing()
-        plain.enable_timing(False)
-        mixed0.step(DT, 1.0, 2)
-        ep, em = sum(plain.energy()[:2]), sum(mixed0.energy()[:2])
-        p_ms = (ptm["pair_ms"] + ptm["other_ms"]) / max(1, ptm["pair_launches"])
-        plain_rate = pi["interactions"] / (1e-3 * (ptm["pair_ms"] + ptm["other_ms"]))
-        result_extra["plain_fp64"] = {
-            "value": plain_rate, "unit": UNIT, "ms_per_step": p_ms,
-            "pair_kernel_ms": ptm["pair_ms"] / max(1, ptm["pair_launches"]),
-            "roofline_frac_fp64": plain_rate * FLOPS_PER_PAIR / f64 if f64 else None,
-            "steps": 2}
+        if big:
+            pairs = sum(len(b["x"]) * (len(b["x"]) - 1) for b in sims)
+            plain_rate = pairs / (1e-3 * force_ms)
+            drift = {"skipped": f"{n0} bodies: the FP64 energy sum is O(N^2) in FP64"}
+            result_extra["plain_fp64"] = {
+                "value": plain_rate, "unit": UNIT, "ms_per_step": None, "force_pass_ms": force_ms,
+                "pair_kernel_ms": force_ms,
+                "roofline_frac_fp64": plain_rate * FLOPS_PER_PAIR / f64 if f64 else None,
+                "steps": 0, "timed": "one FP64 force pass (pair kernel and set-up), CUDA events"}
+        else:
+            # energy over the same cycles from the same state, both forms
+            e0 = sum(plain.energy()[:2])
+            plain.enable_timing(True)
+            pi = plain.step(DT, 1.0, 2)
+            ptm = plain.timing()
+            plain.enable_timing(False)
+            mixed0.step(DT, 1.0, 2)
+            ep, em = sum(plain.energy()[:2]), sum(mixed0.energy()[:2])
+            p_ms = (ptm["pair_ms"] + ptm["other_ms"]) / max(1, ptm["pair_launches"])
+            plain_rate = pi["interactions"] / (1e-3 * (ptm["pair_ms"] + ptm["other_ms"]))
+            drift = {"fp64": abs(ep - e0) / abs(e0), "mixed": abs(em - e0) / abs(e0),
+                     "mixed_vs_fp64": abs(em - ep) / abs(e0)}
+            result_extra["plain_fp64"] = {
+                "value": plain_rate, "unit": UNIT, "ms_per_step": p_ms,
+                "pair_kernel_ms": ptm["pair_ms"] / max(1, ptm["pair_launches"]),
+                "roofline_frac_fp64": plain_rate * FLOPS_PER_PAIR / f64 if f64 else None,
+                "steps": 2}
         result_extra["mixed_over_plain"] = value / plain_rate / ws if plain_rate else None
         result_extra["accuracy"] = {"rel_l2_vs_fp64": float(num / den), "max_rel": float(np.max(err[ok] / mag[ok])),
                                     "median_rel": float(np.median(err[ok] / mag[ok])),
                                     "reference": "plain FP64 GPU forces (bit-identical to the oracle)",
-                                    "energy_drift_2_cycles": {"fp64": abs(ep - e0) / abs(e0),
-                                                              "mixed": abs(em - e0) / abs(e0),
-                                                              "mixed_vs_fp64": abs(em - ep) / abs(e0)}}
+                                    "energy_drift_2_cycles": drift}
         plain.close()
         mixed0.close()
+
+    if args.drift_cycles > 0 and rank == 0:
+        ds = Simulation(prec, device=local, capacity=n0 + 4096)
+        ds.set_stream(stream.cuda_stream)
+        ds.set_option(A.OPT_GRAPH_CYCLES, 10)
+        if bh:
+            ds.set_option(A.OPT_BARNES_HUT, 1)
+        load(ds, sims)
+        ke0, pe0_, p0 = ds.energy()
+        st0 = ds.state()
+        pscale = float(np.sum(st0["mass"] * np.sqrt(st0["vx"] ** 2 + st0["vy"] ** 2 + st0["vz"] ** 2)))
+        done, events = 0, 0
+        while done < args.drift_cycles:
+            k = min(10, args.drift_cycles - done)
+            di = ds.step(DT, 1.0, k)
+            done += di["steps_done"]
+            events += di.get("events", 0)
+        ke1, pe1_, p1 = ds.energy()
+        st1 = ds.state()
+        result_extra["drift"] = {
+            "cycles": done, "form": prec, "bodies_start": n0, "bodies_end": int(len(st1["x"])), "events": events,
+            "mass_rel": abs(float(np.sum(st1["mass"])) - float(np.sum(st0["mass"]))) / float(np.sum(st0["mass"])),
+            "energy_rel": abs((ke1 + pe1_) - (ke0 + pe0_)) / abs(ke0 + pe0_),
+            "momentum_rel": float(np.sqrt(sum((a - b) ** 2 for a, b in zip(p1, p0)))) / pscale,
+            "note": "mass is conserved; energy and momentum are not: a subsume keeps the absorbing body's velocity "
+                    "and an elastic collision with fragments moves mass between bodies as the reference does"}
+        ds.close()
 
     if bh:
         # the whole tree pass (build, walk, collision query) against the FP64

@@ -519,6 +519,19 @@ __device__ __forceinline__ void bh_term(double gm_i, double M, double dx, double
     fz += force * dz / dist;
 }
 
+/* The next group of 32 consecutive sorted bodies for this warp, or -1.  Walk
+ * times vary with the bodies' surroundings, so warps take groups from one
+ * queue until it is empty instead of a fixed share each: no SM idles while
+ * another still holds a long run of groups.  A group is always the same 32
+ * bodies, so the results do not depend on which warp takes it. */
+__device__ __forceinline__ int bh_next_group(DevCtl *ctl, int M)
+{
+    unsigned g = 0;
+    if ((threadIdx.x & 31) == 0) g = atomicAdd(&ctl->bh_next, 1u);
+    g = __shfl_sync(FULL_MASK, g, 0);
+    return g < (unsigned)(M + 31) / 32u ? (int)g : -1;
+}
+
 /* one thread per tree body (sorted order, so a warp walks nearby paths) */
 __global__ void __launch_bounds__(BH_BLOCK) k_bh_force(BodyArrays A, DevCtl *ctl, const unsigned *vals, BhTree t)
 {
@@ -527,8 +540,8 @@ __global__ void __launch_bounds__(BH_BLOCK) k_bh_force(BodyArrays A, DevCtl *ctl
     const int total = (int)ctl->bh_nodes;
     unsigned long long terms = 0;
     /* every lane runs the same number of rounds, for the warp reduction */
-    for (ll base0 = (ll)blockIdx.x * blockDim.x; base0 < M; base0 += (ll)gridDim.x * blockDim.x) {
-        const ll p = base0 + threadIdx.x;
+    for (int grp; (grp = bh_next_group(ctl, (int)M)) >= 0;) {
+        const int p = grp * 32 + (threadIdx.x & 31);
         if (p >= M) continue;
         const unsigned k = vals[p];
         if (A.flags[k] & NBG_F_IS_SUN) continue; /* k_bh_sun */
@@ -677,8 +690,8 @@ __global__ void __launch_bounds__(BH_BLOCK, MINB) k_bh_force_mixed(BodyArrays A,
     const double mroot = t.mass[0];
     const float soft2 = (float)(BH_SOFTENING * BH_SOFTENING);
     unsigned long long terms = 0;
-    for (ll base0 = (ll)blockIdx.x * blockDim.x; base0 < M; base0 += (ll)gridDim.x * blockDim.x) {
-        const ll p = base0 + threadIdx.x;
+    for (int grp; (grp = bh_next_group(ctl, (int)M)) >= 0;) {
+        const int p = grp * 32 + (threadIdx.x & 31);
         unsigned k = 0;
         bool have = p < M;
         if (have) {
@@ -974,10 +987,13 @@ void nbg_launch_bh(const CycleBufs &cb, DevCtl *ctl, cudaStream_t st, bool mixed
         k_bh_prep_mixed<<<ng, BH_BLOCK, 0, st>>>(ctl, t);
         /* CTAs per SM the walk's registers are capped for: the walk is bound
          * by the latency of its node loads, so occupancy is what counts */
+        /* one wave of resident CTAs; their warps share the group queue */
+        const int minb = cb.bh_shape == 1 ? 4 : cb.bh_shape == 2 ? 5 : 3;
+        const int gw = g < cb.sms * minb ? g : cb.sms * minb;
         switch (cb.bh_shape) {
-        case 1: k_bh_force_mixed<4><<<g, BH_BLOCK, 0, st>>>(cb.a, ctl, t.val[0], t); break;
-        case 2: k_bh_force_mixed<5><<<g, BH_BLOCK, 0, st>>>(cb.a, ctl, t.val[0], t); break;
-        default: k_bh_force_mixed<3><<<g, BH_BLOCK, 0, st>>>(cb.a, ctl, t.val[0], t); break;
+        case 1: k_bh_force_mixed<4><<<gw, BH_BLOCK, 0, st>>>(cb.a, ctl, t.val[0], t); break;
+        case 2: k_bh_force_mixed<5><<<gw, BH_BLOCK, 0, st>>>(cb.a, ctl, t.val[0], t); break;
+        default: k_bh_force_mixed<3><<<gw, BH_BLOCK, 0, st>>>(cb.a, ctl, t.val[0], t); break;
         }
     } else {
         k_bh_force<<<g, BH_BLOCK, 0, st>>>(cb.a, ctl, t.val[0], t);

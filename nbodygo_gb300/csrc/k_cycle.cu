@@ -126,6 +126,7 @@ __global__ void __launch_bounds__(NBG_SCAN_BLOCK) k_begin(DevCtl *ctl, SimSegs s
         ctl->bh_count = 0;
         ctl->bh_nodes = 0;
         ctl->bh_rmax = 0ull;
+        ctl->bh_next = 0;
         ctl->cycle_interactions = inter;
         if (part_short) {
             ctl->error = NBG_E_OVERFLOW;

@@ -617,6 +617,9 @@ int nbg_create(int device, int precision, int64_t capacity, nbg_ctx **out)
         ctx->cb.mix_variant = 0;
         ctx->cb.itile = nbg_mix_variant_info(0).block * nbg_mix_variant_info(0).k;
         ctx->cb.slots = nbg_mixed_slots(device, 0);
+        ctx->cb.sms = 0;
+        cudaDeviceGetAttribute(&ctx->cb.sms, cudaDevAttrMultiProcessorCount, device);
+        if (ctx->cb.sms < 1) ctx->cb.sms = 1;
         if ((rc = ensure_cap(ctx, capacity > 0 ? capacity : 1024, 0)) != NBG_OK) break;
         if ((rc = ensure_frag_cap(ctx, 4096)) != NBG_OK) break;
         if ((rc = ensure_adds_cap(ctx, 1024)) != NBG_OK) break;

@@ -86,6 +86,8 @@ struct DevCtl {
     ll bh_count;
     ll bh_nodes;
     ull bh_rmax;
+    unsigned bh_next; /* the walk's next 32-body group (one per warp) */
+    unsigned pad2;
 };
 
 /* A collection may hold several independent simulations stored one after
@@ -205,6 +207,7 @@ struct CycleBufs {
     ll p64_jc;
     int bh;             /* forces from the Barnes-Hut octree */
     int bh_shape;       /* register cap of the mixed walk: 0, 1, 2 = 3, 4, 5 CTAs per SM */
+    int sms;            /* streaming multiprocessors of the device */
     BhTree t;
 };
 
