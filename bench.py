@@ -419,6 +419,9 @@ def main():
     pinned, keep = pinned_like(torch, st, 4096)
     n_h = len(st["x"])
     e2e_int, e2e_t, h2d, d2h, e2e_chunks = 0, 0.0, 0, 0, max(1, min(nchunks, 5))
+    # each call returns once its copies and cycles are done, so the host
+    # clock between the calls splits the step into its phases
+    phase = {"load": 0.0, "step": 0.0, "read": 0.0}
     for k in range(e2e_chunks):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
@@ -426,23 +429,27 @@ def main():
         if len(counts) == 1:
             sim.set_bodies(host)
         else:
-            parts, o = [], 0
-            for c in counts:
-                parts.append({f: a[o:o + c] for f, a in host.items()})
-                o += c
-            sim.set_collections(parts)
+            sim.set_collections_flat(host, counts)
+        t1 = time.perf_counter()
         h2d += sum(a.nbytes for a in host.values())
         info = sim.step(DT, 1.0, chunk)
+        t2 = time.perf_counter()
         out = sim.state(out=pinned)
         counts = sim.sim_counts()
-        e2e_t += time.perf_counter() - t0
+        t3 = time.perf_counter()
+        phase["load"] += t1 - t0
+        phase["step"] += t2 - t1
+        phase["read"] += t3 - t2
+        e2e_t += t3 - t0
         n_h = len(out["x"])
         d2h += sum(a.nbytes for a in out.values())
         e2e_int += info["interactions"]
     e2e = {"value": dist.sum(e2e_int) / dist.max(e2e_t), "unit": UNIT,
            "h2d_bytes_per_step": int(h2d // (e2e_chunks * chunk)),
            "d2h_bytes_per_step": int(d2h // (e2e_chunks * chunk)),
-           "path": "nbg_set_bodies / nbg_set_collections (full state, pinned host) + nbg_step + nbg_get_state "
+           "phases_ms_per_call": {k: round(1e3 * v / e2e_chunks, 3) for k, v in phase.items()},
+           "path": "nbg_set_bodies / nbg_set_collections (full state, pinned host, collections one after another) "
+                   "+ nbg_step + nbg_get_state "
                    "(full state)" + (f", {chunk} cycles per call" if chunk > 1 else "")}
 
     # ---- FP32 / FP64 peaks, plain FP64 comparison, accuracy ----

@@ -47,6 +47,27 @@ def probe_peaks(device=0):
     return f32.value, f64.value, mhz.value
 
 
+def _adjacent(sims, k):
+    """Field k of every collection as one array: a view when the collections'
+    arrays already lie one after another in one buffer (no host copy), else
+    their concatenation."""
+    parts = [np.asarray(b[k]) for b in sims]
+    first = parts[0]
+    if all(p.flags.c_contiguous and p.dtype == first.dtype for p in parts):
+        addr, ok = first.ctypes.data, True
+        for p in parts:
+            if p.ctypes.data != addr:
+                ok = False
+                break
+            addr += p.nbytes
+        if ok and first.ndim == 1:
+            # every part is a live array and they tile one address range, so
+            # the span from the first part's start is valid memory
+            total = sum(len(p) for p in parts)
+            return np.lib.stride_tricks.as_strided(first, shape=(total,), strides=(first.itemsize,))
+    return np.concatenate(parts)
+
+
 class Simulation:
     """A body collection on one GPU with the nbodygo compute cycle."""
 
@@ -138,9 +159,20 @@ class Simulation:
         keys = set(sims[0])
         for b in sims[1:]:
             keys &= set(b)
-        cat = {k: np.concatenate([np.asarray(b[k]) for b in sims]) for k in keys}
-        soa, keep = A.soa_from_arrays(cat)
-        self._check(self.lib.nbg_set_collections(self.ctx, len(sims), counts.ctypes.data_as(C.POINTER(C.c_int64)),
+        cat = {k: _adjacent(sims, k) for k in keys}
+        self.set_collections_flat(cat, counts)
+
+    def set_collections_flat(self, bodies, counts):
+        """Several collections given as one body dict whose arrays hold the
+        collections one after another (collection s has counts[s] bodies):
+        the layout nbg_set_collections takes, so nothing is copied on the
+        host.  Pinned arrays go to the device through the copy kernel."""
+        counts = np.ascontiguousarray(counts, dtype=np.int64)
+        n = int(counts.sum())
+        if any(len(v) != n for v in bodies.values()):
+            raise ValueError("every array must hold sum(counts) bodies")
+        soa, keep = A.soa_from_arrays(bodies)
+        self._check(self.lib.nbg_set_collections(self.ctx, len(counts), counts.ctypes.data_as(C.POINTER(C.c_int64)),
                                                  C.byref(soa)))
         del keep
 
@@ -161,8 +193,8 @@ class Simulation:
         """Body state as a dict of numpy arrays.  With `out` (a dict of
         contiguous arrays, e.g. in pinned memory) the state is copied into
         them, up to their length, and views of the filled part are returned."""
-        n = self.count()
         if out is None:
+            n = self.count()
             out = A.empty_state(n) if fields is None else {f: np.zeros(n, dtype=A.FIELD_DTYPES[f]) for f in fields}
             cap = n
         else:

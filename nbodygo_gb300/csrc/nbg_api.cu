@@ -415,10 +415,15 @@ static int get_field(nbg_ctx *ctx, T *dst, const T *src, ll n)
  * one DMA copy per field would pay a fixed cost each.  Pageable host memory
  * takes cudaMemcpyAsync. */
 #define NBG_COPY_BATCH 32
+/* entry kinds: a plain copy, or a flag word split into one of its host-side
+ * fields (the nbg_soa flags byte, or the collision behaviour) */
+enum { COPY_BYTES = 0, COPY_FLAGS_LOW = 1, COPY_FLAGS_BEHAVIOR = 2 };
+
 struct CopyBatch {
     void *dst[NBG_COPY_BATCH];
     const void *src[NBG_COPY_BATCH];
     ll bytes[NBG_COPY_BATCH];
+    int op[NBG_COPY_BATCH];
     int n;
 };
 
@@ -430,7 +435,14 @@ __global__ void k_copy_batch(CopyBatch b)
     const ll stride = (ll)gridDim.x * blockDim.x;
     const ll t0 = (ll)blockIdx.x * blockDim.x + threadIdx.x;
     const uintptr_t d = (uintptr_t)b.dst[e], s = (uintptr_t)b.src[e];
-    if (((d | s) & 15) == 0) {
+    if (b.op[e] != COPY_BYTES) {
+        const ll u = bytes >> 2;
+        const unsigned *src = (const unsigned *)s;
+        if (b.op[e] == COPY_FLAGS_LOW)
+            for (ll k = t0; k < u; k += stride) ((unsigned *)d)[k] = src[k] & 0xffu;
+        else
+            for (ll k = t0; k < u; k += stride) ((int *)d)[k] = (int)NBG_BEHAVIOR(src[k]);
+    } else if (((d | s) & 15) == 0) {
         const ll u = bytes >> 4;
         for (ll k = t0; k < u; k += stride) ((uint4 *)d)[k] = ((const uint4 *)s)[k];
         for (ll k = (u << 4) + t0; k < bytes; k += stride) ((char *)d)[k] = ((const char *)s)[k];
@@ -487,6 +499,24 @@ static int batch_copy(nbg_ctx *ctx, CopyBatch &b, T *dst, const T *src, ll n, in
     b.dst[b.n] = dir == 0 ? (void *)dst : const_cast<void *>(mapped);
     b.src[b.n] = dir == 0 ? mapped : (const void *)src;
     b.bytes[b.n] = n * (ll)sizeof(T);
+    b.op[b.n] = COPY_BYTES;
+    b.n++;
+    return NBG_OK;
+}
+
+/* device flag words -> one of their fields in pinned host memory (mapped:
+ * the device address of dst); op is COPY_FLAGS_LOW or COPY_FLAGS_BEHAVIOR */
+static int batch_flags_out(nbg_ctx *ctx, CopyBatch &b, const void *mapped, const unsigned *src, ll n, int op)
+{
+    if (n <= 0) return NBG_OK;
+    if (b.n == NBG_COPY_BATCH) {
+        int rc = batch_flush(ctx, b);
+        if (rc != NBG_OK) return rc;
+    }
+    b.dst[b.n] = const_cast<void *>(mapped);
+    b.src[b.n] = src;
+    b.bytes[b.n] = n * (ll)sizeof(unsigned);
+    b.op[b.n] = op;
     b.n++;
     return NBG_OK;
 }
@@ -821,14 +851,22 @@ int nbg_get_state(nbg_ctx *ctx, nbg_soa *h, int64_t cap, int64_t *n_out)
 #undef GETD
     if ((rc = batch_copy(ctx, cb, (ll *)h->id, (const ll *)A.id, n, 1)) != NBG_OK) return rc;
     if ((rc = batch_copy(ctx, cb, (ll *)h->frag_fragments, (const ll *)A.fr_cnt, n, 1)) != NBG_OK) return rc;
-    if (h->flags || h->collision) {
+    /* pinned outputs take their flag fields straight from the copy kernel;
+     * otherwise the words go through pinned staging and are split here */
+    const void *mf = h->flags && n > 0 ? mapped_host(h->flags) : nullptr;
+    const void *mc = h->collision && n > 0 ? mapped_host(h->collision) : nullptr;
+    const bool staged = (h->flags && !mf) || (h->collision && !mc);
+    if (staged) {
         if ((rc = ensure_flags_h(ctx, n)) != NBG_OK) return rc;
         if ((rc = batch_copy(ctx, cb, ctx->flags_h, (const unsigned *)A.flags, n, 1)) != NBG_OK) return rc;
+    } else {
+        if (mf && (rc = batch_flags_out(ctx, cb, mf, A.flags, n, COPY_FLAGS_LOW)) != NBG_OK) return rc;
+        if (mc && (rc = batch_flags_out(ctx, cb, mc, A.flags, n, COPY_FLAGS_BEHAVIOR)) != NBG_OK) return rc;
     }
     if ((rc = batch_flush(ctx, cb)) != NBG_OK) return rc;
     CK(cudaStreamSynchronize(ctx->st));
     const unsigned *fl = ctx->flags_h;
-    for (ll k = 0; k < n && (h->flags || h->collision); k++) {
+    for (ll k = 0; k < n && staged; k++) {
         if (h->flags) h->flags[k] = fl[k] & 0xffu;
         if (h->collision) h->collision[k] = (int32_t)NBG_BEHAVIOR(fl[k]);
     }

@@ -43,3 +43,28 @@ def test_pinned_and_pageable_io_agree():
             assert np.array_equal(a.view(np.uint64), c.view(np.uint64)), f
         else:
             assert np.array_equal(a, c), f
+
+
+def test_pinned_flag_fields_every_behaviour():
+    """The flag byte and the collision behaviour reach pinned outputs through
+    the copy kernel's split; a pinned/pageable mix goes through the staging
+    path.  Both equal the pageable read of a collection holding every
+    behaviour after removals and fragments."""
+    torch = pytest.importorskip("torch")
+    from test_gpu_plain_parity import dense_cluster
+
+    sim = Simulation("fp64")
+    sim.set_bodies(dense_cluster(300, seed=11))
+    sim.step(0.01, 1.0, 4)
+    ref = sim.state()
+    assert len(set(ref["collision"].tolist())) > 1
+    n = len(ref["x"])
+    out, keep = pinned_copy(torch, A.empty_state(n), extra=8)
+    got = sim.state(out=out)
+    for f in ("flags", "collision", "id", "x"):
+        assert np.array_equal(np.asarray(ref[f]), np.asarray(got[f])), f
+    mixed = dict(out)
+    mixed["collision"] = np.zeros(n + 8, dtype=ref["collision"].dtype)  # pageable
+    got = sim.state(out=mixed)
+    for f in ("flags", "collision"):
+        assert np.array_equal(np.asarray(ref[f]), np.asarray(got[f])), f
