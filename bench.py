@@ -418,11 +418,14 @@ def main():
     counts = sim.sim_counts()
     pinned, keep = pinned_like(torch, st, 4096)
     n_h = len(st["x"])
-    e2e_int, e2e_t, h2d, d2h, e2e_chunks = 0, 0.0, 0, 0, max(1, min(nchunks, 5))
+    e2e_int, e2e_t, h2d, d2h, e2e_chunks = 0, 0.0, 0, 0, max(1, min(nchunks, 10))
     # each call returns once its copies and cycles are done, so the host
     # clock between the calls splits the step into its phases
     phase = {"load": 0.0, "step": 0.0, "read": 0.0}
-    for k in range(e2e_chunks):
+    per_call = []
+    # call 0 is an untimed warm-up of the host path (first use of the pinned
+    # arrays by the copy kernel)
+    for k in range(e2e_chunks + 1):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         host = {f: a[:n_h] for f, a in pinned.items()}
@@ -431,23 +434,27 @@ def main():
         else:
             sim.set_collections_flat(host, counts)
         t1 = time.perf_counter()
-        h2d += sum(a.nbytes for a in host.values())
         info = sim.step(DT, 1.0, chunk)
         t2 = time.perf_counter()
         out = sim.state(out=pinned)
         counts = sim.sim_counts()
         t3 = time.perf_counter()
+        n_h = len(out["x"])
+        per_call.append(round(1e3 * (t3 - t0), 3))
+        if k == 0:
+            continue
+        h2d += sum(a.nbytes for a in host.values())
         phase["load"] += t1 - t0
         phase["step"] += t2 - t1
         phase["read"] += t3 - t2
         e2e_t += t3 - t0
-        n_h = len(out["x"])
         d2h += sum(a.nbytes for a in out.values())
         e2e_int += info["interactions"]
     e2e = {"value": dist.sum(e2e_int) / dist.max(e2e_t), "unit": UNIT,
            "h2d_bytes_per_step": int(h2d // (e2e_chunks * chunk)),
            "d2h_bytes_per_step": int(d2h // (e2e_chunks * chunk)),
            "phases_ms_per_call": {k: round(1e3 * v / e2e_chunks, 3) for k, v in phase.items()},
+           "ms_per_call": per_call[1:], "warmup_call_ms": per_call[0],
            "path": "nbg_set_bodies / nbg_set_collections (full state, pinned host, collections one after another) "
                    "+ nbg_step + nbg_get_state "
                    "(full state)" + (f", {chunk} cycles per call" if chunk > 1 else "")}
