@@ -86,6 +86,8 @@ def parse():
     ap.add_argument("--no-plain", action="store_true", help="skip the FP64 comparison run")
     ap.add_argument("--with-plain", action="store_true",
                     help="run the FP64 comparison on the uniform ball too (one FP64 force pass, ~2 min at 1M bodies)")
+    ap.add_argument("--sort-interval", type=int, default=None,
+                    help="mixed: cycles between Morton sorts of the i-tiles (library default 4)")
     ap.add_argument("--drift-cycles", type=int, default=0,
                     help="after the timed run, step a fresh copy of the workload this many cycles and report the "
                          "relative energy and momentum drift (untimed)")
@@ -367,6 +369,8 @@ def main():
     sim.set_option(A.OPT_GRAPH_CYCLES, chunk)
     if bh:
         sim.set_option(A.OPT_BARNES_HUT, 1)
+    if args.sort_interval is not None:
+        sim.set_option(A.OPT_SORT_INTERVAL, args.sort_interval)
     load(sim, sims)
     tuned = None
     if prec == "mixed" and args.shape is not None:
@@ -581,6 +585,7 @@ def main():
             "config": {"workload": f"{args.workload}: {n0} bodies in {len(sims)} simulation(s) ({desc}), "
                                    f"dt={DT}, {prec} precision",
                        "n_bodies": n0, "n_sims": len(sims), "dt": DT,
+                       "sort_interval": (args.sort_interval or 4) if prec == "mixed" and not bh else None,
                        "l2": "flushed (512 MB write) before every timed cycle"
                              + (" graph" if chunk > 1 else ""), "parallelism": f"replicas x{ws}"},
             "e2e": e2e,

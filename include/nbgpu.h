@@ -318,6 +318,12 @@ int nbg_get_timing(nbg_ctx *ctx, nbg_timing *t);
 #define NBG_OPT_BARNES_HUT 8
 /* mixed Barnes-Hut walk: registers capped for 3, 4 or 5 CTAs per SM (0..2) */
 #define NBG_OPT_BH_SHAPE 9
+/* mixed: cycles between Morton sorts of the i-tiles (1..1000, default 4).
+   Bodies move far less than a tile per cycle, so an older order still gives
+   compact tiles; any change of body indices (compaction, loads, edits) sorts
+   again at the next cycle.  The order affects FP32 rounding, never the event
+   set.  1 sorts every cycle. */
+#define NBG_OPT_SORT_INTERVAL 10
 #define NBG_OPT_NEAR_PPM 5   /* mixed: pairs closer than (value * 1e-6) x the i-body's
                                 distance from its tile origin take the near-pair
                                 pass: the exact hi/lo difference, FP64 for a

@@ -44,6 +44,7 @@ OPT_GRAPH_CYCLES = 6
 OPT_MIX_SHAPE = 7
 OPT_BARNES_HUT = 8
 OPT_BH_SHAPE = 9
+OPT_SORT_INTERVAL = 10
 MIX_SHAPES = 15
 
 _pd = C.POINTER(C.c_double)

@@ -1033,6 +1033,7 @@ __global__ void __launch_bounds__(NBG_SCAN_BLOCK) k_end(DevCtl *ctl, SimSegs seg
     ctl->acc_interactions += ctl->cycle_interactions;
     ctl->n = ctl->n_keep + ctl->frag_total + ctl->n_host_adds;
     ctl->n_host_adds = 0;
+    if (changed) ctl->sort_valid = 0; /* bodies changed index */
     ctl->cycle += 1;
     ctl->acc_steps += 1;
 }

@@ -43,7 +43,7 @@ __device__ __forceinline__ unsigned quant10(float x, float inv_span)
  * its range of positions and is ordered inside it. */
 __global__ void k_morton_keys(BodyArrays A, DevCtl *ctl, SimSegs seg, unsigned *keys, unsigned *vals)
 {
-    if (ctl->error) return;
+    if (ctl->error || !ctl->sort_now) return;
     const ll n = ctl->n;
     const bool multi = seg.nsims > 1;
     for (ll k = (ll)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (ll)gridDim.x * blockDim.x) {
@@ -77,7 +77,7 @@ __global__ void k_morton_keys(BodyArrays A, DevCtl *ctl, SimSegs seg, unsigned *
 __global__ void __launch_bounds__(RS_BLOCK) k_rs_hist(DevCtl *ctl, const unsigned *keys, int shift, ll *hist)
 {
     __shared__ unsigned cnt[RS_BINS];
-    if (ctl->error) return;
+    if (ctl->error || !ctl->sort_now) return;
     const ll n = ctl->n;
     const ll nb = (n + RS_TILE - 1) / RS_TILE;
     const ll b = blockIdx.x;
@@ -133,7 +133,7 @@ __device__ __forceinline__ ll rs_block_incl(ll x, ll *warp_tot, ll *block_total)
 __global__ void __launch_bounds__(1024) k_rs_scan_part(DevCtl *ctl, ll *hist)
 {
     __shared__ ll warp_tot[32];
-    if (ctl->error) return;
+    if (ctl->error || !ctl->sort_now) return;
     const ll total = rs_hist_total(ctl);
     const ll c0 = (ll)blockIdx.x * RS_SCAN_CHUNK;
     if (c0 >= total) return;
@@ -150,7 +150,7 @@ __global__ void __launch_bounds__(1024) k_rs_scan_part(DevCtl *ctl, ll *hist)
 __global__ void __launch_bounds__(1024) k_rs_scan_top(DevCtl *ctl, ll *hist)
 {
     __shared__ ll warp_tot[32];
-    if (ctl->error) return;
+    if (ctl->error || !ctl->sort_now) return;
     const ll total = rs_hist_total(ctl);
     const ll nchunk = (total + RS_SCAN_CHUNK - 1) / RS_SCAN_CHUNK;
     ll *sums = hist + total;
@@ -168,7 +168,7 @@ __global__ void __launch_bounds__(1024) k_rs_scan_top(DevCtl *ctl, ll *hist)
 __global__ void __launch_bounds__(1024) k_rs_scan_fin(DevCtl *ctl, ll *hist)
 {
     __shared__ ll warp_tot[32];
-    if (ctl->error) return;
+    if (ctl->error || !ctl->sort_now) return;
     const ll total = rs_hist_total(ctl);
     const ll c0 = (ll)blockIdx.x * RS_SCAN_CHUNK;
     if (c0 >= total) return;
@@ -196,7 +196,7 @@ __global__ void __launch_bounds__(RS_BLOCK) k_rs_scatter(DevCtl *ctl, const unsi
 {
     __shared__ ll base[RS_BINS];
     __shared__ unsigned wcnt[RS_BLOCK / 32][RS_BINS];
-    if (ctl->error) return;
+    if (ctl->error || !ctl->sort_now) return;
     const ll n = ctl->n;
     const ll nb = (n + RS_TILE - 1) / RS_TILE;
     const ll b = blockIdx.x;
@@ -238,9 +238,28 @@ ll nbg_sort_scratch_hist(ll cap)
     return h + (h + RS_SCAN_CHUNK - 1) / RS_SCAN_CHUNK;
 }
 
-/* Leaves the sorted permutation in cb.perm. */
+/* Whether this cycle sorts.  Bodies move a small fraction of a tile's size
+ * per cycle, so an order a few cycles old still gives compact tiles; which i
+ * a tile holds never changes a result's correctness, only its FP32 error
+ * and the near-pair count.  An order is dropped (sort_valid = 0) whenever a
+ * body changes index or the arrays are replaced: compaction, loads, edits,
+ * reallocation, and a cycle that failed and is run again. */
+__global__ void k_sort_decide(DevCtl *ctl)
+{
+    if (ctl->error) return;
+    const int k = ctl->sort_interval > 0 ? ctl->sort_interval : NBG_SORT_INTERVAL_DEFAULT;
+    const bool now = !ctl->sort_valid || ctl->cycle - ctl->sort_cycle >= (ull)k;
+    ctl->sort_now = now;
+    if (now) {
+        ctl->sort_valid = 1;
+        ctl->sort_cycle = ctl->cycle;
+    }
+}
+
+/* Leaves the sorted permutation in cb.perm (when this cycle sorts). */
 void nbg_launch_spatial_sort(const CycleBufs &cb, DevCtl *ctl, cudaStream_t st)
 {
+    k_sort_decide<<<1, 1, 0, st>>>(ctl);
     const int g = (int)((cb.cap + 255) / 256 < 152 * 16 ? (cb.cap + 255) / 256 : 152 * 16);
     k_morton_keys<<<g > 0 ? g : 1, 256, 0, st>>>(cb.a, ctl, cb.seg, cb.skey[0], cb.perm);
     const int nb = (int)((cb.cap + RS_TILE - 1) / RS_TILE);

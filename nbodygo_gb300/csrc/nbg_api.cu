@@ -134,6 +134,7 @@ __global__ void k_set_loaded(DevCtl *ctl, ll n)
 {
     ctl->n = n;
     ctl->n_host_adds = 0;
+    ctl->sort_valid = 0;
 }
 
 __global__ void k_fill_f64(double *p, ll n, double v)
@@ -235,6 +236,16 @@ static ll part_need(const nbg_ctx *ctx, ll cap)
     return NBG_PART_DOUBLES(cap, (ll)ctx->cb.slots * NBG_MIX_CHUNKS_PER_CTA, itile);
 }
 
+/* The mixed path's Morton order no longer matches the bodies: the arrays
+ * were replaced, or bodies were edited or moved from the host. */
+static int drop_order(nbg_ctx *ctx)
+{
+    static const int zero = 0;
+    if (!ctx->ctl) return NBG_OK;
+    CK(cudaMemcpyAsync(&ctx->ctl->sort_valid, &zero, sizeof zero, cudaMemcpyHostToDevice, ctx->st));
+    return NBG_OK;
+}
+
 static int ensure_cap(nbg_ctx *ctx, ll need, ll keep)
 {
     if (need <= ctx->cb.cap) return NBG_OK;
@@ -278,6 +289,8 @@ static int ensure_cap(nbg_ctx *ctx, ll need, ll keep)
     CK(cudaMalloc((void **)&ctx->cb.shist, (size_t)nbg_sort_scratch_hist(cap) * sizeof(ll)));
     ctx->cb.cap = cap;
     invalidate_graph(ctx);
+    int rc = drop_order(ctx);
+    if (rc != NBG_OK) return rc;
     if (ctx->cb.bh) return ensure_bh(ctx, 0);
     return NBG_OK;
 }
@@ -919,6 +932,7 @@ int nbg_apply_edits(nbg_ctx *ctx, const nbg_edit *edits, int64_t k, int32_t *res
     CK(cudaMemcpyAsync(ed, edits, eb, cudaMemcpyHostToDevice, ctx->st));
     CK(cudaMemsetAsync(res, 0, rb, ctx->st));
     nbg_launch_edits(ctx->cb, ctx->ctl, ed, k, res, ctx->st);
+    if ((rc = drop_order(ctx)) != NBG_OK) return rc;
     CK(cudaGetLastError());
     std::vector<int> hr((size_t)k);
     CK(cudaMemcpyAsync(hr.data(), res, rb, cudaMemcpyDeviceToHost, ctx->st));
@@ -937,6 +951,7 @@ int nbg_remove_bodies(nbg_ctx *ctx, int64_t count, int64_t *removed)
     int rc = ensure_scratch(ctx, sizeof(ll));
     if (rc != NBG_OK) return rc;
     nbg_launch_remove(ctx->cb, ctx->ctl, count, (ll *)ctx->scratch, ctx->st);
+    if ((rc = drop_order(ctx)) != NBG_OK) return rc;
     CK(cudaGetLastError());
     ll r = 0;
     CK(cudaMemcpyAsync(&r, ctx->scratch, sizeof r, cudaMemcpyDeviceToHost, ctx->st));
@@ -1036,11 +1051,12 @@ static void launch_cycle(nbg_ctx *ctx, int precision, long ev_base)
     nbg_launch_after_pair(cb, ctx->ctl, st);
     if (ev_base >= 0) cudaEventRecord(get_event(ctx, (size_t)ev_base + 3), st);
     /* begin, fragment count + scan, 10 after the pair kernel, and the pair
-     * kernel; mixed adds reduce, 21 sort, pack, tile origins, i-body set-up
-     * and the output;
+     * kernel; mixed adds reduce, the sort decision and 21 sort launches
+     * (which return at once in cycles that keep the order), pack, tile
+     * origins, i-body set-up and the output;
      * Barnes-Hut replaces the pair kernel with 55 (k_bh.cu) */
     ctx->launches_per_cycle = (cb.bh ? 13 + 55 + (precision == NBG_PRECISION_MIXED ? 1 : 0)
-                                     : precision == NBG_PRECISION_MIXED ? 40 : 13 + nbg_pair_fp64_launches(cb)) +
+                                     : precision == NBG_PRECISION_MIXED ? 41 : 13 + nbg_pair_fp64_launches(cb)) +
                               (cb.ring_head ? 1 : 0);
 }
 
@@ -1140,6 +1156,8 @@ int nbg_step(nbg_ctx *ctx, double dt, double R, int nsteps, nbg_step_info *info)
         h->error = 0;
         int z = 0;
         CK(cudaMemcpyAsync(&ctx->ctl->error, &z, sizeof z, cudaMemcpyHostToDevice, ctx->st));
+        /* the failed cycle may have claimed a sort it never finished */
+        if ((rc = drop_order(ctx)) != NBG_OK) return rc;
     }
     if (info) {
         DevCtl *h = ctx->ctl_h;
@@ -1164,6 +1182,10 @@ int nbg_force_pass(nbg_ctx *ctx)
     for (int attempt = 0;; attempt++) {
         int z = 0;
         CK(cudaMemcpyAsync(&ctx->ctl->error, &z, sizeof z, cudaMemcpyHostToDevice, ctx->st));
+        if (attempt > 0) {
+            int rc = drop_order(ctx);
+            if (rc != NBG_OK) return rc;
+        }
         nbg_launch_begin(ctx->cb, ctx->ctl, ctx->st);
         if (ctx->cb.bh) {
             nbg_launch_bh(ctx->cb, ctx->ctl, ctx->st, ctx->precision == NBG_PRECISION_MIXED);
@@ -1448,6 +1470,11 @@ int nbg_set_option(nbg_ctx *ctx, int key, int64_t value)
             invalidate_graph(ctx);
         }
         return NBG_OK;
+    case NBG_OPT_SORT_INTERVAL: {
+        if (value < 1 || value > 1000) return fail(ctx, NBG_E_ARG, "sort interval must be 1..1000 cycles");
+        const int k = (int)value;
+        return ctl_put(ctx, offsetof(DevCtl, sort_interval), &k, sizeof k);
+    }
     case NBG_OPT_NEAR_PPM: {
         if (value < 0 || value > 10000000) return fail(ctx, NBG_E_ARG, "near radius factor out of range");
         float kappa = (float)((double)value * 1e-6);

@@ -88,7 +88,17 @@ struct DevCtl {
     ull bh_rmax;
     unsigned bh_next; /* the walk's next 32-body group (one per warp) */
     unsigned pad2;
+    /* Morton order of the mixed path (perm): valid while no body changed
+     * index; re-sorted when invalid or sort_interval cycles after the last
+     * sort (0: NBG_SORT_INTERVAL_DEFAULT).  sort_now is this cycle's verdict. */
+    int sort_valid;
+    int sort_now;
+    int sort_interval;
+    int pad3;
+    ull sort_cycle;
 };
+
+#define NBG_SORT_INTERVAL_DEFAULT 4
 
 /* A collection may hold several independent simulations stored one after
  * another: sim s occupies bodies [off[s], off[s+1]) and bodies of different

@@ -161,3 +161,64 @@ def test_every_kernel_shape_gives_the_same_physics():
     ora = OracleSim(threads=8)
     ora.set_bodies(big)
     assert rel_l2(sim.force_pass(), ora.forces()) <= TOL
+
+
+def fp64_forces_by_id(pre, ids):
+    """FP64 force pass on the state `pre`, as (3, len(ids)) for the bodies
+    `ids` (all of which are in `pre`)."""
+    ref = Simulation("fp64")
+    ref.set_bodies(pre)
+    f = np.array(ref.force_pass())
+    ref.close()
+    order = np.argsort(pre["id"])
+    at = order[np.searchsorted(pre["id"], ids, sorter=order)]
+    return f[:, at]
+
+
+def step_and_check(sim, cycles, dt, tol=TOL):
+    """Each cycle: the mixed forces it computed (read from the state after
+    it) against FP64 forces of the state before it, body by body (by id;
+    bodies a cycle created have no reference and are skipped).  Returns the
+    bodies removed over the cycles."""
+    removed = 0
+    for _ in range(cycles):
+        pre = sim.state()
+        info = sim.step(dt, 1.0, 1)
+        removed += info["removed"]
+        post = sim.state()
+        keep = np.isin(post["id"], pre["id"]) & live(post)
+        ids = post["id"][keep]
+        got = np.array([post["fx"][keep], post["fy"][keep], post["fz"][keep]])
+        exp = fp64_forces_by_id(pre, ids)
+        err = rel_l2(got, exp)
+        assert err <= tol, f"rel L2 {err:.3e}"
+    return removed
+
+
+@pytest.mark.parametrize("interval", [1, 8, 1000])
+def test_sort_interval_keeps_forces_accurate(interval):
+    """Cycles that keep an older Morton order (the bodies have moved since)
+    stay within the FP64 tolerance."""
+    b = W.plummer_disk(2048, seed=21)
+    sim = Simulation("mixed")
+    sim.set_option(A.OPT_SORT_INTERVAL, interval)
+    sim.set_bodies(b)
+    step_and_check(sim, 10, 0.5)
+
+
+def test_sort_interval_resorts_after_compaction_and_edits():
+    """With a 1000-cycle interval, compaction (merged bodies) and a host edit
+    that moves a body far away each force a new order: a stale permutation
+    would pair forces with the wrong bodies.  No fragmentation here: a cycle
+    emits fragments and shrinks their parents before its pair pass, so its
+    forces belong to a state that is never read back."""
+    sim = Simulation("mixed", seed=3)
+    sim.set_option(A.OPT_SORT_INTERVAL, 1000)
+    sim.set_bodies(dense_cluster(400, seed=31, behaviors=(A.NONE, A.SUBSUME, A.ELASTIC)))
+    removed = step_and_check(sim, 6, 0.05)
+    assert removed > 0
+    st = sim.state()
+    sim.apply_edits([dict(id=int(st["id"][5]), mask=A.M_X | A.M_Y, x=5000.0, y=-4000.0)])
+    step_and_check(sim, 2, 0.05)
+    with pytest.raises(Exception):
+        sim.set_option(A.OPT_SORT_INTERVAL, 0)
