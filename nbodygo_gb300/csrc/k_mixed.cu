@@ -493,9 +493,10 @@ k_pair_mixed(BodyArrays A, DevCtl *ctl, SimSegs seg, const float4 *__restrict__ 
                 mn[k] = 3.0e38f;
             }
             /* the j pairs this tile holds (a segment's last tile is short) */
+            /* j pairs of this tile that hold bodies: JP, except in a
+             * segment's short last tile */
             const int jpv = je - jt >= JT ? JP : (int)((je - jt + 1) / 2);
-#pragma unroll UNROLL
-            for (int pp = 0; pp < jpv; pp++) {
+            auto pair_step = [&](int pp) {
                 const float4 a = sA[pp], b = sB[pp];
                 const float2 xj = make_float2(a.x, a.y), yj = make_float2(a.z, a.w);
                 const float2 zj = make_float2(b.x, b.y), mj = make_float2(b.z, b.w);
@@ -516,6 +517,13 @@ k_pair_mixed(BodyArrays A, DevCtl *ctl, SimSegs seg, const float4 *__restrict__ 
                     ay[k] = __ffma2_rn(s, dy, ay[k]);
                     az[k] = __ffma2_rn(s, dz, az[k]);
                 }
+            };
+            /* a full tile keeps a constant trip count for the unroller */
+            if (jpv == JP) {
+#pragma unroll UNROLL
+                for (int pp = 0; pp < JP; pp++) pair_step(pp);
+            } else {
+                for (int pp = 0; pp < jpv; pp++) pair_step(pp);
             }
 #pragma unroll
             for (int k = 0; k < K; k++) {
