@@ -246,33 +246,64 @@ def load(sim, sims):
         sim.set_collections(sims)
 
 
-def cpu_baseline_sample(workload, dt):
-    """CPU restatement of the reference cycle, all host threads, on a sample."""
+def cpu_sample(workload):
+    """(list of body sets, description): the bounded sample of a workload that
+    the CPU restatement is timed on, drawn from the workload's own generator."""
     from nbodygo_gb300 import workloads as W
+
+    if workload == "plummer_disk":
+        return [W.plummer_disk(n_each=16384, seed=3)], "plummer_disk with 32,768 bodies"
+    if workload == "ensemble":
+        sims, total = [], 0
+        for b in W.ensemble(seed=5):
+            if sims and total + len(b["x"]) > 49152:
+                continue
+            sims.append(b)
+            total += len(b["x"])
+            if total >= 32768:
+                break
+        return sims, f"{len(sims)} collections of the ensemble, {total:,} bodies"
+    if workload == "uniform":
+        return [W.uniform_ball(32768, seed=4)], "uniform ball of the same radius with 32,768 bodies"
+    if workload == "plummer":
+        return [W.plummer(seed=2)], "plummer with 16,384 bodies (the full workload)"
+    if "_bh" in workload:
+        return [W.plummer(32768, seed=2)], ("plummer with 32,768 bodies, Barnes-Hut (the reference's octree, "
+                                            "built once per cycle)")
+    return [W.disk(seed=1)], "disk with 1,000 bodies (the full workload)"
+
+
+def cpu_cycles(workload, dt, warmup, steps):
+    """Times `steps` cycles of the CPU restatement on every body set of the
+    workload's sample, all host threads: (interactions, seconds, cycles per
+    set, description)."""
     from oracle.oracle import OracleSim
 
+    sets, what = cpu_sample(workload)
     cores = os.cpu_count() or 1
-    if workload in ("plummer_disk", "ensemble", "uniform"):
-        b = W.plummer_disk(n_each=16384, seed=3)
-        what = "plummer_disk with 32768 bodies"
-    elif workload == "plummer":
-        b = W.plummer(seed=2)
-        what = "plummer with 16384 bodies (the full workload)"
-    elif workload.endswith("_bh") or workload.endswith("_bh_mixed"):
-        b = W.plummer(32768, seed=2)
-        what = "plummer with 32768 bodies, Barnes-Hut (the reference's octree, built once per cycle)"
-    else:
-        b = W.disk(seed=1)
-        what = "disk with 1000 bodies (the full workload)"
-    o = OracleSim(threads=cores)
-    if "_bh" in workload:
-        o.set_barnes_hut(True)
-    o.set_bodies(b)
-    steps = 1 if len(b["x"]) > 10000 else 20
-    t0 = time.perf_counter()
-    info = o.step(dt, 1.0, steps)
-    t = time.perf_counter() - t0
-    return {"value": info["interactions"] / t, "unit": UNIT, "cores": cores, "kind": "port",
+    inter, t = 0, 0.0
+    for b in sets:
+        o = OracleSim(threads=cores)
+        if "_bh" in workload:
+            o.set_barnes_hut(True)
+        o.set_bodies(b)
+        for _ in range(warmup):
+            o.step(dt, 1.0, 1)
+        for _ in range(steps):
+            t0 = time.perf_counter()
+            info = o.step(dt, 1.0, 1)
+            t += time.perf_counter() - t0
+            inter += info["interactions"]
+    return inter, t, what
+
+
+def cpu_baseline_sample(workload, dt):
+    """CPU restatement of the reference cycle, all host threads, on a sample."""
+    cores = os.cpu_count() or 1
+    sets, _ = cpu_sample(workload)
+    steps = 1 if sum(len(b["x"]) for b in sets) > 10000 else 20
+    inter, t, what = cpu_cycles(workload, dt, 0, steps)
+    return {"value": inter / t, "unit": UNIT, "cores": cores, "kind": "port",
             "sample": f"{what}, {steps} cycle(s), {t:.2f} s; C restatement of the reference's Go cycle (oracle/)"}
 
 
@@ -280,45 +311,21 @@ def run_reference(args, ws, rank):
     """--impl reference: the CPU restatement, timed per cycle on a sample."""
     if rank != 0:
         return 0
-    from nbodygo_gb300 import workloads as W
-    from oracle.oracle import OracleSim
-
     prec, dt, desc = WORKLOADS[args.workload]
     cores = os.cpu_count() or 1
-    if args.workload in ("plummer_disk", "ensemble", "uniform"):
-        b = W.plummer_disk(n_each=16384, seed=3)
-        sample = "plummer_disk with 32,768 bodies per cycle"
-    elif args.workload == "plummer":
-        b = W.plummer(seed=2)
-        sample = "the full plummer workload (16,384 bodies)"
-    elif "_bh" in args.workload:
-        b = W.plummer(32768, seed=2)
-        sample = "plummer with 32,768 bodies per cycle, Barnes-Hut"
-    else:
-        b = W.disk(seed=1)
-        sample = "the full disk workload (1,000 bodies)"
-    o = OracleSim(threads=cores)
-    if "_bh" in args.workload:
-        o.set_barnes_hut(True)
-    o.set_bodies(b)
-    for _ in range(args.warmup):
-        o.step(dt, 1.0, 1)
-    total_int, total_t = 0, 0.0
-    for _ in range(args.steps):
-        t0 = time.perf_counter()
-        info = o.step(dt, 1.0, 1)
-        total_t += time.perf_counter() - t0
-        total_int += info["interactions"]
+    sets, _ = cpu_sample(args.workload)
+    n = int(sum(len(b["x"]) for b in sets))
+    total_int, total_t, sample = cpu_cycles(args.workload, dt, args.warmup, args.steps)
     v = total_int / total_t
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total_t / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic",
-            "config": {"workload": f"{args.workload} sample: {len(b['x'])} bodies ({desc})",
-                       "n_bodies": int(len(b["x"])), "dt": dt},
+            "config": {"workload": f"{args.workload} sample: {n} bodies in {len(sets)} collection(s) ({desc})",
+                       "n_bodies": n, "dt": dt},
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
-                             "sample": f"{sample}; the C restatement of the reference's Go cycle (oracle/) "
-                                       "with the worker-pool slicing"},
+                             "sample": f"{sample} per cycle; the C restatement of the reference's Go cycle "
+                                       "(oracle/) with the worker-pool slicing"},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     return 0
