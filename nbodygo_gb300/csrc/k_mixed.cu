@@ -379,8 +379,8 @@ k_pair_mixed(BodyArrays A, DevCtl *ctl, SimSegs seg, const float4 *__restrict__ 
     __syncthreads();
     if (chunk >= C) break;
     /* this chunk's units [U, U1): a run of (i-tile, j-range) segments */
-    ll U = chunk * W / C;
-    const ll U1 = (chunk + 1) * W / C;
+    ll U = nbg_chunk_start(chunk, C, W);
+    const ll U1 = nbg_chunk_start(chunk + 1, C, W);
     int sim = U < W ? nbg_sim_of(seg.item_off, seg.nsims, U) : 0;
     while (U < U1) {
         while (seg.item_off[sim + 1] <= U) sim++; /* past the end of a sim (or an empty one) */

@@ -233,13 +233,47 @@ struct MixVariantInfo {
 #define NBG_MIX_MIN_WORK 2048
 #define NBG_MIX_CHUNKS_PER_CTA 32
 
+/* floor(a b / c) for 0 <= a, 0 < c, without forming a b */
+__host__ __device__ __forceinline__ ll nbg_mul_div(ll a, ll b, ll c)
+{
+    return a * (b / c) + a * (b % c) / c;
+}
+
 /* The mixed pair work of a cycle is W units, (i-tile, j-body) pairs in sim,
- * i-tile, j order, cut into C equal chunks: chunk c is units
- * [c W / C, (c + 1) W / C).  Persistent CTAs take chunks from an atomic
- * counter.  This is the chunk that holds unit u. */
+ * i-tile, j order, cut into C chunks that persistent CTAs take from an
+ * atomic counter.  The cut is guided: the first C/4 chunks split the first
+ * three quarters of the work evenly and the other chunks the last quarter,
+ * so the chunks still running when the counter runs out are a ninth of the
+ * first ones and the CTAs finish close together.  The boundaries depend on
+ * C and W alone, never on timing.  With C >= 4 and W >= 2048 C every chunk
+ * holds work.  This is the first unit of chunk c (c = C gives W). */
+__host__ __device__ __forceinline__ ll nbg_chunk_start(ll c, int C, ll W)
+{
+    const int C1 = C / 4;
+    const ll W1 = C1 > 0 ? W - W / 4 : 0;
+    if (c <= C1) return C1 > 0 ? nbg_mul_div(c, W1, C1) : 0;
+    return W1 + nbg_mul_div(c - C1, W - W1, C - C1);
+}
+
+/* the chunk that holds unit u (0 <= u < W) */
 __host__ __device__ __forceinline__ int nbg_work_chunk(ll u, int C, ll W)
 {
-    return (int)(((u + 1) * (ll)C + W - 1) / W - 1);
+    const int C1 = C / 4;
+    const ll W1 = C1 > 0 ? W - W / 4 : 0;
+    ll c0, c1;
+    if (u < W1) {
+        c0 = (ll)((double)u * C1 / (double)W1);
+        c0 = c0 < 0 ? 0 : (c0 > C1 - 1 ? C1 - 1 : c0);
+        c1 = C1 - 1;
+    } else {
+        c0 = C1 + (ll)((double)(u - W1) * (C - C1) / (double)(W - W1));
+        c0 = c0 < C1 ? C1 : (c0 > C - 1 ? C - 1 : c0);
+        c1 = C - 1;
+    }
+    /* the estimate is off by at most one either way */
+    while (c0 > 0 && nbg_chunk_start(c0, C, W) > u) c0--;
+    while (c0 < c1 && nbg_chunk_start(c0 + 1, C, W) <= u) c0++;
+    return (int)c0;
 }
 
 /* Partial sums of the mixed pair kernel: chunk c's share of i-tile g (global
