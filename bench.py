@@ -86,6 +86,8 @@ def parse():
     ap.add_argument("--no-plain", action="store_true", help="skip the FP64 comparison run")
     ap.add_argument("--with-plain", action="store_true",
                     help="run the FP64 comparison on the uniform ball too (one FP64 force pass, ~2 min at 1M bodies)")
+    ap.add_argument("--near-ppm", type=int, default=None,
+                    help="mixed: near-pair radius factor in parts per million (library default 35000)")
     ap.add_argument("--sort-interval", type=int, default=None,
                     help="mixed: cycles between Morton sorts of the i-tiles (library default 4)")
     ap.add_argument("--drift-cycles", type=int, default=0,
@@ -378,6 +380,8 @@ def main():
         sim.set_option(A.OPT_BARNES_HUT, 1)
     if args.sort_interval is not None:
         sim.set_option(A.OPT_SORT_INTERVAL, args.sort_interval)
+    if args.near_ppm is not None:
+        sim.set_option(A.OPT_NEAR_PPM, args.near_ppm)
     load(sim, sims)
     tuned = None
     if prec == "mixed" and args.shape is not None:
@@ -490,6 +494,8 @@ def main():
         force_ms = pe0.elapsed_time(pe1)
         mixed0 = Simulation("mixed", device=local, capacity=n0 + 4096)
         mixed0.set_stream(stream.cuda_stream)
+        if args.near_ppm is not None:
+            mixed0.set_option(A.OPT_NEAR_PPM, args.near_ppm)
         load(mixed0, sims)
         fm = mixed0.force_pass()
         num = np.sqrt(sum(np.sum((a - b) ** 2) for a, b in zip(fm, fp)))

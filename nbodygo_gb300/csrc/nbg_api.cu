@@ -651,7 +651,7 @@ int nbg_create(int device, int precision, int64_t capacity, nbg_ctx **out)
         }
         memset(ctx->ctl_h, 0, sizeof(DevCtl));
         ctx->ctl_h->seed = 0x6e626f6479676f31ull;
-        ctx->ctl_h->near_kappa = 0.07f;
+        ctx->ctl_h->near_kappa = NBG_NEAR_KAPPA_DEFAULT;
         if (cudaMemcpy(ctx->ctl, ctx->ctl_h, sizeof(DevCtl), cudaMemcpyHostToDevice) != cudaSuccess) {
             rc = fail(ctx, NBG_E_CUDA, "control block upload failed");
             break;

@@ -100,6 +100,10 @@ struct DevCtl {
 
 #define NBG_SORT_INTERVAL_DEFAULT 4
 
+/* mixed: pairs closer than this factor x the i-body's distance from its
+ * tile origin take the near-pair pass (NBG_OPT_NEAR_PPM changes it) */
+#define NBG_NEAR_KAPPA_DEFAULT 0.035f
+
 /* A collection may hold several independent simulations stored one after
  * another: sim s occupies bodies [off[s], off[s+1]) and bodies of different
  * sims never interact.  Events, fragments and adds stay inside their sim, so

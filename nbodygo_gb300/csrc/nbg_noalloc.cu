@@ -133,7 +133,7 @@ extern "C" int nbg_forces_mixed_noalloc(const double *x, const double *y, const 
     cb.seg = nbg_seg_carve(base + OFF_SEG, 1);
     DevCtl *ctl = (DevCtl *)(base + OFF_CTL);
 
-    k_noalloc_init<<<1, 1, 0, st>>>(ctl, cb.seg, (ll)n, 0.07f);
+    k_noalloc_init<<<1, 1, 0, st>>>(ctl, cb.seg, (ll)n, NBG_NEAR_KAPPA_DEFAULT);
     nbg_launch_begin(cb, ctl, st); /* work layout of the one collection */
     nbg_launch_mixed_prep(cb, ctl, st);
     nbg_launch_mixed_pair(cb, ctl, st);

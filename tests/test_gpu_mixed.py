@@ -130,13 +130,13 @@ def test_near_pairs_in_fp64_keep_error_down():
     ora.set_bodies(b)
     g = ora.forces()
     errs = {}
-    for ppm in (0, 70000):
+    for ppm in (0, 35000, 70000):  # off, the default, twice the default
         sim = Simulation("mixed")
         sim.set_option(A.OPT_NEAR_PPM, ppm)
         sim.set_bodies(b)
         errs[ppm] = rel_l2(sim.force_pass(), g)
-    assert errs[70000] <= TOL
-    assert errs[70000] <= errs[0]
+    assert errs[35000] <= TOL and errs[70000] <= TOL
+    assert errs[70000] <= errs[35000] <= errs[0]
 
 
 def test_every_kernel_shape_gives_the_same_physics():
