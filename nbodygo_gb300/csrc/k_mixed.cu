@@ -23,10 +23,12 @@
  *    is the reference's, and the force of every near pair is FP64.
  *
  * The pair work of a cycle, W units of (i-tile, one j-body), is cut into C
- * equal chunks, about 32 per resident CTA, whatever the sizes of the sims and
- * tiles; a chunk is a run of (i-tile, j-range) segments.  Persistent CTAs
+ * chunks, about 32 per resident CTA, whatever the sizes of the sims and
+ * tiles; a chunk is a run of (i-tile, j-range) segments.  The cut is guided
+ * (nbg_chunk_start): large chunks first, small ones last.  Persistent CTAs
  * take chunks from an atomic counter, so a CTA that meets many near pairs
- * simply takes fewer.  Each chunk writes its share of an i-tile to a slot of
+ * simply takes fewer, and the small last chunks let the CTAs finish
+ * together.  Each chunk writes its share of an i-tile to a slot of
  * its own, and k_mix_out adds the shares in chunk order, so results do not
  * depend on scheduling.
  */
