@@ -324,17 +324,27 @@ int nbg_get_timing(nbg_ctx *ctx, nbg_timing *t);
    again at the next cycle.  The order affects FP32 rounding, never the event
    set.  1 sorts every cycle. */
 #define NBG_OPT_SORT_INTERVAL 10
+/* plain form, one collection: up to this capacity (default 65536) the pair
+   terms of all (i, j) are computed at once and each body adds its own in j
+   order; above it one thread walks each body's j.  Identical results; the
+   first keeps the FP64 pipes busy when there are few bodies, at the cost of
+   a 48 MB-per-thousand-bodies term buffer. */
+#define NBG_OPT_P64_SPLIT_MAX 11
 #define NBG_OPT_NEAR_PPM 5   /* mixed: pairs closer than (value * 1e-6) x the i-body's
                                 distance from its tile origin take the near-pair
                                 pass: the exact hi/lo difference, FP64 for a
                                 possible overlap (default 35000) */
 int nbg_set_option(nbg_ctx *ctx, int key, int64_t value);
 
-/* Autotuner of the mixed pair kernel.  Seven shapes are compiled (threads per
- * CTA x i-bodies per thread x j per shared-memory tile x unroll):
- *   0: 128x4, 256, 2 (default)   1: 128x4, 256, 1   2: 128x2, 256, 2
- *   3: 256x2, 256, 2             4: 128x4, 512, 2   5: 64x4, 256, 2
- *   6: 128x2, 128, 4
+/* Autotuner of the mixed pair kernel.  Fifteen shapes are compiled, each
+ * threads per CTA x i-bodies per thread, j per shared-memory tile, unroll,
+ * CTAs per SM, in three kinds: sums in registers (R), sums in shared memory
+ * (S), and shared memory with two j-tile buffers filled a tile ahead (D):
+ *   0: R 128x4, 256, 2, 3 (default)  1: R 128x4, 256, 1, 3  2: R 128x2, 256, 2, 4
+ *   3: R 256x2, 256, 2, 2            4: R 128x4, 512, 2, 3  5: R 64x4, 256, 2, 6
+ *   6: R 128x2, 128, 4, 4            7: S 128x2, 256, 2, 5  8: S 128x3, 256, 2, 4
+ *   9: S 128x4, 256, 2, 4           10: S 128x4, 128, 4, 4 11: D 128x2, 128, 4, 4
+ *  12: D 128x2, 256, 2, 4           13: D 128x2, 128, 2, 4 14: D 128x4, 128, 2, 3
  * nbg_autotune times the pair kernel of each on the context's current
  * collection (the best of three force passes after one warm-up) and keeps the
  * fastest.  cache_path (may be NULL) names a text file of earlier results

@@ -45,6 +45,7 @@ OPT_MIX_SHAPE = 7
 OPT_BARNES_HUT = 8
 OPT_BH_SHAPE = 9
 OPT_SORT_INTERVAL = 10
+OPT_P64_SPLIT_MAX = 11
 MIX_SHAPES = 15
 
 _pd = C.POINTER(C.c_double)

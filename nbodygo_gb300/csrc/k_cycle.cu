@@ -340,7 +340,9 @@ __global__ void __launch_bounds__(P64_BLOCK) k_pair_fp64(BodyArrays A, DevCtl *c
  * reference skips is stored as +0.0, and adding +0.0 changes no sum here
  * (the sum starts at +0.0 and can never be -0.0).  j runs in passes of jc;
  * the sums are carried between passes in acc.  One collection. */
-#define P64_JS 16 /* j per block of k_p64_terms: more blocks for the few bodies */
+/* j per block of k_p64_terms: many small blocks keep the FP64 pipes fed
+ * (64 measured 2 % slower from 8,192 to 32,768 bodies) */
+#define P64_JS 16
 __global__ void __launch_bounds__(P64_BLOCK) k_p64_terms(BodyArrays A, DevCtl *ctl, double *T, ll cap, ll jc,
                                                          ll jbase, ull *ev_keys, ll ev_cap)
 {
@@ -349,7 +351,7 @@ __global__ void __launch_bounds__(P64_BLOCK) k_p64_terms(BodyArrays A, DevCtl *c
     if (ctl->error) return;
     const ll n = ctl->n;
     const ll j0 = jbase + (ll)blockIdx.y * P64_JS;
-    if (j0 >= n || (ll)blockIdx.x * P64_BLOCK >= n) return;
+    if (j0 >= n || j0 >= jbase + jc || (ll)blockIdx.x * P64_BLOCK >= n) return;
     const ll i = (ll)blockIdx.x * P64_BLOCK + threadIdx.x;
     const ll jl = j0 + threadIdx.x;
     if (threadIdx.x < P64_JS && jl < n) {
@@ -368,7 +370,9 @@ __global__ void __launch_bounds__(P64_BLOCK) k_p64_terms(BodyArrays A, DevCtl *c
     const bool coll_i = (fi & NBG_F_COLLIDED) != 0;
     const unsigned bi = NBG_BEHAVIOR(fi);
     const double gmi = NBG_G * mi;
-    const int cnt = (n - j0) < P64_JS ? (int)(n - j0) : P64_JS;
+    /* this block's j: to the end of the collection and of this pass */
+    const ll jend = jbase + jc < n ? jbase + jc : n;
+    const int cnt = (jend - j0) < P64_JS ? (int)(jend - j0) : P64_JS;
     double *tx = T, *ty = T + jc * cap, *tz = T + 2 * jc * cap;
     for (int t = 0; t < cnt; t++) {
         const ll j = j0 + t;
@@ -1189,7 +1193,7 @@ void nbg_launch_pair_fp64(const CycleBufs &cb, DevCtl *ctl, cudaStream_t st)
     if (cb.p64_terms && cb.seg.nsims == 1) {
         const ll jc = cb.p64_jc;
         const unsigned gi = (unsigned)((cb.cap + P64_BLOCK - 1) / P64_BLOCK);
-        const unsigned gj = (unsigned)(jc / P64_JS);
+        const unsigned gj = (unsigned)((jc + P64_JS - 1) / P64_JS);
         for (ll jbase = 0; jbase < cb.cap; jbase += jc) {
             k_p64_terms<<<dim3(gi, gj), P64_BLOCK, 0, st>>>(cb.a, ctl, cb.p64_terms, cb.cap, jc, jbase, cb.ev_keys,
                                                              cb.ev_cap);

@@ -47,6 +47,7 @@ struct nbg_ctx {
     size_t scratch_bytes = 0;
     ll launches_per_cycle = 0;
     ll bh_cap = 0; /* capacity the Barnes-Hut buffers were sized for */
+    ll p64_split_max = NBG_P64_SPLIT_MAX_CAP; /* plain form: split pair pass up to this capacity */
     void *ring_host = nullptr; /* the caller's render ring, registered here */
     void *seg_mem = nullptr; /* SimSegs arrays */
     int seg_cap = 0;         /* sims the allocation holds */
@@ -275,11 +276,6 @@ static int ensure_cap(nbg_ctx *ctx, ll need, ll keep)
     ll tiles = (cap + NBG_MIX_MIN_ITILE - 1) / NBG_MIX_MIN_ITILE + NBG_MAX_SIMS + 1;
     CK(cudaMalloc((void **)&ctx->cb.tile_c, (size_t)tiles * sizeof(float4)));
     CK(cudaMalloc((void **)&ctx->cb.iprep, (size_t)cap * sizeof(float4)));
-    if (cap <= NBG_P64_SPLIT_MAX_CAP) {
-        ctx->cb.p64_jc = cap < NBG_P64_SPLIT_JC ? cap : NBG_P64_SPLIT_JC;
-        CK(cudaMalloc((void **)&ctx->cb.p64_terms, (size_t)3 * ctx->cb.p64_jc * cap * sizeof(double)));
-        CK(cudaMalloc((void **)&ctx->cb.p64_acc, (size_t)3 * cap * sizeof(double)));
-    }
     ctx->cb.part_doubles = part_need(ctx, cap);
     CK(cudaMalloc((void **)&ctx->cb.part, (size_t)ctx->cb.part_doubles * sizeof(double)));
     CK(cudaMalloc((void **)&ctx->cb.perm, (size_t)cap * sizeof(unsigned)));
@@ -309,6 +305,39 @@ static int ensure_part(nbg_ctx *ctx, ll need)
 }
 
 /* Barnes-Hut buffers for the current capacity and at least `nodes` nodes */
+/* The plain form's split pair pass (k_p64_terms + k_p64_sum) serves one
+ * collection of capacity up to p64_split_max: one thread per body would leave
+ * the FP64 pipes idle below some 64 thousand bodies.  Its term buffer (3 x
+ * 2048 x capacity doubles) is allocated by the first FP64 pass that wants it
+ * and freed when the form, the collection count or the capacity no longer
+ * do.  If it cannot be allocated, the one-thread-per-body kernel runs: the
+ * two give identical results. */
+static int ensure_p64(nbg_ctx *ctx)
+{
+    CycleBufs &cb = ctx->cb;
+    const bool want = ctx->precision == NBG_PRECISION_FP64 && cb.seg.nsims == 1 && !cb.bh && cb.cap > 0 &&
+                      cb.cap <= ctx->p64_split_max;
+    const ll jc = cb.cap < NBG_P64_SPLIT_JC ? cb.cap : NBG_P64_SPLIT_JC;
+    if (want == (cb.p64_terms != nullptr) && (!want || cb.p64_jc == jc)) return NBG_OK;
+    CK(cudaStreamSynchronize(ctx->st));
+    cudaFree(cb.p64_terms);
+    cudaFree(cb.p64_acc);
+    cb.p64_terms = cb.p64_acc = nullptr;
+    cb.p64_jc = 0;
+    invalidate_graph(ctx);
+    if (!want) return NBG_OK;
+    if (cudaMalloc((void **)&cb.p64_terms, (size_t)3 * jc * cb.cap * sizeof(double)) != cudaSuccess ||
+        cudaMalloc((void **)&cb.p64_acc, (size_t)3 * cb.cap * sizeof(double)) != cudaSuccess) {
+        cudaGetLastError();
+        cudaFree(cb.p64_terms);
+        cb.p64_terms = nullptr;
+        cb.p64_acc = nullptr;
+        return NBG_OK;
+    }
+    cb.p64_jc = jc;
+    return NBG_OK;
+}
+
 static int ensure_bh(nbg_ctx *ctx, ll nodes)
 {
     BhTree &t = ctx->cb.t;
@@ -1106,6 +1135,7 @@ int nbg_step(nbg_ctx *ctx, double dt, double R, int nsteps, nbg_step_info *info)
     while (done < nsteps) {
         int rc = ensure_cap(ctx, ctx->n_host + ctx->pending_adds + 1, ctx->n_host);
         if (rc != NBG_OK) return rc;
+        if ((rc = ensure_p64(ctx)) != NBG_OK) return rc;
         const int todo = nsteps - done;
         if (ctx->timing || !ctx->use_graph || todo < ctx->graph_cycles || todo == 1) {
             for (int s = 0; s < todo; s++) launch_cycle(ctx, ctx->precision, ctx->timing ? 4L * s : -1L);
@@ -1179,6 +1209,10 @@ int nbg_force_pass(nbg_ctx *ctx)
     if (!ctx) return NBG_E_ARG;
     CK(cudaSetDevice(ctx->device));
     if (ctx->cb.bh && ctx->cb.seg.nsims != 1) return fail(ctx, NBG_E_STATE, "Barnes-Hut needs a single collection");
+    {
+        int rc = ensure_p64(ctx);
+        if (rc != NBG_OK) return rc;
+    }
     for (int attempt = 0;; attempt++) {
         int z = 0;
         CK(cudaMemcpyAsync(&ctx->ctl->error, &z, sizeof z, cudaMemcpyHostToDevice, ctx->st));
@@ -1469,6 +1503,10 @@ int nbg_set_option(nbg_ctx *ctx, int key, int64_t value)
             ctx->graph_cycles = (int)value;
             invalidate_graph(ctx);
         }
+        return NBG_OK;
+    case NBG_OPT_P64_SPLIT_MAX:
+        if (value < 0 || value > NBG_MAX_BODIES) return fail(ctx, NBG_E_ARG, "split limit must be 0..2^30");
+        ctx->p64_split_max = value;
         return NBG_OK;
     case NBG_OPT_SORT_INTERVAL: {
         if (value < 1 || value > 1000) return fail(ctx, NBG_E_ARG, "sort interval must be 1..1000 cycles");

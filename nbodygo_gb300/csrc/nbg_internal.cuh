@@ -335,7 +335,7 @@ void nbg_launch_find(const CycleBufs &cb, DevCtl *ctl, ll id, ll *idx_dev, cudaS
 int nbg_pair_fp64_grid(ll cap);
 int nbg_pair_fp64_launches(const CycleBufs &cb);
 /* largest capacity the plain form stores its pair terms for */
-#define NBG_P64_SPLIT_MAX_CAP 8192
+#define NBG_P64_SPLIT_MAX_CAP 65536
 #define NBG_P64_SPLIT_JC 2048
 
 /* k_mixed.cu */

@@ -52,10 +52,29 @@ def test_disk_workload_200_cycles_bit_exact():
     assert gi["events"] == oi["events"]
 
 
-def test_plummer_workload_bit_exact():
-    """Workload 1 (N=16,384 Plummer, elastic, dt=0.01): the first cycles."""
+@pytest.mark.parametrize("split_max", [0, 1 << 20])
+def test_plummer_workload_bit_exact(split_max):
+    """Workload 1 (N=16,384 Plummer, elastic, dt=0.01): the first cycles,
+    through the one-thread-per-body kernel and through the split pass."""
     b = W.plummer()
-    run_both(b, 0.01, 1.0, 3)
+    run_both(b, 0.01, 1.0, 3, gpu_opts={A.OPT_P64_SPLIT_MAX: split_max})
+
+
+def test_split_and_direct_pair_passes_agree():
+    """The two plain pair passes on the same collision-heavy cluster: the same
+    events and the same state, bit for bit, cycle after cycle."""
+    b = dense_cluster(3000, seed=17)
+    a = Simulation("fp64", seed=4)
+    a.set_option(A.OPT_P64_SPLIT_MAX, 0)
+    a.set_bodies(b)
+    c = Simulation("fp64", seed=4)
+    c.set_option(A.OPT_P64_SPLIT_MAX, 1 << 20)
+    c.set_bodies(b)
+    for s in range(6):
+        ia, ic = a.step(0.05, 0.9, 1), c.step(0.05, 0.9, 1)
+        assert ia == ic, f"cycle {s}"
+        assert_events_identical(a.events(), c.events(), f"cycle {s}")
+        assert_states_identical(a.state(), c.state(), where=f"cycle {s}")
 
 
 def test_graph_replay_equals_single_cycles():
