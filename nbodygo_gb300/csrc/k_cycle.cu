@@ -340,9 +340,11 @@ __global__ void __launch_bounds__(P64_BLOCK) k_pair_fp64(BodyArrays A, DevCtl *c
  * reference skips is stored as +0.0, and adding +0.0 changes no sum here
  * (the sum starts at +0.0 and can never be -0.0).  j runs in passes of jc;
  * the sums are carried between passes in acc.  One collection. */
-/* j per block of k_p64_terms: many small blocks keep the FP64 pipes fed
- * (64 measured 2 % slower from 8,192 to 32,768 bodies) */
-#define P64_JS 16
+/* P64_JS: j per block of k_p64_terms.  Many small blocks keep the FP64
+ * pipes fed: 16 j (64 measured 2 % slower from 8,192 to 32,768 bodies), and
+ * 4 for capacities up to 8,192, where the whole pass is only a few thousand
+ * warps of long FP64 division chains. */
+template <int P64_JS>
 __global__ void __launch_bounds__(P64_BLOCK) k_p64_terms(BodyArrays A, DevCtl *ctl, double *T, ll cap, ll jc,
                                                          ll jbase, ull *ev_keys, ll ev_cap)
 {
@@ -350,87 +352,137 @@ __global__ void __launch_bounds__(P64_BLOCK) k_p64_terms(BodyArrays A, DevCtl *c
     __shared__ unsigned sf[P64_JS];
     if (ctl->error) return;
     const ll n = ctl->n;
-    const ll j0 = jbase + (ll)blockIdx.y * P64_JS;
-    if (j0 >= n || j0 >= jbase + jc || (ll)blockIdx.x * P64_BLOCK >= n) return;
-    const ll i = (ll)blockIdx.x * P64_BLOCK + threadIdx.x;
-    const ll jl = j0 + threadIdx.x;
-    if (threadIdx.x < P64_JS && jl < n) {
-        sx[threadIdx.x] = A.x[jl];
-        sy[threadIdx.x] = A.y[jl];
-        sz[threadIdx.x] = A.z[jl];
-        sm[threadIdx.x] = A.m[jl];
-        sr[threadIdx.x] = A.rad[jl];
-        sf[threadIdx.x] = A.flags[jl];
-    }
-    __syncthreads();
-    if (i >= n) return;
-    const double xi = A.x[i], yi = A.y[i], zi = A.z[i], mi = A.m[i], ri = A.rad[i];
-    const unsigned fi = A.flags[i];
-    const bool live_i = (fi & NBG_LIVE_MASK) == NBG_F_EXISTS;
-    const bool coll_i = (fi & NBG_F_COLLIDED) != 0;
-    const unsigned bi = NBG_BEHAVIOR(fi);
-    const double gmi = NBG_G * mi;
-    /* this block's j: to the end of the collection and of this pass */
+    /* this pass's j: to the end of the collection and of the pass */
     const ll jend = jbase + jc < n ? jbase + jc : n;
-    const int cnt = (jend - j0) < P64_JS ? (int)(jend - j0) : P64_JS;
+    if (jbase >= jend) return;
+    /* work items (block of 64 i, block of P64_JS j) of the live bodies only:
+     * a grid sized for the capacity would be mostly empty blocks */
+    const ll nib = (n + P64_BLOCK - 1) / P64_BLOCK;
+    const ll items = nib * ((jend - jbase + P64_JS - 1) / P64_JS);
     double *tx = T, *ty = T + jc * cap, *tz = T + 2 * jc * cap;
-    for (int t = 0; t < cnt; t++) {
-        const ll j = j0 + t;
-        const ll slot = (j - jbase) * cap + i;
-        double ex = 0.0, ey = 0.0, ez = 0.0;
-        if (live_i) {
-            const double dx = sx[t] - xi;
-            const double dy = sy[t] - yi;
-            const double dz = sz[t] - zi;
-            const double dist = sqrt(dx * dx + dy * dy + dz * dz);
-            const double rr = ri + sr[t];
-            const unsigned fj = sf[t];
-            const bool live_j = (fj & NBG_LIVE_MASK) == NBG_F_EXISTS;
-            if (live_j && j != i && (coll_i || dist > rr)) {
-                const double force = gmi * sm[t] / (dist * dist);
-                ex = force * dx / dist;
-                ey = force * dy / dist;
-                ez = force * dz / dist;
-            }
-            if (!coll_i && dist <= rr && j != i) {
-                const int type = nbg_detect_event(bi, NBG_BEHAVIOR(fj), ri, sr[t], dist);
-                if (type >= 0) nbg_emit_event(ctl, ev_keys, ev_cap, i, j, type);
-            }
+    for (ll w = blockIdx.x; w < items; w += gridDim.x) {
+        const ll i = (w % nib) * P64_BLOCK + threadIdx.x;
+        const ll j0 = jbase + (w / nib) * P64_JS;
+        const ll jl = j0 + threadIdx.x;
+        __syncthreads(); /* the previous item's readers are done */
+        if (threadIdx.x < P64_JS && jl < jend) {
+            sx[threadIdx.x] = A.x[jl];
+            sy[threadIdx.x] = A.y[jl];
+            sz[threadIdx.x] = A.z[jl];
+            sm[threadIdx.x] = A.m[jl];
+            sr[threadIdx.x] = A.rad[jl];
+            sf[threadIdx.x] = A.flags[jl];
         }
-        tx[slot] = ex;
-        ty[slot] = ey;
-        tz[slot] = ez;
+        __syncthreads();
+        if (i >= n) continue;
+        const double xi = A.x[i], yi = A.y[i], zi = A.z[i], mi = A.m[i], ri = A.rad[i];
+        const unsigned fi = A.flags[i];
+        const bool live_i = (fi & NBG_LIVE_MASK) == NBG_F_EXISTS;
+        const bool coll_i = (fi & NBG_F_COLLIDED) != 0;
+        const unsigned bi = NBG_BEHAVIOR(fi);
+        const double gmi = NBG_G * mi;
+        const int cnt = (jend - j0) < P64_JS ? (int)(jend - j0) : P64_JS;
+        for (int t = 0; t < cnt; t++) {
+            const ll j = j0 + t;
+            const ll slot = (j - jbase) * cap + i; /* a warp's stores are contiguous */
+            double ex = 0.0, ey = 0.0, ez = 0.0;
+            if (live_i) {
+                const double dx = sx[t] - xi;
+                const double dy = sy[t] - yi;
+                const double dz = sz[t] - zi;
+                const double dist = sqrt(dx * dx + dy * dy + dz * dz);
+                const double rr = ri + sr[t];
+                const unsigned fj = sf[t];
+                const bool live_j = (fj & NBG_LIVE_MASK) == NBG_F_EXISTS;
+                if (live_j && j != i && (coll_i || dist > rr)) {
+                    const double force = gmi * sm[t] / (dist * dist);
+                    ex = force * dx / dist;
+                    ey = force * dy / dist;
+                    ez = force * dz / dist;
+                }
+                if (!coll_i && dist <= rr && j != i) {
+                    const int type = nbg_detect_event(bi, NBG_BEHAVIOR(fj), ri, sr[t], dist);
+                    if (type >= 0) nbg_emit_event(ctl, ev_keys, ev_cap, i, j, type);
+                }
+            }
+            tx[slot] = ex;
+            ty[slot] = ey;
+            tz[slot] = ez;
+        }
     }
 }
 
-__global__ void k_p64_sum(BodyArrays A, DevCtl *ctl, const double *T, double *acc, ll cap, ll jc, ll jbase)
+/* Each body adds its terms in j order.  A block takes 32 bodies: all its
+ * threads load a tile of 32 j x 32 bodies (coalesced rows of 32 bodies),
+ * the next tile's loads go out while this one is added, and warp 0 adds each
+ * body's column in j order, so the sums are formed exactly as the
+ * sequential loop forms them. */
+#define SUM_BODIES 32
+#define SUM_J 32
+#define SUM_THREADS 256
+#define SUM_PER_THREAD (3 * SUM_J * SUM_BODIES / SUM_THREADS)
+__global__ void __launch_bounds__(SUM_THREADS) k_p64_sum(BodyArrays A, DevCtl *ctl, const double *T, double *acc,
+                                                         ll cap, ll jc, ll jbase)
 {
+    __shared__ double tile[3][SUM_J][SUM_BODIES];
     if (ctl->error) return;
     const ll n = ctl->n;
     if (jbase >= n && jbase > 0) return;
-    const ll i = (ll)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    double fx = jbase == 0 ? 0.0 : acc[i];
-    double fy = jbase == 0 ? 0.0 : acc[cap + i];
-    double fz = jbase == 0 ? 0.0 : acc[2 * cap + i];
     const ll je = jbase + jc < n ? jbase + jc : n;
-    const double *tx = T, *ty = T + jc * cap, *tz = T + 2 * jc * cap;
-    for (ll j = jbase; j < je; j++) {
-        const ll slot = (j - jbase) * cap + i;
-        fx += tx[slot];
-        fy += ty[slot];
-        fz += tz[slot];
-    }
-    if (je >= n) {
-        if ((A.flags[i] & NBG_LIVE_MASK) == NBG_F_EXISTS) {
-            A.fx[i] = fx;
-            A.fy[i] = fy;
-            A.fz[i] = fz;
+    const ll cnt = je - jbase;
+    const int tid = threadIdx.x;
+    for (ll i0 = (ll)blockIdx.x * SUM_BODIES; i0 < n; i0 += (ll)gridDim.x * SUM_BODIES) {
+        const ll i = i0 + (tid & (SUM_BODIES - 1));
+        double f[3] = {0.0, 0.0, 0.0};
+        if (tid < SUM_BODIES && jbase > 0 && i < n) {
+            f[0] = acc[i];
+            f[1] = acc[cap + i];
+            f[2] = acc[2 * cap + i];
         }
-    } else {
-        acc[i] = fx;
-        acc[cap + i] = fy;
-        acc[2 * cap + i] = fz;
+        /* element e of a tile: component e / 1024, row (e / 32) % 32, body e % 32 */
+        double r[SUM_PER_THREAD];
+        auto load = [&](ll jt) {
+#pragma unroll
+            for (int q = 0; q < SUM_PER_THREAD; q++) {
+                const int e = tid + q * SUM_THREADS;
+                const int c = e / (SUM_J * SUM_BODIES), row = (e / SUM_BODIES) % SUM_J, b = e % SUM_BODIES;
+                const ll j = jt + row, ib = i0 + b;
+                r[q] = (j < cnt && ib < n) ? T[(ll)c * jc * cap + j * cap + ib] : 0.0;
+            }
+        };
+        load(0);
+        for (ll jt = 0; jt < cnt; jt += SUM_J) {
+            __syncthreads(); /* the previous tile is added */
+#pragma unroll
+            for (int q = 0; q < SUM_PER_THREAD; q++) {
+                const int e = tid + q * SUM_THREADS;
+                tile[e / (SUM_J * SUM_BODIES)][(e / SUM_BODIES) % SUM_J][e % SUM_BODIES] = r[q];
+            }
+            __syncthreads();
+            if (jt + SUM_J < cnt) load(jt + SUM_J);
+            if (tid < SUM_BODIES) {
+                const int m = cnt - jt < SUM_J ? (int)(cnt - jt) : SUM_J;
+                for (int t = 0; t < m; t++) {
+                    f[0] += tile[0][t][tid];
+                    f[1] += tile[1][t][tid];
+                    f[2] += tile[2][t][tid];
+                }
+            }
+        }
+        if (tid < SUM_BODIES && i < n) {
+            if (je >= n) {
+                if ((A.flags[i] & NBG_LIVE_MASK) == NBG_F_EXISTS) {
+                    A.fx[i] = f[0];
+                    A.fy[i] = f[1];
+                    A.fz[i] = f[2];
+                }
+            } else {
+                acc[i] = f[0];
+                acc[cap + i] = f[1];
+                acc[2 * cap + i] = f[2];
+            }
+        }
+        __syncthreads(); /* the tile is free for the next bodies */
     }
 }
 
@@ -1192,13 +1244,23 @@ void nbg_launch_pair_fp64(const CycleBufs &cb, DevCtl *ctl, cudaStream_t st)
 {
     if (cb.p64_terms && cb.seg.nsims == 1) {
         const ll jc = cb.p64_jc;
-        const unsigned gi = (unsigned)((cb.cap + P64_BLOCK - 1) / P64_BLOCK);
-        const unsigned gj = (unsigned)((jc + P64_JS - 1) / P64_JS);
+        /* a grid-stride loop over the live bodies' work items: at most 32
+         * blocks of two warps per SM, fewer when the capacity is small */
+        const int js = cb.cap <= 8192 ? 4 : 16;
+        const ll want = ((cb.cap + P64_BLOCK - 1) / P64_BLOCK) * ((jc + js - 1) / js);
+        const ll most = (ll)(cb.sms > 0 ? cb.sms : 152) * 32;
+        const unsigned g = (unsigned)(want < most ? want : most);
         for (ll jbase = 0; jbase < cb.cap; jbase += jc) {
-            k_p64_terms<<<dim3(gi, gj), P64_BLOCK, 0, st>>>(cb.a, ctl, cb.p64_terms, cb.cap, jc, jbase, cb.ev_keys,
-                                                             cb.ev_cap);
-            k_p64_sum<<<(unsigned)((cb.cap + 255) / 256), 256, 0, st>>>(cb.a, ctl, cb.p64_terms, cb.p64_acc, cb.cap,
-                                                                        jc, jbase);
+            if (js == 4)
+                k_p64_terms<4><<<g, P64_BLOCK, 0, st>>>(cb.a, ctl, cb.p64_terms, cb.cap, jc, jbase, cb.ev_keys,
+                                                         cb.ev_cap);
+            else
+                k_p64_terms<16><<<g, P64_BLOCK, 0, st>>>(cb.a, ctl, cb.p64_terms, cb.cap, jc, jbase, cb.ev_keys,
+                                                          cb.ev_cap);
+            /* 32 bodies per block, at most 8 blocks per SM */
+            const ll sb = (cb.cap + SUM_BODIES - 1) / SUM_BODIES, smost = (ll)(cb.sms > 0 ? cb.sms : 152) * 8;
+            k_p64_sum<<<(unsigned)(sb < smost ? sb : smost), SUM_THREADS, 0, st>>>(cb.a, ctl, cb.p64_terms,
+                                                                                  cb.p64_acc, cb.cap, jc, jbase);
         }
         return;
     }
