@@ -88,6 +88,8 @@ def parse():
                     help="run the FP64 comparison on the uniform ball too (one FP64 force pass, ~2 min at 1M bodies)")
     ap.add_argument("--near-ppm", type=int, default=None,
                     help="mixed: near-pair radius factor in parts per million (library default 35000)")
+    ap.add_argument("--chunks", type=int, default=None,
+                    help="mixed: most chunks the pair work is cut into (library default 32 per resident CTA)")
     ap.add_argument("--p64-split-max", type=int, default=None,
                     help="plain FP64: largest capacity for the split pair pass (library default 65536)")
     ap.add_argument("--sort-interval", type=int, default=None,
@@ -386,6 +388,8 @@ def main():
         sim.set_option(A.OPT_NEAR_PPM, args.near_ppm)
     if args.p64_split_max is not None:
         sim.set_option(A.OPT_P64_SPLIT_MAX, args.p64_split_max)
+    if args.chunks is not None:
+        sim.set_option(A.OPT_SPLIT, args.chunks)
     load(sim, sims)
     tuned = None
     if prec == "mixed" and args.shape is not None:
