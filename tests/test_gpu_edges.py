@@ -1,0 +1,76 @@
+"""Edge cases of the collection on the GPU, through the C ABI: an empty
+collection, a single body, and a collection that merges down to one body,
+in both forms and with the Barnes-Hut force pass; the plain form against the
+oracle, bit for bit."""
+import numpy as np
+import pytest
+
+from nbodygo_gb300 import _abi as A
+from nbodygo_gb300.api import Simulation
+from oracle.oracle import OracleSim
+
+from helpers import assert_states_identical, body_set
+
+pytestmark = pytest.mark.gpu
+
+FORMS = [("fp64", False), ("mixed", False), ("fp64", True), ("mixed", True)]
+
+
+def make(prec, bh, bodies):
+    sim = Simulation(prec, seed=7)
+    if bh:
+        sim.set_option(A.OPT_BARNES_HUT, 1)
+    sim.set_bodies(bodies)
+    return sim
+
+
+@pytest.mark.parametrize("prec,bh", FORMS)
+def test_empty_collection_steps_and_accepts_adds(prec, bh):
+    sim = make(prec, bh, body_set([]))
+    info = sim.step(0.01, 1.0, 3)
+    assert info["steps_done"] == 3 and info["n_bodies"] == 0 and info["interactions"] == 0
+    assert len(sim.state()["x"]) == 0
+    sim.force_pass()
+    ids = sim.add_bodies(body_set([dict(x=1.0, mass=1e10, radius=0.5), dict(x=-1.0, mass=1e10, radius=0.5)]))
+    assert len(ids) == 2
+    info = sim.step(0.01, 1.0, 2)
+    assert info["n_bodies"] == 2
+
+
+@pytest.mark.parametrize("prec,bh", FORMS)
+def test_single_body_moves_in_a_straight_line(prec, bh):
+    b = body_set([dict(x=3.0, y=-2.0, z=1.0, vx=1.5, vy=0.25, vz=-0.5, mass=1e12, radius=1.0)])
+    sim = make(prec, bh, b)
+    ora = OracleSim(seed=7, threads=2)
+    ora.set_bodies(b)
+    for _ in range(5):
+        info = sim.step(0.01, 1.0, 1)
+        ora.step(0.01, 1.0, 1)
+        assert info["n_bodies"] == 1 and info["interactions"] == 0
+    got, exp = sim.state(), ora.state()
+    assert got["fx"][0] == 0.0 and got["fy"][0] == 0.0 and got["fz"][0] == 0.0
+    assert_states_identical(got, exp, fields=("x", "y", "z", "vx", "vy", "vz", "mass", "radius"), where=prec)
+
+
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+def test_merge_down_to_one_body(prec):
+    """A large subsume body absorbs the four small ones inside it in the
+    first cycle (subsume needs the larger radius to reach the other body);
+    the survivor keeps stepping alone.  The plain form follows the oracle bit
+    for bit through the merge."""
+    rows = [dict(x=0.0, mass=5e9, radius=5.0)] + [dict(x=0.8 * k, y=0.3 * k, vx=0.01 * k, mass=1e9 * k, radius=0.5)
+                                                   for k in range(1, 5)]
+    b = body_set(rows, behavior=A.SUBSUME)
+    sim = make(prec, False, b)
+    ora = OracleSim(seed=7, threads=2)
+    ora.set_bodies(b)
+    for c in range(6):
+        sim.step(0.01, 1.0, 1)
+        ora.step(0.01, 1.0, 1)
+        if prec == "fp64":
+            assert_states_identical(sim.state(), ora.state(), where=f"cycle {c}")
+    st = sim.state()
+    assert len(st["x"]) == 1 == ora.count()
+    assert st["mass"][0] == pytest.approx(sum(r["mass"] for r in rows), rel=1e-15)
+    info = sim.step(0.01, 1.0, 3)
+    assert info["n_bodies"] == 1 and info["interactions"] == 0
