@@ -202,7 +202,8 @@ __global__ void __launch_bounds__(NBG_SCAN_BLOCK) k_keep_blocksum(BodyArrays A, 
 /* Single-block exclusive scan of the per-block sums, then the per-sim
  * layout.  mode 0: fragment counts, fragment and host-add starts per sim,
  * capacity checks.  mode 1: surviving bodies, keep starts and the layout
- * after Cycle: sim s gets [kept bodies][its fragments][its host adds]. */
+ * after Cycle: sim s gets [kept bodies][its fragments][its host adds].
+ * mode 2: the block offsets alone. */
 __global__ void __launch_bounds__(NBG_SCAN_BLOCK) k_scan_blocks(DevCtl *ctl, SimSegs seg, const ll *blk_sum,
                                                                 ll *blk_off, int mode, ll cap, ll frag_cap)
 {
@@ -219,6 +220,7 @@ __global__ void __launch_bounds__(NBG_SCAN_BLOCK) k_scan_blocks(DevCtl *ctl, Sim
         carry += tot;
     }
     const int ns = seg.nsims;
+    if (mode == 2) return; /* block offsets only (the carried order) */
     if (mode == 0) {
         block_scan_array(ns, [&](int s) { return seg.frag[s]; }, seg.frag_start);
         const ll hadds = block_scan_array(ns, [&](int s) { return seg.hadd[s]; }, seg.hadd_start);
@@ -1018,8 +1020,10 @@ __device__ static bool cycle_changes(const DevCtl *ctl)
 
 /* Kept body k of sim s goes to new_off[s] + (its rank among kept bodies -
  * keep_start[s]): the order inside each sim is preserved. */
+#define NBG_GONE 0xffffffffu
+
 __global__ void __launch_bounds__(NBG_SCAN_BLOCK) k_compact(BodyArrays A, BodyArrays Bt, DevCtl *ctl, SimSegs seg,
-                                                            const ll *blk_off)
+                                                            const ll *blk_off, unsigned *remap)
 {
     if (ctl->error || !cycle_changes(ctl)) return;
     const ll n = ctl->n;
@@ -1035,10 +1039,72 @@ __global__ void __launch_bounds__(NBG_SCAN_BLOCK) k_compact(BodyArrays A, BodyAr
         const ll ex = block_excl_scan(keep ? 1 : 0, &tot);
         if (keep) {
             const int sim = nbg_sim_of(seg.off, seg.nsims, k);
-            copy_body(A, k, Bt, seg.new_off[sim] + (rank + ex - seg.keep_start[sim]));
+            const ll d = seg.new_off[sim] + (rank + ex - seg.keep_start[sim]);
+            copy_body(A, k, Bt, d);
+            if (remap) remap[k] = (unsigned)d;
+        } else if (remap && k < n) {
+            remap[k] = NBG_GONE;
         }
         rank += tot;
     }
+}
+
+/* The mixed path's Morton order carried through compaction: the kept bodies
+ * keep their sorted sequence under their new indices, and each sim's arrivals
+ * (fragments, host adds) follow its kept bodies.  A sim's sorted positions
+ * cover the same range as its indices, so the stable compaction over
+ * positions uses the per-sim offsets of the body compaction.  Three steps:
+ * kept positions per block, their block offsets (k_scan_blocks mode 2), and
+ * the scatter into the scratch order; k_order_copy then installs it. */
+__global__ void __launch_bounds__(NBG_SCAN_BLOCK) k_order_blocksum(DevCtl *ctl, const unsigned *perm,
+                                                                   const unsigned *remap, ll *blk_sum)
+{
+    if (ctl->error || !cycle_changes(ctl)) return;
+    const ll n = ctl->n;
+    const ll base = (ll)blockIdx.x * NBG_SCAN_TILE;
+    if (base >= n) return;
+    ll s = 0;
+    for (int q = 0; q < NBG_SCAN_ITEMS; q++) {
+        const ll p = base + (ll)q * NBG_SCAN_BLOCK + threadIdx.x;
+        s += p < n && remap[perm[p]] != NBG_GONE ? 1 : 0;
+    }
+    ll tot;
+    block_excl_scan(s, &tot);
+    if (threadIdx.x == 0) blk_sum[blockIdx.x] = tot;
+}
+
+__global__ void __launch_bounds__(NBG_SCAN_BLOCK) k_order_carry(DevCtl *ctl, SimSegs seg, const unsigned *perm,
+                                                                const unsigned *remap, const ll *blk_off,
+                                                                unsigned *order)
+{
+    if (ctl->error || !cycle_changes(ctl)) return;
+    const ll n = ctl->n;
+    const ll base = (ll)blockIdx.x * NBG_SCAN_TILE;
+    if (base >= n) return;
+    ll rank = blk_off[blockIdx.x];
+    for (int q = 0; q < NBG_SCAN_ITEMS; q++) {
+        const ll p = base + (ll)q * NBG_SCAN_BLOCK + threadIdx.x;
+        const unsigned to = p < n ? remap[perm[p]] : NBG_GONE;
+        const bool keep = to != NBG_GONE;
+        ll tot;
+        const ll ex = block_excl_scan(keep ? 1 : 0, &tot);
+        if (keep) {
+            const int sim = nbg_sim_of(seg.off, seg.nsims, p);
+            order[seg.new_off[sim] + (rank + ex - seg.keep_start[sim])] = to;
+        }
+        rank += tot;
+    }
+}
+
+__global__ void k_order_copy(DevCtl *ctl, SimSegs seg, const unsigned *order, unsigned *perm)
+{
+    if (ctl->error || !cycle_changes(ctl)) return;
+    const ll total = seg.new_off[seg.nsims];
+    for (ll k = (ll)blockIdx.x * blockDim.x + threadIdx.x; k < total; k += (ll)gridDim.x * blockDim.x) {
+        const int sim = nbg_sim_of(seg.new_off, seg.nsims, k);
+        perm[k] = k - seg.new_off[sim] < seg.keep[sim] ? order[k] : (unsigned)k; /* arrivals: as they come */
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) ctl->order_carried = 1;
 }
 
 /* Appends each sim's adds after its kept bodies, newest first (the sim's
@@ -1089,7 +1155,9 @@ __global__ void __launch_bounds__(NBG_SCAN_BLOCK) k_end(DevCtl *ctl, SimSegs seg
     ctl->acc_interactions += ctl->cycle_interactions;
     ctl->n = ctl->n_keep + ctl->frag_total + ctl->n_host_adds;
     ctl->n_host_adds = 0;
-    if (changed) ctl->sort_valid = 0; /* bodies changed index */
+    /* bodies changed index: the order is stale unless it was carried along */
+    if (changed && !ctl->order_carried) ctl->sort_valid = 0;
+    ctl->order_carried = 0;
     ctl->cycle += 1;
     ctl->acc_steps += 1;
 }
@@ -1274,7 +1342,7 @@ int nbg_pair_fp64_launches(const CycleBufs &cb)
 
 /* everything after the pair kernel: order events, emit fragments, resolve,
  * integrate, Cycle */
-void nbg_launch_after_pair(const CycleBufs &cb, DevCtl *ctl, cudaStream_t st)
+void nbg_launch_after_pair(const CycleBufs &cb, DevCtl *ctl, cudaStream_t st, bool carry_order)
 {
     const int sg = scan_grid(cb.cap);
     k_sort_events<<<1, SORT_BLOCK, 0, st>>>(ctl, cb.ev_keys, cb.ev_cap);
@@ -1285,9 +1353,18 @@ void nbg_launch_after_pair(const CycleBufs &cb, DevCtl *ctl, cudaStream_t st)
     if (cb.ring_head) k_ring_header<<<1, 1, 0, st>>>(ctl, cb.ring_head, cb.ring_cap, cb.ring_slots);
     k_keep_blocksum<<<sg, NBG_SCAN_BLOCK, 0, st>>>(cb.a, ctl, cb.seg, cb.blk_sum);
     k_scan_blocks<<<1, NBG_SCAN_BLOCK, 0, st>>>(ctl, cb.seg, cb.blk_sum, cb.blk_off, 1, cb.cap, cb.frag_cap);
-    k_compact<<<sg, NBG_SCAN_BLOCK, 0, st>>>(cb.a, cb.b, ctl, cb.seg, cb.blk_off);
+    /* the radix value buffer is free after the sort: old -> new index */
+    unsigned *remap = carry_order ? cb.sval : nullptr;
+    k_compact<<<sg, NBG_SCAN_BLOCK, 0, st>>>(cb.a, cb.b, ctl, cb.seg, cb.blk_off, remap);
     k_append_adds<<<flat_grid(cb.frag_cap + cb.adds_cap), 256, 0, st>>>(cb.b, cb.frags, cb.adds, ctl, cb.seg);
     k_copy_back<<<flat_grid(cb.cap), 256, 0, st>>>(cb.a, cb.b, ctl, cb.seg);
+    if (carry_order) {
+        /* the sorted-key buffer is free after the sort: the scratch order */
+        k_order_blocksum<<<sg, NBG_SCAN_BLOCK, 0, st>>>(ctl, cb.perm, remap, cb.blk_sum);
+        k_scan_blocks<<<1, NBG_SCAN_BLOCK, 0, st>>>(ctl, cb.seg, cb.blk_sum, cb.blk_off, 2, cb.cap, cb.frag_cap);
+        k_order_carry<<<sg, NBG_SCAN_BLOCK, 0, st>>>(ctl, cb.seg, cb.perm, remap, cb.blk_off, cb.skey[0]);
+        k_order_copy<<<flat_grid(cb.cap), 256, 0, st>>>(ctl, cb.seg, cb.skey[0], cb.perm);
+    }
     k_end<<<1, NBG_SCAN_BLOCK, 0, st>>>(ctl, cb.seg);
 }
 

@@ -1077,15 +1077,16 @@ static void launch_cycle(nbg_ctx *ctx, int precision, long ev_base)
         nbg_launch_pair_fp64(cb, ctx->ctl, st);
         if (ev_base >= 0) cudaEventRecord(get_event(ctx, (size_t)ev_base + 2), st);
     }
-    nbg_launch_after_pair(cb, ctx->ctl, st);
+    /* the mixed direct path keeps its Morton order through compaction */
+    nbg_launch_after_pair(cb, ctx->ctl, st, !cb.bh && precision == NBG_PRECISION_MIXED);
     if (ev_base >= 0) cudaEventRecord(get_event(ctx, (size_t)ev_base + 3), st);
     /* begin, fragment count + scan, 10 after the pair kernel, and the pair
      * kernel; mixed adds reduce, the sort decision and 21 sort launches
      * (which return at once in cycles that keep the order), pack, tile
-     * origins, i-body set-up and the output;
-     * Barnes-Hut replaces the pair kernel with 55 (k_bh.cu) */
+     * origins, i-body set-up, the output and 4 that carry the order through
+     * compaction; Barnes-Hut replaces the pair kernel with 55 (k_bh.cu) */
     ctx->launches_per_cycle = (cb.bh ? 13 + 55 + (precision == NBG_PRECISION_MIXED ? 1 : 0)
-                                     : precision == NBG_PRECISION_MIXED ? 41 : 13 + nbg_pair_fp64_launches(cb)) +
+                                     : precision == NBG_PRECISION_MIXED ? 45 : 13 + nbg_pair_fp64_launches(cb)) +
                               (cb.ring_head ? 1 : 0);
 }
 

@@ -94,7 +94,7 @@ struct DevCtl {
     int sort_valid;
     int sort_now;
     int sort_interval;
-    int pad3;
+    int order_carried; /* this cycle's compaction carried the order along */
     ull sort_cycle;
 };
 
@@ -327,7 +327,7 @@ void nbg_launch_bh(const CycleBufs &cb, DevCtl *ctl, cudaStream_t st, bool mixed
 void nbg_launch_begin(const CycleBufs &cb, DevCtl *ctl, cudaStream_t st);
 void nbg_launch_frag_count(const CycleBufs &cb, DevCtl *ctl, cudaStream_t st);
 void nbg_launch_pair_fp64(const CycleBufs &cb, DevCtl *ctl, cudaStream_t st);
-void nbg_launch_after_pair(const CycleBufs &cb, DevCtl *ctl, cudaStream_t st);
+void nbg_launch_after_pair(const CycleBufs &cb, DevCtl *ctl, cudaStream_t st, bool carry_order);
 void nbg_launch_remove(const CycleBufs &cb, DevCtl *ctl, ll count, ll *removed_dev, cudaStream_t st);
 void nbg_launch_edits(const CycleBufs &cb, DevCtl *ctl, const nbg_edit *edits_dev, ll k, int *results_dev, cudaStream_t st);
 void nbg_launch_energy(const CycleBufs &cb, DevCtl *ctl, double *out_dev, cudaStream_t st);
