@@ -5,7 +5,7 @@
  * Some callers of this library may not call cudaMalloc at all: a host
  * framework whose memory pool already owns the device (and forbids
  * allocations behind its back), a real-time loop that must never block in
- * the driver's allocator, or code that runs where an allocation would
+ * the CUDA allocator, or code that runs where an allocation would
  * disturb a memory budget fixed in advance.  nbg_forces_mixed_noalloc serves
  * them.  The caller passes device pointers for the inputs and outputs; every
  * intermediate buffer the force pass needs (sorted packed positions, Morton
