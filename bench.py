@@ -460,7 +460,9 @@ def main():
         info = sim.step(DT, 1.0, chunk)
         t2 = time.perf_counter()
         out = sim.state(out=pinned)
-        counts = sim.sim_counts()
+        # several collections: their sizes after the step; one collection:
+        # the length of what was read
+        counts = sim.sim_counts() if len(counts) > 1 else [len(out["x"])]
         t3 = time.perf_counter()
         n_h = len(out["x"])
         per_call.append(round(1e3 * (t3 - t0), 3))
