@@ -158,3 +158,27 @@ def test_flat_collections_match_separate_parts():
     assert_states_identical(a.state(), b.state())
     with pytest.raises(ValueError):
         b.set_collections_flat(flat, counts[:-1])
+
+
+@pytest.mark.parametrize("interval", [1, 4])
+def test_mixed_batch_graph_replay_equals_single_cycles(interval):
+    """The mixed form decides on the device when to sort and carries the
+    order through compaction; with collisions in some collection every
+    cycle, ten cycles replayed as one CUDA graph, as two graphs of five and
+    as ten single cycles give the same state bit for bit."""
+    sims = small_ensemble()
+    runs = []
+    for cycles_per_graph, calls in ((10, [10]), (5, [5, 5]), (1, [1] * 10)):
+        gpu = Simulation("mixed", seed=9)
+        gpu.set_option(A.OPT_SORT_INTERVAL, interval)
+        gpu.set_option(A.OPT_GRAPH_CYCLES, cycles_per_graph)
+        gpu.set_collections(sims)
+        removed = 0
+        for k in calls:
+            info = gpu.step(0.02, 0.9, k)
+            removed += info["removed"]
+        runs.append((gpu.state(), list(gpu.sim_counts()), removed))
+    assert runs[0][2] > 0  # bodies left some collection: compaction ran
+    for st, counts, _ in runs[1:]:
+        assert counts == runs[0][1]
+        assert_states_identical(st, runs[0][0], where="graph replay vs single cycles")
