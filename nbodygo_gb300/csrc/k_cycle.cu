@@ -415,10 +415,12 @@ __global__ void __launch_bounds__(P64_BLOCK) k_p64_terms(BodyArrays A, DevCtl *c
 }
 
 /* Each body adds its terms in j order.  A block takes 32 bodies: all its
- * threads load a tile of 32 j x 32 bodies (coalesced rows of 32 bodies),
- * the next tile's loads go out while this one is added, and warp 0 adds each
- * body's column in j order, so the sums are formed exactly as the
- * sequential loop forms them. */
+ * threads load a tile of 32 j x 32 bodies x 3 components (coalesced rows of
+ * 32 bodies), the next tile's loads go out while this one is added, and
+ * three warps add the columns in j order, one force component each (FP64
+ * adds run at 1/64 of the FP32 rate, so one warp adding all three left most
+ * of the SM's FP64 units idle).  Each component's sum is formed exactly as
+ * the sequential loop forms it. */
 #define SUM_BODIES 32
 #define SUM_J 32
 #define SUM_THREADS 256
@@ -433,14 +435,12 @@ __global__ void __launch_bounds__(SUM_THREADS) k_p64_sum(BodyArrays A, DevCtl *c
     const ll je = jbase + jc < n ? jbase + jc : n;
     const ll cnt = je - jbase;
     const int tid = threadIdx.x;
+    const int comp = tid / SUM_BODIES; /* warps 0-2: the component this thread adds */
+    const bool adder = comp < 3;
     for (ll i0 = (ll)blockIdx.x * SUM_BODIES; i0 < n; i0 += (ll)gridDim.x * SUM_BODIES) {
         const ll i = i0 + (tid & (SUM_BODIES - 1));
-        double f[3] = {0.0, 0.0, 0.0};
-        if (tid < SUM_BODIES && jbase > 0 && i < n) {
-            f[0] = acc[i];
-            f[1] = acc[cap + i];
-            f[2] = acc[2 * cap + i];
-        }
+        double f = 0.0;
+        if (adder && jbase > 0 && i < n) f = acc[(ll)comp * cap + i];
         /* element e of a tile: component e / 1024, row (e / 32) % 32, body e % 32 */
         double r[SUM_PER_THREAD];
         auto load = [&](ll jt) {
@@ -462,26 +462,17 @@ __global__ void __launch_bounds__(SUM_THREADS) k_p64_sum(BodyArrays A, DevCtl *c
             }
             __syncthreads();
             if (jt + SUM_J < cnt) load(jt + SUM_J);
-            if (tid < SUM_BODIES) {
+            if (adder) {
                 const int m = cnt - jt < SUM_J ? (int)(cnt - jt) : SUM_J;
-                for (int t = 0; t < m; t++) {
-                    f[0] += tile[0][t][tid];
-                    f[1] += tile[1][t][tid];
-                    f[2] += tile[2][t][tid];
-                }
+                const int b = tid & (SUM_BODIES - 1);
+                for (int t = 0; t < m; t++) f += tile[comp][t][b];
             }
         }
-        if (tid < SUM_BODIES && i < n) {
+        if (adder && i < n) {
             if (je >= n) {
-                if ((A.flags[i] & NBG_LIVE_MASK) == NBG_F_EXISTS) {
-                    A.fx[i] = f[0];
-                    A.fy[i] = f[1];
-                    A.fz[i] = f[2];
-                }
+                if ((A.flags[i] & NBG_LIVE_MASK) == NBG_F_EXISTS) (comp == 0 ? A.fx : comp == 1 ? A.fy : A.fz)[i] = f;
             } else {
-                acc[i] = f[0];
-                acc[cap + i] = f[1];
-                acc[2 * cap + i] = f[2];
+                acc[(ll)comp * cap + i] = f;
             }
         }
         __syncthreads(); /* the tile is free for the next bodies */
