@@ -425,7 +425,7 @@ __global__ void __launch_bounds__(P64_BLOCK) k_p64_terms(BodyArrays A, DevCtl *c
 #define SUM_J 32
 #define SUM_THREADS 256
 #define SUM_PER_THREAD (3 * SUM_J * SUM_BODIES / SUM_THREADS)
-__global__ void __launch_bounds__(SUM_THREADS) k_p64_sum(BodyArrays A, DevCtl *ctl, const double *T, double *acc,
+__global__ void __launch_bounds__(SUM_THREADS, 4) k_p64_sum(BodyArrays A, DevCtl *ctl, const double *T, double *acc,
                                                          ll cap, ll jc, ll jbase)
 {
     __shared__ double tile[3][SUM_J][SUM_BODIES];
