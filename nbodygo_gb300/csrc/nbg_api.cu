@@ -588,12 +588,27 @@ static int upload_soa(nbg_ctx *ctx, BodyArrays &D, ll off, const nbg_soa *h, ll 
     if (rc0 != NBG_OK) return rc0;
     CK(cudaStreamSynchronize(ctx->st)); /* the staging's last copy is done */
     unsigned *flags = ctx->flags_h;
-    for (ll k = 0; k < n; k++) {
-        int32_t c = h->collision ? h->collision[k] : NBG_ELASTIC;
-        if (c < NBG_NONE || c > NBG_FRAGMENT) return fail(ctx, NBG_E_ARG, "collision behaviour out of range");
-        uint32_t f = h->flags ? h->flags[k] : NBG_F_EXISTS;
-        flags[k] = (f & 0xffu) | ((unsigned)c << NBG_BEHAVIOR_SHIFT);
+    /* every behaviour is checked before anything is copied; then the flag
+     * words are composed in branch-free loops the compiler vectorises */
+    const int32_t *coll = h->collision;
+    const uint32_t *hf = h->flags;
+    if (coll) {
+        int32_t lo = coll[0], hi = coll[0];
+        for (ll k = 1; k < n; k++) {
+            lo = coll[k] < lo ? coll[k] : lo;
+            hi = coll[k] > hi ? coll[k] : hi;
+        }
+        if (lo < NBG_NONE || hi > NBG_FRAGMENT) return fail(ctx, NBG_E_ARG, "collision behaviour out of range");
     }
+    const unsigned dflt_b = (unsigned)NBG_ELASTIC << NBG_BEHAVIOR_SHIFT;
+    if (coll && hf)
+        for (ll k = 0; k < n; k++) flags[k] = (hf[k] & 0xffu) | ((unsigned)coll[k] << NBG_BEHAVIOR_SHIFT);
+    else if (coll)
+        for (ll k = 0; k < n; k++) flags[k] = NBG_F_EXISTS | ((unsigned)coll[k] << NBG_BEHAVIOR_SHIFT);
+    else if (hf)
+        for (ll k = 0; k < n; k++) flags[k] = (hf[k] & 0xffu) | dflt_b;
+    else
+        for (ll k = 0; k < n; k++) flags[k] = NBG_F_EXISTS | dflt_b;
     int rc;
     CopyBatch cb;
     cb.n = 0;

@@ -74,3 +74,23 @@ def test_merge_down_to_one_body(prec):
     assert st["mass"][0] == pytest.approx(sum(r["mass"] for r in rows), rel=1e-15)
     info = sim.step(0.01, 1.0, 3)
     assert info["n_bodies"] == 1 and info["interactions"] == 0
+
+
+def test_invalid_collision_behaviour_is_rejected_before_any_copy():
+    """A load with a collision behaviour outside 0..3 fails with NBG_E_ARG and
+    leaves the loaded collection as it was."""
+    from nbodygo_gb300.api import NbgError
+
+    good = body_set([dict(x=float(k), mass=1e9, radius=0.1) for k in range(100)])
+    sim = make("fp64", False, good)
+    before = sim.state()
+    bad = body_set([dict(x=float(k), mass=1e9, radius=0.1) for k in range(50)])
+    bad["collision"][7] = 9
+    with pytest.raises(NbgError):
+        sim.set_bodies(bad)
+    after = sim.state()
+    assert_states_identical(after, before, where="after a rejected load")
+    bad["collision"][7] = -1
+    with pytest.raises(NbgError):
+        sim.set_bodies(bad)
+    assert sim.count() == 100
