@@ -320,9 +320,10 @@ int nbg_get_timing(nbg_ctx *ctx, nbg_timing *t);
 #define NBG_OPT_BH_SHAPE 9
 /* mixed: cycles between Morton sorts of the i-tiles (1..1000, default 4).
    Bodies move far less than a tile per cycle, so an older order still gives
-   compact tiles; any change of body indices (compaction, loads, edits) sorts
-   again at the next cycle.  The order affects FP32 rounding, never the event
-   set.  1 sorts every cycle. */
+   compact tiles.  Compaction carries the order along (kept bodies keep their
+   places, arrivals follow); loads and host edits sort again at the next
+   cycle.  The order affects FP32 rounding, never the event set.  1 sorts
+   every cycle. */
 #define NBG_OPT_SORT_INTERVAL 10
 /* plain form, one collection: up to this capacity (default 65536) the pair
    terms of all (i, j) are computed at once and each body adds its own in j

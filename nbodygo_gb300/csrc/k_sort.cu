@@ -1,8 +1,10 @@
 /*
  * k_sort.cu - spatial ordering of the i-tiles of the mixed pair kernel.
  *
- * Every cycle the bodies are ordered along a Morton (Z-order) curve over a
- * 1024^3 grid of the symmetric bounding box [-x_max, x_max]^3: 30-bit keys,
+ * Every few cycles (k_sort_decide) the bodies are ordered along a Morton
+ * (Z-order) curve over a 1024^3 grid of the symmetric bounding box
+ * [-x_max, x_max]^3, and compaction carries the order along in between
+ * (k_order_carry in k_cycle.cu): 30-bit keys,
  * sorted with a stable LSD radix sort (8-bit digits, four passes) whose
  * ranking within a block uses warp match masks, so the order is the same on
  * every run.  Consecutive 512-body slices of the sorted order are compact in
