@@ -222,3 +222,23 @@ def test_sort_interval_resorts_after_compaction_and_edits():
     step_and_check(sim, 2, 0.05)
     with pytest.raises(Exception):
         sim.set_option(A.OPT_SORT_INTERVAL, 0)
+
+
+@pytest.mark.parametrize("kind,n,seed", [("uniform", 3000, 1), ("plummer", 2500, 2), ("disk", 3500, 3),
+                                         ("cluster", 1200, 4), ("uniform", 700, 5), ("plummer", 4096, 6)])
+def test_randomized_forces_within_gate(kind, n, seed):
+    """Mixed forces of seeded collections of several distributions and sizes
+    stay within 1e-6 relative L2 of the oracle."""
+    if kind == "uniform":
+        b = W.uniform_ball(n=n, seed=seed, R=0.5 * n ** (1 / 3) * 10, radius=0.3)
+    elif kind == "plummer":
+        b = W.plummer(n=n, seed=seed)
+    elif kind == "disk":
+        b = W.disk(n=n, seed=seed)
+    else:
+        b = dense_cluster(n, seed=seed)
+    _, f = mixed_forces(b)
+    ora = OracleSim(threads=8)
+    ora.set_bodies(b)
+    err = rel_l2(f, ora.forces())
+    assert err <= TOL, f"{kind} n={n}: rel L2 {err:.3e}"

@@ -243,3 +243,16 @@ def test_energy_diagnostic():
     assert abs(ke - ke_ref) <= 1e-12 * abs(ke_ref)
     assert abs(pe - pe_ref) <= 1e-12 * abs(pe_ref)
     assert abs(mom[0] - float(np.sum(m * vx))) <= 1e-9 * float(np.sum(np.abs(m * vx)))
+
+
+@pytest.mark.parametrize("seed,n,split_max", [(101, 60, 0), (102, 250, 1 << 20), (103, 700, 0), (104, 1500, 1 << 20),
+                                              (105, 333, 1 << 20), (106, 2049, 0)])
+def test_randomized_clusters_bit_exact(seed, n, split_max):
+    """Seeded random clusters of every behaviour and size, through either
+    plain pair pass: state, events and step counters equal the oracle's, cycle
+    after cycle."""
+    rng = np.random.default_rng(seed)
+    b = dense_cluster(n, seed=seed)
+    dt = float(rng.choice([0.01, 0.03, 0.05]))
+    R = float(rng.choice([1.0, 0.8]))
+    run_both(b, dt, R, 8, gpu_opts={A.OPT_P64_SPLIT_MAX: split_max}, seed=seed)
