@@ -242,3 +242,36 @@ def test_randomized_forces_within_gate(kind, n, seed):
     ora.set_bodies(b)
     err = rel_l2(f, ora.forces())
     assert err <= TOL, f"{kind} n={n}: rel L2 {err:.3e}"
+
+
+def _net_force_ratio(f, lo=0, hi=None):
+    fx, fy, fz = (np.asarray(c[lo:hi], dtype=np.float64) for c in f)
+    net = np.sqrt(fx.sum() ** 2 + fy.sum() ** 2 + fz.sum() ** 2)
+    scale = np.sqrt(fx ** 2 + fy ** 2 + fz ** 2).sum()
+    return net / scale
+
+
+def test_full_size_uniform_forces_cancel():
+    """Config 4 at full size (2^20 bodies): gravity is pairwise antisymmetric,
+    so the forces of the mixed pass sum to zero up to rounding."""
+    b = W.uniform_ball()
+    sim = Simulation("mixed", capacity=len(b["x"]))
+    sim.set_bodies(b)
+    ratio = _net_force_ratio(sim.force_pass())
+    assert ratio <= 1e-6, f"net force {ratio:.3e} of the summed magnitudes"
+
+
+def test_full_size_ensemble_forces_cancel_per_collection():
+    """Config 3 at full size (512 collections, 3.3 M bodies): each
+    collection's forces sum to zero up to rounding, so no pair crosses
+    collections and none is counted once."""
+    sims = W.ensemble()
+    sim = Simulation("mixed", capacity=sum(len(s["x"]) for s in sims))
+    sim.set_collections(sims)
+    f = sim.force_pass()
+    o, worst = 0, 0.0
+    for s in sims:
+        n = len(s["x"])
+        worst = max(worst, _net_force_ratio(f, o, o + n))
+        o += n
+    assert worst <= 1e-5, f"worst net force {worst:.3e} of a collection's summed magnitudes"
