@@ -256,3 +256,21 @@ def test_randomized_clusters_bit_exact(seed, n, split_max):
     dt = float(rng.choice([0.01, 0.03, 0.05]))
     R = float(rng.choice([1.0, 0.8]))
     run_both(b, dt, R, 8, gpu_opts={A.OPT_P64_SPLIT_MAX: split_max}, seed=seed)
+
+
+def test_plummer_workload_full_run_bit_exact():
+    """Workload 1 for its full length (N = 16,384, elastic, dt = 0.01, 100
+    cycles, replayed as CUDA graphs of 10): the final state, event and
+    removal counts equal the oracle's bit for bit."""
+    b = W.plummer()
+    sim = Simulation("fp64", seed=123)
+    sim.set_option(A.OPT_GRAPH_CYCLES, 10)
+    sim.set_bodies(b)
+    ora = OracleSim(seed=123, threads=THREADS)
+    ora.set_bodies(b)
+    gi = sim.step(0.01, 1.0, 100)
+    oi = ora.step(0.01, 1.0, 100)
+    assert gi["steps_done"] == 100
+    for k in ("n_bodies", "events", "fragments_emitted", "removed", "interactions"):
+        assert gi[k] == oi[k], f"info {k} {gi[k]} != {oi[k]}"
+    assert_states_identical(sim.state(), ora.state(), where="after 100 cycles")
