@@ -182,3 +182,29 @@ def test_mixed_batch_graph_replay_equals_single_cycles(interval):
     for st, counts, _ in runs[1:]:
         assert counts == runs[0][1]
         assert_states_identical(st, runs[0][0], where="graph replay vs single cycles")
+
+
+def test_ensemble_full_run_conserves_mass_per_collection():
+    """Config 3 for its full length (512 collections, 200 cycles, graphs of
+    10, mixed form): every collection keeps its mass through merges and
+    fragments, every state stays finite, and the collection sizes account
+    for the removals and fragments reported."""
+    sims = W.ensemble()
+    gpu = Simulation("mixed", seed=5, capacity=sum(len(s["x"]) for s in sims) + 65536)
+    gpu.set_option(A.OPT_GRAPH_CYCLES, 10)
+    gpu.set_collections(sims)
+    m0 = np.array([s["mass"].sum() for s in sims])
+    n0 = sum(len(s["x"]) for s in sims)
+    info = gpu.step(0.01, 1.0, 200)
+    assert info["steps_done"] == 200
+    st = gpu.state()
+    counts = gpu.sim_counts()
+    assert len(counts) == len(sims) and counts.sum() == len(st["x"])
+    assert len(st["x"]) == n0 - info["removed"] + info["fragments_emitted"]
+    for f in ("x", "y", "z", "vx", "vy", "vz", "mass"):
+        assert np.all(np.isfinite(st[f])), f
+    o = 0
+    for s, c in enumerate(counts):
+        m1 = st["mass"][o:o + c].sum()
+        assert abs(m1 - m0[s]) <= 1e-12 * m0[s], f"collection {s}: mass {m1!r} != {m0[s]!r}"
+        o += c
