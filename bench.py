@@ -34,7 +34,9 @@ Timing:
 
 `--impl reference` times the CPU restatement of the reference's cycle
 (oracle/), with every host thread, as the reference's worker pool would use
-them.  It runs on a 32,768-body sample of the same distribution per step.
+them.  On the default workload each step is one full cycle of the same
+131,072-body collection (about 10 s on 16 Grace cores); the larger workloads
+(ensemble, uniform, Barnes-Hut) are timed on a stated sample.
 
 Under torchrun (N > 1) each rank runs an independent replica on its own GPU.
 The direct sum of one collection is not sharded, so this is replicas only.
@@ -47,6 +49,7 @@ import os
 import re
 import subprocess
 import sys
+import tempfile
 import time
 
 import numpy as np
@@ -164,14 +167,14 @@ class Clocks:
     def __init__(self, gpu):
         self.gpu = gpu
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_gpu{gpu}.csv")
+        fd, self.path = tempfile.mkstemp(prefix=f"nbg_clocks_gpu{gpu}_", suffix=".csv")
+        os.close(fd)
 
     def start(self):
         q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
         try:
-            os.makedirs(os.path.dirname(self.path), exist_ok=True)
             self.fh = open(self.path, "w")
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={q}",
                                           "--format=csv,noheader,nounits", "-lms", "50"],
@@ -203,6 +206,10 @@ class Clocks:
                 for nm, v in zip(names, p[5:9]):
                     if v.lower() == "active":
                         reasons.add(nm)
+        try:
+            os.unlink(self.path)
+        except OSError:
+            pass
         return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": smax, "reasons": sorted(reasons),
                 "samples": len(sm)}
 
@@ -252,13 +259,33 @@ def load(sim, sims):
         sim.set_collections(sims)
 
 
-def cpu_sample(workload):
-    """(list of body sets, description): the bounded sample of a workload that
-    the CPU restatement is timed on, drawn from the workload's own generator."""
+# workloads whose full collection the CPU restatement runs per timed cycle in
+# seconds (plummer_disk: ~10 s per cycle on 16 Grace cores); the others are
+# timed on a sample drawn from their own generator
+CPU_FULL = ("plummer_disk", "plummer", "disk")
+
+
+def config_of(workload, n0, nsims, ws):
+    """The `config` object of a bench line: the workload, identical in both
+    arms so their lines describe the same job."""
+    prec, dt, desc = WORKLOADS[workload]
+    return {"workload": f"{workload}: {n0} bodies in {nsims} simulation(s) ({desc}), dt={dt}",
+            "n_bodies": n0, "n_sims": nsims, "dt": dt,
+            "l2": "GPU arm: flushed (512 MB write) before every timed cycle"
+                  + (" graph" if workload == "ensemble" else "") + "; CPU arm: not applicable",
+            "parallelism": f"replicas x{ws}"}
+
+
+def cpu_sample(workload, n_each=65536):
+    """(list of body sets, description): what the CPU restatement is timed on.
+    The full workload where a cycle takes seconds (CPU_FULL), otherwise a
+    bounded sample drawn from the workload's own generator."""
     from nbodygo_gb300 import workloads as W
 
-    if workload == "plummer_disk":
-        return [W.plummer_disk(n_each=16384, seed=3)], "plummer_disk with 32,768 bodies"
+    if workload in CPU_FULL:
+        sims = make_workload(workload, n_each, 0)
+        n = int(sum(len(b["x"]) for b in sims))
+        return sims, f"{workload} with {n:,} bodies (the full workload)"
     if workload == "ensemble":
         sims, total = [], 0
         for b in W.ensemble(seed=5):
@@ -270,22 +297,18 @@ def cpu_sample(workload):
                 break
         return sims, f"{len(sims)} collections of the ensemble, {total:,} bodies"
     if workload == "uniform":
-        return [W.uniform_ball(32768, seed=4)], "uniform ball of the same radius with 32,768 bodies"
-    if workload == "plummer":
-        return [W.plummer(seed=2)], "plummer with 16,384 bodies (the full workload)"
-    if "_bh" in workload:
-        return [W.plummer(32768, seed=2)], ("plummer with 32,768 bodies, Barnes-Hut (the reference's octree, "
-                                            "built once per cycle)")
-    return [W.disk(seed=1)], "disk with 1,000 bodies (the full workload)"
+        return [W.uniform_ball(32768, seed=4)], "uniform ball of the same radius with 32,768 bodies (a sample)"
+    return [W.plummer(32768, seed=2)], ("plummer with 32,768 bodies, Barnes-Hut (the reference's octree, "
+                                        "built once per cycle; a sample)")
 
 
-def cpu_cycles(workload, dt, warmup, steps):
+def cpu_cycles(workload, dt, warmup, steps, sample=None):
     """Times `steps` cycles of the CPU restatement on every body set of the
-    workload's sample, all host threads: (interactions, seconds, cycles per
-    set, description)."""
+    workload's CPU sample, all host threads: (interactions, seconds,
+    description)."""
     from oracle.oracle import OracleSim
 
-    sets, what = cpu_sample(workload)
+    sets, what = sample or cpu_sample(workload)
     cores = os.cpu_count() or 1
     inter, t = 0, 0.0
     for b in sets:
@@ -303,38 +326,120 @@ def cpu_cycles(workload, dt, warmup, steps):
     return inter, t, what
 
 
-def cpu_baseline_sample(workload, dt):
-    """CPU restatement of the reference cycle, all host threads, on a sample."""
+def cpu_baseline_sample(workload, dt, n_each=65536):
+    """CPU restatement of the reference cycle, all host threads: one cycle of
+    the full workload where that takes seconds, else cycles of a sample."""
     cores = os.cpu_count() or 1
-    sets, _ = cpu_sample(workload)
-    steps = 1 if sum(len(b["x"]) for b in sets) > 10000 else 20
-    inter, t, what = cpu_cycles(workload, dt, 0, steps)
+    sample = cpu_sample(workload, n_each)
+    steps = 1 if sum(len(b["x"]) for b in sample[0]) > 10000 else 20
+    inter, t, what = cpu_cycles(workload, dt, 0, steps, sample)
     return {"value": inter / t, "unit": UNIT, "cores": cores, "kind": "port",
+            "full_workload": workload in CPU_FULL,
             "sample": f"{what}, {steps} cycle(s), {t:.2f} s; C restatement of the reference's Go cycle (oracle/)"}
 
 
 def run_reference(args, ws, rank):
-    """--impl reference: the CPU restatement, timed per cycle on a sample."""
+    """--impl reference: the CPU restatement of the reference's cycle (its
+    worker-pool slicing over every host thread), each step one cycle of the
+    workload.  Under torchrun only rank 0 runs."""
     if rank != 0:
         return 0
     prec, dt, desc = WORKLOADS[args.workload]
     cores = os.cpu_count() or 1
-    sets, _ = cpu_sample(args.workload)
+    sample = cpu_sample(args.workload, args.n_each)
+    sets = sample[0]
     n = int(sum(len(b["x"]) for b in sets))
-    total_int, total_t, sample = cpu_cycles(args.workload, dt, args.warmup, args.steps)
+    full = args.workload in CPU_FULL
+    total_int, total_t, what = cpu_cycles(args.workload, dt, args.warmup, args.steps, sample)
     v = total_int / total_t
+    if full:
+        config = config_of(args.workload, n, len(sets), ws)
+    else:
+        config = {"workload": f"{args.workload} sample: {n} bodies in {len(sets)} collection(s) ({desc})",
+                  "n_bodies": n, "n_sims": len(sets), "dt": dt}
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total_t / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic",
-            "config": {"workload": f"{args.workload} sample: {n} bodies in {len(sets)} collection(s) ({desc})",
-                       "n_bodies": n, "dt": dt},
-            "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
-                             "sample": f"{sample} per cycle; the C restatement of the reference's Go cycle "
-                                       "(oracle/) with the worker-pool slicing"},
+            "data": "synthetic", "config": config,
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "full_workload": full,
+                             "sample": f"{what}, one cycle per step; the C restatement of the reference's Go "
+                                       "cycle (oracle/) with the worker-pool slicing"},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     return 0
+
+
+G_CONST = 6.673e-11  # cmd/globals/globals.go
+
+
+def force_scale(torch, sims, idx, device):
+    """For the bodies at flat indices idx: the sum over j of |f_ij| =
+    G m_i m_j / d_ij^2 over the pairs the force pass sums (j in the same
+    collection, j != i, j live, d > r_i + r_j: calcForceFrom's overlap skip,
+    cmd/body/body.go:214-225), in FP64 on the GPU.  It is the scale of a
+    body's force with no cancellation between terms."""
+    out = np.zeros(len(idx))
+    off = np.cumsum([0] + [len(b["x"]) for b in sims])
+    idx = np.asarray(idx, dtype=np.int64)
+    sim_of = np.searchsorted(off, idx, side="right") - 1
+    for s in np.unique(sim_of):
+        b = sims[s]
+        live = (np.asarray(b["flags"]) & 0x11) == 0x01  # exists, not fragmenting
+        T = {k: torch.as_tensor(np.asarray(b[k], dtype=np.float64), device=device) for k in ("x", "y", "z", "mass",
+                                                                                             "radius")}
+        mj = T["mass"] * torch.as_tensor(live, device=device)
+        sel = np.nonzero(sim_of == s)[0]
+        loc = idx[sel] - off[s]
+        for a in range(0, len(loc), 64):
+            li = torch.as_tensor(loc[a:a + 64], device=device)
+            d2 = ((T["x"][None, :] - T["x"][li, None]) ** 2 + (T["y"][None, :] - T["y"][li, None]) ** 2
+                  + (T["z"][None, :] - T["z"][li, None]) ** 2)
+            far = d2.sqrt() > (T["radius"][None, :] + T["radius"][li, None])
+            far[torch.arange(len(li), device=device), li] = False
+            w = torch.where(far, mj[None, :] / torch.where(far, d2, torch.ones_like(d2)), torch.zeros_like(d2))
+            out[sel[a:a + 64]] = (G_CONST * T["mass"][li] * w.sum(dim=1)).cpu().numpy()
+    return out
+
+
+def accuracy_block(torch, sims, fm, fp, device, limit=1e-6, top=2048):
+    """Mixed forces fm against the FP64 forces fp (both (fx, fy, fz) over the
+    flat body order).  Besides relative L2 and the plain per-body relative
+    error, each body's error is normalised by the sum of the magnitudes of its
+    terms, sum_j |f_ij|: in a dense core the terms cancel and |f_i| is far
+    smaller than the terms the FP32 arithmetic rounds.  Since
+    sum_j |f_ij| >= |f_i|, the normalised error of a body is at most its plain
+    relative error, so the normalised error is computed for the `top` bodies
+    with the largest plain error, and every other body is bounded by the
+    largest plain error outside them."""
+    mag = np.sqrt(fp[0] ** 2 + fp[1] ** 2 + fp[2] ** 2)
+    err = np.sqrt((fm[0] - fp[0]) ** 2 + (fm[1] - fp[1]) ** 2 + (fm[2] - fp[2]) ** 2)
+    num = np.sqrt(np.sum(err ** 2))
+    den = np.sqrt(np.sum(mag ** 2))
+    ok = np.nonzero(mag > 0)[0]
+    rel = err[ok] / mag[ok]
+    order = np.argsort(rel)[::-1]
+    k = min(top, len(order))
+    worst = ok[order[:k]]
+    scale = force_scale(torch, sims, worst, device)
+    norm = np.where(scale > 0, err[worst] / np.where(scale > 0, scale, 1.0), 0.0)
+    rest = float(rel[order[k]]) if k < len(order) else 0.0
+    max_norm = max(float(norm.max()) if k else 0.0, rest)
+    by_norm = np.argsort(norm)[::-1][:8]
+    rel_l2 = float(num / den)
+    return {
+        "rel_l2_vs_fp64": rel_l2, "max_rel": float(rel.max()), "median_rel": float(np.median(rel)),
+        "p99_9_rel": float(np.quantile(rel, 0.999)), "bodies_above_1e-6_rel": int(np.sum(rel > 1e-6)),
+        "max_rel_normalised": max_norm,
+        "normalised": f"|f_mixed - f_fp64| / sum_j |f_ij| (FP64 term magnitudes) for the {k} bodies with the "
+                      f"largest plain relative error; every other body is bounded by the plain relative error "
+                      f"{rest:.3e} of the next one",
+        "worst_bodies": [{"index": int(worst[q]), "rel": float(err[worst[q]] / mag[worst[q]]),
+                          "normalised": float(norm[q]), "cancellation": float(mag[worst[q]] / scale[q])}
+                         for q in by_norm],
+        "gate": {"limit": limit, "rel_l2_pass": rel_l2 <= limit, "max_normalised_pass": max_norm <= limit,
+                 "reading": "relative L2 over all bodies, and every body's error relative to the sum of its "
+                            "terms' magnitudes"},
+        "reference": "plain FP64 GPU forces (bit-identical to the oracle)"}
 
 
 def pinned_like(torch, st, extra):
@@ -508,11 +613,7 @@ def main():
             mixed0.set_option(A.OPT_NEAR_PPM, args.near_ppm)
         load(mixed0, sims)
         fm = mixed0.force_pass()
-        num = np.sqrt(sum(np.sum((a - b) ** 2) for a, b in zip(fm, fp)))
-        den = np.sqrt(sum(np.sum(b ** 2) for b in fp))
-        mag = np.sqrt(fp[0] ** 2 + fp[1] ** 2 + fp[2] ** 2)
-        err = np.sqrt((fm[0] - fp[0]) ** 2 + (fm[1] - fp[1]) ** 2 + (fm[2] - fp[2]) ** 2)
-        ok = mag > 0
+        accuracy = accuracy_block(torch, sims, fm, fp, f"cuda:{local}")
         if big:
             pairs = sum(len(b["x"]) * (len(b["x"]) - 1) for b in sims)
             plain_rate = pairs / (1e-3 * force_ms)
@@ -541,10 +642,8 @@ def main():
                 "roofline_frac_fp64": plain_rate * FLOPS_PER_PAIR / f64 if f64 else None,
                 "steps": 2}
         result_extra["mixed_over_plain"] = value / plain_rate / ws if plain_rate else None
-        result_extra["accuracy"] = {"rel_l2_vs_fp64": float(num / den), "max_rel": float(np.max(err[ok] / mag[ok])),
-                                    "median_rel": float(np.median(err[ok] / mag[ok])),
-                                    "reference": "plain FP64 GPU forces (bit-identical to the oracle)",
-                                    "energy_drift_2_cycles": drift}
+        accuracy["energy_drift_2_cycles"] = drift
+        result_extra["accuracy"] = accuracy
         plain.close()
         mixed0.close()
 
@@ -595,7 +694,7 @@ def main():
         peak_src = f"DFMA-chain probe on this GPU at {mhz:.0f} MHz (MEASURED_PEAKS.json has no FP64 figure)"
     cpu = None
     if rank == 0 and not args.no_cpu:
-        cpu = cpu_baseline_sample(args.workload, DT)
+        cpu = cpu_baseline_sample(args.workload, DT, args.n_each)
     sim.close()
     if rank == 0:
         line = {
@@ -605,12 +704,9 @@ def main():
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "fp32 pair terms, fp64 state" if prec == "mixed" else "f64",
             "data": "synthetic",
-            "config": {"workload": f"{args.workload}: {n0} bodies in {len(sims)} simulation(s) ({desc}), "
-                                   f"dt={DT}, {prec} precision",
-                       "n_bodies": n0, "n_sims": len(sims), "dt": DT,
-                       "sort_interval": (args.sort_interval or 4) if prec == "mixed" and not bh else None,
-                       "l2": "flushed (512 MB write) before every timed cycle"
-                             + (" graph" if chunk > 1 else ""), "parallelism": f"replicas x{ws}"},
+            "config": config_of(args.workload, n0, len(sims), ws),
+            "form": {"precision": prec, "barnes_hut": bh,
+                     "sort_interval": (args.sort_interval or 4) if prec == "mixed" and not bh else None},
             "e2e": e2e,
             "gpu_launches": int(launches),
             "roofline": {"bound": bound, "achieved": achieved, "peak": peak, "unit": "TFLOP/s",

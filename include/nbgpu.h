@@ -275,8 +275,12 @@ int nbg_energy(nbg_ctx *ctx, double *kinetic, double *potential, double momentum
  *  - n may be at most NBG_NOALLOC_MAX_BODIES; larger n returns NBG_E_ARG.
  *  - The work is queued on `stream` (a cudaStream_t; NULL is the default
  *    stream) and the call returns without waiting.
- *  - The first call on a device looks up the static array's device address;
- *    make that first call before any stream capture.
+ *  - The first call on a device looks up the static array's device address
+ *    (and makes the device's primary context current if no context is);
+ *    make that first call before any stream capture.  The address is kept
+ *    with the id of the context it was found in: after a device reset
+ *    (cudaDeviceReset) the next call, in the new context, looks it up again,
+ *    and that call too belongs before any capture.
  *  - All calls on one device share the array: calls that may overlap on the
  *    GPU (other streams, other host threads) race and must be serialised by
  *    the caller.

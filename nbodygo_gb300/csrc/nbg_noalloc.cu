@@ -17,6 +17,7 @@
  * The kernels are the ones the context path runs (k_mixed.cu, k_sort.cu);
  * only the buffers differ.
  */
+#include <cuda.h> /* CUcontext / CUresult types only; the entry points are resolved at run time */
 #include <mutex>
 #include <string>
 
@@ -54,8 +55,47 @@ static_assert(TOTAL_BYTES == NBG_NOALLOC_BYTES, "NBG_NOALLOC_BYTES in nbgpu.h is
 static __device__ __align__(256) unsigned char g_noalloc_scratch[TOTAL_BYTES];
 
 #define NOALLOC_MAX_DEVICES 64
-static unsigned char *g_scratch_addr[NOALLOC_MAX_DEVICES];
+/* The scratch array's device address on each device, with the id of the
+ * context it was looked up in.  A device reset (cudaDeviceReset by the host
+ * framework) destroys the context and the module with it; the next context
+ * gets a new id, so the address is looked up again instead of reused. */
+struct ScratchSlot {
+    unsigned long long ctx_id;
+    unsigned char *addr;
+};
+static ScratchSlot g_scratch[NOALLOC_MAX_DEVICES];
 static std::mutex g_setup_mutex;
+
+/* Driver entry points for the id of the current context, resolved through
+ * the runtime (the library does not link the driver library itself). */
+typedef CUresult (*PfnCtxGetCurrent)(CUcontext *);
+typedef CUresult (*PfnCtxGetId)(CUcontext, unsigned long long *);
+
+/* Id of the context current on this thread; 0 if there is none or the
+ * driver cannot tell (then the address is looked up on every call).  Called
+ * with g_setup_mutex held. */
+static unsigned long long current_ctx_id()
+{
+    static bool resolved = false;
+    static PfnCtxGetCurrent get_current = nullptr;
+    static PfnCtxGetId get_id = nullptr;
+    if (!resolved) {
+        resolved = true;
+        cudaDriverEntryPointQueryResult q1, q2;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", (void **)&get_current, 12000, cudaEnableDefault,
+                                             &q1) != cudaSuccess || q1 != cudaDriverEntryPointSuccess)
+            get_current = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", (void **)&get_id, 12000, cudaEnableDefault, &q2) !=
+                cudaSuccess || q2 != cudaDriverEntryPointSuccess)
+            get_id = nullptr;
+    }
+    if (!get_current || !get_id) return 0;
+    CUcontext ctx = nullptr;
+    unsigned long long id = 0;
+    if (get_current(&ctx) != CUDA_SUCCESS || !ctx) return 0;
+    if (get_id(ctx, &id) != CUDA_SUCCESS) return 0;
+    return id;
+}
 
 /* The control block's reductions and counters, and the per-sim arrays, must
  * start at zero; the collection is one sim of n bodies. */
@@ -86,17 +126,26 @@ extern "C" int nbg_forces_mixed_noalloc(const double *x, const double *y, const 
         return noalloc_fail(NBG_E_CUDA, "nbg_forces_mixed_noalloc: no current CUDA device");
     unsigned char *base;
     {
-        /* once per device, with that device current: the device address of
-         * the scratch array */
+        /* once per device context, with that device current: the device
+         * address of the scratch array */
         std::lock_guard<std::mutex> lock(g_setup_mutex);
-        if (!g_scratch_addr[dev]) {
+        unsigned long long id = current_ctx_id();
+        if (id == 0) {
+            /* no context current on this thread yet: make the device's
+             * primary context current, as the runtime's first call would */
+            if (cudaSetDevice(dev) != cudaSuccess)
+                return noalloc_fail(NBG_E_CUDA, "nbg_forces_mixed_noalloc: cudaSetDevice failed");
+            id = current_ctx_id();
+        }
+        if (id == 0 || g_scratch[dev].ctx_id != id || !g_scratch[dev].addr) {
             void *ptr = nullptr;
             cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
             if (e != cudaSuccess || !ptr)
                 return noalloc_fail(NBG_E_CUDA, "nbg_forces_mixed_noalloc: cudaGetSymbolAddress failed");
-            g_scratch_addr[dev] = (unsigned char *)ptr;
+            g_scratch[dev].ctx_id = id;
+            g_scratch[dev].addr = (unsigned char *)ptr;
         }
-        base = g_scratch_addr[dev];
+        base = g_scratch[dev].addr;
     }
     if (n == 0) return NBG_OK;
     cudaStream_t st = (cudaStream_t)stream;

@@ -23,3 +23,18 @@ def test_reference_arm_prints_one_contract_line():
     assert d["cpu_baseline"]["kind"] == "port" and d["cpu_baseline"]["cores"] >= 1
     assert d["e2e"]["h2d_bytes_per_step"] == 0 and d["e2e"]["d2h_bytes_per_step"] == 0
     assert d["config"]["n_bodies"] == 1000
+    # the full workload, described by the same config object the GPU arm prints
+    import bench
+
+    assert d["cpu_baseline"]["full_workload"] is True
+    assert d["config"] == bench.config_of("disk", 1000, 1, 1)
+
+
+def test_default_workload_is_timed_whole_on_the_cpu():
+    """The headline workload is one the CPU restatement runs in full, so both
+    arms measure the same 131,072-body job."""
+    import bench
+
+    assert "plummer_disk" in bench.CPU_FULL
+    sims, what = bench.cpu_sample("plummer_disk", 64)
+    assert len(sims) == 1 and len(sims[0]["x"]) == 128 and "full workload" in what
