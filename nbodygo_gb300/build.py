@@ -20,6 +20,9 @@ BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libnbgpu.so")
 ORACLE_DIR = os.path.join(ROOT, "oracle")
 ORACLE_LIB = os.path.join(ORACLE_DIR, "libnbg_oracle.so")
+# the same oracle with the platform libm's sin/cos/tan/asin/acos/atan2 in
+# place of nbg_math.h: bounds the effect of that substitution (tests only)
+ORACLE_LIBM_LIB = os.path.join(ORACLE_DIR, "libnbg_oracle_libm.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
@@ -57,15 +60,20 @@ def _stale(target, deps):
 
 def build_oracle(force=False, verbose=False):
     src = os.path.join(ORACLE_DIR, "nbg_oracle.c")
-    deps = [src, os.path.join(ORACLE_DIR, "nbg_oracle.h"), os.path.join(ROOT, "include", "nbgpu.h")]
+    deps = [src, os.path.join(ORACLE_DIR, "nbg_oracle.h"), os.path.join(ROOT, "include", "nbgpu.h"), __file__]
     deps += [os.path.join(CSRC, h) for h in ("nbg_math.h", "nbg_shared.h")]
-    if not force and not _stale(ORACLE_LIB, deps):
-        return ORACLE_LIB
-    cmd = [os.environ.get("CC", "gcc"), "-O2", "-std=c11", "-ffp-contract=off", "-fno-fast-math", "-fPIC",
-           "-shared", "-pthread", "-D_GNU_SOURCE", src, "-o", ORACLE_LIB, "-lm"]
-    if verbose:
-        print(" ".join(cmd))
-    subprocess.run(cmd, check=True)
+    procs = []
+    for lib, defs in ((ORACLE_LIB, []), (ORACLE_LIBM_LIB, ["-DNBG_ORACLE_LIBM"])):
+        if not force and not _stale(lib, deps):
+            continue
+        cmd = [os.environ.get("CC", "gcc"), "-O2", "-std=c11", "-ffp-contract=off", "-fno-fast-math", "-fPIC",
+               "-shared", "-pthread", "-D_GNU_SOURCE"] + defs + [src, "-o", lib, "-lm"]
+        if verbose:
+            print(" ".join(cmd))
+        procs.append((cmd, subprocess.Popen(cmd)))
+    for cmd, p in procs:
+        if p.wait() != 0:
+            raise RuntimeError("oracle build failed: " + " ".join(cmd))
     return ORACLE_LIB
 
 

@@ -959,8 +959,8 @@ void nbg_launch_bh(const CycleBufs &cb, DevCtl *ctl, cudaStream_t st, bool mixed
 {
     const BhTree &t = cb.t;
     const ll cap = cb.cap;
-    int g = (int)((cap + BH_BLOCK - 1) / BH_BLOCK);
-    if (g > 152 * 8) g = 152 * 8;
+    const ll gmost = (ll)(cb.sms > 0 ? cb.sms : 1) * 8;
+    int g = (int)((cap + BH_BLOCK - 1) / BH_BLOCK < gmost ? (cap + BH_BLOCK - 1) / BH_BLOCK : gmost);
     if (g < 1) g = 1;
     k_bh_bounds<<<g, BH_BLOCK, 0, st>>>(cb.a, ctl);
     k_bh_keys<<<g, BH_BLOCK, 0, st>>>(cb.a, ctl, t.key[0], t.val[0]);
@@ -979,8 +979,8 @@ void nbg_launch_bh(const CycleBufs &cb, DevCtl *ctl, cudaStream_t st, bool mixed
     k_bh_count_top<<<1, 1024, 0, st>>>(ctl, t.blk, t.node_cap);
     k_bh_count_scan<<<sb, BH_SCAN_BLOCK, 0, st>>>(ctl, t.base, t.blk);
     k_bh_nodes<<<g, BH_BLOCK, 0, st>>>(ctl, t.key[0], t.base, t);
-    int ng = (int)((t.node_cap + BH_BLOCK - 1) / BH_BLOCK);
-    if (ng > 152 * 8) ng = 152 * 8;
+    int ng = (int)((t.node_cap + BH_BLOCK - 1) / BH_BLOCK < gmost ? (t.node_cap + BH_BLOCK - 1) / BH_BLOCK : gmost);
+    if (ng < 1) ng = 1;
     for (int level = BH_LEVELS; level >= 0; level--)
         k_bh_mass<<<ng, BH_BLOCK, 0, st>>>(cb.a, ctl, t.val[0], t, level);
     if (mixed) {

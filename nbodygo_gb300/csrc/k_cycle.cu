@@ -1273,12 +1273,6 @@ __global__ void __launch_bounds__(EN_BLOCK) k_energy(BodyArrays A, DevCtl *ctl, 
 
 static int scan_grid(ll cap) { return (int)((cap + NBG_SCAN_TILE - 1) / NBG_SCAN_TILE); }
 
-static int flat_grid(ll cap)
-{
-    ll g = (cap + 255) / 256;
-    if (g > 152 * 16) g = 152 * 16;
-    return (int)(g < 1 ? 1 : g);
-}
 
 void nbg_launch_begin(const CycleBufs &cb, DevCtl *ctl, cudaStream_t st)
 {
@@ -1307,7 +1301,7 @@ void nbg_launch_pair_fp64(const CycleBufs &cb, DevCtl *ctl, cudaStream_t st)
          * blocks of two warps per SM, fewer when the capacity is small */
         const int js = cb.cap <= 8192 ? 4 : 16;
         const ll want = ((cb.cap + P64_BLOCK - 1) / P64_BLOCK) * ((jc + js - 1) / js);
-        const ll most = (ll)(cb.sms > 0 ? cb.sms : 152) * 32;
+        const ll most = (ll)(cb.sms > 0 ? cb.sms : 1) * 32;
         const unsigned g = (unsigned)(want < most ? want : most);
         for (ll jbase = 0; jbase < cb.cap; jbase += jc) {
             if (js == 4)
@@ -1317,7 +1311,7 @@ void nbg_launch_pair_fp64(const CycleBufs &cb, DevCtl *ctl, cudaStream_t st)
                 k_p64_terms<16><<<g, P64_BLOCK, 0, st>>>(cb.a, ctl, cb.p64_terms, cb.cap, jc, jbase, cb.ev_keys,
                                                           cb.ev_cap);
             /* 32 bodies per block, at most 8 blocks per SM */
-            const ll sb = (cb.cap + SUM_BODIES - 1) / SUM_BODIES, smost = (ll)(cb.sms > 0 ? cb.sms : 152) * 8;
+            const ll sb = (cb.cap + SUM_BODIES - 1) / SUM_BODIES, smost = (ll)(cb.sms > 0 ? cb.sms : 1) * 8;
             k_p64_sum<<<(unsigned)(sb < smost ? sb : smost), SUM_THREADS, 0, st>>>(cb.a, ctl, cb.p64_terms,
                                                                                   cb.p64_acc, cb.cap, jc, jbase);
         }
@@ -1340,21 +1334,21 @@ void nbg_launch_after_pair(const CycleBufs &cb, DevCtl *ctl, cudaStream_t st, bo
     k_frag_emit<<<sg, NBG_SCAN_BLOCK, 0, st>>>(cb.a, cb.frags, ctl, cb.blk_off);
     /* the radix-sort key buffer is free after the pair pass: per-body owner words */
     k_resolve<<<cb.seg.nsims, RESOLVE_BLOCK, 0, st>>>(cb.a, ctl, cb.seg, cb.ev_keys, cb.ev_out, cb.skey[1]);
-    k_integrate<<<flat_grid(cb.cap), 256, 0, st>>>(cb.a, ctl, cb.rend, cb.ring_rend, cb.ring_cap, cb.ring_slots);
+    k_integrate<<<nbg_flat_grid(cb, cb.cap), 256, 0, st>>>(cb.a, ctl, cb.rend, cb.ring_rend, cb.ring_cap, cb.ring_slots);
     if (cb.ring_head) k_ring_header<<<1, 1, 0, st>>>(ctl, cb.ring_head, cb.ring_cap, cb.ring_slots);
     k_keep_blocksum<<<sg, NBG_SCAN_BLOCK, 0, st>>>(cb.a, ctl, cb.seg, cb.blk_sum);
     k_scan_blocks<<<1, NBG_SCAN_BLOCK, 0, st>>>(ctl, cb.seg, cb.blk_sum, cb.blk_off, 1, cb.cap, cb.frag_cap);
     /* the radix value buffer is free after the sort: old -> new index */
     unsigned *remap = carry_order ? cb.sval : nullptr;
     k_compact<<<sg, NBG_SCAN_BLOCK, 0, st>>>(cb.a, cb.b, ctl, cb.seg, cb.blk_off, remap);
-    k_append_adds<<<flat_grid(cb.frag_cap + cb.adds_cap), 256, 0, st>>>(cb.b, cb.frags, cb.adds, ctl, cb.seg);
-    k_copy_back<<<flat_grid(cb.cap), 256, 0, st>>>(cb.a, cb.b, ctl, cb.seg);
+    k_append_adds<<<nbg_flat_grid(cb, cb.frag_cap + cb.adds_cap), 256, 0, st>>>(cb.b, cb.frags, cb.adds, ctl, cb.seg);
+    k_copy_back<<<nbg_flat_grid(cb, cb.cap), 256, 0, st>>>(cb.a, cb.b, ctl, cb.seg);
     if (carry_order) {
         /* the sorted-key buffer is free after the sort: the scratch order */
         k_order_blocksum<<<sg, NBG_SCAN_BLOCK, 0, st>>>(ctl, cb.perm, remap, cb.blk_sum);
         k_scan_blocks<<<1, NBG_SCAN_BLOCK, 0, st>>>(ctl, cb.seg, cb.blk_sum, cb.blk_off, 2, cb.cap, cb.frag_cap);
         k_order_carry<<<sg, NBG_SCAN_BLOCK, 0, st>>>(ctl, cb.seg, cb.perm, remap, cb.blk_off, cb.skey[0]);
-        k_order_copy<<<flat_grid(cb.cap), 256, 0, st>>>(ctl, cb.seg, cb.skey[0], cb.perm);
+        k_order_copy<<<nbg_flat_grid(cb, cb.cap), 256, 0, st>>>(ctl, cb.seg, cb.skey[0], cb.perm);
     }
     k_end<<<1, NBG_SCAN_BLOCK, 0, st>>>(ctl, cb.seg);
 }
@@ -1367,12 +1361,12 @@ void nbg_launch_remove(const CycleBufs &cb, DevCtl *ctl, ll count, ll *removed_d
 void nbg_launch_edits(const CycleBufs &cb, DevCtl *ctl, const nbg_edit *edits_dev, ll k, int *results_dev,
                       cudaStream_t st)
 {
-    k_edits<<<flat_grid(cb.cap), 256, 0, st>>>(cb.a, ctl, edits_dev, k, results_dev);
+    k_edits<<<nbg_flat_grid(cb, cb.cap), 256, 0, st>>>(cb.a, ctl, edits_dev, k, results_dev);
 }
 
 void nbg_launch_find(const CycleBufs &cb, DevCtl *ctl, ll id, ll *idx_dev, cudaStream_t st)
 {
-    k_find<<<flat_grid(cb.cap), 256, 0, st>>>(cb.a, ctl, id, idx_dev);
+    k_find<<<nbg_flat_grid(cb, cb.cap), 256, 0, st>>>(cb.a, ctl, id, idx_dev);
 }
 
 void nbg_launch_energy(const CycleBufs &cb, DevCtl *ctl, double *out_dev, cudaStream_t st)

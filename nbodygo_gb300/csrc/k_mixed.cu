@@ -689,22 +689,16 @@ int nbg_mixed_slots(int device, int variant)
     return slots;
 }
 
-static int flat_grid(ll cap)
-{
-    ll g = (cap + 255) / 256;
-    if (g > 152 * 16) g = 152 * 16;
-    return (int)(g < 1 ? 1 : g);
-}
 
 void nbg_launch_mixed_prep(const CycleBufs &cb, DevCtl *ctl, cudaStream_t st)
 {
-    const int fg = flat_grid(cb.cap);
+    const int fg = nbg_flat_grid(cb, cb.cap);
     k_mix_reduce<<<fg, 256, 0, st>>>(cb.a, ctl, cb.seg);
     nbg_launch_spatial_sort(cb, ctl, st);
     k_mix_pack<<<fg, 256, 0, st>>>(cb.a, ctl, cb.perm, cb.jhi, cb.jlo);
     const int itile = cb.itile > 0 ? cb.itile : NBG_MIX_ITILE;
     ll tiles = (cb.cap + itile - 1) / itile + cb.seg.nsims;
-    if (tiles > 152 * 64) tiles = 152 * 64;
+    if (tiles > (ll)(cb.sms > 0 ? cb.sms : 1) * 64) tiles = (ll)(cb.sms > 0 ? cb.sms : 1) * 64;
     k_mix_tiles<<<(int)tiles, TILES_BLOCK, 0, st>>>(ctl, cb.seg, cb.jhi, cb.jlo, cb.tile_c, itile);
     k_mix_iprep<<<fg, 256, 0, st>>>(ctl, cb.seg, cb.jhi, cb.jlo, cb.tile_c, cb.iprep, itile);
 }
@@ -725,6 +719,6 @@ void nbg_launch_mixed_pair(const CycleBufs &cb, DevCtl *ctl, cudaStream_t st)
 
 void nbg_launch_mixed_out(const CycleBufs &cb, DevCtl *ctl, cudaStream_t st)
 {
-    k_mix_out<<<flat_grid(cb.cap), 256, 0, st>>>(cb.a, ctl, cb.seg, cb.perm, cb.part,
+    k_mix_out<<<nbg_flat_grid(cb, cb.cap), 256, 0, st>>>(cb.a, ctl, cb.seg, cb.perm, cb.part,
                                                  cb.itile > 0 ? cb.itile : NBG_MIX_ITILE);
 }

@@ -262,8 +262,8 @@ __global__ void k_sort_decide(DevCtl *ctl)
 void nbg_launch_spatial_sort(const CycleBufs &cb, DevCtl *ctl, cudaStream_t st)
 {
     k_sort_decide<<<1, 1, 0, st>>>(ctl);
-    const int g = (int)((cb.cap + 255) / 256 < 152 * 16 ? (cb.cap + 255) / 256 : 152 * 16);
-    k_morton_keys<<<g > 0 ? g : 1, 256, 0, st>>>(cb.a, ctl, cb.seg, cb.skey[0], cb.perm);
+    const int g = nbg_flat_grid(cb, cb.cap);
+    k_morton_keys<<<g, 256, 0, st>>>(cb.a, ctl, cb.seg, cb.skey[0], cb.perm);
     const int nb = (int)((cb.cap + RS_TILE - 1) / RS_TILE);
     const int nchunk = (int)(((ll)nb * RS_BINS + RS_SCAN_CHUNK - 1) / RS_SCAN_CHUNK);
     unsigned *kin = cb.skey[0], *vin = cb.perm, *kout = cb.skey[1], *vout = cb.sval;

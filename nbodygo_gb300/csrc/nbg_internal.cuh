@@ -225,6 +225,17 @@ struct CycleBufs {
     BhTree t;
 };
 
+/* Grid of a grid-stride kernel over `items` items, 256 threads per CTA:
+ * one CTA per 256 items, at most `per_sm` CTAs per streaming multiprocessor
+ * of the device the buffers live on. */
+static inline int nbg_flat_grid(const CycleBufs &cb, ll items, int per_sm = 16)
+{
+    const ll most = (ll)(cb.sms > 0 ? cb.sms : 1) * per_sm;
+    ll g = (items + 255) / 256;
+    if (g > most) g = most;
+    return (int)(g < 1 ? 1 : g);
+}
+
 /* Shapes of the mixed pair kernel the autotuner chooses from. */
 struct MixVariantInfo {
     int block, k, jt, unroll;

@@ -179,6 +179,8 @@ extern "C" int nbg_forces_mixed_noalloc(const double *x, const double *y, const 
     cb.mix_variant = 0; /* the default shape: 512-body i-tiles */
     cb.itile = NBG_MIX_ITILE;
     cb.slots = nbg_mixed_slots(dev, 0);
+    if (cudaDeviceGetAttribute(&cb.sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || cb.sms < 1)
+        return noalloc_fail(NBG_E_CUDA, "nbg_forces_mixed_noalloc: no multiprocessor count for the device");
     cb.seg = nbg_seg_carve(base + OFF_SEG, 1);
     DevCtl *ctl = (DevCtl *)(base + OFF_CTL);
 

@@ -38,6 +38,28 @@
 #include "../nbodygo_gb300/csrc/nbg_math.h"
 #include "../nbodygo_gb300/csrc/nbg_shared.h"
 
+/* The transcendentals of calcElasticCollision (cmd/body/collisioncalc.go:
+ * 104-160).  The shipping oracle uses nbg_math.h, the functions the GPU uses,
+ * so the two agree bit for bit.  Built with -DNBG_ORACLE_LIBM (as
+ * libnbg_oracle_libm.so) it takes the platform libm's instead: a second
+ * instrument that bounds how far that shared substitution can move a
+ * trajectory, since Go's math package cannot run here. */
+#ifdef NBG_ORACLE_LIBM
+#define O_SIN sin
+#define O_COS cos
+#define O_TAN tan
+#define O_ASIN asin
+#define O_ACOS acos
+#define O_ATAN2 atan2
+#else
+#define O_SIN nbg_sin
+#define O_COS nbg_cos
+#define O_TAN nbg_tan
+#define O_ASIN nbg_asin
+#define O_ACOS nbg_acos
+#define O_ATAN2 nbg_atan2
+#endif
+
 /* ---- body record: cmd/body/body.go:26-52 -------------------------------- */
 
 typedef struct ob_frag {
@@ -531,15 +553,15 @@ static coll_res calc_elastic(const ob_body *b, const ob_body *o)
     vy1 = -vy21;
     vz1 = -vz21;
 
-    theta2 = nbg_acos(z2 / d);
+    theta2 = O_ACOS(z2 / d);
     if (x2 == 0 && y2 == 0)
         phi2 = 0;
     else
-        phi2 = nbg_atan2(y2, x2);
-    st = nbg_sin(theta2);
-    ct = nbg_cos(theta2);
-    sp = nbg_sin(phi2);
-    cp = nbg_cos(phi2);
+        phi2 = O_ATAN2(y2, x2);
+    st = O_SIN(theta2);
+    ct = O_COS(theta2);
+    sp = O_SIN(phi2);
+    cp = O_COS(phi2);
 
     vx1r = ct * cp * vx1 + ct * sp * vy1 - st * vz1;
     vy1r = cp * vy1 - sp * vx1;
@@ -549,24 +571,24 @@ static coll_res calc_elastic(const ob_body *b, const ob_body *o)
         fvz1r = 1;
     else if (fvz1r < -1)
         fvz1r = -1;
-    thetav = nbg_acos(fvz1r);
+    thetav = O_ACOS(fvz1r);
     if (vx1r == 0 && vy1r == 0)
         phiv = 0;
     else
-        phiv = nbg_atan2(vy1r, vx1r);
+        phiv = O_ATAN2(vy1r, vx1r);
 
-    dr = d * nbg_sin(thetav) / r12;
+    dr = d * O_SIN(thetav) / r12;
 
     if (thetav > NBG_PIO2_HI || fabs(dr) > 1) {
         res.collided = 0;
         return res;
     }
-    alpha = nbg_asin(-dr);
+    alpha = O_ASIN(-dr);
     beta = phiv;
-    sbeta = nbg_sin(beta);
-    cbeta = nbg_cos(beta);
+    sbeta = O_SIN(beta);
+    cbeta = O_COS(beta);
 
-    a = nbg_tan(thetav + alpha);
+    a = O_TAN(thetav + alpha);
     dvz2 = 2 * (vz1r + a * (cbeta * vx1r + sbeta * vy1r)) / ((1 + a * a) * (1 + m21));
 
     vz2r = dvz2;

@@ -13,17 +13,20 @@ from nbodygo_gb300 import _abi as A
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libnbg_oracle.so")
-_LIB = None
+# the same restatement with the platform libm's transcendentals in the elastic
+# collision instead of nbg_math.h (bounds the effect of that substitution)
+LIBM_LIB_PATH = os.path.join(HERE, "libnbg_oracle_libm.so")
+_LIBS = {}
 
 
-def load():
-    global _LIB
-    if _LIB is not None:
-        return _LIB
-    if not os.path.exists(LIB_PATH):
+def load(libm=False):
+    if libm in _LIBS:
+        return _LIBS[libm]
+    path = LIBM_LIB_PATH if libm else LIB_PATH
+    if not os.path.exists(path):
         from nbodygo_gb300 import build as _b
         _b.build_oracle()
-    lib = C.CDLL(LIB_PATH)
+    lib = C.CDLL(path)
     P = C.c_void_p
     pd = C.POINTER(C.c_double)
     sig = {
@@ -57,15 +60,15 @@ def load():
         fn = getattr(lib, name)
         fn.restype = res
         fn.argtypes = args
-    _LIB = lib
+    _LIBS[libm] = lib
     return lib
 
 
 class OracleSim:
     """Same surface as nbodygo_gb300.api.Simulation, on the CPU restatement."""
 
-    def __init__(self, seed=0x6E626F6479676F31, threads=1):
-        self.lib = load()
+    def __init__(self, seed=0x6E626F6479676F31, threads=1, libm=False):
+        self.lib = load(libm)
         self.s = self.lib.nbo_create(int(seed) & (2 ** 64 - 1))
         self.threads = threads
 
