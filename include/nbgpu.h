@@ -42,9 +42,10 @@ extern "C" {
 #define NBG_E_CUDA 1     /* a CUDA runtime call failed */
 #define NBG_E_ARG 2      /* bad argument (null pointer, size, enum value) */
 #define NBG_E_OVERFLOW 3 /* a device buffer was too small; state is unchanged */
-#define NBG_E_TIMEOUT 4  /* a bounded device wait gave up */
+#define NBG_E_TIMEOUT 4  /* nbg_step reached its deadline (NBG_OPT_STEP_DEADLINE_MS) */
 #define NBG_E_NAN 5      /* non-finite value where a finite one is required */
 #define NBG_E_STATE 6    /* call not valid in the context's current state */
+#define NBG_E_CANCELLED 7 /* nbg_step stopped by nbg_cancel */
 
 /* collision behaviours, values of globals.CollisionBehavior
  * (cmd/globals/globals.go:9-16) */
@@ -176,7 +177,8 @@ int nbg_set_bodies(nbg_ctx *ctx, const nbg_soa *host, int64_t n);
  * and one nbg_step advances all of them with the same dt and R.  This is
  * the batched form: many small simulations share each kernel launch.  No
  * counterpart in the reference, which runs one collection per process.
- * nbg_add_bodies and nbg_remove_bodies need a single collection. */
+ * nbg_add_bodies and nbg_remove_bodies need a single collection; their
+ * per-collection forms (nbg_add_bodies_to, nbg_remove_bodies_from) take one. */
 int nbg_set_collections(nbg_ctx *ctx, int64_t nsims, const int64_t *counts, const nbg_soa *host);
 /* Body count of each collection (up to cap entries); *nsims = collections. */
 int nbg_sim_counts(nbg_ctx *ctx, int64_t *counts, int64_t cap, int64_t *nsims);
@@ -204,13 +206,60 @@ int nbg_remove_bodies(nbg_ctx *ctx, int64_t count, int64_t *removed);
  * id into element 0 of `host`; *found = 0 if there is none. */
 int nbg_get_body(nbg_ctx *ctx, int64_t id, nbg_soa *host, int32_t *found);
 
+/* The same four controls addressed to collection `sim` (0-based, in the
+ * order nbg_set_collections loaded them) of a context holding several: the
+ * gRPC AddBody / ModBody / RemoveBodies / GetBody of one simulation
+ * (cmd/sim/grpcsimcb.go:15-70), each collection behaving as its own
+ * reference process.  sim = -1 means every collection for nbg_apply_edits_in
+ * and nbg_get_body_in.  Adds are appended by that collection's next Cycle,
+ * newest first; their ids come from the context's one counter unless given.
+ * processDeletes spreads `count` removals over that collection alone
+ * (computation-runner.go:176-216). */
+int nbg_add_bodies_to(nbg_ctx *ctx, int64_t sim, const nbg_soa *host, int64_t n, int64_t *ids_out);
+int nbg_apply_edits_in(nbg_ctx *ctx, int64_t sim, const nbg_edit *edits, int64_t k, int32_t *results);
+int nbg_remove_bodies_from(nbg_ctx *ctx, int64_t sim, int64_t count, int64_t *removed);
+int nbg_get_body_in(nbg_ctx *ctx, int64_t sim, int64_t id, nbg_soa *host, int32_t *found);
+
+/* ---- snapshots ---------------------------------------------------------- */
+
+/*
+ * A binary snapshot of everything the next cycle reads, so a run can stop
+ * and resume later, in this or another context, and repeat the
+ * uninterrupted run bit for bit.  The reference's CSV format
+ * (cmd/sim/fromcsv.go:46-116) holds only the public Body fields; a snapshot
+ * adds the private ones a cycle carries over (r, fragmenting and its
+ * fragInfo, collided, the stale force a fragmenting body re-applies,
+ * body.go:49-52,152-155), the NextId counter (body.go:316-329), the cycle
+ * index that keys the fragment generator, its seed, the host adds staged
+ * for the next Cycle, the collections' sizes, the precision form, kernel
+ * shape and options, and in the mixed form the bodies' current Morton order.
+ *
+ * nbg_save_state: *size receives the snapshot's bytes; with buf NULL that is
+ * all it does (a size query).  A cap below the size returns NBG_E_OVERFLOW.
+ * nbg_load_state replaces the context's bodies, collections, staged adds,
+ * counters and options with the snapshot's.  The layout is described in
+ * nbg_api.cu; values are in the machine's byte order.
+ */
+int nbg_save_state(nbg_ctx *ctx, void *buf, int64_t cap, int64_t *size);
+int nbg_load_state(nbg_ctx *ctx, const void *buf, int64_t size);
+
 /* ---- the cycle ---------------------------------------------------------- */
 
 /* Runs `nsteps` compute cycles with time step dt (timeScaling) and
  * coefficient of restitution R.  nsteps > 1 replays a CUDA graph of one cycle.
  * On NBG_E_OVERFLOW the context grows the buffer that was short and the
- * interrupted cycle can be re-run: state is left as it was before it. */
+ * interrupted cycle can be re-run: state is left as it was before it.
+ * A long call can be stopped: nbg_cancel, or the call's deadline, ends it at
+ * a cycle boundary within about two launches (graphs or single cycles) and
+ * it returns NBG_E_CANCELLED or NBG_E_TIMEOUT with *info filled and the
+ * state that after the info->steps_done cycles it ran. */
 int nbg_step(nbg_ctx *ctx, double dt, double R, int nsteps, nbg_step_info *info);
+
+/* Asks the nbg_step running on ctx - or, if none is, the next one - to stop
+ * at the next cycle boundary.  Safe to call from any thread: it is the one
+ * call that may overlap another call on the same context (the reference's
+ * runner stops between cycles the same way, computation-runner.go:225-245). */
+int nbg_cancel(nbg_ctx *ctx);
 
 /* Runs only the force + collision-detection pass of a cycle on the current
  * state: the forces of bodies that exist and are not fragmenting are
@@ -335,6 +384,9 @@ int nbg_get_timing(nbg_ctx *ctx, nbg_timing *t);
    first keeps the FP64 pipes busy when there are few bodies, at the cost of
    a 48 MB-per-thousand-bodies term buffer. */
 #define NBG_OPT_P64_SPLIT_MAX 11
+/* wall-clock limit of one nbg_step call in milliseconds (0 = none): the call
+   launches no further cycle once it has passed, and returns NBG_E_TIMEOUT */
+#define NBG_OPT_STEP_DEADLINE_MS 12
 #define NBG_OPT_NEAR_PPM 5   /* mixed: pairs closer than (value * 1e-6) x the i-body's
                                 distance from its tile origin take the near-pair
                                 pass: the exact hi/lo difference, FP64 for a

@@ -15,6 +15,7 @@ NBG_E_OVERFLOW = 3
 NBG_E_TIMEOUT = 4
 NBG_E_NAN = 5
 NBG_E_STATE = 6
+NBG_E_CANCELLED = 7
 
 NONE, SUBSUME, ELASTIC, FRAGMENT = 0, 1, 2, 3
 
@@ -45,6 +46,7 @@ OPT_MIX_SHAPE = 7
 OPT_BARNES_HUT = 8
 OPT_BH_SHAPE = 9
 OPT_SORT_INTERVAL = 10
+OPT_STEP_DEADLINE_MS = 12
 OPT_P64_SPLIT_MAX = 11
 MIX_SHAPES = 15
 
@@ -177,7 +179,14 @@ def declare(lib):
         "nbg_apply_edits": (C.c_int, [P, C.POINTER(NbgEdit), C.c_int64, _pi32]),
         "nbg_remove_bodies": (C.c_int, [P, C.c_int64, _pi64]),
         "nbg_get_body": (C.c_int, [P, C.c_int64, C.POINTER(NbgSoa), _pi32]),
+        "nbg_add_bodies_to": (C.c_int, [P, C.c_int64, C.POINTER(NbgSoa), C.c_int64, _pi64]),
+        "nbg_apply_edits_in": (C.c_int, [P, C.c_int64, C.POINTER(NbgEdit), C.c_int64, _pi32]),
+        "nbg_remove_bodies_from": (C.c_int, [P, C.c_int64, C.c_int64, _pi64]),
+        "nbg_get_body_in": (C.c_int, [P, C.c_int64, C.c_int64, C.POINTER(NbgSoa), _pi32]),
+        "nbg_save_state": (C.c_int, [P, C.c_void_p, C.c_int64, _pi64]),
+        "nbg_load_state": (C.c_int, [P, C.c_void_p, C.c_int64]),
         "nbg_step": (C.c_int, [P, C.c_double, C.c_double, C.c_int, C.POINTER(NbgStepInfo)]),
+        "nbg_cancel": (C.c_int, [P]),
         "nbg_force_pass": (C.c_int, [P]),
         "nbg_get_renderables": (C.c_int, [P, C.c_void_p, C.c_int64, _pi64]),
         "nbg_get_events": (C.c_int, [P, C.c_void_p, C.c_int64, _pi64]),

@@ -206,40 +206,88 @@ class Simulation:
         m = min(cap, got.value)
         return {k: v[:m] for k, v in out.items()}
 
-    def add_bodies(self, bodies):
+    def add_bodies(self, bodies, sim=None):
+        """Enqueue(NewAdd) for every body; `sim` names one collection of a
+        context holding several (nbg_add_bodies_to).  Returns the ids."""
         n = len(bodies["x"])
         soa, keep = A.soa_from_arrays(bodies)
         ids = np.zeros(max(n, 1), dtype=np.int64)
-        self._check(self.lib.nbg_add_bodies(self.ctx, C.byref(soa), n, ids.ctypes.data_as(C.POINTER(C.c_int64))))
+        pids = ids.ctypes.data_as(C.POINTER(C.c_int64))
+        if sim is None:
+            self._check(self.lib.nbg_add_bodies(self.ctx, C.byref(soa), n, pids))
+        else:
+            self._check(self.lib.nbg_add_bodies_to(self.ctx, int(sim), C.byref(soa), n, pids))
         del keep
         return ids[:n]
 
-    def apply_edits(self, edits):
+    def apply_edits(self, edits, sim=None):
+        """ModBody by id; `sim` limits the edits to one collection."""
         arr = A.edit_array(edits)
         res = np.zeros(max(1, len(edits)), dtype=np.int32)
-        self._check(self.lib.nbg_apply_edits(self.ctx, arr, len(edits), res.ctypes.data_as(C.POINTER(C.c_int32))))
+        pres = res.ctypes.data_as(C.POINTER(C.c_int32))
+        if sim is None:
+            self._check(self.lib.nbg_apply_edits(self.ctx, arr, len(edits), pres))
+        else:
+            self._check(self.lib.nbg_apply_edits_in(self.ctx, int(sim), arr, len(edits), pres))
         return res[:len(edits)]
 
-    def remove_bodies(self, count):
+    def remove_bodies(self, count, sim=None):
+        """processDeletes; `sim` names one collection of several."""
         v = C.c_int64()
-        self._check(self.lib.nbg_remove_bodies(self.ctx, int(count), C.byref(v)))
+        if sim is None:
+            self._check(self.lib.nbg_remove_bodies(self.ctx, int(count), C.byref(v)))
+        else:
+            self._check(self.lib.nbg_remove_bodies_from(self.ctx, int(sim), int(count), C.byref(v)))
         return v.value
 
-    def get_body(self, body_id):
+    def get_body(self, body_id, sim=None):
         out = A.empty_state(1)
         soa, keep = A.soa_from_arrays(out)
         found = C.c_int32()
-        self._check(self.lib.nbg_get_body(self.ctx, int(body_id), C.byref(soa), C.byref(found)))
+        if sim is None:
+            self._check(self.lib.nbg_get_body(self.ctx, int(body_id), C.byref(soa), C.byref(found)))
+        else:
+            self._check(self.lib.nbg_get_body_in(self.ctx, int(sim), int(body_id), C.byref(soa), C.byref(found)))
         del keep
         if not found.value:
             return None
         return {k: v[0] for k, v in out.items()}
+
+    # ---- snapshots ----
+    def save_state(self):
+        """The context's full state as a snapshot (bytes), to resume later
+        with load_state in this or another context."""
+        size = C.c_int64()
+        self._check(self.lib.nbg_save_state(self.ctx, None, 0, C.byref(size)))
+        buf = C.create_string_buffer(size.value)
+        self._check(self.lib.nbg_save_state(self.ctx, buf, size.value, C.byref(size)))
+        return buf.raw[:size.value]
+
+    def load_state(self, snapshot):
+        data = bytes(snapshot)
+        self._check(self.lib.nbg_load_state(self.ctx, data, len(data)))
 
     # ---- the cycle ----
     def step(self, dt, R=1.0, nsteps=1):
         info = A.NbgStepInfo()
         self._check(self.lib.nbg_step(self.ctx, float(dt), float(R), int(nsteps), C.byref(info)))
         return {f: getattr(info, f) for f, _ in A.NbgStepInfo._fields_}
+
+    def step_until(self, dt, R=1.0, nsteps=1):
+        """Like step, but a call stopped by cancel() or the deadline option
+        (OPT_STEP_DEADLINE_MS) returns (info, status) instead of raising:
+        status is NBG_OK, NBG_E_CANCELLED or NBG_E_TIMEOUT, and info counts
+        the cycles that ran."""
+        info = A.NbgStepInfo()
+        rc = self.lib.nbg_step(self.ctx, float(dt), float(R), int(nsteps), C.byref(info))
+        if rc not in (A.NBG_OK, A.NBG_E_CANCELLED, A.NBG_E_TIMEOUT):
+            self._check(rc)
+        return {f: getattr(info, f) for f, _ in A.NbgStepInfo._fields_}, rc
+
+    def cancel(self):
+        """Stops the running (or next) step call at a cycle boundary; safe
+        from another thread."""
+        self._check(self.lib.nbg_cancel(self.ctx))
 
     def force_pass(self):
         """Recomputes the forces of the current state (no other change)."""

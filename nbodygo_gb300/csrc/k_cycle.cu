@@ -1157,25 +1157,35 @@ __global__ void __launch_bounds__(NBG_SCAN_BLOCK) k_end(DevCtl *ctl, SimSegs seg
 /* cycle-boundary edits                                                     */
 /* ------------------------------------------------------------------------ */
 
-/* processDeletes, computation-runner.go:176-216 (sequential by nature). */
-__global__ void k_remove(BodyArrays A, DevCtl *ctl, ll count, ll *removed)
+/* Bodies [lo, hi) of collection sim (sim < 0: the whole array). */
+__device__ __forceinline__ void sim_range(const DevCtl *ctl, const SimSegs &seg, int sim, ll &lo, ll &hi)
+{
+    lo = sim >= 0 ? seg.off[sim] : 0;
+    hi = sim >= 0 ? seg.off[sim + 1] : ctl->n;
+}
+
+/* processDeletes, computation-runner.go:176-216 (sequential by nature), over
+ * collection sim (sim < 0: the whole array, one collection). */
+__global__ void k_remove(BodyArrays A, DevCtl *ctl, SimSegs seg, int sim, ll count, ll *removed)
 {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
-    const ll n = ctl->n;
+    ll lo, hi;
+    sim_range(ctl, seg, sim, lo, hi);
+    const ll n = hi - lo;
     ll rem = 0;
     if (count == -1) {
-        for (ll k = 0; k < n; k++) {
+        for (ll k = lo; k < hi; k++) {
             if (A.flags[k] & NBG_F_EXISTS) {
                 A.m[k] = 0;
                 A.flags[k] &= ~NBG_F_EXISTS;
                 rem++;
             }
         }
-    } else {
+    } else if (n > 0) {
         const ll step = count > n ? 1 : n / count;
         ll iter = 0;
         bool should = false;
-        for (ll k = 0; k < n; k++) {
+        for (ll k = lo; k < hi; k++) {
             if (iter % step == 0) should = true;
             iter++;
             unsigned f = A.flags[k];
@@ -1190,11 +1200,13 @@ __global__ void k_remove(BodyArrays A, DevCtl *ctl, ll count, ll *removed)
     *removed = rem;
 }
 
-/* ApplyMods for bodies matched by id (body.go:274-313, after parsing). */
-__global__ void k_edits(BodyArrays A, DevCtl *ctl, const nbg_edit *E, ll ne, int *results)
+/* ApplyMods for bodies matched by id (body.go:274-313, after parsing), in
+ * collection sim (sim < 0: every collection). */
+__global__ void k_edits(BodyArrays A, DevCtl *ctl, SimSegs seg, int sim, const nbg_edit *E, ll ne, int *results)
 {
-    const ll n = ctl->n;
-    for (ll k = (ll)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (ll)gridDim.x * blockDim.x) {
+    ll lo, hi;
+    sim_range(ctl, seg, sim, lo, hi);
+    for (ll k = lo + (ll)blockIdx.x * blockDim.x + threadIdx.x; k < hi; k += (ll)gridDim.x * blockDim.x) {
         const ll id = A.id[k];
         for (ll q = 0; q < ne; q++) {
             const nbg_edit e = E[q];
@@ -1221,11 +1233,20 @@ __global__ void k_edits(BodyArrays A, DevCtl *ctl, const nbg_edit *E, ll ne, int
     }
 }
 
-__global__ void k_find(BodyArrays A, DevCtl *ctl, ll id, ll *idx)
+/* The first body with this id in collection sim (sim < 0: anywhere). */
+__global__ void k_find(BodyArrays A, DevCtl *ctl, SimSegs seg, int sim, ll id, ll *idx)
 {
-    const ll n = ctl->n;
-    for (ll k = (ll)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (ll)gridDim.x * blockDim.x)
+    ll lo, hi;
+    sim_range(ctl, seg, sim, lo, hi);
+    for (ll k = lo + (ll)blockIdx.x * blockDim.x + threadIdx.x; k < hi; k += (ll)gridDim.x * blockDim.x)
         if (A.id[k] == id) atomicMin((long long *)idx, (long long)k);
+}
+
+/* dst[k] = src[index[k]] for k < n: every field of a body record. */
+__global__ void k_gather_bodies(BodyArrays S, BodyArrays D, const ll *index, ll n)
+{
+    for (ll k = (ll)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (ll)gridDim.x * blockDim.x)
+        copy_body(S, index[k], D, k);
 }
 
 /* Kinetic and pairwise potential energy plus momentum, per-block partials
@@ -1353,20 +1374,26 @@ void nbg_launch_after_pair(const CycleBufs &cb, DevCtl *ctl, cudaStream_t st, bo
     k_end<<<1, NBG_SCAN_BLOCK, 0, st>>>(ctl, cb.seg);
 }
 
-void nbg_launch_remove(const CycleBufs &cb, DevCtl *ctl, ll count, ll *removed_dev, cudaStream_t st)
+void nbg_launch_remove(const CycleBufs &cb, DevCtl *ctl, int sim, ll count, ll *removed_dev, cudaStream_t st)
 {
-    k_remove<<<1, 32, 0, st>>>(cb.a, ctl, count, removed_dev);
+    k_remove<<<1, 32, 0, st>>>(cb.a, ctl, cb.seg, sim, count, removed_dev);
 }
 
-void nbg_launch_edits(const CycleBufs &cb, DevCtl *ctl, const nbg_edit *edits_dev, ll k, int *results_dev,
+void nbg_launch_edits(const CycleBufs &cb, DevCtl *ctl, int sim, const nbg_edit *edits_dev, ll k, int *results_dev,
                       cudaStream_t st)
 {
-    k_edits<<<nbg_flat_grid(cb, cb.cap), 256, 0, st>>>(cb.a, ctl, edits_dev, k, results_dev);
+    k_edits<<<nbg_flat_grid(cb, cb.cap), 256, 0, st>>>(cb.a, ctl, cb.seg, sim, edits_dev, k, results_dev);
 }
 
-void nbg_launch_find(const CycleBufs &cb, DevCtl *ctl, ll id, ll *idx_dev, cudaStream_t st)
+void nbg_launch_find(const CycleBufs &cb, DevCtl *ctl, int sim, ll id, ll *idx_dev, cudaStream_t st)
 {
-    k_find<<<nbg_flat_grid(cb, cb.cap), 256, 0, st>>>(cb.a, ctl, id, idx_dev);
+    k_find<<<nbg_flat_grid(cb, cb.cap), 256, 0, st>>>(cb.a, ctl, cb.seg, sim, id, idx_dev);
+}
+
+void nbg_launch_gather(const CycleBufs &cb, const BodyArrays &src, const BodyArrays &dst, const ll *index_dev, ll n,
+                       cudaStream_t st)
+{
+    if (n > 0) k_gather_bodies<<<nbg_flat_grid(cb, n), 256, 0, st>>>(src, dst, index_dev, n);
 }
 
 void nbg_launch_energy(const CycleBufs &cb, DevCtl *ctl, double *out_dev, cudaStream_t st)

@@ -15,6 +15,8 @@
  * recomputes); the remaining kernels return at once, the host grows the
  * buffer and re-runs the cycle.
  */
+#include <atomic>
+#include <chrono>
 #include <cstdio>
 #include <cstdlib>
 #include <algorithm>
@@ -35,6 +37,9 @@ struct nbg_ctx {
     std::string err;
     ll n_host = 0;          /* bodies in the array, as of the last sync */
     ll pending_adds = 0;    /* host adds staged for the next cycle */
+    /* collection of each staged add, in the order of cb.adds: grouped by
+     * collection, arrival order within one (the order k_append_adds reads) */
+    std::vector<int> add_sim;
     bool timing = false;
     nbg_timing tacc{};
     std::vector<cudaEvent_t> evs;
@@ -54,6 +59,11 @@ struct nbg_ctx {
     ll *seg_h = nullptr;     /* pinned staging of the segment offsets */
     unsigned *flags_h = nullptr; /* pinned staging for the packed flag words */
     ll flags_cap = 0;
+    /* stopping a long nbg_step at a cycle boundary: nbg_cancel (any thread)
+     * and the wall-clock limit of one call (NBG_OPT_STEP_DEADLINE_MS) */
+    std::atomic<int> cancel{0};
+    ll deadline_ms = 0;
+    cudaEvent_t win[2] = {nullptr, nullptr}; /* the last two launches in flight */
 };
 
 /* (Re)allocates the per-sim arrays for nsims sims and uploads the offsets of
@@ -746,6 +756,8 @@ void nbg_destroy(nbg_ctx *ctx)
     cudaFree(ctx->ctl);
     if (ctx->ctl_h) cudaFreeHost(ctx->ctl_h);
     for (cudaEvent_t e : ctx->evs) cudaEventDestroy(e);
+    for (cudaEvent_t e : ctx->win)
+        if (e) cudaEventDestroy(e);
     if (ctx->own_st) cudaStreamDestroy(ctx->own_st);
     delete ctx;
 }
@@ -820,6 +832,7 @@ int nbg_set_collections(nbg_ctx *ctx, int64_t nsims, const int64_t *counts, cons
     CK(cudaSetDevice(ctx->device));
     CK(cudaStreamSynchronize(ctx->st));
     ctx->pending_adds = 0; /* a new collection drops staged adds */
+    ctx->add_sim.clear();
     int rc = ensure_cap(ctx, n, 0);
     if (rc != NBG_OK) return rc;
     if ((rc = upload_soa(ctx, ctx->cb.a, 0, host, n)) != NBG_OK) return rc;
@@ -930,16 +943,44 @@ int nbg_get_state(nbg_ctx *ctx, nbg_soa *h, int64_t cap, int64_t *n_out)
     return NBG_OK;
 }
 
-int nbg_add_bodies(nbg_ctx *ctx, const nbg_soa *host, int64_t n, int64_t *ids_out)
+/* a view of the arrays starting at body `off` */
+static BodyArrays arrays_at(const BodyArrays &A, ll off)
+{
+    BodyArrays v = A;
+    double **f[NBG_NF64];
+    f64_fields(v, f);
+    for (int q = 0; q < NBG_NF64; q++) *f[q] += off;
+    v.fr_cnt += off;
+    v.id += off;
+    v.flags += off;
+    return v;
+}
+
+/* Uploads the staged-add count of every collection (seg.hadd) and their
+ * total (the layout kernels recompute it from seg.hadd at the next cycle). */
+static int put_staged_counts(nbg_ctx *ctx)
+{
+    const int ns = ctx->cb.seg.nsims;
+    ll *h = ctx->seg_h; /* pinned; its previous copy was synchronised */
+    for (int s = 0; s < ns; s++) h[s] = 0;
+    for (int s : ctx->add_sim) h[s]++;
+    CK(cudaMemcpyAsync(ctx->cb.seg.hadd, h, (size_t)ns * sizeof(ll), cudaMemcpyHostToDevice, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
+    ll pa = ctx->pending_adds;
+    return ctl_put(ctx, offsetof(DevCtl, n_host_adds), &pa, sizeof pa);
+}
+
+int nbg_add_bodies_to(nbg_ctx *ctx, int64_t sim, const nbg_soa *host, int64_t n, int64_t *ids_out)
 {
     if (!ctx || n < 0 || (n > 0 && !host)) return fail(ctx, NBG_E_ARG, "bad arguments");
+    if (sim < 0 || sim >= ctx->cb.seg.nsims) return fail(ctx, NBG_E_ARG, "collection index out of range");
     if (n == 0) return NBG_OK;
-    if (ctx->cb.seg.nsims != 1) return fail(ctx, NBG_E_STATE, "adds need a single-collection context");
     CK(cudaSetDevice(ctx->device));
     int rc = sync_ctl(ctx);
     if (rc != NBG_OK) return rc;
-    if ((rc = ensure_adds_cap(ctx, ctx->pending_adds + n)) != NBG_OK) return rc;
-    if ((rc = ensure_cap(ctx, ctx->n_host + ctx->pending_adds + n, ctx->n_host)) != NBG_OK) return rc;
+    const ll pend = ctx->pending_adds;
+    if ((rc = ensure_adds_cap(ctx, pend + n)) != NBG_OK) return rc;
+    if ((rc = ensure_cap(ctx, ctx->n_host + pend + n, ctx->n_host)) != NBG_OK) return rc;
     std::vector<ll> ids((size_t)n);
     ll next = ctx->ctl_h->next_id;
     for (ll k = 0; k < n; k++) {
@@ -948,21 +989,52 @@ int nbg_add_bodies(nbg_ctx *ctx, const nbg_soa *host, int64_t n, int64_t *ids_ou
     }
     nbg_soa tmp = *host;
     tmp.id = (int64_t *)ids.data();
-    if ((rc = upload_soa(ctx, ctx->cb.adds, ctx->pending_adds, &tmp, n)) != NBG_OK) return rc;
-    ctx->pending_adds += n;
-    ll pa = ctx->pending_adds;
-    if ((rc = ctl_put(ctx, offsetof(DevCtl, n_host_adds), &pa, sizeof pa)) != NBG_OK) return rc;
-    CK(cudaMemcpyAsync(ctx->cb.seg.hadd, &pa, sizeof pa, cudaMemcpyHostToDevice, ctx->st));
-    CK(cudaStreamSynchronize(ctx->st));
+    if ((rc = upload_soa(ctx, ctx->cb.adds, pend, &tmp, n)) != NBG_OK) return rc;
+    /* keep the staged adds grouped by collection: the new ones belong after
+     * the last staged add of collections <= sim */
+    ll p = 0;
+    while (p < pend && ctx->add_sim[(size_t)p] <= (int)sim) p++;
+    if (p < pend) {
+        /* rotate [p, pend + n) so the new bodies come first: through the
+         * compaction target, which is free between cycles */
+        const ll m = pend + n - p;
+        if ((rc = ensure_scratch(ctx, (size_t)m * sizeof(ll))) != NBG_OK) return rc;
+        std::vector<ll> idx((size_t)m);
+        for (ll t = 0; t < m; t++) idx[(size_t)t] = t < n ? pend + t : p + (t - n);
+        CK(cudaMemcpyAsync(ctx->scratch, idx.data(), (size_t)m * sizeof(ll), cudaMemcpyHostToDevice, ctx->st));
+        nbg_launch_gather(ctx->cb, ctx->cb.adds, ctx->cb.b, (const ll *)ctx->scratch, m, ctx->st);
+        CK(cudaGetLastError());
+        BodyArrays dst = arrays_at(ctx->cb.adds, p);
+        CK(copy_arrays(dst, ctx->cb.b, m, ctx->st));
+        CK(cudaStreamSynchronize(ctx->st));
+    }
+    ctx->add_sim.insert(ctx->add_sim.begin() + p, (size_t)n, (int)sim);
+    ctx->pending_adds = pend + n;
+    if ((rc = put_staged_counts(ctx)) != NBG_OK) return rc;
     if ((rc = ctl_put(ctx, offsetof(DevCtl, next_id), &next, sizeof next)) != NBG_OK) return rc;
     if (ids_out)
         for (ll k = 0; k < n; k++) ids_out[k] = ids[(size_t)k];
     return NBG_OK;
 }
 
+int nbg_add_bodies(nbg_ctx *ctx, const nbg_soa *host, int64_t n, int64_t *ids_out)
+{
+    if (!ctx || n < 0 || (n > 0 && !host)) return fail(ctx, NBG_E_ARG, "bad arguments");
+    if (n == 0) return NBG_OK;
+    if (ctx->cb.seg.nsims != 1)
+        return fail(ctx, NBG_E_STATE, "several collections: name one with nbg_add_bodies_to");
+    return nbg_add_bodies_to(ctx, 0, host, n, ids_out);
+}
+
 int nbg_apply_edits(nbg_ctx *ctx, const nbg_edit *edits, int64_t k, int32_t *results)
 {
+    return nbg_apply_edits_in(ctx, -1, edits, k, results);
+}
+
+int nbg_apply_edits_in(nbg_ctx *ctx, int64_t sim, const nbg_edit *edits, int64_t k, int32_t *results)
+{
     if (!ctx || k < 0 || (k > 0 && !edits)) return fail(ctx, NBG_E_ARG, "bad arguments");
+    if (sim < -1 || sim >= ctx->cb.seg.nsims) return fail(ctx, NBG_E_ARG, "collection index out of range");
     if (k == 0) return NBG_OK;
     for (ll q = 0; q < k; q++)
         if ((edits[q].mask & NBG_M_COLLISION) && (edits[q].collision < NBG_NONE || edits[q].collision > NBG_FRAGMENT))
@@ -975,7 +1047,7 @@ int nbg_apply_edits(nbg_ctx *ctx, const nbg_edit *edits, int64_t k, int32_t *res
     int *res = (int *)((char *)ctx->scratch + ((eb + 255) / 256) * 256);
     CK(cudaMemcpyAsync(ed, edits, eb, cudaMemcpyHostToDevice, ctx->st));
     CK(cudaMemsetAsync(res, 0, rb, ctx->st));
-    nbg_launch_edits(ctx->cb, ctx->ctl, ed, k, res, ctx->st);
+    nbg_launch_edits(ctx->cb, ctx->ctl, (int)sim, ed, k, res, ctx->st);
     if ((rc = drop_order(ctx)) != NBG_OK) return rc;
     CK(cudaGetLastError());
     std::vector<int> hr((size_t)k);
@@ -989,12 +1061,20 @@ int nbg_apply_edits(nbg_ctx *ctx, const nbg_edit *edits, int64_t k, int32_t *res
 int nbg_remove_bodies(nbg_ctx *ctx, int64_t count, int64_t *removed)
 {
     if (!ctx) return NBG_E_ARG;
+    if (ctx->cb.seg.nsims != 1)
+        return fail(ctx, NBG_E_STATE, "several collections: name one with nbg_remove_bodies_from");
+    return nbg_remove_bodies_from(ctx, 0, count, removed);
+}
+
+int nbg_remove_bodies_from(nbg_ctx *ctx, int64_t sim, int64_t count, int64_t *removed)
+{
+    if (!ctx) return NBG_E_ARG;
     if (count == 0 || count < -1) return fail(ctx, NBG_E_ARG, "count must be -1 or positive");
-    if (ctx->cb.seg.nsims != 1) return fail(ctx, NBG_E_STATE, "RemoveBodies needs a single-collection context");
+    if (sim < 0 || sim >= ctx->cb.seg.nsims) return fail(ctx, NBG_E_ARG, "collection index out of range");
     CK(cudaSetDevice(ctx->device));
     int rc = ensure_scratch(ctx, sizeof(ll));
     if (rc != NBG_OK) return rc;
-    nbg_launch_remove(ctx->cb, ctx->ctl, count, (ll *)ctx->scratch, ctx->st);
+    nbg_launch_remove(ctx->cb, ctx->ctl, (int)sim, count, (ll *)ctx->scratch, ctx->st);
     if ((rc = drop_order(ctx)) != NBG_OK) return rc;
     CK(cudaGetLastError());
     ll r = 0;
@@ -1006,13 +1086,19 @@ int nbg_remove_bodies(nbg_ctx *ctx, int64_t count, int64_t *removed)
 
 int nbg_get_body(nbg_ctx *ctx, int64_t id, nbg_soa *h, int32_t *found)
 {
+    return nbg_get_body_in(ctx, -1, id, h, found);
+}
+
+int nbg_get_body_in(nbg_ctx *ctx, int64_t sim, int64_t id, nbg_soa *h, int32_t *found)
+{
     if (!ctx || !h || !found) return fail(ctx, NBG_E_ARG, "bad arguments");
+    if (sim < -1 || sim >= ctx->cb.seg.nsims) return fail(ctx, NBG_E_ARG, "collection index out of range");
     CK(cudaSetDevice(ctx->device));
     int rc = ensure_scratch(ctx, sizeof(ll));
     if (rc != NBG_OK) return rc;
     ll big = (ll)1 << 62;
     CK(cudaMemcpyAsync(ctx->scratch, &big, sizeof big, cudaMemcpyHostToDevice, ctx->st));
-    nbg_launch_find(ctx->cb, ctx->ctl, id, (ll *)ctx->scratch, ctx->st);
+    nbg_launch_find(ctx->cb, ctx->ctl, (int)sim, id, (ll *)ctx->scratch, ctx->st);
     CK(cudaGetLastError());
     ll idx = 0;
     CK(cudaMemcpyAsync(&idx, ctx->scratch, sizeof idx, cudaMemcpyDeviceToHost, ctx->st));
@@ -1053,6 +1139,210 @@ int nbg_get_body(nbg_ctx *ctx, int64_t id, nbg_soa *h, int32_t *found)
     CK(cudaStreamSynchronize(ctx->st));
     if (h->flags) h->flags[0] = f & 0xffu;
     if (h->collision) h->collision[0] = (int32_t)NBG_BEHAVIOR(f);
+    return NBG_OK;
+}
+
+/* ---- snapshots -------------------------------------------------------------
+ * Everything a later cycle reads, so a run resumed from a snapshot repeats
+ * the uninterrupted run bit for bit:
+ *   header (NBG_SNAP_HEADER_BYTES): counters, options and the layout below;
+ *   the body count of each collection, then its staged host adds;
+ *   the body arrays: the 20 FP64 fields of BodyArrays in declaration order,
+ *     fragment counts and ids (int64), flag words (uint32: NBG_F_* bits and
+ *     the behaviour), each field n values, padded to 8 bytes;
+ *   the staged host adds in the same layout (grouped by collection, arrival
+ *     order within one);
+ *   mixed form: the Morton order of the bodies (uint32 per body) when one is
+ *     current, so the FP32 pair sums group the same bodies.
+ * Values are stored in the machine's byte order (little-endian on x86-64 and
+ * aarch64); the header records the field count and per-body bytes. */
+static int select_variant(nbg_ctx *ctx, int v);
+
+#define NBG_SNAP_HEADER_BYTES 256
+#define NBG_SNAP_VERSION 1
+static const char NBG_SNAP_MAGIC[8] = {'N', 'B', 'G', 'S', 'N', 'A', 'P', '1'};
+
+struct SnapHeader {
+    char magic[8];
+    uint32_t version, header_bytes;
+    int32_t precision, nsims;
+    int64_t n, pending_adds, next_id;
+    uint64_t cycle, seed, sort_cycle;
+    int32_t sort_valid, sort_interval;
+    float near_kappa;
+    int32_t mix_variant, barnes_hut, has_order;
+    int32_t f64_fields, body_bytes;
+    int64_t total_bytes;
+};
+static_assert(sizeof(SnapHeader) <= NBG_SNAP_HEADER_BYTES, "snapshot header too large");
+
+static ll align8(ll v) { return (v + 7) & ~(ll)7; }
+
+/* bytes of one block of body arrays holding n bodies */
+static ll snap_arrays_bytes(ll n) { return (NBG_NF64 + 2) * align8(n * 8) + align8(n * 4); }
+
+struct SnapLayout {
+    ll counts, hadd, bodies, adds, order, total;
+};
+
+static SnapLayout snap_layout(ll nsims, ll n, ll pending, bool order)
+{
+    SnapLayout L;
+    L.counts = NBG_SNAP_HEADER_BYTES;
+    L.hadd = L.counts + nsims * 8;
+    L.bodies = L.hadd + nsims * 8;
+    L.adds = L.bodies + snap_arrays_bytes(n);
+    L.order = L.adds + snap_arrays_bytes(pending);
+    L.total = L.order + (order ? align8(n * 4) : 0);
+    return L;
+}
+
+/* Copies n bodies between device arrays A and the block at host address
+ * blk (to_host: device to host), stream-ordered; the caller synchronises. */
+static int snap_copy_arrays(nbg_ctx *ctx, BodyArrays &A, char *blk, ll n, bool to_host)
+{
+    if (n <= 0) return NBG_OK;
+    double **f[NBG_NF64];
+    f64_fields(A, f);
+    const cudaMemcpyKind kind = to_host ? cudaMemcpyDeviceToHost : cudaMemcpyHostToDevice;
+    ll o = 0;
+    for (int q = 0; q < NBG_NF64 + 3; q++) {
+        void *dev = q < NBG_NF64 ? (void *)*f[q] : q == NBG_NF64 ? (void *)A.fr_cnt : q == NBG_NF64 + 1
+                                                                    ? (void *)A.id : (void *)A.flags;
+        const ll bytes = n * (q < NBG_NF64 + 2 ? 8 : 4);
+        if (to_host)
+            CK(cudaMemcpyAsync(blk + o, dev, (size_t)bytes, kind, ctx->st));
+        else
+            CK(cudaMemcpyAsync(dev, blk + o, (size_t)bytes, kind, ctx->st));
+        o += align8(bytes);
+    }
+    return NBG_OK;
+}
+
+int nbg_save_state(nbg_ctx *ctx, void *buf, int64_t cap, int64_t *size)
+{
+    if (!ctx || !size || cap < 0) return fail(ctx, NBG_E_ARG, "bad arguments");
+    CK(cudaSetDevice(ctx->device));
+    int rc = sync_ctl(ctx);
+    if (rc != NBG_OK) return rc;
+    const DevCtl *h = ctx->ctl_h;
+    const ll n = h->n, pend = ctx->pending_adds;
+    const int ns = ctx->cb.seg.nsims;
+    const bool order = ctx->precision == NBG_PRECISION_MIXED && !ctx->cb.bh && h->sort_valid;
+    const SnapLayout L = snap_layout(ns, n, pend, order);
+    *size = L.total;
+    if (!buf) return NBG_OK;
+    if (cap < L.total) {
+        char m[128];
+        snprintf(m, sizeof m, "snapshot buffer too small: %lld bytes needed", (long long)L.total);
+        return fail(ctx, NBG_E_OVERFLOW, m);
+    }
+    char *out = (char *)buf;
+    memset(out, 0, NBG_SNAP_HEADER_BYTES);
+    SnapHeader H;
+    memset(&H, 0, sizeof H);
+    memcpy(H.magic, NBG_SNAP_MAGIC, 8);
+    H.version = NBG_SNAP_VERSION;
+    H.header_bytes = NBG_SNAP_HEADER_BYTES;
+    H.precision = ctx->precision;
+    H.nsims = ns;
+    H.n = n;
+    H.pending_adds = pend;
+    H.next_id = h->next_id;
+    H.cycle = h->cycle;
+    H.seed = h->seed;
+    H.sort_cycle = h->sort_cycle;
+    H.sort_valid = order ? 1 : 0;
+    H.sort_interval = h->sort_interval;
+    H.near_kappa = h->near_kappa;
+    H.mix_variant = ctx->cb.mix_variant;
+    H.barnes_hut = ctx->cb.bh;
+    H.has_order = order ? 1 : 0;
+    H.f64_fields = NBG_NF64;
+    H.body_bytes = NBG_NF64 * 8 + 8 + 8 + 4;
+    H.total_bytes = L.total;
+    memcpy(out, &H, sizeof H);
+    std::vector<ll> off((size_t)ns + 1);
+    CK(cudaMemcpyAsync(off.data(), ctx->cb.seg.off, off.size() * sizeof(ll), cudaMemcpyDeviceToHost, ctx->st));
+    if ((rc = snap_copy_arrays(ctx, ctx->cb.a, out + L.bodies, n, true)) != NBG_OK) return rc;
+    if ((rc = snap_copy_arrays(ctx, ctx->cb.adds, out + L.adds, pend, true)) != NBG_OK) return rc;
+    if (order) CK(cudaMemcpyAsync(out + L.order, ctx->cb.perm, (size_t)n * 4, cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
+    ll *counts = (ll *)(out + L.counts), *hadd = (ll *)(out + L.hadd);
+    for (int s = 0; s < ns; s++) {
+        counts[s] = off[(size_t)s + 1] - off[(size_t)s];
+        hadd[s] = 0;
+    }
+    for (int s : ctx->add_sim) hadd[s]++;
+    return NBG_OK;
+}
+
+int nbg_load_state(nbg_ctx *ctx, const void *buf, int64_t size)
+{
+    if (!ctx || !buf || size < NBG_SNAP_HEADER_BYTES) return fail(ctx, NBG_E_ARG, "not a snapshot: too short");
+    const char *in = (const char *)buf;
+    SnapHeader H;
+    memcpy(&H, in, sizeof H);
+    if (memcmp(H.magic, NBG_SNAP_MAGIC, 8) != 0) return fail(ctx, NBG_E_ARG, "not a snapshot: bad magic");
+    if (H.version != NBG_SNAP_VERSION || H.header_bytes != NBG_SNAP_HEADER_BYTES || H.f64_fields != NBG_NF64 ||
+        H.body_bytes != NBG_NF64 * 8 + 8 + 8 + 4)
+        return fail(ctx, NBG_E_ARG, "snapshot of another format version");
+    if (H.nsims < 1 || H.nsims > NBG_MAX_SIMS || H.n < 0 || H.n > NBG_MAX_BODIES || H.pending_adds < 0 ||
+        H.pending_adds > NBG_MAX_BODIES ||
+        (H.precision != NBG_PRECISION_FP64 && H.precision != NBG_PRECISION_MIXED) || H.mix_variant < 0 ||
+        H.mix_variant >= NBG_MIX_VARIANTS || H.sort_interval < 0 || H.sort_interval > 1000)
+        return fail(ctx, NBG_E_ARG, "snapshot header out of range");
+    const SnapLayout L = snap_layout(H.nsims, H.n, H.pending_adds, H.has_order != 0);
+    if (L.total != H.total_bytes || L.total > size) return fail(ctx, NBG_E_ARG, "snapshot truncated");
+    const ll *counts = (const ll *)(in + L.counts), *hadd = (const ll *)(in + L.hadd);
+    ll nsum = 0, asum = 0;
+    for (int s = 0; s < H.nsims; s++) {
+        if (counts[s] < 0 || hadd[s] < 0) return fail(ctx, NBG_E_ARG, "snapshot counts out of range");
+        nsum += counts[s];
+        asum += hadd[s];
+    }
+    if (nsum != H.n || asum != H.pending_adds) return fail(ctx, NBG_E_ARG, "snapshot counts do not add up");
+    CK(cudaSetDevice(ctx->device));
+    CK(cudaStreamSynchronize(ctx->st));
+    int rc;
+    /* the form and kernel shape the run used */
+    ctx->precision = H.precision;
+    if ((rc = nbg_set_option(ctx, NBG_OPT_BARNES_HUT, H.barnes_hut)) != NBG_OK) return rc;
+    if (H.mix_variant != ctx->cb.mix_variant && (rc = select_variant(ctx, H.mix_variant)) != NBG_OK) return rc;
+    ctx->pending_adds = 0;
+    ctx->add_sim.clear();
+    if ((rc = ensure_cap(ctx, H.n + H.pending_adds + 1, 0)) != NBG_OK) return rc;
+    char *src = const_cast<char *>(in);
+    if ((rc = snap_copy_arrays(ctx, ctx->cb.a, src + L.bodies, H.n, false)) != NBG_OK) return rc;
+    bool reshaped = false;
+    if ((rc = set_segments(ctx, H.nsims, counts, &reshaped)) != NBG_OK) return rc;
+    if (reshaped) invalidate_graph(ctx);
+    k_set_loaded<<<1, 1, 0, ctx->st>>>(ctx->ctl, H.n);
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(ctx->st)); /* the segment staging is free again */
+    ctx->n_host = H.n;
+    if (H.pending_adds > 0) {
+        if ((rc = ensure_adds_cap(ctx, H.pending_adds)) != NBG_OK) return rc;
+        if ((rc = snap_copy_arrays(ctx, ctx->cb.adds, src + L.adds, H.pending_adds, false)) != NBG_OK) return rc;
+        for (int s = 0; s < H.nsims; s++) ctx->add_sim.insert(ctx->add_sim.end(), (size_t)hadd[s], s);
+        ctx->pending_adds = H.pending_adds;
+    }
+    if ((rc = put_staged_counts(ctx)) != NBG_OK) return rc;
+    if (H.has_order) CK(cudaMemcpyAsync(ctx->cb.perm, in + L.order, (size_t)H.n * 4, cudaMemcpyHostToDevice, ctx->st));
+    /* counters and options, after k_set_loaded cleared the order */
+    DevCtl *h = ctx->ctl_h;
+    if ((rc = sync_ctl(ctx)) != NBG_OK) return rc;
+    h->next_id = H.next_id;
+    h->cycle = H.cycle;
+    h->seed = H.seed;
+    h->sort_valid = H.has_order ? 1 : 0;
+    h->sort_cycle = H.sort_cycle;
+    h->sort_interval = H.sort_interval;
+    h->near_kappa = H.near_kappa;
+    h->rend_n = 0;
+    h->last_ev_n = 0;
+    CK(cudaMemcpyAsync(ctx->ctl, h, sizeof(DevCtl), cudaMemcpyHostToDevice, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
     return NBG_OK;
 }
 
@@ -1122,8 +1412,43 @@ static int build_graph(nbg_ctx *ctx)
     return NBG_OK;
 }
 
-struct StepParams {
-    double dt, R;
+/* Launches of one nbg_step call, at most two in flight: before each launch
+ * after the second, the host waits for the launch two back to finish and
+ * then honours a cancel request or the call's deadline, so a long call
+ * stops within about two launches of cycles, at a cycle boundary. */
+struct LaunchWindow {
+    nbg_ctx *ctx;
+    std::chrono::steady_clock::time_point deadline;
+    bool has_deadline;
+    int issued = 0;
+    int stop = NBG_OK; /* NBG_E_CANCELLED or NBG_E_TIMEOUT once asked to stop */
+
+    /* true if the next launch may go */
+    bool admit(int *err)
+    {
+        *err = NBG_OK;
+        if (stop != NBG_OK) return false;
+        if (issued >= 2) {
+            cudaError_t e = cudaEventSynchronize(ctx->win[issued % 2]);
+            if (e != cudaSuccess) {
+                *err = fail(ctx, NBG_E_CUDA, std::string("cudaEventSynchronize: ") + cudaGetErrorString(e));
+                return false;
+            }
+        }
+        if (ctx->cancel.exchange(0) != 0)
+            stop = NBG_E_CANCELLED;
+        else if (has_deadline && std::chrono::steady_clock::now() >= deadline)
+            stop = NBG_E_TIMEOUT;
+        return stop == NBG_OK;
+    }
+    /* after a launch */
+    int issued_one()
+    {
+        cudaError_t e = cudaEventRecord(ctx->win[issued % 2], ctx->st);
+        issued++;
+        if (e != cudaSuccess) return fail(ctx, NBG_E_CUDA, std::string("cudaEventRecord: ") + cudaGetErrorString(e));
+        return NBG_OK;
+    }
 };
 
 int nbg_step(nbg_ctx *ctx, double dt, double R, int nsteps, nbg_step_info *info)
@@ -1146,6 +1471,10 @@ int nbg_step(nbg_ctx *ctx, double dt, double R, int nsteps, nbg_step_info *info)
         CK(cudaMemcpyAsync(ctx->ctl, h, sizeof(DevCtl), cudaMemcpyHostToDevice, ctx->st));
     }
     ctx->tacc = nbg_timing{};
+    for (cudaEvent_t &e : ctx->win)
+        if (!e) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    LaunchWindow win{ctx, std::chrono::steady_clock::now() + std::chrono::milliseconds(ctx->deadline_ms),
+                     ctx->deadline_ms > 0};
     int done = 0;
     int retries = 0;
     while (done < nsteps) {
@@ -1154,14 +1483,27 @@ int nbg_step(nbg_ctx *ctx, double dt, double R, int nsteps, nbg_step_info *info)
         if ((rc = ensure_p64(ctx)) != NBG_OK) return rc;
         const int todo = nsteps - done;
         if (ctx->timing || !ctx->use_graph || todo < ctx->graph_cycles || todo == 1) {
-            for (int s = 0; s < todo; s++) launch_cycle(ctx, ctx->precision, ctx->timing ? 4L * s : -1L);
+            for (int s = 0; s < todo; s++) {
+                if (!win.admit(&rc)) break;
+                launch_cycle(ctx, ctx->precision, ctx->timing ? 4L * s : -1L);
+                if ((rc = win.issued_one()) != NBG_OK) break;
+            }
         } else {
             /* whole graphs of graph_cycles cycles, the remainder directly */
             if ((rc = build_graph(ctx)) != NBG_OK) return rc;
             const int graphs = todo / ctx->graph_cycles;
-            for (int s = 0; s < graphs; s++) CK(cudaGraphLaunch(ctx->graph, ctx->st));
-            for (int s = graphs * ctx->graph_cycles; s < todo; s++) launch_cycle(ctx, ctx->precision, -1L);
+            for (int s = 0; s < graphs && rc == NBG_OK; s++) {
+                if (!win.admit(&rc)) break;
+                CK(cudaGraphLaunch(ctx->graph, ctx->st));
+                rc = win.issued_one();
+            }
+            for (int s = graphs * ctx->graph_cycles; s < todo && rc == NBG_OK && win.stop == NBG_OK; s++) {
+                if (!win.admit(&rc)) break;
+                launch_cycle(ctx, ctx->precision, -1L);
+                rc = win.issued_one();
+            }
         }
+        if (rc != NBG_OK) return rc;
         CK(cudaGetLastError());
         if ((rc = sync_ctl(ctx)) != NBG_OK) return rc;
         DevCtl *h = ctx->ctl_h;
@@ -1178,8 +1520,13 @@ int nbg_step(nbg_ctx *ctx, double dt, double R, int nsteps, nbg_step_info *info)
             }
         }
         ctx->tacc.kernel_launches += (ll)(now - done) * ctx->launches_per_cycle;
-        if (now > done) ctx->pending_adds = 0; /* consumed by the first cycle */
+        if (now > done) {
+            /* consumed by the first cycle */
+            ctx->pending_adds = 0;
+            ctx->add_sim.clear();
+        }
         done = now;
+        if (h->error == 0 && win.stop != NBG_OK) break; /* stopped at a cycle boundary */
         if (h->error == 0) continue;
         if (h->error != NBG_E_OVERFLOW || ++retries > 8) {
             char m[160];
@@ -1217,6 +1564,19 @@ int nbg_step(nbg_ctx *ctx, double dt, double R, int nsteps, nbg_step_info *info)
         info->next_id = h->next_id;
         info->bh_terms = h->acc_bh_terms;
     }
+    if (win.stop != NBG_OK && done < nsteps) {
+        char m[160];
+        snprintf(m, sizeof m, "%s after %d of %d cycles; the state is that after those cycles",
+                 win.stop == NBG_E_CANCELLED ? "cancelled" : "deadline reached", done, nsteps);
+        return fail(ctx, win.stop, m);
+    }
+    return NBG_OK;
+}
+
+int nbg_cancel(nbg_ctx *ctx)
+{
+    if (!ctx) return NBG_E_ARG;
+    ctx->cancel.store(1);
     return NBG_OK;
 }
 
@@ -1519,6 +1879,10 @@ int nbg_set_option(nbg_ctx *ctx, int key, int64_t value)
             ctx->graph_cycles = (int)value;
             invalidate_graph(ctx);
         }
+        return NBG_OK;
+    case NBG_OPT_STEP_DEADLINE_MS:
+        if (value < 0 || value > ((ll)1 << 40)) return fail(ctx, NBG_E_ARG, "deadline must be 0..2^40 ms");
+        ctx->deadline_ms = value;
         return NBG_OK;
     case NBG_OPT_P64_SPLIT_MAX:
         if (value < 0 || value > NBG_MAX_BODIES) return fail(ctx, NBG_E_ARG, "split limit must be 0..2^30");

@@ -339,10 +339,15 @@ void nbg_launch_begin(const CycleBufs &cb, DevCtl *ctl, cudaStream_t st);
 void nbg_launch_frag_count(const CycleBufs &cb, DevCtl *ctl, cudaStream_t st);
 void nbg_launch_pair_fp64(const CycleBufs &cb, DevCtl *ctl, cudaStream_t st);
 void nbg_launch_after_pair(const CycleBufs &cb, DevCtl *ctl, cudaStream_t st, bool carry_order);
-void nbg_launch_remove(const CycleBufs &cb, DevCtl *ctl, ll count, ll *removed_dev, cudaStream_t st);
-void nbg_launch_edits(const CycleBufs &cb, DevCtl *ctl, const nbg_edit *edits_dev, ll k, int *results_dev, cudaStream_t st);
+/* sim < 0: every collection (the whole array) */
+void nbg_launch_remove(const CycleBufs &cb, DevCtl *ctl, int sim, ll count, ll *removed_dev, cudaStream_t st);
+void nbg_launch_edits(const CycleBufs &cb, DevCtl *ctl, int sim, const nbg_edit *edits_dev, ll k, int *results_dev,
+                      cudaStream_t st);
 void nbg_launch_energy(const CycleBufs &cb, DevCtl *ctl, double *out_dev, cudaStream_t st);
-void nbg_launch_find(const CycleBufs &cb, DevCtl *ctl, ll id, ll *idx_dev, cudaStream_t st);
+void nbg_launch_find(const CycleBufs &cb, DevCtl *ctl, int sim, ll id, ll *idx_dev, cudaStream_t st);
+/* dst[k] = src[index[k]], k < n, every field (index on the device) */
+void nbg_launch_gather(const CycleBufs &cb, const BodyArrays &src, const BodyArrays &dst, const ll *index_dev, ll n,
+                       cudaStream_t st);
 int nbg_pair_fp64_grid(ll cap);
 int nbg_pair_fp64_launches(const CycleBufs &cb);
 /* largest capacity the plain form stores its pair terms for */
