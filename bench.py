@@ -90,7 +90,7 @@ def parse():
     ap.add_argument("--with-plain", action="store_true",
                     help="run the FP64 comparison on the uniform ball too (one FP64 force pass, ~2 min at 1M bodies)")
     ap.add_argument("--near-ppm", type=int, default=None,
-                    help="mixed: near-pair radius factor in parts per million (library default 35000)")
+                    help="mixed: near-pair radius factor in parts per million (library default 50000)")
     ap.add_argument("--chunks", type=int, default=None,
                     help="mixed: most chunks the pair work is cut into (library default 32 per resident CTA)")
     ap.add_argument("--p64-split-max", type=int, default=None,

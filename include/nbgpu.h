@@ -387,10 +387,17 @@ int nbg_get_timing(nbg_ctx *ctx, nbg_timing *t);
 /* wall-clock limit of one nbg_step call in milliseconds (0 = none): the call
    launches no further cycle once it has passed, and returns NBG_E_TIMEOUT */
 #define NBG_OPT_STEP_DEADLINE_MS 12
+/* ordering of a cycle's detected events (ProcessMods' order): up to 4,096
+   are sorted by one block in shared memory; more by a multi-block radix sort
+   when the cycle's launches include it, else by that one block in global
+   memory.  0 (default): include it in the calls after one whose busiest cycle
+   had more than 4,096 events, until a call stays under 1,024; 1: always;
+   2: never.  The order, and so every result, is the same either way. */
+#define NBG_OPT_EVENT_SORT 13
 #define NBG_OPT_NEAR_PPM 5   /* mixed: pairs closer than (value * 1e-6) x the i-body's
                                 distance from its tile origin take the near-pair
                                 pass: the exact hi/lo difference, FP64 for a
-                                possible overlap (default 35000) */
+                                possible overlap (default 50000) */
 int nbg_set_option(nbg_ctx *ctx, int key, int64_t value);
 
 /* Autotuner of the mixed pair kernel.  Fifteen shapes are compiled, each

@@ -47,6 +47,7 @@ OPT_BARNES_HUT = 8
 OPT_BH_SHAPE = 9
 OPT_SORT_INTERVAL = 10
 OPT_STEP_DEADLINE_MS = 12
+OPT_EVENT_SORT = 13
 OPT_P64_SPLIT_MAX = 11
 MIX_SHAPES = 15
 

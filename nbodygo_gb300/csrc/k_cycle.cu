@@ -484,9 +484,13 @@ __global__ void __launch_bounds__(SUM_THREADS, 4) k_p64_sum(BodyArrays A, DevCtl
 /* ------------------------------------------------------------------------ */
 
 #define SORT_BLOCK 1024
-#define SORT_SMEM 4096
+#define SORT_SMEM NBG_EV_BLOCK_SORT
 
-__global__ void __launch_bounds__(SORT_BLOCK) k_sort_events(DevCtl *ctl, ull *keys, ll cap)
+/* Orders the cycle's events by key (i, then j): up to SORT_SMEM in shared
+ * memory by one block.  More are left to the multi-block radix sort that
+ * follows when radix_follows is set; otherwise this block sorts them in
+ * global memory (bitonic, slow but correct). */
+__global__ void __launch_bounds__(SORT_BLOCK) k_sort_events(DevCtl *ctl, ull *keys, ll cap, int radix_follows)
 {
     __shared__ ull s[SORT_SMEM];
     __shared__ int bail;
@@ -498,11 +502,12 @@ __global__ void __launch_bounds__(SORT_BLOCK) k_sort_events(DevCtl *ctl, ull *ke
             ctl->error_need = ctl->ev_count;
             bail = 1;
         }
+        if (!bail && ctl->ev_count > ctl->acc_ev_max) ctl->acc_ev_max = ctl->ev_count;
     }
     __syncthreads();
     if (bail) return;
     const ll cnt = ctl->ev_count;
-    if (cnt <= 1) return;
+    if (cnt <= 1 || (cnt > SORT_SMEM && radix_follows)) return;
     ll P = 1;
     while (P < cnt) P <<= 1;
     ull *d = keys;
@@ -1351,7 +1356,8 @@ int nbg_pair_fp64_launches(const CycleBufs &cb)
 void nbg_launch_after_pair(const CycleBufs &cb, DevCtl *ctl, cudaStream_t st, bool carry_order)
 {
     const int sg = scan_grid(cb.cap);
-    k_sort_events<<<1, SORT_BLOCK, 0, st>>>(ctl, cb.ev_keys, cb.ev_cap);
+    k_sort_events<<<1, SORT_BLOCK, 0, st>>>(ctl, cb.ev_keys, cb.ev_cap, cb.ev_radix);
+    if (cb.ev_radix) nbg_launch_event_radix(cb, ctl, st);
     k_frag_emit<<<sg, NBG_SCAN_BLOCK, 0, st>>>(cb.a, cb.frags, ctl, cb.blk_off);
     /* the radix-sort key buffer is free after the pair pass: per-body owner words */
     k_resolve<<<cb.seg.nsims, RESOLVE_BLOCK, 0, st>>>(cb.a, ctl, cb.seg, cb.ev_keys, cb.ev_out, cb.skey[1]);

@@ -75,12 +75,29 @@ __global__ void k_morton_keys(BodyArrays A, DevCtl *ctl, SimSegs seg, unsigned *
     }
 }
 
+/* What a radix pass sorts.  RS_MORTON: the bodies' Morton keys (32-bit,
+ * with the permutation as values), in cycles that sort.  RS_EVENTS: the
+ * detected events' 64-bit keys i<<32 | j<<2 | type, when there are more than
+ * the one-block sort of k_cycle.cu holds.  The count comes from the control
+ * block, so one captured graph serves every count: passes with nothing to
+ * sort return at once. */
+#define RS_MORTON 0
+#define RS_EVENTS 1
+
+__device__ __forceinline__ ll rs_count(const DevCtl *ctl, int what)
+{
+    if (ctl->error) return 0;
+    if (what == RS_MORTON) return ctl->sort_now ? ctl->n : 0;
+    return ctl->ev_count > NBG_EV_BLOCK_SORT ? ctl->ev_count : 0;
+}
+
 /* per-block digit histogram, digit-major: hist[d * nb + b] */
-__global__ void __launch_bounds__(RS_BLOCK) k_rs_hist(DevCtl *ctl, const unsigned *keys, int shift, ll *hist)
+template <typename K>
+__global__ void __launch_bounds__(RS_BLOCK) k_rs_hist(DevCtl *ctl, int what, const K *keys, int shift, ll *hist)
 {
     __shared__ unsigned cnt[RS_BINS];
-    if (ctl->error || !ctl->sort_now) return;
-    const ll n = ctl->n;
+    const ll n = rs_count(ctl, what);
+    if (n == 0) return;
     const ll nb = (n + RS_TILE - 1) / RS_TILE;
     const ll b = blockIdx.x;
     if (b >= nb) return;
@@ -89,7 +106,7 @@ __global__ void __launch_bounds__(RS_BLOCK) k_rs_hist(DevCtl *ctl, const unsigne
     const ll base = b * RS_TILE;
     for (int q = 0; q < RS_ITEMS; q++) {
         ll k = base + (ll)q * RS_BLOCK + threadIdx.x;
-        if (k < n) atomicAdd(&cnt[(keys[k] >> shift) & 0xffu], 1u);
+        if (k < n) atomicAdd(&cnt[(unsigned)(keys[k] >> shift) & 0xffu], 1u);
     }
     __syncthreads();
     for (int d = threadIdx.x; d < RS_BINS; d += RS_BLOCK) hist[(ll)d * nb + b] = cnt[d];
@@ -102,9 +119,9 @@ __global__ void __launch_bounds__(RS_BLOCK) k_rs_hist(DevCtl *ctl, const unsigne
 #define RS_SCAN_ITEMS 8
 #define RS_SCAN_CHUNK (1024 * RS_SCAN_ITEMS)
 
-__device__ __forceinline__ ll rs_hist_total(const DevCtl *ctl)
+__device__ __forceinline__ ll rs_hist_total(const DevCtl *ctl, int what)
 {
-    return ((ctl->n + RS_TILE - 1) / RS_TILE) * RS_BINS;
+    return ((rs_count(ctl, what) + RS_TILE - 1) / RS_TILE) * RS_BINS;
 }
 
 /* block-wide inclusive scan of one value per thread (1024 threads) */
@@ -132,11 +149,11 @@ __device__ __forceinline__ ll rs_block_incl(ll x, ll *warp_tot, ll *block_total)
     return r;
 }
 
-__global__ void __launch_bounds__(1024) k_rs_scan_part(DevCtl *ctl, ll *hist)
+__global__ void __launch_bounds__(1024) k_rs_scan_part(DevCtl *ctl, int what, ll *hist)
 {
     __shared__ ll warp_tot[32];
-    if (ctl->error || !ctl->sort_now) return;
-    const ll total = rs_hist_total(ctl);
+    const ll total = rs_hist_total(ctl, what);
+    if (total == 0) return;
     const ll c0 = (ll)blockIdx.x * RS_SCAN_CHUNK;
     if (c0 >= total) return;
     ll s = 0;
@@ -149,11 +166,11 @@ __global__ void __launch_bounds__(1024) k_rs_scan_part(DevCtl *ctl, ll *hist)
     if (threadIdx.x == 0) hist[total + blockIdx.x] = tot;
 }
 
-__global__ void __launch_bounds__(1024) k_rs_scan_top(DevCtl *ctl, ll *hist)
+__global__ void __launch_bounds__(1024) k_rs_scan_top(DevCtl *ctl, int what, ll *hist)
 {
     __shared__ ll warp_tot[32];
-    if (ctl->error || !ctl->sort_now) return;
-    const ll total = rs_hist_total(ctl);
+    const ll total = rs_hist_total(ctl, what);
+    if (total == 0) return;
     const ll nchunk = (total + RS_SCAN_CHUNK - 1) / RS_SCAN_CHUNK;
     ll *sums = hist + total;
     ll carry = 0;
@@ -167,11 +184,11 @@ __global__ void __launch_bounds__(1024) k_rs_scan_top(DevCtl *ctl, ll *hist)
     }
 }
 
-__global__ void __launch_bounds__(1024) k_rs_scan_fin(DevCtl *ctl, ll *hist)
+__global__ void __launch_bounds__(1024) k_rs_scan_fin(DevCtl *ctl, int what, ll *hist)
 {
     __shared__ ll warp_tot[32];
-    if (ctl->error || !ctl->sort_now) return;
-    const ll total = rs_hist_total(ctl);
+    const ll total = rs_hist_total(ctl, what);
+    if (total == 0) return;
     const ll c0 = (ll)blockIdx.x * RS_SCAN_CHUNK;
     if (c0 >= total) return;
     /* thread t takes RS_SCAN_ITEMS consecutive entries */
@@ -191,15 +208,17 @@ __global__ void __launch_bounds__(1024) k_rs_scan_fin(DevCtl *ctl, ll *hist)
     }
 }
 
-/* stable scatter: element order within a block is kept per digit */
-__global__ void __launch_bounds__(RS_BLOCK) k_rs_scatter(DevCtl *ctl, const unsigned *keys_in, const unsigned *vals_in,
-                                                        unsigned *keys_out, unsigned *vals_out, int shift,
-                                                        const ll *offs)
+/* stable scatter: element order within a block is kept per digit (vals
+ * NULL: keys only) */
+template <typename K>
+__global__ void __launch_bounds__(RS_BLOCK) k_rs_scatter(DevCtl *ctl, int what, const K *keys_in,
+                                                        const unsigned *vals_in, K *keys_out, unsigned *vals_out,
+                                                        int shift, const ll *offs)
 {
     __shared__ ll base[RS_BINS];
     __shared__ unsigned wcnt[RS_BLOCK / 32][RS_BINS];
-    if (ctl->error || !ctl->sort_now) return;
-    const ll n = ctl->n;
+    const ll n = rs_count(ctl, what);
+    if (n == 0) return;
     const ll nb = (n + RS_TILE - 1) / RS_TILE;
     const ll b = blockIdx.x;
     if (b >= nb) return;
@@ -211,8 +230,8 @@ __global__ void __launch_bounds__(RS_BLOCK) k_rs_scatter(DevCtl *ctl, const unsi
         __syncthreads();
         const ll k = b * RS_TILE + (ll)q * RS_BLOCK + threadIdx.x;
         const bool ok = k < n;
-        const unsigned key = ok ? keys_in[k] : 0u;
-        const unsigned d = ok ? (key >> shift) & 0xffu : RS_BINS; /* RS_BINS never matches a real digit */
+        const K key = ok ? keys_in[k] : (K)0;
+        const unsigned d = ok ? (unsigned)(key >> shift) & 0xffu : RS_BINS; /* RS_BINS never matches a real digit */
         const unsigned peers = __match_any_sync(0xffffffffu, d);
         const unsigned rank = __popc(peers & lt);
         if (ok && rank == 0) wcnt[w][d] = __popc(peers);
@@ -221,7 +240,7 @@ __global__ void __launch_bounds__(RS_BLOCK) k_rs_scatter(DevCtl *ctl, const unsi
             ll pos = base[d] + rank;
             for (int v = 0; v < w; v++) pos += wcnt[v][d];
             keys_out[pos] = key;
-            vals_out[pos] = vals_in[k];
+            if (vals_in) vals_out[pos] = vals_in[k];
         }
         __syncthreads();
         for (int dd = threadIdx.x; dd < RS_BINS; dd += RS_BLOCK) {
@@ -269,11 +288,11 @@ void nbg_launch_spatial_sort(const CycleBufs &cb, DevCtl *ctl, cudaStream_t st)
     unsigned *kin = cb.skey[0], *vin = cb.perm, *kout = cb.skey[1], *vout = cb.sval;
     for (int pass = 0; pass < 4; pass++) {
         const int shift = 8 * pass;
-        k_rs_hist<<<nb, RS_BLOCK, 0, st>>>(ctl, kin, shift, cb.shist);
-        k_rs_scan_part<<<nchunk, 1024, 0, st>>>(ctl, cb.shist);
-        k_rs_scan_top<<<1, 1024, 0, st>>>(ctl, cb.shist);
-        k_rs_scan_fin<<<nchunk, 1024, 0, st>>>(ctl, cb.shist);
-        k_rs_scatter<<<nb, RS_BLOCK, 0, st>>>(ctl, kin, vin, kout, vout, shift, cb.shist);
+        k_rs_hist<unsigned><<<nb, RS_BLOCK, 0, st>>>(ctl, RS_MORTON, kin, shift, cb.shist);
+        k_rs_scan_part<<<nchunk, 1024, 0, st>>>(ctl, RS_MORTON, cb.shist);
+        k_rs_scan_top<<<1, 1024, 0, st>>>(ctl, RS_MORTON, cb.shist);
+        k_rs_scan_fin<<<nchunk, 1024, 0, st>>>(ctl, RS_MORTON, cb.shist);
+        k_rs_scatter<unsigned><<<nb, RS_BLOCK, 0, st>>>(ctl, RS_MORTON, kin, vin, kout, vout, shift, cb.shist);
         unsigned *t = kin;
         kin = kout;
         kout = t;
@@ -282,4 +301,41 @@ void nbg_launch_spatial_sort(const CycleBufs &cb, DevCtl *ctl, cudaStream_t st)
         vout = t;
     }
     /* four passes: the result is back in skey[0] / perm */
+}
+
+/* Events beyond the one-block sort: a stable LSD radix sort of their keys
+ * i<<32 | j<<2 | type on the bits that hold j (from bit 2) and i (from bit
+ * 32), 8-bit digits, between the event list and its ping-pong buffer.  An
+ * ordered pair (i, j) is detected once, so (i, j) decides the order and the
+ * type bits need no pass.  Digits may overlap (the last j digit reaches into
+ * i's bits): the lexicographic order over the passes is still the key order.
+ * The two halves take the same number of passes, so the result ends in the
+ * event list. */
+void nbg_launch_event_radix(const CycleBufs &cb, DevCtl *ctl, cudaStream_t st)
+{
+    int kb = 1; /* bits of a body index */
+    while (kb < 31 && ((ll)1 << kb) < cb.cap) kb++;
+    const int per_half = (kb + 7) / 8;
+    const int nb = (int)((cb.ev_cap + RS_TILE - 1) / RS_TILE);
+    const int nchunk = (int)(((ll)nb * RS_BINS + RS_SCAN_CHUNK - 1) / RS_SCAN_CHUNK);
+    ull *kin = cb.ev_keys, *kout = cb.ev_sort;
+    for (int pass = 0; pass < 2 * per_half; pass++) {
+        const int shift = pass < per_half ? 2 + 8 * pass : 32 + 8 * (pass - per_half);
+        k_rs_hist<ull><<<nb, RS_BLOCK, 0, st>>>(ctl, RS_EVENTS, kin, shift, cb.ev_hist);
+        k_rs_scan_part<<<nchunk, 1024, 0, st>>>(ctl, RS_EVENTS, cb.ev_hist);
+        k_rs_scan_top<<<1, 1024, 0, st>>>(ctl, RS_EVENTS, cb.ev_hist);
+        k_rs_scan_fin<<<nchunk, 1024, 0, st>>>(ctl, RS_EVENTS, cb.ev_hist);
+        k_rs_scatter<ull><<<nb, RS_BLOCK, 0, st>>>(ctl, RS_EVENTS, kin, nullptr, kout, nullptr, shift, cb.ev_hist);
+        ull *t = kin;
+        kin = kout;
+        kout = t;
+    }
+}
+
+/* launches of nbg_launch_event_radix for a capacity */
+int nbg_event_radix_launches(const CycleBufs &cb)
+{
+    int kb = 1;
+    while (kb < 31 && ((ll)1 << kb) < cb.cap) kb++;
+    return 2 * ((kb + 7) / 8) * 5;
 }

@@ -63,6 +63,8 @@ struct nbg_ctx {
      * and the wall-clock limit of one call (NBG_OPT_STEP_DEADLINE_MS) */
     std::atomic<int> cancel{0};
     ll deadline_ms = 0;
+    int ev_sort_mode = 0; /* NBG_OPT_EVENT_SORT */
+    int ev_radix_auto = 0; /* automatic choice for the next call */
     cudaEvent_t win[2] = {nullptr, nullptr}; /* the last two launches in flight */
 };
 
@@ -410,19 +412,36 @@ static int ensure_adds_cap(nbg_ctx *ctx, ll need)
     return NBG_OK;
 }
 
-static int ensure_ev_cap(nbg_ctx *ctx, ll need)
+static void free_events(CycleBufs &cb)
 {
-    if (need <= ctx->cb.ev_cap) return NBG_OK;
-    ll c = next_pow2(need > 65536 ? need : 65536);
-    cudaFree(ctx->cb.ev_keys);
-    cudaFree(ctx->cb.ev_out);
-    ctx->cb.ev_keys = nullptr;
-    ctx->cb.ev_out = nullptr;
+    cudaFree(cb.ev_keys);
+    cudaFree(cb.ev_out);
+    cudaFree(cb.ev_sort);
+    cudaFree(cb.ev_hist);
+    cb.ev_keys = cb.ev_sort = nullptr;
+    cb.ev_out = nullptr;
+    cb.ev_hist = nullptr;
+    cb.ev_cap = 0;
+}
+
+/* the event list of capacity c (a power of two), its sorted output and the
+ * multi-block sort's ping-pong buffer and histogram */
+static int alloc_events(nbg_ctx *ctx, ll c)
+{
+    free_events(ctx->cb);
     CK(cudaMalloc((void **)&ctx->cb.ev_keys, (size_t)c * sizeof(ull)));
     CK(cudaMalloc((void **)&ctx->cb.ev_out, (size_t)c * sizeof(nbg_event)));
+    CK(cudaMalloc((void **)&ctx->cb.ev_sort, (size_t)c * sizeof(ull)));
+    CK(cudaMalloc((void **)&ctx->cb.ev_hist, (size_t)nbg_sort_scratch_hist(c) * sizeof(ll)));
     ctx->cb.ev_cap = c;
     invalidate_graph(ctx);
     return NBG_OK;
+}
+
+static int ensure_ev_cap(nbg_ctx *ctx, ll need)
+{
+    if (need <= ctx->cb.ev_cap) return NBG_OK;
+    return alloc_events(ctx, next_pow2(need > 65536 ? need : 65536));
 }
 
 static int ensure_scratch(nbg_ctx *ctx, size_t bytes)
@@ -744,8 +763,7 @@ void nbg_destroy(nbg_ctx *ctx)
     free_arrays(ctx->cb.b);
     free_arrays(ctx->cb.adds);
     free_arrays(ctx->cb.frags);
-    cudaFree(ctx->cb.ev_keys);
-    cudaFree(ctx->cb.ev_out);
+    free_events(ctx->cb);
     free_cap_buffers(ctx->cb);
     nbg_bh_free(ctx->cb.t);
     if (ctx->ring_host) cudaHostUnregister(ctx->ring_host);
@@ -1390,7 +1408,8 @@ static void launch_cycle(nbg_ctx *ctx, int precision, long ev_base)
      * (which return at once in cycles that keep the order), pack, tile
      * origins, i-body set-up, the output and 4 that carry the order through
      * compaction; Barnes-Hut replaces the pair kernel with 55 (k_bh.cu) */
-    ctx->launches_per_cycle = (cb.bh ? 13 + 55 + (precision == NBG_PRECISION_MIXED ? 1 : 0)
+    ctx->launches_per_cycle = (cb.ev_radix ? nbg_event_radix_launches(cb) : 0) +
+                              (cb.bh ? 13 + 55 + (precision == NBG_PRECISION_MIXED ? 1 : 0)
                                      : precision == NBG_PRECISION_MIXED ? 45 : 13 + nbg_pair_fp64_launches(cb)) +
                               (cb.ring_head ? 1 : 0);
 }
@@ -1468,9 +1487,19 @@ int nbg_step(nbg_ctx *ctx, double dt, double R, int nsteps, nbg_step_info *info)
         h->error_need = 0;
         h->acc_steps = h->acc_interactions = h->acc_events = h->acc_frags = h->acc_removed = h->acc_nan = 0;
         h->acc_bh_terms = 0;
+        h->acc_ev_max = 0;
         CK(cudaMemcpyAsync(ctx->ctl, h, sizeof(DevCtl), cudaMemcpyHostToDevice, ctx->st));
     }
     ctx->tacc = nbg_timing{};
+    {
+        /* whether the cycles launch the multi-block event sort: forced by the
+         * option, else as the last call's busiest cycle asked */
+        const int want = ctx->ev_sort_mode == 1 ? 1 : ctx->ev_sort_mode == 2 ? 0 : ctx->ev_radix_auto;
+        if (want != ctx->cb.ev_radix) {
+            ctx->cb.ev_radix = want;
+            invalidate_graph(ctx);
+        }
+    }
     for (cudaEvent_t &e : ctx->win)
         if (!e) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     LaunchWindow win{ctx, std::chrono::steady_clock::now() + std::chrono::milliseconds(ctx->deadline_ms),
@@ -1551,6 +1580,16 @@ int nbg_step(nbg_ctx *ctx, double dt, double R, int nsteps, nbg_step_info *info)
         CK(cudaMemcpyAsync(&ctx->ctl->error, &z, sizeof z, cudaMemcpyHostToDevice, ctx->st));
         /* the failed cycle may have claimed a sort it never finished */
         if ((rc = drop_order(ctx)) != NBG_OK) return rc;
+    }
+    {
+        /* a cycle with more events than one block sorts in shared memory
+         * makes the next calls launch the multi-block sort; they drop it once
+         * a call stays well below that */
+        const ll evmax = ctx->ctl_h->acc_ev_max;
+        if (evmax > NBG_EV_BLOCK_SORT)
+            ctx->ev_radix_auto = 1;
+        else if (evmax <= NBG_EV_BLOCK_SORT / 4 && done > 0)
+            ctx->ev_radix_auto = 0;
     }
     if (info) {
         DevCtl *h = ctx->ctl_h;
@@ -1880,6 +1919,10 @@ int nbg_set_option(nbg_ctx *ctx, int key, int64_t value)
             invalidate_graph(ctx);
         }
         return NBG_OK;
+    case NBG_OPT_EVENT_SORT:
+        if (value < 0 || value > 2) return fail(ctx, NBG_E_ARG, "event sort mode must be 0..2");
+        ctx->ev_sort_mode = (int)value;
+        return NBG_OK;
     case NBG_OPT_STEP_DEADLINE_MS:
         if (value < 0 || value > ((ll)1 << 40)) return fail(ctx, NBG_E_ARG, "deadline must be 0..2^40 ms");
         ctx->deadline_ms = value;
@@ -1902,17 +1945,7 @@ int nbg_set_option(nbg_ctx *ctx, int key, int64_t value)
         if (value < 1 || value > ((ll)1 << 34)) return fail(ctx, NBG_E_ARG, "event capacity out of range");
         CK(cudaSetDevice(ctx->device));
         CK(cudaStreamSynchronize(ctx->st));
-        ctx->cb.ev_cap = 0;
-        ll c = next_pow2(value);
-        cudaFree(ctx->cb.ev_keys);
-        cudaFree(ctx->cb.ev_out);
-        ctx->cb.ev_keys = nullptr;
-        ctx->cb.ev_out = nullptr;
-        CK(cudaMalloc((void **)&ctx->cb.ev_keys, (size_t)c * sizeof(ull)));
-        CK(cudaMalloc((void **)&ctx->cb.ev_out, (size_t)c * sizeof(nbg_event)));
-        ctx->cb.ev_cap = c;
-        invalidate_graph(ctx);
-        return NBG_OK;
+        return alloc_events(ctx, next_pow2(value));
     }
     case NBG_OPT_FRAG_CAP: {
         if (value < 1 || value > NBG_MAX_BODIES) return fail(ctx, NBG_E_ARG, "fragment capacity out of range");

@@ -78,6 +78,7 @@ struct DevCtl {
     ll rend_n;       /* renderables written by the last cycle */
     ll last_ev_n;    /* resolved events recorded by the last cycle */
     ll cycle_interactions; /* sum over sims of n_s (n_s - 1) at the cycle start */
+    ll acc_ev_max;   /* most events one cycle of this nbg_step call detected */
     ll work_next;    /* mixed: next chunk for the persistent CTAs */
     /* Barnes-Hut (k_bh.cu): bounds of the tree bodies as order-preserving
      * integer images of doubles, the tree body count, nodes built, and the
@@ -100,9 +101,13 @@ struct DevCtl {
 
 #define NBG_SORT_INTERVAL_DEFAULT 4
 
+/* events sorted by one block in shared memory; more take the multi-block
+ * radix sort (when the cycle's launches include it) */
+#define NBG_EV_BLOCK_SORT 4096
+
 /* mixed: pairs closer than this factor x the i-body's distance from its
  * tile origin take the near-pair pass (NBG_OPT_NEAR_PPM changes it) */
-#define NBG_NEAR_KAPPA_DEFAULT 0.035f
+#define NBG_NEAR_KAPPA_DEFAULT 0.05f
 
 /* A collection may hold several independent simulations stored one after
  * another: sim s occupies bodies [off[s], off[s+1]) and bodies of different
@@ -189,8 +194,10 @@ struct CycleBufs {
     BodyArrays frags;   /* fragments emitted this cycle (arrival order) */
     ll cap, frag_cap, adds_cap;
     ull *ev_keys;
-    ull *ev_sort;       /* scratch for sorting when the count exceeds shared memory */
+    ull *ev_sort;       /* ping-pong partner of ev_keys for the multi-block event sort */
+    ll *ev_hist;        /* its digit histogram and chunk sums (nbg_sort_scratch_hist(ev_cap)) */
     ll ev_cap;
+    int ev_radix;       /* this cycle's launches include the multi-block event sort */
     nbg_event *ev_out;  /* resolved events of the last cycle */
     nbg_renderable *rend;
     ll *blk_sum;        /* per-block counts for the scans */
@@ -363,6 +370,8 @@ MixVariantInfo nbg_mix_variant_info(int variant);
 
 /* k_sort.cu */
 void nbg_launch_spatial_sort(const CycleBufs &cb, DevCtl *ctl, cudaStream_t st);
+void nbg_launch_event_radix(const CycleBufs &cb, DevCtl *ctl, cudaStream_t st);
+int nbg_event_radix_launches(const CycleBufs &cb);
 ll nbg_sort_scratch_hist(ll cap);
 
 /* k_probe.cu */
