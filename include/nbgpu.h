@@ -362,7 +362,7 @@ int nbg_get_timing(nbg_ctx *ctx, nbg_timing *t);
 #define NBG_OPT_FRAG_CAP 4   /* fragments one cycle may emit */
 #define NBG_OPT_GRAPH_CYCLES 6 /* cycles captured in one CUDA graph (default 1) */
 #define NBG_OPT_MIX_SHAPE 7    /* shape of the mixed pair kernel, 0..NBG_MIX_SHAPES-1 (see nbg_autotune) */
-#define NBG_MIX_SHAPES 15
+#define NBG_MIX_SHAPES 16
 /* 1: forces from the Barnes-Hut octree of cmd/body/octree.go (opening angle
  * 0.3, softening 1e-4, suns summed directly) with the FP64 arithmetic of the
  * plain form, in either precision; collisions stay exact.  This is the

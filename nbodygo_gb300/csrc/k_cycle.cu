@@ -80,7 +80,7 @@ __device__ static ll block_scan_array(int ns, F f, ll *out)
  * at least NBG_MIX_MIN_WORK units each, and few enough that the partial-sum
  * slots fit in part_doubles); the interaction count.  One block. */
 __global__ void __launch_bounds__(NBG_SCAN_BLOCK) k_begin(DevCtl *ctl, SimSegs seg, int slots, int work_cap, int itile,
-                                                          ll part_doubles)
+                                                          ll part_doubles, int sym, ll jpart_units)
 {
     if (ctl->error) return;
     const int ns = seg.nsims;
@@ -93,11 +93,19 @@ __global__ void __launch_bounds__(NBG_SCAN_BLOCK) k_begin(DevCtl *ctl, SimSegs s
     block_scan_array(ns, [&](int s) { return (off[s + 1] - off[s] + 63) / 64; }, seg.tile_off);
     const ll mtiles = block_scan_array(
         ns, [&](int s) { return (off[s + 1] - off[s] + itile - 1) / itile; }, seg.mtile_off);
+    /* one-sided kernel: (i-tile, j-body) units; symmetric kernel: the
+     * (block, block) pairs a <= b of each collection, T (T + 1) / 2 of them */
     const ll W = block_scan_array(
-        ns, [&](int s) { return (seg.mtile_off[s + 1] - seg.mtile_off[s]) * (off[s + 1] - off[s]); }, seg.item_off);
+        ns,
+        [&](int s) {
+            const ll T = seg.mtile_off[s + 1] - seg.mtile_off[s];
+            return sym ? T * (T + 1) / 2 : T * (off[s + 1] - off[s]);
+        },
+        seg.item_off);
     ll P = (ll)slots * NBG_MIX_CHUNKS_PER_CTA;
     if (work_cap > 0 && P > work_cap) P = work_cap;
-    if (P > W / NBG_MIX_MIN_WORK) P = W / NBG_MIX_MIN_WORK;
+    /* every chunk must hold work: the smallest guided chunk is W / (3 P) */
+    if (P > W / (sym ? 4 : NBG_MIX_MIN_WORK)) P = W / (sym ? 4 : NBG_MIX_MIN_WORK);
     const ll part_slots = part_doubles / (3ll * itile);
     if (P > part_slots - mtiles + 1) P = part_slots - mtiles + 1;
     if (P < 1) P = 1;
@@ -132,6 +140,10 @@ __global__ void __launch_bounds__(NBG_SCAN_BLOCK) k_begin(DevCtl *ctl, SimSegs s
             ctl->error = NBG_E_OVERFLOW;
             ctl->error_what = 4;
             ctl->error_need = (mtiles + P - 1) * 3ll * itile;
+        } else if (sym && W > jpart_units) {
+            ctl->error = NBG_E_OVERFLOW;
+            ctl->error_what = 6;
+            ctl->error_need = W;
         }
     }
 }
@@ -1303,7 +1315,7 @@ static int scan_grid(ll cap) { return (int)((cap + NBG_SCAN_TILE - 1) / NBG_SCAN
 void nbg_launch_begin(const CycleBufs &cb, DevCtl *ctl, cudaStream_t st)
 {
     k_begin<<<1, NBG_SCAN_BLOCK, 0, st>>>(ctl, cb.seg, cb.slots, cb.work_cap, cb.itile > 0 ? cb.itile : NBG_MIX_ITILE,
-                                          cb.part_doubles);
+                                          cb.part_doubles, cb.mix_variant == NBG_MIX_SYM, cb.jpart_units);
 }
 
 void nbg_launch_frag_count(const CycleBufs &cb, DevCtl *ctl, cudaStream_t st)

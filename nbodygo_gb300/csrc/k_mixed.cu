@@ -631,6 +631,413 @@ __global__ void k_mix_out(BodyArrays A, DevCtl *ctl, SimSegs seg, const unsigned
     }
 }
 
+/* ---- the symmetric pair kernel ---------------------------------------------
+ * Gravity is antisymmetric, f_ji = -f_ij, so each unordered pair is computed
+ * once and its term added to both bodies: 16 FMA-pipe lane operations per
+ * pair where the one-sided kernel spends 12 per direction, 24 per pair.
+ *
+ * Work.  A collection's sorted bodies form blocks of SYM_B (the i-tiles of
+ * the one-sided kernel, with the same origins and i-body set-up).  The
+ * units are the block pairs (a, b), a <= b, of each collection, row by row:
+ * row a holds (a, a) .. (a, T-1).  They are cut into chunks like the
+ * one-sided work; a chunk keeps block a's bodies in registers along a row.
+ *
+ * An off-diagonal unit (a < b).  Block b is staged in shared memory,
+ * re-centred on block a's origin.  Each warp holds 128 i-bodies (4 per lane)
+ * and takes block b in sub-blocks of 64 j: each lane loads two j (one packed
+ * f32x2 pair) and the j-pairs rotate through the warp's lanes with
+ * shuffles, 32 steps, carrying their force sums, so every lane meets every
+ * pair and every j-pair returns home with the sum of its 128 i-terms.  The
+ * per-warp sums of the j meet in shared memory and are added in warp order;
+ * the unit writes them as its own slot of FP32 j-partials.
+ *
+ * A diagonal unit (a == a) is one-sided: every body of the block against
+ * every other, i-sums only (both directions of each pair are in the block).
+ *
+ * Near pairs.  A pair closer than the i-body's near-pair threshold (the one
+ * the one-sided kernel uses, from the i-side error bound, which the shared dx
+ * carries to both directions) is masked out of both fast sums.  After the
+ * unit, the lanes that met one re-evaluate their near pairs exactly in FP64
+ * (candidate_pair: the reference's expressions, the overlap skip, the event
+ * i -> j), and the owners of the j that were met re-evaluate the same pairs
+ * from their side (the event j -> i and the j term).  Both sides decide
+ * "near" with the same FP32 expression, so they agree pair by pair.  Every
+ * sum is formed in a fixed order: results do not depend on scheduling.
+ *
+ * Sums.  i-sums fold into (hi, lo) pairs every 256 j and go to the one-sided
+ * kernel's per-(row, chunk) FP64 slots; j-sums of a unit (128 terms per
+ * warp, 4 warps) go to the unit's FP32 slot.  k_sym_out adds a body's row
+ * slots in chunk order, then its column's unit slots in row order, in FP64. */
+
+#define SYM_THREADS 128
+#define SYM_KI 4
+#define SYM_B (SYM_THREADS * SYM_KI) /* 512 bodies per block */
+#define SYM_WARPS (SYM_THREADS / 32)
+#define SYM_JP (SYM_B / 2)    /* j pairs per block */
+#define SYM_NSUB (SYM_B / 64) /* 64-j sub-blocks a warp rotates through */
+#define SYM_FOLD 4            /* sub-blocks between folds of the i-sums */
+static_assert(SYM_B == NBG_MIX_ITILE, "blocks are the i-tiles of the default shape");
+static_assert(SYM_NSUB % SYM_FOLD == 0, "whole folds per unit");
+
+/* first unit of row a in a collection of T blocks (rows a .. T-1 wide) */
+__host__ __device__ __forceinline__ ll sym_row_start(ll a, ll T) { return a * T - a * (a - 1) / 2; }
+
+/* row of unit v (0 <= v < T (T + 1) / 2) */
+__device__ __forceinline__ ll sym_row_of(ll v, ll T)
+{
+    const double b = 2.0 * (double)T + 1.0;
+    ll a = (ll)((b - sqrt(fmax(b * b - 8.0 * (double)v, 0.0))) * 0.5);
+    a = a < 0 ? 0 : (a > T - 1 ? T - 1 : a);
+    while (a > 0 && sym_row_start(a, T) > v) a--;
+    while (a < T - 1 && sym_row_start(a + 1, T) <= v) a++;
+    return a;
+}
+
+__device__ __forceinline__ float2 shfl2(float2 v, int src)
+{
+    return make_float2(__shfl_sync(FULL_MASK, v.x, src), __shfl_sync(FULL_MASK, v.y, src));
+}
+
+/* the FP32 near-pair decision and squared distance of one pair, as the fast
+ * loops form it (so the exact passes find exactly the masked pairs) */
+__device__ __forceinline__ float sym_r2(float xj, float yj, float zj, float nxi, float nyi, float nzi)
+{
+    const float dx = __fadd_rn(xj, nxi), dy = __fadd_rn(yj, nyi), dz = __fadd_rn(zj, nzi);
+    return __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
+}
+
+template <int MINB>
+__global__ void __launch_bounds__(SYM_THREADS, MINB)
+k_pair_sym(BodyArrays A, DevCtl *ctl, SimSegs seg, const float4 *__restrict__ jhi, const float4 *__restrict__ jlo,
+           const float4 *__restrict__ tile_c, const float4 *__restrict__ iprep, const unsigned *__restrict__ perm,
+           double *__restrict__ part, float *__restrict__ jpart, ull *ev_keys, ll ev_cap)
+{
+    /* block b, re-centred on block a's origin: j pair pp is (x0, x1, y0, y1),
+     * (z0, z1, m0, m1) */
+    __shared__ float4 sA[SYM_JP], sB[SYM_JP];
+    __shared__ float2 jacc[SYM_WARPS][3][SYM_JP]; /* per-warp j sums of the unit */
+    __shared__ float sfold[6][SYM_B];             /* i sums: (hi, lo) per component */
+    __shared__ unsigned char jnear[SYM_B];        /* j met a near pair in this unit */
+    __shared__ ll s_chunk;
+    if (ctl->error) return;
+    const int C = ctl->splits;
+    const ll W = ctl->work_total;
+    double ms = ctl->m_scale;
+    if (!(ms > 0.0)) ms = 1.0;
+    const double inv_ms = 1.0 / ms;
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    const int src = (lane + 1) & 31;
+
+    for (;;) {
+    if (tid == 0) s_chunk = (ll)atomicAdd((unsigned long long *)&ctl->work_next, 1ull);
+    __syncthreads();
+    const ll chunk = s_chunk;
+    __syncthreads();
+    if (chunk >= C) break;
+    ll U = nbg_chunk_start(chunk, C, W);
+    const ll U1 = nbg_chunk_start(chunk + 1, C, W);
+    int sim = U < W ? nbg_sim_of(seg.item_off, seg.nsims, U) : 0;
+    while (U < U1) {
+        while (seg.item_off[sim + 1] <= U) sim++;
+        const ll s0 = seg.off[sim], n = seg.off[sim + 1];
+        const ll T = seg.mtile_off[sim + 1] - seg.mtile_off[sim];
+        const ll v = U - seg.item_off[sim];
+        const ll a = sym_row_of(v, T);
+        const ll b0 = a + (v - sym_row_start(a, T));
+        const ll cnt = T - b0 < U1 - U ? T - b0 : U1 - U; /* units of row a in this chunk */
+        const ll g = seg.mtile_off[sim] + a;
+        const ll ibase = s0 + a * SYM_B;
+        const float4 c = tile_c[g];
+
+        /* block a: re-centred positions (negated, duplicated for the packed
+         * arithmetic), thresholds, and masses (negated) for the j terms;
+         * slots past the collection sit at the sentinel, massless */
+        float2 nx[SYM_KI], ny[SYM_KI], nz[SYM_KI], nm[SYM_KI];
+        float thr[SYM_KI];
+#pragma unroll
+        for (int k = 0; k < SYM_KI; k++) {
+            const ll p = ibase + (ll)k * SYM_THREADS + tid;
+            float xr = SENTINEL_POS, yr = SENTINEL_POS, zr = SENTINEL_POS, t = -1.f, m = 0.f;
+            if (p < n) {
+                const float4 q = iprep[p];
+                xr = q.x;
+                yr = q.y;
+                zr = q.z;
+                t = q.w;
+                m = jhi[p].w;
+            }
+            nx[k] = make_float2(-xr, -xr);
+            ny[k] = make_float2(-yr, -yr);
+            nz[k] = make_float2(-zr, -zr);
+            nm[k] = make_float2(-m, -m);
+            thr[k] = t;
+#pragma unroll
+            for (int cc = 0; cc < 6; cc++) sfold[cc][k * SYM_THREADS + tid] = 0.f;
+        }
+
+        for (ll bb = b0; bb < b0 + cnt; bb++) {
+            const ll u = U + (bb - b0); /* this unit's global index */
+            const ll jb = s0 + bb * SYM_B;
+            const bool diag = bb == a;
+            __syncthreads(); /* the previous unit's readers are done */
+            for (int sp = tid; sp < SYM_JP; sp += SYM_THREADS) {
+                float vv[2][4];
+#pragma unroll
+                for (int e = 0; e < 2; e++) {
+                    const ll q = jb + 2 * sp + e;
+                    float4 h = make_float4(0.f, 0.f, 0.f, 0.f), l = h;
+                    if (q < n) {
+                        h = jhi[q];
+                        l = jlo[q];
+                    }
+                    if (q < n && !packed_special(l)) {
+                        vv[e][0] = (h.x - c.x) + l.x;
+                        vv[e][1] = (h.y - c.y) + l.y;
+                        vv[e][2] = (h.z - c.z) + l.z;
+                        vv[e][3] = h.w;
+                    } else {
+                        vv[e][0] = vv[e][1] = vv[e][2] = SENTINEL_POS;
+                        vv[e][3] = 0.f;
+                    }
+                    jnear[2 * sp + e] = 0;
+                }
+                sA[sp] = make_float4(vv[0][0], vv[1][0], vv[0][1], vv[1][1]);
+                sB[sp] = make_float4(vv[0][2], vv[1][2], vv[0][3], vv[1][3]);
+            }
+            __syncthreads();
+
+            float2 ax[SYM_KI], ay[SYM_KI], az[SYM_KI];
+            unsigned nearmask = 0; /* bit k: i-body k met a near pair (besides itself) */
+            int selfnear[SYM_KI];
+#pragma unroll
+            for (int k = 0; k < SYM_KI; k++) {
+                ax[k] = ay[k] = az[k] = make_float2(0.f, 0.f);
+                selfnear[k] = 0;
+            }
+            auto fold = [&]() {
+#pragma unroll
+                for (int k = 0; k < SYM_KI; k++) {
+                    const int li = k * SYM_THREADS + tid;
+                    two_sum_add(sfold[0][li], sfold[1][li], ax[k].x + ax[k].y);
+                    two_sum_add(sfold[2][li], sfold[3][li], ay[k].x + ay[k].y);
+                    two_sum_add(sfold[4][li], sfold[5][li], az[k].x + az[k].y);
+                    ax[k] = ay[k] = az[k] = make_float2(0.f, 0.f);
+                }
+            };
+            if (!diag) {
+                /* symmetric: rotate 64-j sub-blocks through the warp */
+                for (int r = 0; r < SYM_NSUB; r++) {
+                    const int pp0 = ((w + r) % SYM_NSUB) * 32 + lane;
+                    const float4 qa = sA[pp0], qb = sB[pp0];
+                    float2 xj = make_float2(qa.x, qa.y), yj = make_float2(qa.z, qa.w);
+                    float2 zj = make_float2(qb.x, qb.y), mj = make_float2(qb.z, qb.w);
+                    float2 fx = make_float2(0.f, 0.f), fy = fx, fz = fx;
+#pragma unroll 2
+                    for (int s = 0; s < 32; s++) {
+#pragma unroll
+                        for (int k = 0; k < SYM_KI; k++) {
+                            const float2 dx = __fadd2_rn(xj, nx[k]);
+                            const float2 dy = __fadd2_rn(yj, ny[k]);
+                            const float2 dz = __fadd2_rn(zj, nz[k]);
+                            float2 r2 = __fmul2_rn(dx, dx);
+                            r2 = __ffma2_rn(dy, dy, r2);
+                            r2 = __ffma2_rn(dz, dz, r2);
+                            const bool n0 = r2.x < thr[k], n1 = r2.y < thr[k];
+                            if (n0 | n1) nearmask |= 1u << k;
+                            const float2 inv = make_float2(rsqrt_sfu(r2.x), rsqrt_sfu(r2.y));
+                            float2 inv3 = __fmul2_rn(__fmul2_rn(inv, inv), inv);
+                            inv3.x = n0 ? 0.f : inv3.x;
+                            inv3.y = n1 ? 0.f : inv3.y;
+                            const float2 si = __fmul2_rn(mj, inv3);
+                            const float2 sj = __fmul2_rn(nm[k], inv3);
+                            ax[k] = __ffma2_rn(si, dx, ax[k]);
+                            ay[k] = __ffma2_rn(si, dy, ay[k]);
+                            az[k] = __ffma2_rn(si, dz, az[k]);
+                            fx = __ffma2_rn(sj, dx, fx);
+                            fy = __ffma2_rn(sj, dy, fy);
+                            fz = __ffma2_rn(sj, dz, fz);
+                        }
+                        /* the next lane's pair, with its sums, moves here */
+                        xj = shfl2(xj, src);
+                        yj = shfl2(yj, src);
+                        zj = shfl2(zj, src);
+                        mj = shfl2(mj, src);
+                        fx = shfl2(fx, src);
+                        fy = shfl2(fy, src);
+                        fz = shfl2(fz, src);
+                    }
+                    /* 32 steps: the pair is home with the sums of all 128 i */
+                    jacc[w][0][pp0] = fx;
+                    jacc[w][1][pp0] = fy;
+                    jacc[w][2][pp0] = fz;
+                    if ((r + 1) % SYM_FOLD == 0) fold();
+                }
+            } else {
+                /* diagonal: one-sided over the block, pairs broadcast */
+                for (int pp = 0; pp < SYM_JP; pp++) {
+                    const float4 qa = sA[pp], qb = sB[pp];
+                    const float2 xj = make_float2(qa.x, qa.y), yj = make_float2(qa.z, qa.w);
+                    const float2 zj = make_float2(qb.x, qb.y), mj = make_float2(qb.z, qb.w);
+#pragma unroll
+                    for (int k = 0; k < SYM_KI; k++) {
+                        const float2 dx = __fadd2_rn(xj, nx[k]);
+                        const float2 dy = __fadd2_rn(yj, ny[k]);
+                        const float2 dz = __fadd2_rn(zj, nz[k]);
+                        float2 r2 = __fmul2_rn(dx, dx);
+                        r2 = __ffma2_rn(dy, dy, r2);
+                        r2 = __ffma2_rn(dz, dz, r2);
+                        const bool n0 = r2.x < thr[k], n1 = r2.y < thr[k];
+                        selfnear[k] += (int)n0 + (int)n1;
+                        const float2 inv = make_float2(rsqrt_sfu(r2.x), rsqrt_sfu(r2.y));
+                        float2 inv3 = __fmul2_rn(__fmul2_rn(inv, inv), inv);
+                        inv3.x = n0 ? 0.f : inv3.x;
+                        inv3.y = n1 ? 0.f : inv3.y;
+                        const float2 si = __fmul2_rn(mj, inv3);
+                        ax[k] = __ffma2_rn(si, dx, ax[k]);
+                        ay[k] = __ffma2_rn(si, dy, ay[k]);
+                        az[k] = __ffma2_rn(si, dz, az[k]);
+                    }
+                    if ((pp + 1) % 128 == 0) fold();
+                }
+                /* a live body's own pair is near (distance 0); one more is a
+                 * genuine near pair */
+#pragma unroll
+                for (int k = 0; k < SYM_KI; k++)
+                    if (selfnear[k] > 1) nearmask |= 1u << k;
+            }
+
+            /* exact pass, i side: this thread's near pairs, j in block order */
+#pragma unroll
+            for (int k = 0; k < SYM_KI; k++) {
+                if (!(nearmask & (1u << k))) continue;
+                const int li = k * SYM_THREADS + tid;
+                const ll p = ibase + li;
+                const ll i = perm[p];
+                for (int jj = 0; jj < SYM_B; jj++) {
+                    const ll q = jb + jj;
+                    if (q >= n || (diag && jj == li)) continue;
+                    const float4 qa = sA[jj >> 1], qb = sB[jj >> 1];
+                    const int e = jj & 1;
+                    const float r2 = sym_r2(e ? qa.y : qa.x, e ? qa.w : qa.z, e ? qb.y : qb.x, nx[k].x, ny[k].x,
+                                            nz[k].x);
+                    if (!(r2 < thr[k])) continue;
+                    double tx, ty, tz;
+                    candidate_pair(A, ctl, ev_keys, ev_cap, i, (ll)perm[q], inv_ms, tx, ty, tz);
+                    fold64(sfold[0][li], sfold[1][li], tx);
+                    fold64(sfold[2][li], sfold[3][li], ty);
+                    fold64(sfold[4][li], sfold[5][li], tz);
+                    jnear[jj] = 1;
+                }
+            }
+            if (diag) continue; /* a diagonal unit has no j slot */
+            __syncthreads(); /* jacc and jnear complete */
+
+            /* j side: the unit's sums in warp order, plus the exact terms of
+             * the j that met a near pair, i in block order */
+            float *jo = jpart + u * 3 * SYM_B;
+            for (int jj = tid; jj < SYM_B; jj += SYM_THREADS) {
+                const int pp = jj >> 1, e = jj & 1;
+                float sx = 0.f, sy = 0.f, sz = 0.f;
+#pragma unroll
+                for (int ww = 0; ww < SYM_WARPS; ww++) {
+                    sx += e ? jacc[ww][0][pp].y : jacc[ww][0][pp].x;
+                    sy += e ? jacc[ww][1][pp].y : jacc[ww][1][pp].x;
+                    sz += e ? jacc[ww][2][pp].y : jacc[ww][2][pp].x;
+                }
+                const ll q = jb + jj;
+                if (jnear[jj] && q < n) {
+                    const float4 qa = sA[pp], qb = sB[pp];
+                    const float xj = e ? qa.y : qa.x, yj = e ? qa.w : qa.z, zj = e ? qb.y : qb.x;
+                    const ll j = perm[q];
+                    double ex = 0.0, ey = 0.0, ez = 0.0;
+                    for (int ii = 0; ii < SYM_B; ii++) {
+                        const ll p = ibase + ii;
+                        if (p >= n) break;
+                        const float4 ip = iprep[p];
+                        const float r2 = sym_r2(xj, yj, zj, -ip.x, -ip.y, -ip.z);
+                        if (!(r2 < ip.w)) continue;
+                        double tx, ty, tz;
+                        candidate_pair(A, ctl, ev_keys, ev_cap, j, (ll)perm[p], inv_ms, tx, ty, tz);
+                        ex += tx;
+                        ey += ty;
+                        ez += tz;
+                    }
+                    sx = (float)((double)sx + ex);
+                    sy = (float)((double)sy + ey);
+                    sz = (float)((double)sz + ez);
+                }
+                jo[jj] = sx;
+                jo[SYM_B + jj] = sy;
+                jo[2 * SYM_B + jj] = sz;
+            }
+        }
+        /* this chunk's share of row a's i sums: slot g + chunk */
+        __syncthreads();
+        double *o = part + (g + chunk) * 3 * SYM_B;
+#pragma unroll
+        for (int k = 0; k < SYM_KI; k++) {
+            const int li = k * SYM_THREADS + tid;
+            o[li] = (double)sfold[0][li] + (double)sfold[1][li];
+            o[SYM_B + li] = (double)sfold[2][li] + (double)sfold[3][li];
+            o[2 * SYM_B + li] = (double)sfold[4][li] + (double)sfold[5][li];
+        }
+        U += cnt;
+    }
+    }
+}
+
+/* f = (G m_i m_scale) * (body p's row slots in chunk order, then its
+ * column's unit slots in row order), written to body perm[p]. */
+__global__ void k_sym_out(BodyArrays A, DevCtl *ctl, SimSegs seg, const unsigned *perm, const double *part,
+                          const float *jpart)
+{
+    if (ctl->error) return;
+    const ll n = ctl->n;
+    const int C = ctl->splits;
+    const ll W = ctl->work_total;
+    double ms = ctl->m_scale;
+    if (!(ms > 0.0)) ms = 1.0;
+    for (ll p = (ll)blockIdx.x * blockDim.x + threadIdx.x; p < n; p += (ll)gridDim.x * blockDim.x) {
+        const ll i = perm[p];
+        const unsigned f = A.flags[i];
+        if ((f & NBG_LIVE_MASK) != NBG_F_EXISTS) continue;
+        const double x = A.x[i], y = A.y[i], z = A.z[i], r = A.rad[i];
+        if (is_special(x, y, z, r)) {
+            const bool has_nan = x != x || y != y || z != z || r != r;
+            const double vv = has_nan ? 0.0 : nbg_nan();
+            A.fx[i] = vv;
+            A.fy[i] = vv;
+            A.fz[i] = vv;
+            continue;
+        }
+        const int sim = nbg_sim_of(seg.off, seg.nsims, p);
+        const ll s0 = seg.off[sim];
+        const ll T = seg.mtile_off[sim + 1] - seg.mtile_off[sim];
+        const ll a = (p - s0) / SYM_B;
+        const int li = (int)(p - s0 - a * SYM_B);
+        const ll g = seg.mtile_off[sim] + a;
+        const ll u0 = seg.item_off[sim] + sym_row_start(a, T);
+        const int c0 = nbg_work_chunk(u0, C, W), c1 = nbg_work_chunk(u0 + (T - a) - 1, C, W);
+        double sx = 0, sy = 0, sz = 0;
+        for (int cc = c0; cc <= c1; cc++) {
+            const double *o = part + (g + cc) * 3 * SYM_B;
+            sx += o[li];
+            sy += o[SYM_B + li];
+            sz += o[2 * SYM_B + li];
+        }
+        for (ll aa = 0; aa < a; aa++) {
+            const float *q = jpart + (seg.item_off[sim] + sym_row_start(aa, T) + (a - aa)) * 3 * SYM_B;
+            sx += (double)q[li];
+            sy += (double)q[SYM_B + li];
+            sz += (double)q[2 * SYM_B + li];
+        }
+        const double gm = NBG_G * A.m[i] * ms;
+        A.fx[i] = gm * sx;
+        A.fy[i] = gm * sy;
+        A.fz[i] = gm * sz;
+    }
+}
+
 /* ---- kernel shapes ---------------------------------------------------------
  * (kind, threads per CTA, i-bodies per thread, j per shared-memory tile,
  * unroll of the j loop, CTAs per SM the register budget is set for).  Kind 0:
@@ -657,6 +1064,9 @@ __global__ void k_mix_out(BodyArrays A, DevCtl *ctl, SimSegs seg, const unsigned
 /* the kernel of a shape */
 #define MIX_KERNEL(kind, b, k, jt, u, mb) k_pair_mixed<b, k, jt, u, mb, (kind) >= 1, (kind) == 2>
 
+/* the symmetric kernel's register cap: CTAs per SM */
+#define SYM_MINB 4
+
 MixVariantInfo nbg_mix_variant_info(int variant)
 {
     switch (variant) {
@@ -664,6 +1074,7 @@ MixVariantInfo nbg_mix_variant_info(int variant)
     case id: return MixVariantInfo{b, k, jt, u};
         MIX_VARIANTS(X)
 #undef X
+    case NBG_MIX_SYM: return MixVariantInfo{SYM_THREADS, SYM_KI, SYM_B, 2};
     default: return MixVariantInfo{0, 0, 0, 0};
     }
 }
@@ -681,6 +1092,9 @@ int nbg_mixed_slots(int device, int variant)
     case id: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, MIX_KERNEL(kind, b, k, jt, u, mb), b, 0); break;
         MIX_VARIANTS(X)
 #undef X
+    case NBG_MIX_SYM:
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pair_sym<SYM_MINB>, SYM_THREADS, 0);
+        break;
     }
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
     int slots = per_sm * sms;
@@ -714,11 +1128,21 @@ void nbg_launch_mixed_pair(const CycleBufs &cb, DevCtl *ctl, cudaStream_t st)
         break;
         MIX_VARIANTS(X)
 #undef X
+    case NBG_MIX_SYM:
+        k_pair_sym<SYM_MINB><<<cb.slots, SYM_THREADS, 0, st>>>(cb.a, ctl, cb.seg, cb.jhi, cb.jlo, cb.tile_c, cb.iprep,
+                                                               cb.perm, cb.part, cb.jpart, cb.ev_keys, cb.ev_cap);
+        break;
     }
 }
 
 void nbg_launch_mixed_out(const CycleBufs &cb, DevCtl *ctl, cudaStream_t st)
 {
-    k_mix_out<<<nbg_flat_grid(cb, cb.cap), 256, 0, st>>>(cb.a, ctl, cb.seg, cb.perm, cb.part,
-                                                 cb.itile > 0 ? cb.itile : NBG_MIX_ITILE);
+    if (cb.mix_variant == NBG_MIX_SYM)
+        k_sym_out<<<nbg_flat_grid(cb, cb.cap), 256, 0, st>>>(cb.a, ctl, cb.seg, cb.perm, cb.part, cb.jpart);
+    else
+        k_mix_out<<<nbg_flat_grid(cb, cb.cap), 256, 0, st>>>(cb.a, ctl, cb.seg, cb.perm, cb.part,
+                                                             cb.itile > 0 ? cb.itile : NBG_MIX_ITILE);
 }
+
+/* units of the symmetric kernel's work for a collection of T blocks */
+ll nbg_sym_units(ll T) { return T * (T + 1) / 2; }

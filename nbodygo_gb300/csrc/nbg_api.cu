@@ -382,6 +382,21 @@ static void free_cap_buffers(CycleBufs &cb)
     cudaFree(cb.shist);
 }
 
+/* the symmetric mixed kernel's j-partial slots: at least `need` units (with
+ * a quarter to spare, as collections grow by fragments and adds) */
+static int ensure_jpart(nbg_ctx *ctx, ll need)
+{
+    if (need <= ctx->cb.jpart_units) return NBG_OK;
+    const ll units = need + need / 4 + 16;
+    cudaFree(ctx->cb.jpart);
+    ctx->cb.jpart = nullptr;
+    ctx->cb.jpart_units = 0;
+    CK(cudaMalloc((void **)&ctx->cb.jpart, (size_t)units * 3 * NBG_MIX_ITILE * sizeof(float)));
+    ctx->cb.jpart_units = units;
+    invalidate_graph(ctx);
+    return NBG_OK;
+}
+
 static int ensure_frag_cap(nbg_ctx *ctx, ll need)
 {
     if (need <= ctx->cb.frag_cap) return NBG_OK;
@@ -765,6 +780,7 @@ void nbg_destroy(nbg_ctx *ctx)
     free_arrays(ctx->cb.frags);
     free_events(ctx->cb);
     free_cap_buffers(ctx->cb);
+    cudaFree(ctx->cb.jpart);
     nbg_bh_free(ctx->cb.t);
     if (ctx->ring_host) cudaHostUnregister(ctx->ring_host);
     if (ctx->flags_h) cudaFreeHost(ctx->flags_h);
@@ -1572,6 +1588,8 @@ int nbg_step(nbg_ctx *ctx, double dt, double R, int nsteps, nbg_step_info *info)
             rc = ensure_part(ctx, h->error_need);
         else if (h->error_what == 5)
             rc = ensure_bh(ctx, h->error_need);
+        else if (h->error_what == 6)
+            rc = ensure_jpart(ctx, h->error_need);
         else
             rc = ensure_frag_cap(ctx, h->error_need);
         if (rc != NBG_OK) return rc;
@@ -1649,8 +1667,13 @@ int nbg_force_pass(nbg_ctx *ctx)
         int rc = sync_ctl(ctx);
         if (rc != NBG_OK) return rc;
         const DevCtl *h = ctx->ctl_h;
-        if (h->error == NBG_E_OVERFLOW && h->error_what == 5 && attempt < 4) {
-            if ((rc = ensure_bh(ctx, h->error_need)) != NBG_OK) return rc;
+        if (h->error == NBG_E_OVERFLOW && attempt < 4 &&
+            (h->error_what == 4 || h->error_what == 5 || h->error_what == 6)) {
+            /* a buffer of the force pass was short: grow it, run again */
+            rc = h->error_what == 4 ? ensure_part(ctx, h->error_need)
+                 : h->error_what == 5 ? ensure_bh(ctx, h->error_need)
+                                      : ensure_jpart(ctx, h->error_need);
+            if (rc != NBG_OK) return rc;
             continue;
         }
         if (h->error) return fail(ctx, h->error, "force pass failed");
@@ -1685,6 +1708,9 @@ static int time_mixed_pair(nbg_ctx *ctx, float *ms)
     CK(cudaGetLastError());
     CK(cudaEventSynchronize(e1));
     CK(cudaEventElapsedTime(ms, e0, e1));
+    int rc = sync_ctl(ctx);
+    if (rc != NBG_OK) return rc;
+    if (ctx->ctl_h->error) return fail(ctx, ctx->ctl_h->error, "autotune: the timed force pass failed");
     return NBG_OK;
 }
 
@@ -1732,6 +1758,11 @@ int nbg_autotune(nbg_ctx *ctx, const char *cache_path, int *variant, double *bes
         const int prev = ctx->cb.mix_variant;
         for (int v = 0; v < NBG_MIX_VARIANTS; v++) {
             if ((rc = select_variant(ctx, v)) != NBG_OK) return rc;
+            /* one untimed force pass grows the buffers this shape needs */
+            if ((rc = nbg_force_pass(ctx)) != NBG_OK) {
+                select_variant(ctx, prev);
+                return rc;
+            }
             float ms = 0, t = 1e30f;
             for (int rep = 0; rep < 4; rep++) {
                 if ((rc = time_mixed_pair(ctx, &ms)) != NBG_OK) {

@@ -57,7 +57,8 @@ struct DevCtl {
     int error;       /* sticky NBG_E_* raised by a kernel */
     int pad0;
     ll error_need;   /* for NBG_E_OVERFLOW: the size that would have fitted */
-    int error_what;  /* 1 = bodies, 2 = events, 3 = fragments, 4 = partials */
+    int error_what;  /* 1 = bodies, 2 = events, 3 = fragments, 4 = partials, 5 = octree nodes,
+                      * 6 = symmetric kernel j-partial units */
     int splits;      /* mixed: chunks the pair work is cut into (C) */
     ll work_total;   /* mixed: pair work W in (i-tile, j-body) units */
     /* per-cycle values */
@@ -216,6 +217,8 @@ struct CycleBufs {
     int work_cap;       /* most CTAs the mixed pair work is divided among (0 = slots) */
     int slots;          /* resident CTAs of the mixed kernel on this device */
     int mix_variant;    /* shape of the mixed pair kernel (see nbg_mix_variant_info) */
+    float *jpart;       /* symmetric kernel: FP32 j sums per unit, 3 x itile each */
+    ll jpart_units;     /* units jpart holds */
     int itile;          /* i-bodies per work item of that shape */
     /* render ring in mapped host memory (device addresses; NULL: none) */
     nbg_ring_slot *ring_head;
@@ -248,6 +251,8 @@ struct MixVariantInfo {
     int block, k, jt, unroll;
 };
 #define NBG_MIX_VARIANTS NBG_MIX_SHAPES
+/* the symmetric kernel (each unordered pair once, k_pair_sym): the last shape */
+#define NBG_MIX_SYM (NBG_MIX_SHAPES - 1)
 #define NBG_MIX_MIN_ITILE 256
 #define NBG_MIX_MAX_ITILE 512
 /* fewest (i-tile, j-body) units of pair work in a chunk, and chunks per
@@ -366,6 +371,7 @@ void nbg_launch_mixed_prep(const CycleBufs &cb, DevCtl *ctl, cudaStream_t st);
 void nbg_launch_mixed_pair(const CycleBufs &cb, DevCtl *ctl, cudaStream_t st);
 void nbg_launch_mixed_out(const CycleBufs &cb, DevCtl *ctl, cudaStream_t st);
 int nbg_mixed_slots(int device, int variant);
+ll nbg_sym_units(ll blocks);
 MixVariantInfo nbg_mix_variant_info(int variant);
 
 /* k_sort.cu */
