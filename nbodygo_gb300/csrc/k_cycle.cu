@@ -832,8 +832,127 @@ __device__ static void resolve_one(BodyArrays &A, ull key, nbg_event *out)
     *out = e;
 }
 
+/* ---- resolution links: the events of a busy cycle in dataflow order ------
+ * ProcessMods resolves events one after another, newest first.  Two events
+ * that share no body commute, so an event may be resolved as soon as every
+ * earlier event on each of its bodies is: the per-body chains of events in
+ * processing order are the only order that matters.  For cycles with more
+ * events than the one-block sort holds, the chains are built from the sorted
+ * (body, event) incidences, and k_resolve works through the ready events
+ * round by round, touching only those - the result is the sequential one
+ * bit for bit, however many events resolve at once. */
+
+__device__ __forceinline__ bool links_on(const DevCtl *ctl)
+{
+    return ctl->error == 0 && ctl->ev_count > NBG_EV_BLOCK_SORT;
+}
+
+/* sim s holds the sorted events [ev_lo[s], ev_lo[s + 1]) */
+__global__ void k_ev_ranges(DevCtl *ctl, SimSegs seg, const ull *keys, ll *ev_lo)
+{
+    if (!links_on(ctl)) return;
+    const ll cnt = ctl->ev_count;
+    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s <= seg.nsims; s += gridDim.x * blockDim.x)
+        ev_lo[s] = s == seg.nsims ? cnt : (s == 0 ? 0 : lower_bound_u64(keys, cnt, (ull)seg.off[s] << 32));
+}
+
+/* The two incidences of the event at sorted position t, processing index o
+ * (its sim's events in reverse key order): body << (ob + 1) | o << 1 | side */
+__global__ void k_ev_incid(DevCtl *ctl, SimSegs seg, const ull *keys, const ll *ev_lo, ull *inc, int ob)
+{
+    if (!links_on(ctl)) return;
+    const ll cnt = ctl->ev_count;
+    for (ll t = (ll)blockIdx.x * blockDim.x + threadIdx.x; t < cnt; t += (ll)gridDim.x * blockDim.x) {
+        const ull key = keys[t];
+        ll b1, b2;
+        unsigned ty;
+        event_bodies(key, b1, b2, ty);
+        const int s = seg.nsims == 1 ? 0 : nbg_sim_of(seg.off, seg.nsims, (ll)(key >> 32));
+        const ull o = (ull)(ev_lo[s] + ev_lo[s + 1] - 1 - t);
+        inc[2 * t] = ((ull)b1 << (ob + 1)) | (o << 1);
+        inc[2 * t + 1] = ((ull)b2 << (ob + 1)) | (o << 1) | 1ull;
+    }
+}
+
+/* From the sorted incidences: each event's next event on each of its bodies
+ * (link[2 o + side], -1: none) and previous one (pred[2 o + side]). */
+__global__ void k_ev_links(DevCtl *ctl, const ull *inc, int ob, ll *link, ll *pred)
+{
+    if (!links_on(ctl)) return;
+    const ll m2 = 2 * ctl->ev_count;
+    const ull omask = (1ull << ob) - 1ull;
+    for (ll t = (ll)blockIdx.x * blockDim.x + threadIdx.x; t < m2; t += (ll)gridDim.x * blockDim.x) {
+        const ull k = inc[t];
+        const ull b = k >> (ob + 1);
+        const ll slot = 2 * (ll)((k >> 1) & omask) + (ll)(k & 1ull);
+        link[slot] = t + 1 < m2 && (inc[t + 1] >> (ob + 1)) == b ? (ll)((inc[t + 1] >> 1) & omask) : -1;
+        pred[slot] = t > 0 && (inc[t - 1] >> (ob + 1)) == b ? (ll)((inc[t - 1] >> 1) & omask) : -1;
+    }
+}
+
+/* unresolved predecessors of each event: one per body, once if both bodies'
+ * previous event is the same */
+__global__ void k_ev_pending(DevCtl *ctl, const ll *pred, int *pend)
+{
+    if (!links_on(ctl)) return;
+    const ll m = ctl->ev_count;
+    for (ll o = (ll)blockIdx.x * blockDim.x + threadIdx.x; o < m; o += (ll)gridDim.x * blockDim.x) {
+        const ll p0 = pred[2 * o], p1 = pred[2 * o + 1];
+        pend[o] = (p0 >= 0 ? 1 : 0) + (p1 >= 0 && p1 != p0 ? 1 : 0);
+    }
+}
+
+/* Resolution of one sim's events through its links: round by round, every
+ * ready event (all earlier events on its bodies resolved) at once. */
+__device__ static void resolve_dataflow(BodyArrays &A, DevCtl *ctl, const ull *keys, nbg_event *ev_out, ll lo, ll hi,
+                                        const ll *link, int *pend, ll *front, ll ev_cap)
+{
+    __shared__ ll s_n[2];
+    __shared__ ll s_total;
+    const int tid = threadIdx.x;
+    ll *fr[2] = {front + lo, front + ev_cap + lo};
+    if (tid == 0) {
+        s_n[0] = s_n[1] = 0;
+        s_total = 0;
+    }
+    __syncthreads();
+    for (ll o = lo + tid; o < hi; o += RESOLVE_BLOCK)
+        if (pend[o] == 0) fr[0][atomicAdd((unsigned long long *)&s_n[0], 1ull)] = o;
+    __syncthreads();
+    int cur = 0;
+    ll done = 0;
+    while (s_n[cur] > 0) {
+        const ll nr = s_n[cur];
+        for (ll x = tid; x < nr; x += RESOLVE_BLOCK) {
+            const ll o = fr[cur][x];
+            resolve_one(A, keys[lo + hi - 1 - o], &ev_out[o]);
+            done++;
+            const ll n0 = link[2 * o], n1 = link[2 * o + 1];
+            if (n0 >= 0 && atomicSub(&pend[n0], 1) == 1)
+                fr[cur ^ 1][atomicAdd((unsigned long long *)&s_n[cur ^ 1], 1ull)] = n0;
+            if (n1 >= 0 && n1 != n0 && atomicSub(&pend[n1], 1) == 1)
+                fr[cur ^ 1][atomicAdd((unsigned long long *)&s_n[cur ^ 1], 1ull)] = n1;
+        }
+        __syncthreads(); /* this round's bodies are written, the next frontier complete */
+        if (tid == 0) s_n[cur] = 0;
+        cur ^= 1;
+        __syncthreads();
+    }
+    atomicAdd((unsigned long long *)&s_total, (ull)done);
+    __syncthreads();
+    /* every event has a chain of predecessors back to a ready one, so all
+     * resolve; anything else is a broken invariant, reported as such */
+    if (tid == 0 && s_total != (ull)(hi - lo)) {
+        ctl->error = NBG_E_STATE;
+        ctl->error_what = 7;
+        ctl->error_need = hi - lo - (ll)s_total;
+    }
+}
+
 __global__ void __launch_bounds__(RESOLVE_BLOCK) k_resolve(BodyArrays A, DevCtl *ctl, SimSegs seg, const ull *keys,
-                                                           nbg_event *ev_out, unsigned *owner)
+                                                           nbg_event *ev_out, unsigned *owner, int links,
+                                                           const ll *ev_lo, const ll *link, int *pend, ll *front,
+                                                           ll ev_cap)
 {
     __shared__ int s_left, s_done;
     if (ctl->error) return;
@@ -847,6 +966,11 @@ __global__ void __launch_bounds__(RESOLVE_BLOCK) k_resolve(BodyArrays A, DevCtl 
         ctl->acc_frags += ctl->frag_total;
     }
     if (s >= seg.nsims) return;
+    if (links && cnt > NBG_EV_BLOCK_SORT) {
+        const ll lo = ev_lo[s], hi = ev_lo[s + 1];
+        if (hi > lo) resolve_dataflow(A, ctl, keys, ev_out, lo, hi, link, pend, front, ev_cap);
+        return;
+    }
     const ll lo = seg.nsims == 1 ? 0 : lower_bound_u64(keys, cnt, (ull)seg.off[s] << 32);
     const ll hi = seg.nsims == 1 ? cnt : lower_bound_u64(keys, cnt, (ull)seg.off[s + 1] << 32);
     const ll m = hi - lo;
@@ -1369,10 +1493,27 @@ void nbg_launch_after_pair(const CycleBufs &cb, DevCtl *ctl, cudaStream_t st, bo
 {
     const int sg = scan_grid(cb.cap);
     k_sort_events<<<1, SORT_BLOCK, 0, st>>>(ctl, cb.ev_keys, cb.ev_cap, cb.ev_radix);
-    if (cb.ev_radix) nbg_launch_event_radix(cb, ctl, st);
+    int links = 0;
+    if (cb.ev_radix) {
+        nbg_launch_event_radix(cb, ctl, st);
+        /* the links, when a body index and an event index fit one key */
+        int kb = 1, ob = 1;
+        while (kb < 31 && ((ll)1 << kb) < cb.cap) kb++;
+        while (ob < 40 && ((ll)1 << ob) < cb.ev_cap) ob++;
+        if (kb + ob + 1 <= 64) {
+            links = 1;
+            const int eg = nbg_flat_grid(cb, 2 * cb.ev_cap);
+            k_ev_ranges<<<(cb.seg.nsims + 256) / 256, 256, 0, st>>>(ctl, cb.seg, cb.ev_keys, cb.ev_lo);
+            k_ev_incid<<<eg, 256, 0, st>>>(ctl, cb.seg, cb.ev_keys, cb.ev_lo, cb.inc[0], ob);
+            const ull *sorted = nbg_launch_incidence_radix(cb, ctl, kb + ob, st);
+            k_ev_links<<<eg, 256, 0, st>>>(ctl, sorted, ob, cb.ev_link, cb.ev_front);
+            k_ev_pending<<<eg, 256, 0, st>>>(ctl, cb.ev_front, cb.ev_pend);
+        }
+    }
     k_frag_emit<<<sg, NBG_SCAN_BLOCK, 0, st>>>(cb.a, cb.frags, ctl, cb.blk_off);
     /* the radix-sort key buffer is free after the pair pass: per-body owner words */
-    k_resolve<<<cb.seg.nsims, RESOLVE_BLOCK, 0, st>>>(cb.a, ctl, cb.seg, cb.ev_keys, cb.ev_out, cb.skey[1]);
+    k_resolve<<<cb.seg.nsims, RESOLVE_BLOCK, 0, st>>>(cb.a, ctl, cb.seg, cb.ev_keys, cb.ev_out, cb.skey[1], links,
+                                                      cb.ev_lo, cb.ev_link, cb.ev_pend, cb.ev_front, cb.ev_cap);
     k_integrate<<<nbg_flat_grid(cb, cb.cap), 256, 0, st>>>(cb.a, ctl, cb.rend, cb.ring_rend, cb.ring_cap, cb.ring_slots);
     if (cb.ring_head) k_ring_header<<<1, 1, 0, st>>>(ctl, cb.ring_head, cb.ring_cap, cb.ring_slots);
     k_keep_blocksum<<<sg, NBG_SCAN_BLOCK, 0, st>>>(cb.a, ctl, cb.seg, cb.blk_sum);

@@ -83,12 +83,14 @@ __global__ void k_morton_keys(BodyArrays A, DevCtl *ctl, SimSegs seg, unsigned *
  * sort return at once. */
 #define RS_MORTON 0
 #define RS_EVENTS 1
+#define RS_INCIDENCES 2 /* two (body, event) keys per event, for the resolution's links */
 
 __device__ __forceinline__ ll rs_count(const DevCtl *ctl, int what)
 {
     if (ctl->error) return 0;
     if (what == RS_MORTON) return ctl->sort_now ? ctl->n : 0;
-    return ctl->ev_count > NBG_EV_BLOCK_SORT ? ctl->ev_count : 0;
+    if (ctl->ev_count <= NBG_EV_BLOCK_SORT) return 0;
+    return what == RS_EVENTS ? ctl->ev_count : 2 * ctl->ev_count;
 }
 
 /* per-block digit histogram, digit-major: hist[d * nb + b] */
@@ -332,10 +334,38 @@ void nbg_launch_event_radix(const CycleBufs &cb, DevCtl *ctl, cudaStream_t st)
     }
 }
 
-/* launches of nbg_launch_event_radix for a capacity */
+/* launches of the multi-block event sort and, when they fit one key, the
+ * resolution's links (nbg_launch_after_pair) */
 int nbg_event_radix_launches(const CycleBufs &cb)
 {
-    int kb = 1;
+    int kb = 1, ob = 1;
     while (kb < 31 && ((ll)1 << kb) < cb.cap) kb++;
-    return 2 * ((kb + 7) / 8) * 5;
+    while (ob < 40 && ((ll)1 << ob) < cb.ev_cap) ob++;
+    int n = 2 * ((kb + 7) / 8) * 5;
+    if (kb + ob + 1 <= 64) n += 4 + ((kb + ob + 7) / 8) * 5;
+    return n;
+}
+
+/* The (body, event) incidence keys of the resolution's links (k_cycle.cu),
+ * sorted on their body and event bits: `bits` above the lowest (which tells
+ * the event's side) in 8-bit digits.  Returns the buffer holding the
+ * result: inc[0] after an even number of passes, inc[1] after an odd. */
+ull *nbg_launch_incidence_radix(const CycleBufs &cb, DevCtl *ctl, int bits, cudaStream_t st)
+{
+    const ll cap2 = 2 * cb.ev_cap;
+    const int nb = (int)((cap2 + RS_TILE - 1) / RS_TILE);
+    const int nchunk = (int)(((ll)nb * RS_BINS + RS_SCAN_CHUNK - 1) / RS_SCAN_CHUNK);
+    ull *kin = cb.inc[0], *kout = cb.inc[1];
+    for (int shift = 1; shift < 1 + bits; shift += 8) {
+        k_rs_hist<ull><<<nb, RS_BLOCK, 0, st>>>(ctl, RS_INCIDENCES, kin, shift, cb.inc_hist);
+        k_rs_scan_part<<<nchunk, 1024, 0, st>>>(ctl, RS_INCIDENCES, cb.inc_hist);
+        k_rs_scan_top<<<1, 1024, 0, st>>>(ctl, RS_INCIDENCES, cb.inc_hist);
+        k_rs_scan_fin<<<nchunk, 1024, 0, st>>>(ctl, RS_INCIDENCES, cb.inc_hist);
+        k_rs_scatter<ull><<<nb, RS_BLOCK, 0, st>>>(ctl, RS_INCIDENCES, kin, nullptr, kout, nullptr, shift,
+                                                   cb.inc_hist);
+        ull *t = kin;
+        kin = kout;
+        kout = t;
+    }
+    return kin;
 }

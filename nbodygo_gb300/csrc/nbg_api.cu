@@ -433,9 +433,17 @@ static void free_events(CycleBufs &cb)
     cudaFree(cb.ev_out);
     cudaFree(cb.ev_sort);
     cudaFree(cb.ev_hist);
-    cb.ev_keys = cb.ev_sort = nullptr;
+    cudaFree(cb.inc[0]);
+    cudaFree(cb.inc[1]);
+    cudaFree(cb.inc_hist);
+    cudaFree(cb.ev_link);
+    cudaFree(cb.ev_pend);
+    cudaFree(cb.ev_front);
+    cudaFree(cb.ev_lo);
+    cb.ev_keys = cb.ev_sort = cb.inc[0] = cb.inc[1] = nullptr;
     cb.ev_out = nullptr;
-    cb.ev_hist = nullptr;
+    cb.ev_hist = cb.inc_hist = cb.ev_link = cb.ev_front = cb.ev_lo = nullptr;
+    cb.ev_pend = nullptr;
     cb.ev_cap = 0;
 }
 
@@ -448,6 +456,14 @@ static int alloc_events(nbg_ctx *ctx, ll c)
     CK(cudaMalloc((void **)&ctx->cb.ev_out, (size_t)c * sizeof(nbg_event)));
     CK(cudaMalloc((void **)&ctx->cb.ev_sort, (size_t)c * sizeof(ull)));
     CK(cudaMalloc((void **)&ctx->cb.ev_hist, (size_t)nbg_sort_scratch_hist(c) * sizeof(ll)));
+    /* the resolution's links (busy cycles) */
+    CK(cudaMalloc((void **)&ctx->cb.inc[0], (size_t)(2 * c) * sizeof(ull)));
+    CK(cudaMalloc((void **)&ctx->cb.inc[1], (size_t)(2 * c) * sizeof(ull)));
+    CK(cudaMalloc((void **)&ctx->cb.inc_hist, (size_t)nbg_sort_scratch_hist(2 * c) * sizeof(ll)));
+    CK(cudaMalloc((void **)&ctx->cb.ev_link, (size_t)(2 * c) * sizeof(ll)));
+    CK(cudaMalloc((void **)&ctx->cb.ev_pend, (size_t)c * sizeof(int)));
+    CK(cudaMalloc((void **)&ctx->cb.ev_front, (size_t)(2 * c) * sizeof(ll)));
+    CK(cudaMalloc((void **)&ctx->cb.ev_lo, (size_t)(NBG_MAX_SIMS + 1) * sizeof(ll)));
     ctx->cb.ev_cap = c;
     invalidate_graph(ctx);
     return NBG_OK;

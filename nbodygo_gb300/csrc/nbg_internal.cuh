@@ -198,7 +198,18 @@ struct CycleBufs {
     ull *ev_sort;       /* ping-pong partner of ev_keys for the multi-block event sort */
     ll *ev_hist;        /* its digit histogram and chunk sums (nbg_sort_scratch_hist(ev_cap)) */
     ll ev_cap;
-    int ev_radix;       /* this cycle's launches include the multi-block event sort */
+    int ev_radix;       /* this cycle's launches include the multi-block event sort and the
+                         * resolution's links (dataflow order) */
+    /* resolution links, for cycles beyond the one-block sort: incidence keys
+     * (ping-pong, 2 ev_cap each) and their histogram; per event (processing
+     * index) the next event on each of its bodies, the count of unresolved
+     * predecessors, and the frontier lists (2 ev_cap); each sim's event range */
+    ull *inc[2];
+    ll *inc_hist;
+    ll *ev_link;
+    int *ev_pend;
+    ll *ev_front;
+    ll *ev_lo;
     nbg_event *ev_out;  /* resolved events of the last cycle */
     nbg_renderable *rend;
     ll *blk_sum;        /* per-block counts for the scans */
@@ -377,6 +388,7 @@ MixVariantInfo nbg_mix_variant_info(int variant);
 /* k_sort.cu */
 void nbg_launch_spatial_sort(const CycleBufs &cb, DevCtl *ctl, cudaStream_t st);
 void nbg_launch_event_radix(const CycleBufs &cb, DevCtl *ctl, cudaStream_t st);
+ull *nbg_launch_incidence_radix(const CycleBufs &cb, DevCtl *ctl, int bits, cudaStream_t st);
 int nbg_event_radix_launches(const CycleBufs &cb);
 ll nbg_sort_scratch_hist(ll cap);
 
