@@ -611,9 +611,13 @@ def main():
         mixed0.set_stream(stream.cuda_stream)
         if args.near_ppm is not None:
             mixed0.set_option(A.OPT_NEAR_PPM, args.near_ppm)
+        if tuned is not None:
+            # the forces of the kernel shape that was timed
+            mixed0.set_option(A.OPT_MIX_SHAPE, tuned["shape"])
         load(mixed0, sims)
         fm = mixed0.force_pass()
         accuracy = accuracy_block(torch, sims, fm, fp, f"cuda:{local}")
+        accuracy["kernel_shape"] = tuned["shape"] if tuned is not None else 0
         if big:
             pairs = sum(len(b["x"]) * (len(b["x"]) - 1) for b in sims)
             plain_rate = pairs / (1e-3 * force_ms)

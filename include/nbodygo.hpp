@@ -34,6 +34,7 @@
 #include <cstdint>
 #include <cstdio>
 #include <cstdlib>
+#include <cstring>
 #include <fstream>
 #include <map>
 #include <memory>
@@ -603,7 +604,41 @@ class ComputationRunner {
     }
     uint64_t Computations() const { return computations_; }
 
+    /* A checkpoint of the whole simulation: the library snapshot
+     * (nbg_save_state: every body field, private ones included, the id
+     * counter, the fragment generator's cycle key, staged adds, options)
+     * after a small runner header (its dt, R and computation count).
+     * LoadSnapshot, in this runner or another, resumes the run bit for bit.
+     * No counterpart in the reference, whose CSV (FromCsv / ToCsv) keeps only
+     * the public fields. */
+    std::vector<uint8_t> SaveSnapshot() const
+    {
+        int64_t size = 0;
+        bc_.check(nbg_save_state(bc_.ctx(), nullptr, 0, &size));
+        std::vector<uint8_t> out(kRunnerHeader + (size_t)size);
+        std::memcpy(out.data(), "NBGRUN01", 8);
+        std::memcpy(out.data() + 8, &dt_, 8);
+        std::memcpy(out.data() + 16, &R_, 8);
+        std::memcpy(out.data() + 24, &computations_, 8);
+        bc_.check(nbg_save_state(bc_.ctx(), out.data() + kRunnerHeader, size, &size));
+        return out;
+    }
+    void LoadSnapshot(const std::vector<uint8_t> &snap)
+    {
+        if (snap.size() < kRunnerHeader || std::memcmp(snap.data(), "NBGRUN01", 8) != 0)
+            throw Error(NBG_E_ARG, "not a runner snapshot");
+        bc_.check(nbg_load_state(bc_.ctx(), snap.data() + kRunnerHeader, (int64_t)(snap.size() - kRunnerHeader)));
+        std::memcpy(&dt_, snap.data() + 8, 8);
+        std::memcpy(&R_, snap.data() + 16, 8);
+        std::memcpy(&computations_, snap.data() + 24, 8);
+        has_dt_ = has_R_ = has_del_ = false;
+        int64_t dev_next = 0;
+        bc_.check(nbg_get_next_id(bc_.ctx(), &dev_next));
+        AdvanceNextId(dev_next);
+    }
+
   private:
+    static constexpr size_t kRunnerHeader = 32;
     BodyCollection &bc_;
     int workers_;
     double dt_, R_ = 1.0;

@@ -312,6 +312,42 @@ static void TestRunnerCycle()
     std::printf("ok   %s\n", cur_test);
 }
 
+/* Not a reference test: a checkpoint taken mid-run and resumed in a fresh
+ * collection and runner repeats the uninterrupted run bit for bit. */
+static void TestRunnerSnapshot()
+{
+    cur_test = "TestRunnerSnapshot";
+    auto cluster = []() {
+        std::vector<Body> v;
+        for (int k = 0; k < 64; k++) {
+            const double a = 0.7 * k;
+            v.push_back(NewBody(k + 1, 8 * std::cos(a), 8 * std::sin(a), 0.3 * (k % 5), -std::sin(a), std::cos(a),
+                                0, 1e11 * (1 + k % 3), 1.0, k % 2 ? Elastic : Subsume, Random, 0, 0, false,
+                                "b" + std::to_string(k), "", false));
+        }
+        return v;
+    };
+    BodyCollection ba(cluster());
+    ComputationRunner ra(4, 0.05, false, ba);
+    ra.SetCoefficientOfRestitution(0.8);
+    for (int c = 0; c < 10; c++) ra.RunOneComputation();
+    const std::vector<uint8_t> snap = ra.SaveSnapshot();
+    for (int c = 0; c < 10; c++) ra.RunOneComputation();
+    BodyCollection bb(std::vector<Body>{});
+    ComputationRunner rb(4, 1.0, false, bb);
+    rb.LoadSnapshot(snap);
+    CHECK(rb.TimeScaling() == 0.05 && rb.CoefficientOfRestitution() == 0.8 && rb.Computations() == 10,
+          "runner settings restored");
+    for (int c = 0; c < 10; c++) rb.RunOneComputation();
+    const std::vector<Body> x = ba.GetArray(), y = bb.GetArray();
+    CHECK(x.size() == y.size() && x.size() < 64, "same bodies, some merged");
+    for (size_t k = 0; k < x.size(); k++)
+        CHECK(x[k].Id == y[k].Id && x[k].X == y[k].X && x[k].Y == y[k].Y && x[k].Z == y[k].Z &&
+                  x[k].Vx == y[k].Vx && x[k].Vy == y[k].Vy && x[k].Vz == y[k].Vz && x[k].Mass == y[k].Mass,
+              "bit-identical state after the resume");
+    std::printf("ok   %s\n", cur_test);
+}
+
 int main(int argc, char **argv)
 {
     const std::string mode = argc > 1 ? argv[1] : "host";
@@ -333,6 +369,7 @@ int main(int argc, char **argv)
             TestRunnerSetters();
             TestRunnerBarnesHut();
             TestRunnerCycle();
+            TestRunnerSnapshot();
         } catch (const Error &e) {
             std::printf("FAIL %s: nbg status %d: %s\n", cur_test, e.code, e.what());
             g_fail = 1;

@@ -44,5 +44,5 @@ def test_mirror_against_reference_tests(tmp_path):
     out = _run(_compile(tmp_path), "gpu", 600)
     for name in ("TestInitSize", "TestRemove", "TestGetByID", "TestGetByName", "TestModByID",
                  "TestModByIDNoMatch", "TestModByName", "TestModByClass", "TestAdds", "TestRunnerSetters",
-                 "TestRunnerBarnesHut", "TestRunnerCycle"):
+                 "TestRunnerBarnesHut", "TestRunnerCycle", "TestRunnerSnapshot"):
         assert "ok   " + name in out, out
