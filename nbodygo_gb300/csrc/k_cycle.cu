@@ -1439,7 +1439,7 @@ static int scan_grid(ll cap) { return (int)((cap + NBG_SCAN_TILE - 1) / NBG_SCAN
 void nbg_launch_begin(const CycleBufs &cb, DevCtl *ctl, cudaStream_t st)
 {
     k_begin<<<1, NBG_SCAN_BLOCK, 0, st>>>(ctl, cb.seg, cb.slots, cb.work_cap, cb.itile > 0 ? cb.itile : NBG_MIX_ITILE,
-                                          cb.part_doubles, cb.mix_variant == NBG_MIX_SYM, cb.jpart_units);
+                                          cb.part_doubles, nbg_mix_is_sym(cb.mix_variant), cb.jpart_units);
 }
 
 void nbg_launch_frag_count(const CycleBufs &cb, DevCtl *ctl, cudaStream_t st)

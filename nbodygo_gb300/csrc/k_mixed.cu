@@ -32,6 +32,8 @@
  * its own, and k_mix_out adds the shares in chunk order, so results do not
  * depend on scheduling.
  */
+#include <type_traits>
+
 #include "nbg_internal.cuh"
 #include "nbg_math.h"
 #include "nbg_shared.h"
@@ -141,7 +143,7 @@ __device__ __forceinline__ bool packed_special(const float4 &lo) { return lo.x !
 /* origin of each i-tile: centre of the bounding box of its bodies */
 #define TILES_BLOCK 128
 __global__ void __launch_bounds__(TILES_BLOCK) k_mix_tiles(DevCtl *ctl, SimSegs seg, const float4 *jhi,
-                                                           const float4 *jlo, float4 *tile_c, int itile)
+                                                           const float4 *jlo, float4 *tile_c, float *tile_t, int itile)
 {
     __shared__ float red[6][TILES_BLOCK / 32];
     if (ctl->error) return;
@@ -174,7 +176,7 @@ __global__ void __launch_bounds__(TILES_BLOCK) k_mix_tiles(DevCtl *ctl, SimSegs 
         }
     __syncthreads();
     if (threadIdx.x == 0) {
-        float c3[3];
+        float c3[3], e2 = 0.f, amax = 0.f;
         for (int c = 0; c < 3; c++) {
             float l = red[c][0], h = red[3 + c][0];
             for (int q = 1; q < TILES_BLOCK / 32; q++) {
@@ -182,8 +184,15 @@ __global__ void __launch_bounds__(TILES_BLOCK) k_mix_tiles(DevCtl *ctl, SimSegs 
                 h = fmaxf(h, red[3 + c][q]);
             }
             c3[c] = (l <= h) ? 0.5f * l + 0.5f * h : 0.f;
+            const float e = l <= h ? fmaxf(h - c3[c], c3[c] - l) : 0.f;
+            e2 += e * e;
+            amax = fmaxf(amax, l <= h ? fmaxf(fabsf(l), fabsf(h)) : 0.f);
         }
-        tile_c[tile] = make_float4(c3[0], c3[1], c3[2], 0.f);
+        /* .w: a radius about the origin that holds every body of the tile,
+         * rounded up past the FP32 arithmetic and the bodies' lo parts */
+        const float rad = sqrtf(e2) * (1.0f + 0x1p-16f) + amax * 0x1p-20f;
+        tile_c[tile] = make_float4(c3[0], c3[1], c3[2], rad);
+        if (tile_t) tile_t[tile] = 0.f;
     }
     __syncthreads(); /* red[] is rewritten by the next tile */
     }
@@ -276,7 +285,7 @@ __device__ __forceinline__ void i_body_setup(const float4 *__restrict__ jhi, con
  * cycle; the pair kernel reads them for each chunk that covers the body */
 __global__ void k_mix_iprep(DevCtl *ctl, SimSegs seg, const float4 *__restrict__ jhi,
                             const float4 *__restrict__ jlo, const float4 *__restrict__ tile_c, float4 *iprep,
-                            int itile)
+                            float *tile_t, int itile)
 {
     if (ctl->error) return;
     const ll n = ctl->n;
@@ -286,10 +295,14 @@ __global__ void k_mix_iprep(DevCtl *ctl, SimSegs seg, const float4 *__restrict__
     for (ll p = (ll)blockIdx.x * blockDim.x + threadIdx.x; p < n; p += (ll)gridDim.x * blockDim.x) {
         const int sim = nbg_sim_of(seg.off, seg.nsims, p);
         const ll s0 = seg.off[sim];
-        const float4 c = tile_c[seg.mtile_off[sim] + (p - s0) / itile];
+        const ll tile = seg.mtile_off[sim] + (p - s0) / itile;
+        const float4 c = tile_c[tile];
         float xr, yr, zr, t;
         i_body_setup(jhi, jlo, p, seg.off[sim + 1], c, rmax, xmax, kappa, xr, yr, zr, t);
         iprep[p] = make_float4(xr, yr, zr, t);
+        /* the tile's largest near-pair threshold (positive floats order as
+         * their bit patterns) */
+        if (tile_t && t > 0.f) atomicMax((unsigned *)&tile_t[tile], __float_as_uint(t));
     }
 }
 
@@ -709,8 +722,9 @@ __device__ __forceinline__ float sym_r2(float xj, float yj, float zj, float nxi,
 template <int MINB>
 __global__ void __launch_bounds__(SYM_THREADS, MINB)
 k_pair_sym(BodyArrays A, DevCtl *ctl, SimSegs seg, const float4 *__restrict__ jhi, const float4 *__restrict__ jlo,
-           const float4 *__restrict__ tile_c, const float4 *__restrict__ iprep, const unsigned *__restrict__ perm,
-           double *__restrict__ part, float *__restrict__ jpart, ull *ev_keys, ll ev_cap)
+           const float4 *__restrict__ tile_c, const float *__restrict__ tile_t, const float4 *__restrict__ iprep,
+           const unsigned *__restrict__ perm, double *__restrict__ part, float *__restrict__ jpart, ull *ev_keys,
+           ll ev_cap)
 {
     /* block b, re-centred on block a's origin: j pair pp is (x0, x1, y0, y1),
      * (z0, z1, m0, m1) */
@@ -824,7 +838,18 @@ k_pair_sym(BodyArrays A, DevCtl *ctl, SimSegs seg, const float4 *__restrict__ jh
                     ax[k] = ay[k] = az[k] = make_float2(0.f, 0.f);
                 }
             };
+            /* A unit whose blocks' bounding spheres lie farther apart than
+             * block a's largest near-pair radius holds no near pair: its
+             * loop needs no mask (uniform over the CTA). */
+            bool far = false;
             if (!diag) {
+                const float4 cj = tile_c[seg.mtile_off[sim] + bb];
+                const float ex = cj.x - c.x, ey = cj.y - c.y, ez = cj.z - c.z;
+                const float gap = sqrtf(ex * ex + ey * ey + ez * ez) * (1.0f - 0x1p-18f) - c.w - cj.w;
+                far = gap > 0.f && gap * gap > tile_t[g] * (1.0f + 0x1p-10f);
+            }
+            auto rotate = [&](auto masked) {
+                constexpr bool MASK = decltype(masked)::value;
                 /* symmetric: rotate 64-j sub-blocks through the warp */
                 for (int r = 0; r < SYM_NSUB; r++) {
                     const int pp0 = ((w + r) % SYM_NSUB) * 32 + lane;
@@ -842,12 +867,14 @@ k_pair_sym(BodyArrays A, DevCtl *ctl, SimSegs seg, const float4 *__restrict__ jh
                             float2 r2 = __fmul2_rn(dx, dx);
                             r2 = __ffma2_rn(dy, dy, r2);
                             r2 = __ffma2_rn(dz, dz, r2);
-                            const bool n0 = r2.x < thr[k], n1 = r2.y < thr[k];
-                            if (n0 | n1) nearmask |= 1u << k;
                             const float2 inv = make_float2(rsqrt_sfu(r2.x), rsqrt_sfu(r2.y));
                             float2 inv3 = __fmul2_rn(__fmul2_rn(inv, inv), inv);
-                            inv3.x = n0 ? 0.f : inv3.x;
-                            inv3.y = n1 ? 0.f : inv3.y;
+                            if (MASK) {
+                                const bool n0 = r2.x < thr[k], n1 = r2.y < thr[k];
+                                if (n0 | n1) nearmask |= 1u << k;
+                                inv3.x = n0 ? 0.f : inv3.x;
+                                inv3.y = n1 ? 0.f : inv3.y;
+                            }
                             const float2 si = __fmul2_rn(mj, inv3);
                             const float2 sj = __fmul2_rn(nm[k], inv3);
                             ax[k] = __ffma2_rn(si, dx, ax[k]);
@@ -872,6 +899,12 @@ k_pair_sym(BodyArrays A, DevCtl *ctl, SimSegs seg, const float4 *__restrict__ jh
                     jacc[w][2][pp0] = fz;
                     if ((r + 1) % SYM_FOLD == 0) fold();
                 }
+            };
+            if (!diag) {
+                if (far)
+                    rotate(std::false_type{});
+                else
+                    rotate(std::true_type{});
             } else {
                 /* diagonal: one-sided over the block, pairs broadcast */
                 for (int pp = 0; pp < SYM_JP; pp++) {
@@ -1064,8 +1097,9 @@ __global__ void k_sym_out(BodyArrays A, DevCtl *ctl, SimSegs seg, const unsigned
 /* the kernel of a shape */
 #define MIX_KERNEL(kind, b, k, jt, u, mb) k_pair_mixed<b, k, jt, u, mb, (kind) >= 1, (kind) == 2>
 
-/* the symmetric kernel's register cap: CTAs per SM */
-#define SYM_MINB 4
+/* the symmetric kernel's shapes: registers capped for 4 or 5 CTAs per SM */
+#define SYM_MINB_A 4
+#define SYM_MINB_B 5
 
 MixVariantInfo nbg_mix_variant_info(int variant)
 {
@@ -1074,7 +1108,8 @@ MixVariantInfo nbg_mix_variant_info(int variant)
     case id: return MixVariantInfo{b, k, jt, u};
         MIX_VARIANTS(X)
 #undef X
-    case NBG_MIX_SYM: return MixVariantInfo{SYM_THREADS, SYM_KI, SYM_B, 2};
+    case NBG_MIX_SYM:
+    case NBG_MIX_SYM + 1: return MixVariantInfo{SYM_THREADS, SYM_KI, SYM_B, 2};
     default: return MixVariantInfo{0, 0, 0, 0};
     }
 }
@@ -1093,7 +1128,10 @@ int nbg_mixed_slots(int device, int variant)
         MIX_VARIANTS(X)
 #undef X
     case NBG_MIX_SYM:
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pair_sym<SYM_MINB>, SYM_THREADS, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pair_sym<SYM_MINB_A>, SYM_THREADS, 0);
+        break;
+    case NBG_MIX_SYM + 1:
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pair_sym<SYM_MINB_B>, SYM_THREADS, 0);
         break;
     }
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
@@ -1113,8 +1151,8 @@ void nbg_launch_mixed_prep(const CycleBufs &cb, DevCtl *ctl, cudaStream_t st)
     const int itile = cb.itile > 0 ? cb.itile : NBG_MIX_ITILE;
     ll tiles = (cb.cap + itile - 1) / itile + cb.seg.nsims;
     if (tiles > (ll)(cb.sms > 0 ? cb.sms : 1) * 64) tiles = (ll)(cb.sms > 0 ? cb.sms : 1) * 64;
-    k_mix_tiles<<<(int)tiles, TILES_BLOCK, 0, st>>>(ctl, cb.seg, cb.jhi, cb.jlo, cb.tile_c, itile);
-    k_mix_iprep<<<fg, 256, 0, st>>>(ctl, cb.seg, cb.jhi, cb.jlo, cb.tile_c, cb.iprep, itile);
+    k_mix_tiles<<<(int)tiles, TILES_BLOCK, 0, st>>>(ctl, cb.seg, cb.jhi, cb.jlo, cb.tile_c, cb.tile_t, itile);
+    k_mix_iprep<<<fg, 256, 0, st>>>(ctl, cb.seg, cb.jhi, cb.jlo, cb.tile_c, cb.iprep, cb.tile_t, itile);
 }
 
 void nbg_launch_mixed_pair(const CycleBufs &cb, DevCtl *ctl, cudaStream_t st)
@@ -1129,15 +1167,21 @@ void nbg_launch_mixed_pair(const CycleBufs &cb, DevCtl *ctl, cudaStream_t st)
         MIX_VARIANTS(X)
 #undef X
     case NBG_MIX_SYM:
-        k_pair_sym<SYM_MINB><<<cb.slots, SYM_THREADS, 0, st>>>(cb.a, ctl, cb.seg, cb.jhi, cb.jlo, cb.tile_c, cb.iprep,
-                                                               cb.perm, cb.part, cb.jpart, cb.ev_keys, cb.ev_cap);
+        k_pair_sym<SYM_MINB_A><<<cb.slots, SYM_THREADS, 0, st>>>(cb.a, ctl, cb.seg, cb.jhi, cb.jlo, cb.tile_c,
+                                                                 cb.tile_t, cb.iprep, cb.perm, cb.part, cb.jpart,
+                                                                 cb.ev_keys, cb.ev_cap);
+        break;
+    case NBG_MIX_SYM + 1:
+        k_pair_sym<SYM_MINB_B><<<cb.slots, SYM_THREADS, 0, st>>>(cb.a, ctl, cb.seg, cb.jhi, cb.jlo, cb.tile_c,
+                                                                 cb.tile_t, cb.iprep, cb.perm, cb.part, cb.jpart,
+                                                                 cb.ev_keys, cb.ev_cap);
         break;
     }
 }
 
 void nbg_launch_mixed_out(const CycleBufs &cb, DevCtl *ctl, cudaStream_t st)
 {
-    if (cb.mix_variant == NBG_MIX_SYM)
+    if (nbg_mix_is_sym(cb.mix_variant))
         k_sym_out<<<nbg_flat_grid(cb, cb.cap), 256, 0, st>>>(cb.a, ctl, cb.seg, cb.perm, cb.part, cb.jpart);
     else
         k_mix_out<<<nbg_flat_grid(cb, cb.cap), 256, 0, st>>>(cb.a, ctl, cb.seg, cb.perm, cb.part,

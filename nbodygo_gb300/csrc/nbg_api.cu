@@ -287,6 +287,7 @@ static int ensure_cap(nbg_ctx *ctx, ll need, ll keep)
     /* every sim may end in a partial tile: at most cap / itile + nsims tiles */
     ll tiles = (cap + NBG_MIX_MIN_ITILE - 1) / NBG_MIX_MIN_ITILE + NBG_MAX_SIMS + 1;
     CK(cudaMalloc((void **)&ctx->cb.tile_c, (size_t)tiles * sizeof(float4)));
+    CK(cudaMalloc((void **)&ctx->cb.tile_t, (size_t)tiles * sizeof(float)));
     CK(cudaMalloc((void **)&ctx->cb.iprep, (size_t)cap * sizeof(float4)));
     ctx->cb.part_doubles = part_need(ctx, cap);
     CK(cudaMalloc((void **)&ctx->cb.part, (size_t)ctx->cb.part_doubles * sizeof(double)));
@@ -369,6 +370,7 @@ static void free_cap_buffers(CycleBufs &cb)
     cudaFree(cb.jhi);
     cudaFree(cb.jlo);
     cudaFree(cb.tile_c);
+    cudaFree(cb.tile_t);
     cudaFree(cb.iprep);
     cudaFree(cb.p64_terms);
     cudaFree(cb.p64_acc);

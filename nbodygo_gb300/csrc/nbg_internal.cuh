@@ -217,7 +217,8 @@ struct CycleBufs {
     ll nblk_cap;
     /* mixed form (indexed by sorted position) */
     float4 *jhi, *jlo;
-    float4 *tile_c;
+    float4 *tile_c;     /* per i-tile: origin (xyz) and a radius holding its bodies (w) */
+    float *tile_t;      /* per i-tile: the largest near-pair threshold of its bodies (NULL: not kept) */
     float4 *iprep;      /* per sorted position: re-centred x, y, z and near-pair threshold */
     double *part;
     unsigned *perm;     /* sorted position -> body index */
@@ -262,8 +263,10 @@ struct MixVariantInfo {
     int block, k, jt, unroll;
 };
 #define NBG_MIX_VARIANTS NBG_MIX_SHAPES
-/* the symmetric kernel (each unordered pair once, k_pair_sym): the last shape */
-#define NBG_MIX_SYM (NBG_MIX_SHAPES - 1)
+/* the symmetric kernel (each unordered pair once, k_pair_sym): the last two
+ * shapes (registers capped for 4 and 5 CTAs per SM) */
+#define NBG_MIX_SYM (NBG_MIX_SHAPES - 2)
+__host__ __device__ __forceinline__ bool nbg_mix_is_sym(int variant) { return variant >= NBG_MIX_SYM; }
 #define NBG_MIX_MIN_ITILE 256
 #define NBG_MIX_MAX_ITILE 512
 /* fewest (i-tile, j-body) units of pair work in a chunk, and chunks per

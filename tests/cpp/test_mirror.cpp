@@ -322,7 +322,7 @@ static void TestRunnerSnapshot()
         for (int k = 0; k < 64; k++) {
             const double a = 0.7 * k;
             v.push_back(NewBody(k + 1, 8 * std::cos(a), 8 * std::sin(a), 0.3 * (k % 5), -std::sin(a), std::cos(a),
-                                0, 1e11 * (1 + k % 3), 1.0, k % 2 ? Elastic : Subsume, Random, 0, 0, false,
+                                0, 1e11 * (1 + k % 3), 0.6 + 0.2 * (k % 4), k % 2 ? Elastic : Subsume, Random, 0, 0, false,
                                 "b" + std::to_string(k), "", false));
         }
         return v;

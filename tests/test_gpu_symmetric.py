@@ -1,4 +1,5 @@
-"""The symmetric mixed pair kernel (shape NBG_MIX_SHAPES - 1, k_pair_sym):
+"""The symmetric mixed pair kernel (the last two shapes, k_pair_sym with
+registers capped for 4 and 5 CTAs per SM):
 each unordered pair computed once and added to both bodies.  It must give
 the FP64 forces within the mixed tolerance on collections of several
 512-body blocks (where pairs rotate through the warps), ragged last blocks,
@@ -18,7 +19,8 @@ from test_gpu_plain_parity import dense_cluster
 
 pytestmark = pytest.mark.gpu
 TOL = 1e-6
-SYM = A.MIX_SHAPES - 1
+SYM = A.MIX_SHAPES - 2
+SHAPES = (A.MIX_SHAPES - 2, A.MIX_SHAPES - 1)
 
 
 def forces(b, shape=SYM, sims=None):
@@ -37,16 +39,18 @@ def oracle_forces(b):
     return np.array(o.forces())
 
 
+@pytest.mark.parametrize("shape", SHAPES)
 @pytest.mark.parametrize("n", [513, 1023, 1025, 4096, 5000])
-def test_plummer_against_the_oracle(n):
+def test_plummer_against_the_oracle(n, shape):
     b = W.plummer(n=n, seed=n)
-    f = forces(b)
+    f = forces(b, shape=shape)
     assert rel_l2(f, oracle_forces(b)) <= TOL
 
 
-def test_plummer_disk_against_the_oracle_and_the_one_sided_kernel():
+@pytest.mark.parametrize("shape", SHAPES)
+def test_plummer_disk_against_the_oracle_and_the_one_sided_kernel(shape):
     b = W.plummer_disk(n_each=8192, seed=3)
-    f = forces(b)
+    f = forces(b, shape=shape)
     g = oracle_forces(b)
     assert rel_l2(f, g) <= TOL
     assert rel_l2(f, forces(b, shape=7)) <= TOL
@@ -80,12 +84,13 @@ def test_several_collections():
         o += k
 
 
-def test_dense_cluster_events_and_forces():
+@pytest.mark.parametrize("shape", SHAPES)
+def test_dense_cluster_events_and_forces(shape):
     """Near and overlapping pairs in every block pair: exact FP64 terms on
     both sides, and the oracle's event list."""
     b = dense_cluster(3000, seed=61)
     with Simulation("mixed", seed=5) as s:
-        s.set_option(A.OPT_MIX_SHAPE, SYM)
+        s.set_option(A.OPT_MIX_SHAPE, shape)
         s.set_bodies(b)
         f = np.array(s.force_pass())
         s.step(0.05, 0.9, 1)
