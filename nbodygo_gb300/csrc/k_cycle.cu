@@ -923,6 +923,29 @@ __device__ static void resolve_dataflow(BodyArrays &A, DevCtl *ctl, const ull *k
     ll done = 0;
     while (s_n[cur] > 0) {
         const ll nr = s_n[cur];
+        if (nr == 1) {
+            /* a chain (one body in every event): one thread follows it for
+             * as long as each event readies exactly one successor, without
+             * a barrier per event */
+            if (tid == 0) {
+                ll o = fr[cur][0];
+                for (;;) {
+                    resolve_one(A, keys[lo + hi - 1 - o], &ev_out[o]);
+                    done++;
+                    const ll n0 = link[2 * o], n1 = link[2 * o + 1];
+                    ll rd[2];
+                    int nready = 0;
+                    if (n0 >= 0 && atomicSub(&pend[n0], 1) == 1) rd[nready++] = n0;
+                    if (n1 >= 0 && n1 != n0 && atomicSub(&pend[n1], 1) == 1) rd[nready++] = n1;
+                    if (nready == 1) {
+                        o = rd[0];
+                        continue;
+                    }
+                    for (int q = 0; q < nready; q++) fr[cur ^ 1][s_n[cur ^ 1]++] = rd[q];
+                    break;
+                }
+            }
+        } else
         for (ll x = tid; x < nr; x += RESOLVE_BLOCK) {
             const ll o = fr[cur][x];
             resolve_one(A, keys[lo + hi - 1 - o], &ev_out[o]);
