@@ -38,10 +38,11 @@ them.  On the default workload each step is one full cycle of the same
 131,072-body collection (about 10 s on 16 Grace cores); the larger workloads
 (ensemble, uniform, Barnes-Hut) are timed on a stated sample.
 
-Under torchrun (N > 1) each rank runs an independent replica on its own GPU.
-The direct sum of one collection is not sharded, so this is replicas only.
-`value` is the sum over ranks of the work done, divided by the slowest rank's
-time.
+Under torchrun (N > 1) each rank runs on its own GPU.  The direct sum of one
+collection is not sharded: each rank runs an independent replica.  The
+ensemble's 512 independent collections are split across the ranks instead
+(shard_collections), one job with no exchange.  `value` is the sum over ranks
+of the work done, divided by the slowest rank's time.
 """
 import argparse
 import json
@@ -232,15 +233,35 @@ def measured_hbm():
         return {}
 
 
-def make_workload(name, n_each, rank):
-    """(list of body dicts, one per simulation) for a workload."""
+def shard_collections(sizes, ws):
+    """The collections each of ws ranks runs: largest pair work n (n - 1)
+    first, each to the rank with the least work so far (ties to the lower
+    rank).  Deterministic, so every rank derives the same split without an
+    exchange; every collection goes to exactly one rank."""
+    load = [0] * ws
+    shards = [[] for _ in range(ws)]
+    for s in sorted(range(len(sizes)), key=lambda k: (-sizes[k] * (sizes[k] - 1), k)):
+        r = min(range(ws), key=lambda q: (load[q], q))
+        shards[r].append(s)
+        load[r] += sizes[s] * (sizes[s] - 1)
+    return [sorted(x) for x in shards]
+
+
+def make_workload(name, n_each, rank, ws=1):
+    """(list of body dicts, one per simulation) for a workload.  The ensemble
+    is one job split across the ranks (its collections are independent);
+    every other workload is one replica per rank with its own seed."""
     from nbodygo_gb300 import workloads as W
 
     seed_off = 1000 * rank
     if name == "plummer_disk":
         return [W.plummer_disk(n_each=n_each, seed=3 + seed_off)]
     if name == "ensemble":
-        return W.ensemble(seed=5 + seed_off)
+        sims = W.ensemble(seed=5)
+        if ws > 1:
+            mine = shard_collections([len(b["x"]) for b in sims], ws)[rank]
+            sims = [sims[k] for k in mine]
+        return sims
     if name == "uniform":
         return [W.uniform_ball(seed=4 + seed_off)]
     if name == "plummer":
@@ -273,7 +294,8 @@ def config_of(workload, n0, nsims, ws):
             "n_bodies": n0, "n_sims": nsims, "dt": dt,
             "l2": "GPU arm: flushed (512 MB write) before every timed cycle"
                   + (" graph" if workload == "ensemble" else "") + "; CPU arm: not applicable",
-            "parallelism": f"replicas x{ws}"}
+            "parallelism": (f"collections split over {ws} ranks" if workload == "ensemble" and ws > 1
+                            else f"replicas x{ws}")}
 
 
 def cpu_sample(workload, n_each=65536):
@@ -476,7 +498,8 @@ def main():
     # stream, which nbg_set_stream does not take)
     stream = torch.cuda.Stream()
     torch.cuda.set_stream(stream)
-    sims = make_workload(args.workload, args.n_each, rank)
+    sims = make_workload(args.workload, args.n_each, rank, ws)
+    sharded = args.workload == "ensemble" and ws > 1
     n0 = int(sum(len(b["x"]) for b in sims))
     chunk = 10 if args.workload == "ensemble" else 1
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
@@ -528,6 +551,9 @@ def main():
     per_chunk = [a.elapsed_time(b) for a, b in ev]
     t_ms = sum(per_chunk)
     value, t_max, work = aggregate(dist, interactions, t_ms)
+    # the job's size: one replica's, or the whole ensemble split over ranks
+    job_bodies = int(dist.sum(n0)) if sharded else n0
+    job_sims = int(dist.sum(len(sims))) if sharded else len(sims)
 
     # ---- pair-kernel time (library timing mode, same stream) ----
     sim.enable_timing(True)
@@ -705,10 +731,10 @@ def main():
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": cycles,
             "warmup": args.warmup, "ms_per_step": t_max / cycles,
             "ms_per_chunk_each": [round(v, 4) for v in per_chunk], "cycles_per_chunk": chunk,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "higher_is_better": True, "scaling": "strong" if sharded else "weak", "vs_baseline": None,
             "dtype": "fp32 pair terms, fp64 state" if prec == "mixed" else "f64",
             "data": "synthetic",
-            "config": config_of(args.workload, n0, len(sims), ws),
+            "config": config_of(args.workload, job_bodies, job_sims, ws),
             "form": {"precision": prec, "barnes_hut": bh,
                      "sort_interval": (args.sort_interval or 4) if prec == "mixed" and not bh else None},
             "e2e": e2e,
