@@ -397,7 +397,9 @@ int nbg_get_timing(nbg_ctx *ctx, nbg_timing *t);
 #define NBG_OPT_NEAR_PPM 5   /* mixed: pairs closer than (value * 1e-6) x the i-body's
                                 distance from its tile origin take the near-pair
                                 pass: the exact hi/lo difference, FP64 for a
-                                possible overlap (default 50000) */
+                                possible overlap (default 50000; twice the
+                                value in collections of at most 2,048 bodies,
+                                where a tile spans the collection) */
 int nbg_set_option(nbg_ctx *ctx, int key, int64_t value);
 
 /* Autotuner of the mixed pair kernel.  Seventeen shapes are compiled, the first fifteen each

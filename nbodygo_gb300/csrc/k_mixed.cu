@@ -291,10 +291,15 @@ __global__ void k_mix_iprep(DevCtl *ctl, SimSegs seg, const float4 *__restrict__
     const ll n = ctl->n;
     const float rmax = __uint_as_float(ctl->rmax_bits);
     const float xmax = __uint_as_float(ctl->xmax_bits);
-    const double kappa = (double)ctl->near_kappa;
+    const double kappa0 = (double)ctl->near_kappa;
     for (ll p = (ll)blockIdx.x * blockDim.x + threadIdx.x; p < n; p += (ll)gridDim.x * blockDim.x) {
         const int sim = nbg_sim_of(seg.off, seg.nsims, p);
         const ll s0 = seg.off[sim];
+        /* In a small collection one or two tiles span it all, so a body's
+         * offset from its tile origin is large next to its neighbours'
+         * distances, and the neighbours carry much of its force: twice the
+         * factor there.  Such collections hold a small share of the work. */
+        const double kappa = seg.off[sim + 1] - s0 <= NBG_NEAR_SMALL_N ? 2.0 * kappa0 : kappa0;
         const ll tile = seg.mtile_off[sim] + (p - s0) / itile;
         const float4 c = tile_c[tile];
         float xr, yr, zr, t;

@@ -109,6 +109,8 @@ struct DevCtl {
 /* mixed: pairs closer than this factor x the i-body's distance from its
  * tile origin take the near-pair pass (NBG_OPT_NEAR_PPM changes it) */
 #define NBG_NEAR_KAPPA_DEFAULT 0.05f
+/* collections of at most this many bodies use twice the near-pair factor */
+#define NBG_NEAR_SMALL_N 2048
 
 /* A collection may hold several independent simulations stored one after
  * another: sim s occupies bodies [off[s], off[s+1]) and bodies of different
