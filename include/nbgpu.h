@@ -362,7 +362,7 @@ int nbg_get_timing(nbg_ctx *ctx, nbg_timing *t);
 #define NBG_OPT_FRAG_CAP 4   /* fragments one cycle may emit */
 #define NBG_OPT_GRAPH_CYCLES 6 /* cycles captured in one CUDA graph (default 1) */
 #define NBG_OPT_MIX_SHAPE 7    /* shape of the mixed pair kernel, 0..NBG_MIX_SHAPES-1 (see nbg_autotune) */
-#define NBG_MIX_SHAPES 17
+#define NBG_MIX_SHAPES 19
 /* 1: forces from the Barnes-Hut octree of cmd/body/octree.go (opening angle
  * 0.3, softening 1e-4, suns summed directly) with the FP64 arithmetic of the
  * plain form, in either precision; collisions stay exact.  This is the
@@ -402,7 +402,7 @@ int nbg_get_timing(nbg_ctx *ctx, nbg_timing *t);
                                 where a tile spans the collection) */
 int nbg_set_option(nbg_ctx *ctx, int key, int64_t value);
 
-/* Autotuner of the mixed pair kernel.  Seventeen shapes are compiled, the first fifteen each
+/* Autotuner of the mixed pair kernel.  Nineteen shapes are compiled, the first fifteen each
  * threads per CTA x i-bodies per thread, j per shared-memory tile, unroll,
  * CTAs per SM, in three kinds: sums in registers (R), sums in shared memory
  * (S), and shared memory with two j-tile buffers filled a tile ahead (D):
@@ -411,10 +411,14 @@ int nbg_set_option(nbg_ctx *ctx, int key, int64_t value);
  *   6: R 128x2, 128, 4, 4            7: S 128x2, 256, 2, 5  8: S 128x3, 256, 2, 4
  *   9: S 128x4, 256, 2, 4           10: S 128x4, 128, 4, 4 11: D 128x2, 128, 4, 4
  *  12: D 128x2, 256, 2, 4           13: D 128x2, 128, 2, 4 14: D 128x4, 128, 2, 3
- * and two of the symmetric kernel, which computes each unordered pair once
+ * two of the symmetric kernel, which computes each unordered pair once
  * and adds its term to both bodies (512-body blocks, 4 i-bodies per thread,
  * j pairs rotated through each warp's lanes):
  *  15: 128x4, 4 CTAs/SM              16: 128x4, 5 CTAs/SM
+ * and two more one-sided shapes of kind B, sums in shared memory with the
+ * raw j tiles brought into shared memory by bulk copies (cp.async.bulk on an
+ * mbarrier) issued two tiles ahead and re-centred from there:
+ *  17: B 128x2, 256, 2, 5           18: B 128x4, 256, 2, 4
  * nbg_autotune times the pair kernel of each on the context's current
  * collection (the best of three force passes after one warm-up) and keeps the
  * fastest.  cache_path (may be NULL) names a text file of earlier results

@@ -49,7 +49,8 @@ OPT_SORT_INTERVAL = 10
 OPT_STEP_DEADLINE_MS = 12
 OPT_EVENT_SORT = 13
 OPT_P64_SPLIT_MAX = 11
-MIX_SHAPES = 17
+MIX_SHAPES = 19
+MIX_SYM = 15  # shapes 15 and 16: the symmetric kernel
 
 _pd = C.POINTER(C.c_double)
 _pi64 = C.POINTER(C.c_int64)

@@ -17,10 +17,13 @@
  *    TwoSum (Knuth), so the accumulated rounding error stays that of a
  *    128-term sum; each item's total is written as FP64;
  *  - a pair closer than a conservative bound - the larger of r_i + r_max plus
- *    the FP32 error bound, and near_kappa times the i-tile's extent - is
- *    re-evaluated in FP64 with the reference's exact expressions: that FP64
- *    dist decides the overlap skip and the collision test, so the event set
- *    is the reference's, and the force of every near pair is FP64.
+ *    the FP32 error bound, and near_kappa times the body's offset from its
+ *    i-tile's origin - takes a near-pair pass: dx from the difference of the
+ *    hi/lo parts (error ~2^-24 |dx|), a Newton-refined reciprocal square
+ *    root, and the term added to the compensated sums directly;
+ *  - a near pair within 2^-10 of touching is re-evaluated in FP64 with the
+ *    reference's exact expressions: that FP64 dist decides the overlap skip
+ *    and the collision test, so the event set is the reference's.
  *
  * The pair work of a cycle, W units of (i-tile, one j-body), is cut into C
  * chunks, about 32 per resident CTA, whatever the sizes of the sims and
@@ -346,6 +349,18 @@ __device__ __forceinline__ void near_pass_j(const BodyArrays &A, DevCtl *ctl, ul
             fold64(fhz, flz, qz);
             return;
         }
+        /* A near pair can carry most of the body's force, so its term is
+         * made as exact as FP32 allows: one Newton step on the SFU's
+         * reciprocal square root (relative error 2^-22.9 -> ~2^-24), and
+         * the term goes straight into the (hi, lo) sums rather than through
+         * the tile's FP32 sum, whose roundings would be ulps of this term */
+        float inv = rsqrt_sfu(r2);
+        inv = inv * (1.5f - 0.5f * r2 * inv * inv);
+        const float s = m * inv * inv * inv;
+        two_sum_add(fhx, flx, s * dx);
+        two_sum_add(fhy, fly, s * dy);
+        two_sum_add(fhz, flz, s * dz);
+        return;
     }
     const float inv = rsqrt_sfu(r2);
     const float s = m * inv * inv * inv;
@@ -354,10 +369,61 @@ __device__ __forceinline__ void near_pass_j(const BodyArrays &A, DevCtl *ctl, ul
     tz += s * dz;
 }
 
+/* ---- bulk copies into shared memory ----------------------------------------
+ * cp.async.bulk (the copy engine, no registers) completing on an mbarrier:
+ * the issuing thread arms the barrier with the bytes it expects, and every
+ * thread waits for the barrier's phase.  Waits give up after about two
+ * seconds of SM clock. */
+__device__ __forceinline__ unsigned smem_addr(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(ull *bar, unsigned count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(ull *bar, unsigned bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
+                 : "memory");
+}
+
+/* bytes (a multiple of 16, both addresses 16-byte aligned) from global src
+ * to shared dst, completing on bar */
+__device__ __forceinline__ void bulk_to_smem(void *dst, const void *src, unsigned bytes, ull *bar)
+{
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_addr(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_addr(bar))
+                 : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(ull *bar, unsigned parity)
+{
+    unsigned ok;
+    asm volatile("{\n\t.reg .pred p;\n\t"
+                 "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                 "selp.u32 %0, 1, 0, p;\n\t}"
+                 : "=r"(ok)
+                 : "r"(smem_addr(bar)), "r"(parity)
+                 : "memory");
+    return ok != 0;
+}
+
+/* true once the phase of parity `parity` has completed; false after ~2^32
+ * SM clocks */
+__device__ __forceinline__ bool mbar_wait_bounded(ull *bar, unsigned parity)
+{
+    if (mbar_try_wait(bar, parity)) return true;
+    const long long t0 = clock64();
+    while (!mbar_try_wait(bar, parity))
+        if (clock64() - t0 > (1ll << 32)) return false;
+    return true;
+}
+
 /* Everything in this kernel is indexed by sorted position (p for i, q for
  * j); perm maps a position to the body index used by the FP64 arrays and the
  * event keys. */
-template <int BLOCK, int K, int JT, int UNROLL, int MINB, bool SF, bool DB>
+template <int BLOCK, int K, int JT, int UNROLL, int MINB, bool SF, bool DB, bool BULK>
 __global__ void __launch_bounds__(BLOCK, MINB)
 k_pair_mixed(BodyArrays A, DevCtl *ctl, SimSegs seg, const float4 *__restrict__ jhi, const float4 *__restrict__ jlo,
              const float4 *__restrict__ tile_c, const float4 *__restrict__ iprep, const unsigned *__restrict__ perm,
@@ -367,10 +433,16 @@ k_pair_mixed(BodyArrays A, DevCtl *ctl, SimSegs seg, const float4 *__restrict__ 
     constexpr int ITILE = BLOCK * K;
     static_assert(ITILE >= NBG_MIX_MIN_ITILE, "tile-origin buffer is sized for the smallest i-tile");
     static_assert(ITILE <= NBG_MIX_MAX_ITILE, "partial-sum buffer is sized for the largest i-tile");
+    static_assert(!(DB && BULK), "one way of filling the tiles");
     /* DB: two tile buffers; the next tile's raw j is loaded into registers
      * while this tile is computed, and stored to the other buffer after it,
-     * so a tile costs one barrier and its global loads are hidden */
-    __shared__ float4 sAb[DB ? 2 : 1][JP], sBb[DB ? 2 : 1][JP];
+     * so a tile costs one barrier and its global loads are hidden.
+     * BULK: two tile buffers too, and the raw j of the tiles after the next
+     * are copied into two raw buffers by bulk copies issued ahead; each
+     * tile re-centres the next one's raw j from shared memory. */
+    __shared__ float4 sAb[DB || BULK ? 2 : 1][JP], sBb[DB || BULK ? 2 : 1][JP];
+    __shared__ alignas(128) float4 rawH[BULK ? 2 : 1][BULK ? JT : 1], rawL[BULK ? 2 : 1][BULK ? JT : 1];
+    __shared__ alignas(8) ull mbar[2];
     constexpr int PPT = (JP + BLOCK - 1) / BLOCK; /* j pairs a thread fills */
     float4 pre[DB ? PPT : 1][2][2];
     /* SF: each i-body's (hi, lo) sums and near-pair threshold live in shared
@@ -391,6 +463,18 @@ k_pair_mixed(BodyArrays A, DevCtl *ctl, SimSegs seg, const float4 *__restrict__ 
     const float xmax = __uint_as_float(ctl->xmax_bits);
     const double kappa = (double)ctl->near_kappa;
     const int tid = threadIdx.x;
+    /* BULK: bit b of ph is the parity of mbar[b]'s next phase, bit b of pend
+     * says a copy into raw buffer b is in flight (both the same in every
+     * thread) */
+    unsigned ph = 0, pend = 0;
+    if (BULK) {
+        if (tid == 0) {
+            mbar_init(&mbar[0], 1);
+            mbar_init(&mbar[1], 1);
+            asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        }
+        __syncthreads();
+    }
 
     for (;;) {
     if (tid == 0) s_chunk = (ll)atomicAdd((unsigned long long *)&ctl->work_next, 1ull);
@@ -479,15 +563,67 @@ k_pair_mixed(BodyArrays A, DevCtl *ctl, SimSegs seg, const float4 *__restrict__ 
                 }
             }
         };
+        /* BULK: the segment's raw tile u (j from jb + u JT) goes to raw
+         * buffer u & 1 through mbar[u & 1]; its re-centred pairs to tile
+         * buffer u & 1 */
+        auto issue = [&](ll q0, int b) {
+            pend |= 1u << b;
+            if (tid == 0) {
+                const unsigned cnt = (unsigned)(je - q0 < JT ? je - q0 : JT);
+                /* the buffer's last readers, before a barrier, read it
+                 * through the generic proxy */
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                mbar_expect_tx(&mbar[b], 2u * 16u * cnt);
+                bulk_to_smem(&rawH[b][0], jhi + q0, 16u * cnt, &mbar[b]);
+                bulk_to_smem(&rawL[b][0], jlo + q0, 16u * cnt, &mbar[b]);
+            }
+        };
+        /* waits for raw buffer b (the tile from q0) and re-centres it into
+         * tile buffer b; false if the copy did not complete */
+        auto unpack = [&](ll q0, int b) -> bool {
+            if (!mbar_wait_bounded(&mbar[b], (ph >> b) & 1u)) return false;
+            ph ^= 1u << b;
+            pend &= ~(1u << b);
+            for (int sp = tid; sp < JP; sp += BLOCK) {
+                const float4 h[2] = {rawH[b][2 * sp], rawH[b][2 * sp + 1]};
+                const float4 l[2] = {rawL[b][2 * sp], rawL[b][2 * sp + 1]};
+                pack(h, l, q0 + 2 * sp, sAb[b][sp], sBb[b][sp]);
+            }
+            return true;
+        };
+        /* a copy that did not complete: the cycle fails with NBG_E_TIMEOUT
+         * after a second bounded wait for the copies still in flight */
+        auto give_up = [&]() {
+            if (tid == 0) {
+                ctl->error = NBG_E_TIMEOUT;
+                ctl->error_what = 8;
+            }
+            for (int b = 0; b < 2; b++)
+                if (pend & (1u << b)) mbar_wait_bounded(&mbar[b], (ph >> b) & 1u);
+        };
         int buf = 0;
         if (DB) {
             load_raw(jb);
             __syncthreads(); /* the previous segment's readers are done */
             store_raw(0, jb);
         }
+        if (BULK) {
+            /* the previous segment's readers of every buffer finished before
+             * its last barrier */
+            issue(jb, 0);
+            if (jb + JT < je) issue(jb + JT, 1);
+            const bool ok = unpack(jb, 0);
+            if (__syncthreads_or(!ok)) {
+                give_up();
+                return;
+            }
+            if (jb + 2 * JT < je) issue(jb + 2 * JT, 0);
+        }
         for (ll jt = jb; jt < je; jt += JT) {
-            const float4 *sA = sAb[DB ? buf : 0], *sB = sBb[DB ? buf : 0];
-            if (DB) {
+            const float4 *sA = sAb[DB || BULK ? buf : 0], *sB = sBb[DB || BULK ? buf : 0];
+            if (BULK) {
+                /* this tile was re-centred before the last barrier */
+            } else if (DB) {
                 __syncthreads(); /* this tile is stored */
                 if (jt + JT < je) load_raw(jt + JT);
             } else {
@@ -579,7 +715,17 @@ k_pair_mixed(BodyArrays A, DevCtl *ctl, SimSegs seg, const float4 *__restrict__ 
                 two_sum_add(FOLD(2, k), FOLD(3, k), ay[k].x + ay[k].y);
                 two_sum_add(FOLD(4, k), FOLD(5, k), az[k].x + az[k].y);
             }
-            if (DB) {
+            if (BULK) {
+                /* tile buffer buf ^ 1 was last read by the previous tile,
+                 * before the last barrier */
+                const bool ok = jt + JT < je ? unpack(jt + JT, buf ^ 1) : true;
+                if (__syncthreads_or(!ok)) {
+                    give_up();
+                    return;
+                }
+                if (jt + 3 * JT < je) issue(jt + 3 * JT, buf ^ 1);
+                buf ^= 1;
+            } else if (DB) {
                 /* the other buffer's last readers finished the previous tile
                  * before this tile's barrier */
                 if (jt + JT < je) store_raw(buf ^ 1, jt + JT);
@@ -1080,8 +1226,11 @@ __global__ void k_sym_out(BodyArrays A, DevCtl *ctl, SimSegs seg, const unsigned
  * (kind, threads per CTA, i-bodies per thread, j per shared-memory tile,
  * unroll of the j loop, CTAs per SM the register budget is set for).  Kind 0:
  * sums in registers; 1: sums in shared memory; 2: sums in shared memory and
- * two tile buffers filled from registers loaded a tile ahead.  Variant 0 is
- * the default; the autotuner (nbg_autotune) measures the others. */
+ * two tile buffers filled from registers loaded a tile ahead; 3: sums in
+ * shared memory and two tile buffers re-centred from raw tiles that bulk
+ * copies bring into shared memory two tiles ahead.  Shapes 15 and 16 are
+ * the symmetric kernel's.  Variant 0 is the default; the autotuner
+ * (nbg_autotune) measures the others. */
 #define MIX_VARIANTS(X)              \
     X(0, 0, 128, 4, 256, 2, 3)       \
     X(1, 0, 128, 4, 256, 1, 3)       \
@@ -1097,10 +1246,12 @@ __global__ void k_sym_out(BodyArrays A, DevCtl *ctl, SimSegs seg, const unsigned
     X(11, 2, 128, 2, 128, 4, 4)      \
     X(12, 2, 128, 2, 256, 2, 4)      \
     X(13, 2, 128, 2, 128, 2, 4)      \
-    X(14, 2, 128, 4, 128, 2, 3)
+    X(14, 2, 128, 4, 128, 2, 3)      \
+    X(17, 3, 128, 2, 256, 2, 5)      \
+    X(18, 3, 128, 4, 256, 2, 4)
 
 /* the kernel of a shape */
-#define MIX_KERNEL(kind, b, k, jt, u, mb) k_pair_mixed<b, k, jt, u, mb, (kind) >= 1, (kind) == 2>
+#define MIX_KERNEL(kind, b, k, jt, u, mb) k_pair_mixed<b, k, jt, u, mb, (kind) >= 1, (kind) == 2, (kind) == 3>
 
 /* the symmetric kernel's shapes: registers capped for 4 or 5 CTAs per SM */
 #define SYM_MINB_A 4

