@@ -42,7 +42,7 @@ extern "C" {
 #define NBG_E_CUDA 1     /* a CUDA runtime call failed */
 #define NBG_E_ARG 2      /* bad argument (null pointer, size, enum value) */
 #define NBG_E_OVERFLOW 3 /* a device buffer was too small; state is unchanged */
-#define NBG_E_TIMEOUT 4  /* nbg_step reached its deadline (NBG_OPT_STEP_DEADLINE_MS) */
+#define NBG_E_TIMEOUT 4  /* nbg_step reached its deadline (NBG_OPT_STEP_DEADLINE_MS), or a device wait gave up */
 #define NBG_E_NAN 5      /* non-finite value where a finite one is required */
 #define NBG_E_STATE 6    /* call not valid in the context's current state */
 #define NBG_E_CANCELLED 7 /* nbg_step stopped by nbg_cancel */
@@ -394,6 +394,12 @@ int nbg_get_timing(nbg_ctx *ctx, nbg_timing *t);
    had more than 4,096 events, until a call stays under 1,024; 1: always;
    2: never.  The order, and so every result, is the same either way. */
 #define NBG_OPT_EVENT_SORT 13
+/* test hook for the bounded device waits: 1 makes the bulk-copy shapes (17,
+   18) arm each mbarrier for 16 bytes more than their copies bring, so no
+   wait completes; every wait gives up after about 2 s of SM clock, the CTA
+   waits (bounded again) for its copies and leaves, and the cycle fails with
+   NBG_E_TIMEOUT.  The context stays usable; 0 (default) turns it off. */
+#define NBG_OPT_TEST_WAIT_STALL 14
 #define NBG_OPT_NEAR_PPM 5   /* mixed: pairs closer than (value * 1e-6) x the i-body's
                                 distance from its tile origin take the near-pair
                                 pass: the exact hi/lo difference, FP64 for a

@@ -467,6 +467,7 @@ k_pair_mixed(BodyArrays A, DevCtl *ctl, SimSegs seg, const float4 *__restrict__ 
      * says a copy into raw buffer b is in flight (both the same in every
      * thread) */
     unsigned ph = 0, pend = 0;
+    const unsigned tx_extra = BULK ? ctl->test_tx_extra : 0u;
     if (BULK) {
         if (tid == 0) {
             mbar_init(&mbar[0], 1);
@@ -573,7 +574,7 @@ k_pair_mixed(BodyArrays A, DevCtl *ctl, SimSegs seg, const float4 *__restrict__ 
                 /* the buffer's last readers, before a barrier, read it
                  * through the generic proxy */
                 asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-                mbar_expect_tx(&mbar[b], 2u * 16u * cnt);
+                mbar_expect_tx(&mbar[b], 2u * 16u * cnt + tx_extra);
                 bulk_to_smem(&rawH[b][0], jhi + q0, 16u * cnt, &mbar[b]);
                 bulk_to_smem(&rawL[b][0], jlo + q0, 16u * cnt, &mbar[b]);
             }

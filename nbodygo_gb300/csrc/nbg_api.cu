@@ -1595,6 +1595,8 @@ int nbg_step(nbg_ctx *ctx, double dt, double R, int nsteps, nbg_step_info *info)
             char m[160];
             snprintf(m, sizeof m, "cycle %d failed: status %d (what %d, need %lld)", done, h->error, h->error_what,
                      (long long)h->error_need);
+            /* the failed cycle may have claimed a sort it never finished */
+            drop_order(ctx);
             return fail(ctx, h->error, m);
         }
         /* grow the short buffer and re-run the interrupted cycle */
@@ -1972,6 +1974,12 @@ int nbg_set_option(nbg_ctx *ctx, int key, int64_t value)
         if (value < 0 || value > 2) return fail(ctx, NBG_E_ARG, "event sort mode must be 0..2");
         ctx->ev_sort_mode = (int)value;
         return NBG_OK;
+    case NBG_OPT_TEST_WAIT_STALL: {
+        if (value < 0 || value > 1) return fail(ctx, NBG_E_ARG, "wait-stall hook must be 0 or 1");
+        const unsigned extra = value ? 16u : 0u;
+        ctx->ctl_h->test_tx_extra = extra;
+        return ctl_put(ctx, offsetof(DevCtl, test_tx_extra), &extra, sizeof extra);
+    }
     case NBG_OPT_STEP_DEADLINE_MS:
         if (value < 0 || value > ((ll)1 << 40)) return fail(ctx, NBG_E_ARG, "deadline must be 0..2^40 ms");
         ctx->deadline_ms = value;

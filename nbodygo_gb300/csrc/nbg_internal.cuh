@@ -74,7 +74,9 @@ struct DevCtl {
     /* mixed form: pairs closer than near_kappa * (extent of the i-tile around
      * its origin) are evaluated in FP64 (set by the host) */
     float near_kappa;
-    int pad1;
+    /* test hook (NBG_OPT_TEST_WAIT_STALL): bytes the bulk-copy shapes add to
+     * each mbarrier's expected count, so that no phase completes; 0 */
+    unsigned test_tx_extra;
     /* accumulated over the cycles of one nbg_step call */
     ll acc_steps, acc_interactions, acc_events, acc_frags, acc_removed, acc_nan, acc_bh_terms;
     ll rend_n;       /* renderables written by the last cycle */
