@@ -467,7 +467,6 @@ k_pair_mixed(BodyArrays A, DevCtl *ctl, SimSegs seg, const float4 *__restrict__ 
      * says a copy into raw buffer b is in flight (both the same in every
      * thread) */
     unsigned ph = 0, pend = 0;
-    const unsigned tx_extra = BULK ? ctl->test_tx_extra : 0u;
     if (BULK) {
         if (tid == 0) {
             mbar_init(&mbar[0], 1);
@@ -569,12 +568,12 @@ k_pair_mixed(BodyArrays A, DevCtl *ctl, SimSegs seg, const float4 *__restrict__ 
          * buffer u & 1 */
         auto issue = [&](ll q0, int b) {
             pend |= 1u << b;
-            if (tid == 0) {
+            if constexpr (BULK) if (tid == 0) {
                 const unsigned cnt = (unsigned)(je - q0 < JT ? je - q0 : JT);
                 /* the buffer's last readers, before a barrier, read it
                  * through the generic proxy */
                 asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-                mbar_expect_tx(&mbar[b], 2u * 16u * cnt + tx_extra);
+                mbar_expect_tx(&mbar[b], 2u * 16u * cnt + ctl->test_tx_extra);
                 bulk_to_smem(&rawH[b][0], jhi + q0, 16u * cnt, &mbar[b]);
                 bulk_to_smem(&rawL[b][0], jlo + q0, 16u * cnt, &mbar[b]);
             }
@@ -582,13 +581,15 @@ k_pair_mixed(BodyArrays A, DevCtl *ctl, SimSegs seg, const float4 *__restrict__ 
         /* waits for raw buffer b (the tile from q0) and re-centres it into
          * tile buffer b; false if the copy did not complete */
         auto unpack = [&](ll q0, int b) -> bool {
-            if (!mbar_wait_bounded(&mbar[b], (ph >> b) & 1u)) return false;
-            ph ^= 1u << b;
-            pend &= ~(1u << b);
-            for (int sp = tid; sp < JP; sp += BLOCK) {
-                const float4 h[2] = {rawH[b][2 * sp], rawH[b][2 * sp + 1]};
-                const float4 l[2] = {rawL[b][2 * sp], rawL[b][2 * sp + 1]};
-                pack(h, l, q0 + 2 * sp, sAb[b][sp], sBb[b][sp]);
+            if constexpr (BULK) {
+                if (!mbar_wait_bounded(&mbar[b], (ph >> b) & 1u)) return false;
+                ph ^= 1u << b;
+                pend &= ~(1u << b);
+                for (int sp = tid; sp < JP; sp += BLOCK) {
+                    const float4 h[2] = {rawH[b][2 * sp], rawH[b][2 * sp + 1]};
+                    const float4 l[2] = {rawL[b][2 * sp], rawL[b][2 * sp + 1]};
+                    pack(h, l, q0 + 2 * sp, sAb[b][sp], sBb[b][sp]);
+                }
             }
             return true;
         };
