@@ -208,3 +208,58 @@ def test_ensemble_full_run_conserves_mass_per_collection():
         m1 = st["mass"][o:o + c].sum()
         assert abs(m1 - m0[s]) <= 1e-12 * m0[s], f"collection {s}: mass {m1!r} != {m0[s]!r}"
         o += c
+
+
+def _empty_like(b):
+    return {k: np.asarray(v)[:0] for k, v in b.items()}
+
+
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+def test_empty_collections_in_a_batch(prec):
+    """Collections with no bodies at the start, in the middle and at the end
+    of a batch: the others step exactly as alone (plain: bit for bit against
+    their oracles; mixed: forces within the tolerance of FP64), the empty
+    ones stay empty, and an add into an empty one lands there alone."""
+    full = [W.disk(n=300, seed=11), dense_cluster(120, seed=12), W.plummer(n=500, seed=13)]
+    e = _empty_like(full[0])
+    sims = [e, full[0], e, e, full[1], full[2], e]
+    counts0 = [len(b["x"]) for b in sims]
+    dt, R = 0.02, 0.9
+    with Simulation(prec, seed=77) as gpu:
+        gpu.set_collections(sims)
+        assert list(gpu.sim_counts()) == counts0
+        if prec == "mixed":
+            f = np.array(gpu.force_pass())
+            with Simulation("fp64") as p:
+                p.set_collections(sims)
+                g = np.array(p.force_pass())
+            assert rel_l2(f, g) <= 1e-6
+        oracles = []
+        for b in sims:
+            o = OracleSim(seed=77, threads=2)
+            o.set_bodies(b)
+            oracles.append(o)
+        for cycle in range(6):
+            gpu.step(dt, R, 1)
+            for o in oracles:
+                o.step(dt, R, 1)
+            counts = gpu.sim_counts()
+            # the mixed form's events are exact on a given state; its states
+            # drift from FP64 within the tolerance, so only the first cycle's
+            # counts must agree there
+            if prec == "fp64" or cycle == 0:
+                assert list(counts) == [o.count() for o in oracles], f"cycle {cycle}"
+            assert counts[0] == counts[2] == counts[3] == counts[6] == 0
+            if prec == "fp64":
+                parts = split_state(gpu.state(), counts)
+                for s, (got, o) in enumerate(zip(parts, oracles)):
+                    if counts[s]:
+                        fields = [k for k in got if k != "id"]
+                        assert_states_identical(got, o.state(), fields=fields, where=f"cycle {cycle} sim {s}")
+        add = W.uniform_ball(n=5, seed=14, R=20.0, radius=0.5)
+        gpu.add_bodies(add, sim=2)
+        gpu.step(dt, R, 1)
+        counts = gpu.sim_counts()
+        assert counts[2] == 5 and counts[0] == 0 and counts[3] == 0 and counts[6] == 0
+        part = split_state(gpu.state(), counts)[2]
+        assert np.all(np.isin(part["mass"], add["mass"]))
