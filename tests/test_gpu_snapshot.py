@@ -112,6 +112,23 @@ def test_batched_context_with_staged_adds_resumes_bit_exact():
     assert_states_identical(b.state(), a.state(), where="batched resumed vs uninterrupted")
 
 
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+def test_barnes_hut_context_resumes_bit_exact(prec):
+    """The octree is rebuilt from the body state every cycle, so a
+    Barnes-Hut run resumes bit for bit too, in both precisions, through
+    collisions of every behaviour."""
+    bodies = dense_cluster(400, seed=41)
+
+    def make():
+        s = Simulation(prec, seed=6)
+        s.set_option(A.OPT_BARNES_HUT, 1)
+        return s
+
+    a, b, _ = resumed(make, lambda s: s.set_bodies(bodies), 5, 7, 0.05, 0.9)
+    assert_states_identical(b.state(), a.state(), where=f"{prec} Barnes-Hut resumed vs uninterrupted")
+    assert_events_identical(b.events(), a.events(), where="last cycle")
+
+
 def test_snapshot_size_query_and_rejections():
     bodies = W.disk(n=100, seed=3)
     import ctypes as C
