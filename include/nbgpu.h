@@ -367,7 +367,8 @@ int nbg_get_timing(nbg_ctx *ctx, nbg_timing *t);
  * 0.3, softening 1e-4, suns summed directly) with the FP64 arithmetic of the
  * plain form, in either precision; collisions stay exact.  This is the
  * reference's --barnes-hut path with its missing Octree.Build call made
- * (body_collection.go:298-300).  Needs a single collection. */
+ * (body_collection.go:298-300).  With several collections each gets its own
+ * tree, the one a context holding it alone would build. */
 #define NBG_OPT_BARNES_HUT 8
 /* mixed Barnes-Hut walk: registers capped for 3, 4 or 5 CTAs per SM (0..2) */
 #define NBG_OPT_BH_SHAPE 9

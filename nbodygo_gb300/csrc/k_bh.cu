@@ -46,7 +46,16 @@
  *    without end for two bodies at one position);
  *  - the sun's direct sum is a parallel reduction, not array order.
  *
- * One collection per context.
+ * Several collections (nbg_set_collections): one tree per collection, each
+ * exactly the tree a context holding that collection alone builds.  Every
+ * collection gets its own bounding box and root cube; after the key passes
+ * the sort takes two more stable passes on the collection index (tree
+ * bodies; the others go last), so each collection's tree bodies are one run
+ * of sorted positions, in key order.  Node boundaries are found within each
+ * run, the depth-first numbering then puts each collection's nodes in one
+ * range with its root first, and the walks, the suns' sums and the collision
+ * query stay inside the body's own collection.  Walk groups of 32 bodies
+ * start at each collection's first sorted position, as they would alone.
  */
 #include "nbg_internal.cuh"
 #include "nbg_math.h"
@@ -86,11 +95,12 @@ __device__ __forceinline__ bool tree_body(const BodyArrays &A, ll k)
     return fabs(x) <= NBG_DBL_MAX && fabs(y) <= NBG_DBL_MAX && fabs(z) <= NBG_DBL_MAX;
 }
 
-/* the root cube, octree.go:174-183 */
-__device__ __forceinline__ void bh_root(const DevCtl *ctl, double &cx, double &cy, double &cz, double &half)
+/* the root cube of collection s, octree.go:174-183 */
+__device__ __forceinline__ void bh_root(const BhTree &t, int s, double &cx, double &cy, double &cz, double &half)
 {
-    const double minX = ord_dbl(ctl->bh_lo[0]), minY = ord_dbl(ctl->bh_lo[1]), minZ = ord_dbl(ctl->bh_lo[2]);
-    const double maxX = ord_dbl(ctl->bh_hi[0]), maxY = ord_dbl(ctl->bh_hi[1]), maxZ = ord_dbl(ctl->bh_hi[2]);
+    const ull *b = t.sbox + 6 * (ll)s;
+    const double minX = ord_dbl(b[0]), minY = ord_dbl(b[1]), minZ = ord_dbl(b[2]);
+    const double maxX = ord_dbl(b[3]), maxY = ord_dbl(b[4]), maxZ = ord_dbl(b[5]);
     cx = (minX + maxX) / 2;
     cy = (minY + maxY) / 2;
     cz = (minZ + maxZ) / 2;
@@ -99,54 +109,129 @@ __device__ __forceinline__ void bh_root(const DevCtl *ctl, double &cx, double &c
 
 /* ---- 1. bounds, keys -------------------------------------------------------- */
 
-__global__ void __launch_bounds__(BH_BLOCK) k_bh_bounds(BodyArrays A, DevCtl *ctl)
+/* empty boxes and counts for every collection */
+__global__ void __launch_bounds__(1024) k_bh_reset(DevCtl *ctl, SimSegs seg, BhTree t)
 {
     if (ctl->error) return;
-    const ll n = ctl->n;
-    double lo[3] = {NBG_DBL_MAX, NBG_DBL_MAX, NBG_DBL_MAX}, hi[3] = {-NBG_DBL_MAX, -NBG_DBL_MAX, -NBG_DBL_MAX};
-    double rmax = 0;
-    unsigned cnt = 0;
-    for (ll k = (ll)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (ll)gridDim.x * blockDim.x) {
-        const double r = A.rad[k];
-        if (r > rmax) rmax = r;
-        if (!tree_body(A, k)) continue;
-        const double v[3] = {A.x[k], A.y[k], A.z[k]};
+    for (int s = threadIdx.x; s < seg.nsims; s += blockDim.x) {
+        ull *b = t.sbox + 6 * (ll)s;
         for (int c = 0; c < 3; c++) {
-            lo[c] = fmin(lo[c], v[c]);
-            hi[c] = fmax(hi[c], v[c]);
+            b[c] = ~0ull;
+            b[3 + c] = 0ull;
         }
-        cnt++;
+        t.scount[s] = 0;
     }
-    for (int o = 16; o > 0; o >>= 1) {
-        for (int c = 0; c < 3; c++) {
-            lo[c] = fmin(lo[c], __shfl_xor_sync(FULL_MASK, lo[c], o));
-            hi[c] = fmax(hi[c], __shfl_xor_sync(FULL_MASK, hi[c], o));
-        }
-        rmax = fmax(rmax, __shfl_xor_sync(FULL_MASK, rmax, o));
-        cnt += __shfl_xor_sync(FULL_MASK, cnt, o);
-    }
-    if ((threadIdx.x & 31) == 0 && cnt > 0) {
-        for (int c = 0; c < 3; c++) {
-            atomicMin((unsigned long long *)&ctl->bh_lo[c], (unsigned long long)dbl_ord(lo[c]));
-            atomicMax((unsigned long long *)&ctl->bh_hi[c], (unsigned long long)dbl_ord(hi[c]));
-        }
-        atomicAdd((unsigned long long *)&ctl->bh_count, (unsigned long long)cnt);
-    }
-    if ((threadIdx.x & 31) == 0) atomicMax((unsigned long long *)&ctl->bh_rmax, (unsigned long long)dbl_ord(rmax));
 }
 
-/* octant path of every tree body; other bodies get the largest key */
-__global__ void __launch_bounds__(BH_BLOCK) k_bh_keys(BodyArrays A, DevCtl *ctl, ull *keys, unsigned *vals)
+/* each collection's bounding box and tree-body count, and the largest
+ * radius of any body */
+__global__ void __launch_bounds__(BH_BLOCK) k_bh_bounds(BodyArrays A, DevCtl *ctl, SimSegs seg, BhTree t)
 {
     if (ctl->error) return;
     const ll n = ctl->n;
-    double cx0, cy0, cz0, half0;
-    bh_root(ctl, cx0, cy0, cz0, half0);
+    const int lane = threadIdx.x & 31;
+    double rmax = 0;
+    /* warp-uniform trip count: every lane takes part in the reductions */
+    for (ll base = (ll)blockIdx.x * blockDim.x; base < n; base += (ll)gridDim.x * blockDim.x) {
+        const ll k = base + threadIdx.x;
+        ull lo[3] = {~0ull, ~0ull, ~0ull}, hi[3] = {0ull, 0ull, 0ull};
+        unsigned cnt = 0;
+        int sim = -1;
+        if (k < n) {
+            const double r = A.rad[k];
+            if (r > rmax) rmax = r;
+            sim = nbg_sim_of(seg.off, seg.nsims, k);
+            if (tree_body(A, k)) {
+                lo[0] = hi[0] = dbl_ord(A.x[k]);
+                lo[1] = hi[1] = dbl_ord(A.y[k]);
+                lo[2] = hi[2] = dbl_ord(A.z[k]);
+                cnt = 1;
+            }
+        }
+        /* bodies lie in collection order, so the collections of a warp are
+         * runs of lanes: a segmented reduction down each run leaves its sum
+         * in the run's first lane */
+        for (int o = 1; o < 32; o <<= 1) {
+            const int so = __shfl_down_sync(FULL_MASK, sim, o);
+            ull l[3], h[3];
+            for (int c = 0; c < 3; c++) {
+                l[c] = __shfl_down_sync(FULL_MASK, lo[c], o);
+                h[c] = __shfl_down_sync(FULL_MASK, hi[c], o);
+            }
+            const unsigned co = __shfl_down_sync(FULL_MASK, cnt, o);
+            if (lane + o < 32 && so == sim) {
+                for (int c = 0; c < 3; c++) {
+                    lo[c] = l[c] < lo[c] ? l[c] : lo[c];
+                    hi[c] = h[c] > hi[c] ? h[c] : hi[c];
+                }
+                cnt += co;
+            }
+        }
+        const int sprev = __shfl_up_sync(FULL_MASK, sim, 1);
+        if (sim >= 0 && cnt > 0 && (lane == 0 || sprev != sim)) {
+            ull *b = t.sbox + 6 * (ll)sim;
+            for (int c = 0; c < 3; c++) {
+                atomicMin((unsigned long long *)&b[c], (unsigned long long)lo[c]);
+                atomicMax((unsigned long long *)&b[3 + c], (unsigned long long)hi[c]);
+            }
+            atomicAdd((unsigned long long *)&t.scount[sim], (unsigned long long)cnt);
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) rmax = fmax(rmax, __shfl_xor_sync(FULL_MASK, rmax, o));
+    if (lane == 0) atomicMax((unsigned long long *)&ctl->bh_rmax, (unsigned long long)dbl_ord(rmax));
+}
+
+/* each collection's first sorted position and first walk group (exclusive
+ * scans over the collections, one warp), and the tree-body total */
+__global__ void __launch_bounds__(32) k_bh_segs(DevCtl *ctl, SimSegs seg, BhTree t)
+{
+    if (ctl->error) return;
+    const int ns = seg.nsims, lane = threadIdx.x;
+    const int per = (ns + 31) / 32;
+    const int s0 = lane * per, s1 = s0 + per < ns ? s0 + per : ns;
+    ll c = 0, g = 0;
+    for (int s = s0; s < s1; s++) {
+        c += t.scount[s];
+        g += (t.scount[s] + 31) / 32;
+    }
+    ll xc = c, xg = g;
+    for (int o = 1; o < 32; o <<= 1) {
+        const ll yc = __shfl_up_sync(FULL_MASK, xc, o), yg = __shfl_up_sync(FULL_MASK, xg, o);
+        if (lane >= o) {
+            xc += yc;
+            xg += yg;
+        }
+    }
+    ll oc = xc - c, og = xg - g;
+    for (int s = s0; s < s1; s++) {
+        t.stree[s] = oc;
+        t.sgrp[s] = og;
+        oc += t.scount[s];
+        og += (t.scount[s] + 31) / 32;
+    }
+    if (lane == 31) {
+        t.stree[ns] = xc;
+        t.sgrp[ns] = xg;
+        ctl->bh_count = xc;
+    }
+}
+
+/* the collection whose run of sorted tree positions holds p (0 <= p < M) */
+__device__ __forceinline__ int bh_run_of(const BhTree &t, int nsims, ll p) { return nbg_sim_of(t.stree, nsims, p); }
+
+/* octant path of every tree body in its collection's cube; other bodies
+ * get the largest key */
+__global__ void __launch_bounds__(BH_BLOCK) k_bh_keys(BodyArrays A, DevCtl *ctl, SimSegs seg, BhTree t, ull *keys,
+                                                      unsigned *vals)
+{
+    if (ctl->error) return;
+    const ll n = ctl->n;
     for (ll k = (ll)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (ll)gridDim.x * blockDim.x) {
         ull key = ~0ull;
-        if (ctl->bh_count > 0 && tree_body(A, k)) {
+        if (tree_body(A, k)) {
             const double x = A.x[k], y = A.y[k], z = A.z[k];
-            double cx = cx0, cy = cy0, cz = cz0, half = half0;
+            double cx, cy, cz, half;
+            bh_root(t, nbg_sim_of(seg.off, seg.nsims, k), cx, cy, cz, half);
             key = 0;
             for (int d = 0; d < BH_LEVELS; d++) {
                 const unsigned oct = (x >= cx ? 1u : 0u) | (y >= cy ? 2u : 0u) | (z >= cz ? 4u : 0u);
@@ -165,7 +250,18 @@ __global__ void __launch_bounds__(BH_BLOCK) k_bh_keys(BodyArrays A, DevCtl *ctl,
 
 /* ---- 2. 64-bit LSD radix sort (stable) ----------------------------------- */
 
-__global__ void __launch_bounds__(BH_RS_BLOCK) k_bh_rs_hist(DevCtl *ctl, const ull *keys, int shift, ll *hist)
+/* The digit of a sort pass: 8 bits of the key (simpass < 0), or, in the
+ * two passes that group the tree bodies by collection, 8 bits of the
+ * collection index (nsims for a body outside the trees, so those go last) */
+__device__ __forceinline__ unsigned bh_digit(const SimSegs &seg, ull key, unsigned val, int shift, int simpass)
+{
+    if (simpass < 0) return (unsigned)(key >> shift) & 0xffu;
+    const unsigned d = key == ~0ull ? (unsigned)seg.nsims : (unsigned)nbg_sim_of(seg.off, seg.nsims, (ll)val);
+    return (d >> (8 * simpass)) & 0xffu;
+}
+
+__global__ void __launch_bounds__(BH_RS_BLOCK) k_bh_rs_hist(DevCtl *ctl, SimSegs seg, const ull *keys,
+                                                          const unsigned *vals, int shift, int simpass, ll *hist)
 {
     __shared__ unsigned cnt[BH_RS_BINS];
     if (ctl->error) return;
@@ -177,7 +273,7 @@ __global__ void __launch_bounds__(BH_RS_BLOCK) k_bh_rs_hist(DevCtl *ctl, const u
     __syncthreads();
     for (int q = 0; q < BH_RS_ITEMS; q++) {
         const ll k = b * BH_RS_TILE + (ll)q * BH_RS_BLOCK + threadIdx.x;
-        if (k < n) atomicAdd(&cnt[(unsigned)(keys[k] >> shift) & 0xffu], 1u);
+        if (k < n) atomicAdd(&cnt[bh_digit(seg, keys[k], vals[k], shift, simpass)], 1u);
     }
     __syncthreads();
     for (int d = threadIdx.x; d < BH_RS_BINS; d += BH_RS_BLOCK) hist[(ll)d * nb + b] = cnt[d];
@@ -226,9 +322,10 @@ __global__ void __launch_bounds__(1024) k_bh_rs_scan(DevCtl *ctl, ll *hist)
     }
 }
 
-__global__ void __launch_bounds__(BH_RS_BLOCK) k_bh_rs_scatter(DevCtl *ctl, const ull *keys_in,
+__global__ void __launch_bounds__(BH_RS_BLOCK) k_bh_rs_scatter(DevCtl *ctl, SimSegs seg, const ull *keys_in,
                                                              const unsigned *vals_in, ull *keys_out,
-                                                             unsigned *vals_out, int shift, const ll *offs)
+                                                             unsigned *vals_out, int shift, int simpass,
+                                                             const ll *offs)
 {
     __shared__ ll base[BH_RS_BINS];
     __shared__ unsigned wcnt[BH_RS_BLOCK / 32][BH_RS_BINS];
@@ -246,7 +343,8 @@ __global__ void __launch_bounds__(BH_RS_BLOCK) k_bh_rs_scatter(DevCtl *ctl, cons
         const ll k = b * BH_RS_TILE + (ll)q * BH_RS_BLOCK + threadIdx.x;
         const bool ok = k < n;
         const ull key = ok ? keys_in[k] : 0ull;
-        const unsigned d = ok ? (unsigned)(key >> shift) & 0xffu : BH_RS_BINS;
+        const unsigned val = ok ? vals_in[k] : 0u;
+        const unsigned d = ok ? bh_digit(seg, key, val, shift, simpass) : BH_RS_BINS;
         const unsigned peers = __match_any_sync(FULL_MASK, d);
         const unsigned rank = __popc(peers & lt);
         if (ok && rank == 0) wcnt[w][d] = __popc(peers);
@@ -255,7 +353,7 @@ __global__ void __launch_bounds__(BH_RS_BLOCK) k_bh_rs_scatter(DevCtl *ctl, cons
             ll pos = base[d] + rank;
             for (int v = 0; v < w; v++) pos += wcnt[v][d];
             keys_out[pos] = key;
-            vals_out[pos] = vals_in[k];
+            vals_out[pos] = val;
         }
         __syncthreads();
         for (int dd = threadIdx.x; dd < BH_RS_BINS; dd += BH_RS_BLOCK) {
@@ -277,19 +375,20 @@ __device__ __forceinline__ int common_levels(ull a, ull b)
     return (__clzll((long long)x) - 1) / 3;
 }
 
-/* first and last level of the nodes that start at sorted position p (none
- * when first > last) */
-__device__ __forceinline__ void node_levels(const ull *keys, ll p, ll M, int &d0, int &d1)
+/* first and last level of the nodes that start at sorted position p of its
+ * collection's run [lo, hi) (none when first > last) */
+__device__ __forceinline__ void node_levels(const ull *keys, ll p, ll lo, ll hi, int &d0, int &d1)
 {
-    const int cp = p == 0 ? -1 : common_levels(keys[p - 1], keys[p]);
-    const int cn = p == M - 1 ? -1 : common_levels(keys[p], keys[p + 1]);
-    d0 = p == 0 ? 0 : cp + 1;
+    const int cp = p == lo ? -1 : common_levels(keys[p - 1], keys[p]);
+    const int cn = p == hi - 1 ? -1 : common_levels(keys[p], keys[p + 1]);
+    d0 = p == lo ? 0 : cp + 1;
     const int e = cn + 1 > d0 ? cn + 1 : d0;
     d1 = e < BH_LEVELS ? e : BH_LEVELS;
 }
 
 /* per-block sums of the node counts of sorted positions [0, M) */
-__global__ void __launch_bounds__(BH_SCAN_BLOCK) k_bh_count(DevCtl *ctl, const ull *keys, ll *base, ll *blk)
+__global__ void __launch_bounds__(BH_SCAN_BLOCK) k_bh_count(DevCtl *ctl, SimSegs seg, BhTree t, const ull *keys,
+                                                            ll *base, ll *blk)
 {
     __shared__ ll red[BH_SCAN_BLOCK / 32];
     if (ctl->error) return;
@@ -301,8 +400,9 @@ __global__ void __launch_bounds__(BH_SCAN_BLOCK) k_bh_count(DevCtl *ctl, const u
         const ll p = b0 + (ll)q * BH_SCAN_BLOCK + threadIdx.x;
         ll c = 0;
         if (p < M) {
+            const int r = bh_run_of(t, seg.nsims, p);
             int d0, d1;
-            node_levels(keys, p, M, d0, d1);
+            node_levels(keys, p, t.stree[r], t.stree[r + 1], d0, d1);
             c = d1 >= d0 ? d1 - d0 + 1 : 0;
         }
         if (p <= M) base[p] = c; /* base[M] = 0: the scan leaves the total there */
@@ -396,21 +496,31 @@ __global__ void __launch_bounds__(BH_SCAN_BLOCK) k_bh_count_scan(DevCtl *ctl, ll
     }
 }
 
+/* each collection's root node: the first node of its run (nodes of an
+ * empty collection: the empty range at the next one's root) */
+__global__ void __launch_bounds__(1024) k_bh_roots(DevCtl *ctl, SimSegs seg, BhTree t, const ll *base)
+{
+    if (ctl->error) return;
+    for (int s = threadIdx.x; s <= seg.nsims; s += blockDim.x) t.sroot[s] = base[t.stree[s]];
+}
+
 /* one thread per sorted position: every node that starts there */
-__global__ void __launch_bounds__(BH_BLOCK) k_bh_nodes(DevCtl *ctl, const ull *keys, const ll *base, BhTree t)
+__global__ void __launch_bounds__(BH_BLOCK) k_bh_nodes(DevCtl *ctl, SimSegs seg, const ull *keys, const ll *base,
+                                                       BhTree t)
 {
     if (ctl->error) return;
     const ll M = ctl->bh_count;
     const ll total = ctl->bh_nodes;
-    double cx0, cy0, cz0, half0;
-    bh_root(ctl, cx0, cy0, cz0, half0);
     for (ll p = (ll)blockIdx.x * blockDim.x + threadIdx.x; p < M; p += (ll)gridDim.x * blockDim.x) {
+        const int r = bh_run_of(t, seg.nsims, p);
+        const ll lo = t.stree[r], hi = t.stree[r + 1];
         int d0, d1;
-        node_levels(keys, p, M, d0, d1);
+        node_levels(keys, p, lo, hi, d0, d1);
         if (d1 < d0) continue;
         const ull key = keys[p];
         /* the cube of the level-d0 node: descend d0 levels along the key */
-        double cx = cx0, cy = cy0, cz = cz0, half = half0;
+        double cx, cy, cz, half;
+        bh_root(t, r, cx, cy, cz, half);
         for (int d = 0; d < d0; d++) {
             const unsigned oct = (unsigned)(key >> (3 * (BH_LEVELS - 1 - d))) & 7u;
             const double q = half / 2;
@@ -421,20 +531,21 @@ __global__ void __launch_bounds__(BH_BLOCK) k_bh_nodes(DevCtl *ctl, const ull *k
         }
         for (int d = d0; d <= d1; d++) {
             const ll id = base[p] + (d - d0);
-            /* end of the body range: the first key past this node's prefix */
-            ll end = M;
+            /* end of the body range: the first key of the run past this
+             * node's prefix */
+            ll end = hi;
             if (d > 0) {
                 const int sh = 3 * (BH_LEVELS - d);
                 const ull pre = key >> sh;
-                ll lo = p + 1, hi = M;
-                while (lo < hi) {
-                    const ll mid = (lo + hi) >> 1;
+                ll a = p + 1, b = hi;
+                while (a < b) {
+                    const ll mid = (a + b) >> 1;
                     if ((keys[mid] >> sh) <= pre)
-                        lo = mid + 1;
+                        a = mid + 1;
                     else
-                        hi = mid;
+                        b = mid;
                 }
-                end = lo;
+                end = a;
             }
             t.start[id] = (int)p;
             t.end[id] = (int)end;
@@ -524,31 +635,45 @@ __device__ __forceinline__ void bh_term(double gm_i, double M, double dx, double
  * queue until it is empty instead of a fixed share each: no SM idles while
  * another still holds a long run of groups.  A group is always the same 32
  * bodies, so the results do not depend on which warp takes it. */
-__device__ __forceinline__ int bh_next_group(DevCtl *ctl, int M)
+__device__ __forceinline__ int bh_next_group(DevCtl *ctl, ll groups)
 {
     unsigned g = 0;
     if ((threadIdx.x & 31) == 0) g = atomicAdd(&ctl->bh_next, 1u);
     g = __shfl_sync(FULL_MASK, g, 0);
-    return g < (unsigned)(M + 31) / 32u ? (int)g : -1;
+    return (ll)g < groups ? (int)g : -1;
+}
+
+/* Group g holds sorted positions [p0, p1) of collection s: the groups of a
+ * collection start at its first sorted position, 32 bodies each, so a
+ * collection's groups are those it would have alone. */
+__device__ __forceinline__ void bh_group(const BhTree &t, int nsims, int g, int &s, ll &p0, ll &p1)
+{
+    s = nbg_sim_of(t.sgrp, nsims, g);
+    p0 = t.stree[s] + 32ll * (g - t.sgrp[s]);
+    p1 = p0 + 32 < t.stree[s + 1] ? p0 + 32 : t.stree[s + 1];
 }
 
 /* one thread per tree body (sorted order, so a warp walks nearby paths) */
-__global__ void __launch_bounds__(BH_BLOCK) k_bh_force(BodyArrays A, DevCtl *ctl, const unsigned *vals, BhTree t)
+__global__ void __launch_bounds__(BH_BLOCK) k_bh_force(BodyArrays A, DevCtl *ctl, SimSegs seg, const unsigned *vals,
+                                                       BhTree t)
 {
     if (ctl->error) return;
-    const ll M = ctl->bh_count;
-    const int total = (int)ctl->bh_nodes;
+    const ll groups = t.sgrp[seg.nsims];
     unsigned long long terms = 0;
     /* every lane runs the same number of rounds, for the warp reduction */
-    for (int grp; (grp = bh_next_group(ctl, (int)M)) >= 0;) {
-        const int p = grp * 32 + (threadIdx.x & 31);
-        if (p >= M) continue;
+    for (int grp; (grp = bh_next_group(ctl, groups)) >= 0;) {
+        int r;
+        ll p0, p1;
+        bh_group(t, seg.nsims, grp, r, p0, p1);
+        const ll p = p0 + (threadIdx.x & 31);
+        if (p >= p1) continue;
+        const int total = (int)t.sroot[r + 1]; /* the end of the collection's nodes */
         const unsigned k = vals[p];
         if (A.flags[k] & NBG_F_IS_SUN) continue; /* k_bh_sun */
         const double x = A.x[k], y = A.y[k], z = A.z[k];
         const double gm = NBG_G * A.m[k];
         double fx = 0, fy = 0, fz = 0;
-        int id = 0;
+        int id = (int)t.sroot[r];
         while (id < total) {
             const double Mn = t.mass[id];
             if (Mn == 0) {
@@ -609,14 +734,15 @@ __global__ void __launch_bounds__(BH_BLOCK) k_bh_force(BodyArrays A, DevCtl *ctl
  * lane sums its terms in FP32 and, every 64 nodes, the warp folds them into
  * (hi, lo) FP32 pairs: the GB300 FP64 pipe is 1/64 of the FP32 rate, and a
  * few FP64 folds per node kept it saturated. */
-__global__ void __launch_bounds__(BH_BLOCK) k_bh_prep_mixed(DevCtl *ctl, BhTree t)
+__global__ void __launch_bounds__(BH_BLOCK) k_bh_prep_mixed(DevCtl *ctl, SimSegs seg, BhTree t)
 {
     if (ctl->error) return;
     const ll total = ctl->bh_nodes;
     if (total <= 0) return;
-    const double mroot = t.mass[0];
-    const double inv_root = mroot != 0 ? 1.0 / mroot : 0.0;
     for (ll id = (ll)blockIdx.x * blockDim.x + threadIdx.x; id < total; id += (ll)gridDim.x * blockDim.x) {
+        /* masses relative to the root of the node's own tree */
+        const double mroot = t.mass[t.sroot[nbg_sim_of(t.sroot, seg.nsims, id)]];
+        const double inv_root = mroot != 0 ? 1.0 / mroot : 0.0;
         const double M = t.mass[id];
         float4 a = make_float4(0.f, 0.f, 0.f, 0.f), b = make_float4(0.f, 0.f, 0.f, 0.f);
         if (M != 0) {
@@ -680,20 +806,23 @@ __device__ __noinline__ int bucket_terms(const BodyArrays &A, const unsigned *va
 }
 
 template <int MINB>
-__global__ void __launch_bounds__(BH_BLOCK, MINB) k_bh_force_mixed(BodyArrays A, DevCtl *ctl, const unsigned *vals,
-                                                                BhTree t)
+__global__ void __launch_bounds__(BH_BLOCK, MINB) k_bh_force_mixed(BodyArrays A, DevCtl *ctl, SimSegs seg,
+                                                                const unsigned *vals, BhTree t)
 {
     if (ctl->error) return;
-    const ll M = ctl->bh_count;
-    const int total = (int)ctl->bh_nodes;
-    if (total <= 0) return;
-    const double mroot = t.mass[0];
+    if (ctl->bh_nodes <= 0) return;
+    const ll groups = t.sgrp[seg.nsims];
     const float soft2 = (float)(BH_SOFTENING * BH_SOFTENING);
     unsigned long long terms = 0;
-    for (int grp; (grp = bh_next_group(ctl, (int)M)) >= 0;) {
-        const int p = grp * 32 + (threadIdx.x & 31);
+    for (int grp; (grp = bh_next_group(ctl, groups)) >= 0;) {
+        int r;
+        ll p0, p1;
+        bh_group(t, seg.nsims, grp, r, p0, p1);
+        const ll p = p0 + (threadIdx.x & 31);
+        const int root = (int)t.sroot[r], total = (int)t.sroot[r + 1];
+        const double mroot = t.mass[root];
         unsigned k = 0;
-        bool have = p < M;
+        bool have = p < p1;
         if (have) {
             k = vals[p];
             have = !(A.flags[k] & NBG_F_IS_SUN); /* k_bh_sun */
@@ -720,9 +849,9 @@ __global__ void __launch_bounds__(BH_BLOCK, MINB) k_bh_force_mixed(BodyArrays A,
          * node accepted an ancestor, whose subtree ends at or after this
          * node's.  So the next address is known right after the vote, and its
          * loads are in flight while the lanes add their terms. */
-        int id = 0;
-        float4 a = t.fa[0], b = t.fb[0];
-        int4 c = t.fc[0];
+        int id = root;
+        float4 a = t.fa[root], b = t.fb[root];
+        int4 c = t.fc[root];
         while (id < total) {
             const int sk = c.x;
             const unsigned fl = (unsigned)c.w;
@@ -779,7 +908,7 @@ __global__ void __launch_bounds__(BH_BLOCK, MINB) k_bh_force_mixed(BodyArrays A,
 /* a sun sums every tree body directly (directForce, octree.go:310-325): each
  * CTA scans a run of bodies for suns, and sums every sun it finds with all
  * its threads, in a fixed-order block reduction */
-__global__ void __launch_bounds__(BH_BLOCK) k_bh_sun(BodyArrays A, DevCtl *ctl)
+__global__ void __launch_bounds__(BH_BLOCK) k_bh_sun(BodyArrays A, DevCtl *ctl, SimSegs seg)
 {
     __shared__ double red[3][BH_BLOCK];
     __shared__ unsigned s_mask[BH_BLOCK / 32];
@@ -802,7 +931,11 @@ __global__ void __launch_bounds__(BH_BLOCK) k_bh_sun(BodyArrays A, DevCtl *ctl)
                 const double x = A.x[k], y = A.y[k], z = A.z[k];
                 const double gm = NBG_G * A.m[k];
                 double fx = 0, fy = 0, fz = 0;
-                for (ll j = threadIdx.x; j < n; j += blockDim.x) {
+                /* the bodies of the sun's own collection, each thread the
+                 * same share of them as if the collection were alone */
+                const int sim = nbg_sim_of(seg.off, seg.nsims, k);
+                const ll j0 = seg.off[sim], j1 = seg.off[sim + 1];
+                for (ll j = j0 + threadIdx.x; j < j1; j += blockDim.x) {
                     if (j == k || (A.flags[j] & NBG_LIVE_MASK) != NBG_F_EXISTS) continue;
                     bh_term(gm, A.m[j], A.x[j] - x, A.y[j] - y, A.z[j] - z, fx, fy, fz);
                 }
@@ -844,19 +977,20 @@ __device__ __forceinline__ void bh_test_pair(const BodyArrays &A, DevCtl *ctl, u
     }
 }
 
-__global__ void __launch_bounds__(BH_BLOCK) k_bh_collide(BodyArrays A, DevCtl *ctl, const unsigned *vals, BhTree t,
-                                                         ull *ev_keys, ll ev_cap)
+__global__ void __launch_bounds__(BH_BLOCK) k_bh_collide(BodyArrays A, DevCtl *ctl, SimSegs seg,
+                                                         const unsigned *vals, BhTree t, ull *ev_keys, ll ev_cap)
 {
     if (ctl->error) return;
     const ll n = ctl->n;
     const ll M = ctl->bh_count;
-    const int total = (int)ctl->bh_nodes;
     const double rmax = ord_dbl(ctl->bh_rmax);
-    double cx0, cy0, cz0, half0;
-    bh_root(ctl, cx0, cy0, cz0, half0);
-    /* every coordinate, centre and half in the tree is at most this large */
-    const float span = (float)((fabs(cx0) + fabs(cy0) + fabs(cz0) + 3 * half0) * (1.0 + 0x1p-20));
     for (ll p = (ll)blockIdx.x * blockDim.x + threadIdx.x; p < M; p += (ll)gridDim.x * blockDim.x) {
+        const int r = bh_run_of(t, seg.nsims, p);
+        double cx0, cy0, cz0, half0;
+        bh_root(t, r, cx0, cy0, cz0, half0);
+        /* every coordinate, centre and half in the tree is at most this large */
+        const float span = (float)((fabs(cx0) + fabs(cy0) + fabs(cz0) + 3 * half0) * (1.0 + 0x1p-20));
+        const int total = (int)t.sroot[r + 1];
         const unsigned i = vals[p];
         const unsigned fi = A.flags[i];
         if (fi & NBG_F_COLLIDED) continue; /* Collided's guard (always clear here) */
@@ -872,7 +1006,7 @@ __global__ void __launch_bounds__(BH_BLOCK) k_bh_collide(BodyArrays A, DevCtl *c
         const float R = (float)(Rd * (1.0 + 0x1p-20)) + span * 0x1p-18f;
         const float R2 = R * R * (1.0f + 0x1p-18f);
         const float xf = (float)xi, yf = (float)yi, zf = (float)zi;
-        int id = 0;
+        int id = (int)t.sroot[r];
         while (id < total) {
             const float4 q = t.fd[id];
             const float ax = fmaxf(fabsf(xf - q.x) - q.w, 0.f);
@@ -892,8 +1026,19 @@ __global__ void __launch_bounds__(BH_BLOCK) k_bh_collide(BodyArrays A, DevCtl *c
                 id = id + 1;
             }
         }
-        /* bodies outside the tree */
-        for (ll q = M; q < n; q++) bh_test_pair(A, ctl, ev_keys, ev_cap, i, xi, yi, zi, ri, bi, vals[q]);
+        /* bodies of the collection outside its tree: they sit past every
+         * tree body in ascending body order, so the collection's are one run */
+        const ll lo_b = seg.off[r], hi_b = seg.off[r + 1];
+        ll a = M, b = n;
+        while (a < b) {
+            const ll mid = (a + b) >> 1;
+            if ((ll)vals[mid] < lo_b)
+                a = mid + 1;
+            else
+                b = mid;
+        }
+        for (ll q = a; q < n && (ll)vals[q] < hi_b; q++)
+            bh_test_pair(A, ctl, ev_keys, ev_cap, i, xi, yi, zi, ri, bi, vals[q]);
     }
 }
 
@@ -934,6 +1079,11 @@ int nbg_bh_alloc(BhTree &t, ll cap, ll node_cap)
     ALLOC(t.fb, node_cap);
     ALLOC(t.fc, node_cap);
     ALLOC(t.fd, node_cap);
+    ALLOC(t.sbox, 6 * (ll)NBG_MAX_SIMS);
+    ALLOC(t.scount, NBG_MAX_SIMS + 1);
+    ALLOC(t.stree, NBG_MAX_SIMS + 1);
+    ALLOC(t.sroot, NBG_MAX_SIMS + 1);
+    ALLOC(t.sgrp, NBG_MAX_SIMS + 1);
 #undef ALLOC
     if (!ok) {
         nbg_bh_free(t);
@@ -947,7 +1097,8 @@ void nbg_bh_free(BhTree &t)
 {
     void *ps[] = {t.key[0], t.key[1], t.val[0], t.val[1], t.hist, t.base, t.blk, t.mass, t.mx, t.my,
                   t.mz, t.cmx, t.cmy, t.cmz, t.cx, t.cy, t.cz, t.half, t.skip, t.start,
-                  t.end, t.first, t.level, t.flags, t.fa, t.fb, t.fc, t.fd};
+                  t.end, t.first, t.level, t.flags, t.fa, t.fb, t.fc, t.fd,
+                  t.sbox, t.scount, t.stree, t.sroot, t.sgrp};
     for (void *p : ps) cudaFree(p);
     memset(&t, 0, sizeof t);
 }
@@ -958,46 +1109,62 @@ void nbg_bh_free(BhTree &t)
 void nbg_launch_bh(const CycleBufs &cb, DevCtl *ctl, cudaStream_t st, bool mixed)
 {
     const BhTree &t = cb.t;
+    const SimSegs &seg = cb.seg;
     const ll cap = cb.cap;
     const ll gmost = (ll)(cb.sms > 0 ? cb.sms : 1) * 8;
     int g = (int)((cap + BH_BLOCK - 1) / BH_BLOCK < gmost ? (cap + BH_BLOCK - 1) / BH_BLOCK : gmost);
     if (g < 1) g = 1;
-    k_bh_bounds<<<g, BH_BLOCK, 0, st>>>(cb.a, ctl);
-    k_bh_keys<<<g, BH_BLOCK, 0, st>>>(cb.a, ctl, t.key[0], t.val[0]);
+    k_bh_reset<<<1, 1024, 0, st>>>(ctl, seg, t);
+    k_bh_bounds<<<g, BH_BLOCK, 0, st>>>(cb.a, ctl, seg, t);
+    k_bh_segs<<<1, 32, 0, st>>>(ctl, seg, t);
+    k_bh_keys<<<g, BH_BLOCK, 0, st>>>(cb.a, ctl, seg, t, t.key[0], t.val[0]);
     const int nb = (int)((cap + BH_RS_TILE - 1) / BH_RS_TILE);
+    /* eight passes of the key, then (several collections) two of the
+     * collection index: an even count, so the sorted keys and values end in
+     * buffer 0 */
+    const int passes = seg.nsims > 1 ? 10 : 8;
     int in = 0;
-    for (int pass = 0; pass < 8; pass++) {
-        k_bh_rs_hist<<<nb, BH_RS_BLOCK, 0, st>>>(ctl, t.key[in], 8 * pass, t.hist);
+    for (int pass = 0; pass < passes; pass++) {
+        const int shift = pass < 8 ? 8 * pass : 0, simpass = pass < 8 ? -1 : pass - 8;
+        k_bh_rs_hist<<<nb, BH_RS_BLOCK, 0, st>>>(ctl, seg, t.key[in], t.val[in], shift, simpass, t.hist);
         k_bh_rs_scan<<<1, 1024, 0, st>>>(ctl, t.hist);
-        k_bh_rs_scatter<<<nb, BH_RS_BLOCK, 0, st>>>(ctl, t.key[in], t.val[in], t.key[in ^ 1], t.val[in ^ 1],
-                                                   8 * pass, t.hist);
+        k_bh_rs_scatter<<<nb, BH_RS_BLOCK, 0, st>>>(ctl, seg, t.key[in], t.val[in], t.key[in ^ 1], t.val[in ^ 1],
+                                                   shift, simpass, t.hist);
         in ^= 1;
     }
-    /* eight passes: sorted keys and values are back in buffer 0 */
     const int sb = (int)(cap / BH_SCAN_TILE + 1);
-    k_bh_count<<<sb, BH_SCAN_BLOCK, 0, st>>>(ctl, t.key[0], t.base, t.blk);
+    k_bh_count<<<sb, BH_SCAN_BLOCK, 0, st>>>(ctl, seg, t, t.key[0], t.base, t.blk);
     k_bh_count_top<<<1, 1024, 0, st>>>(ctl, t.blk, t.node_cap);
     k_bh_count_scan<<<sb, BH_SCAN_BLOCK, 0, st>>>(ctl, t.base, t.blk);
-    k_bh_nodes<<<g, BH_BLOCK, 0, st>>>(ctl, t.key[0], t.base, t);
+    k_bh_roots<<<1, 1024, 0, st>>>(ctl, seg, t, t.base);
+    k_bh_nodes<<<g, BH_BLOCK, 0, st>>>(ctl, seg, t.key[0], t.base, t);
     int ng = (int)((t.node_cap + BH_BLOCK - 1) / BH_BLOCK < gmost ? (t.node_cap + BH_BLOCK - 1) / BH_BLOCK : gmost);
     if (ng < 1) ng = 1;
     for (int level = BH_LEVELS; level >= 0; level--)
         k_bh_mass<<<ng, BH_BLOCK, 0, st>>>(cb.a, ctl, t.val[0], t, level);
     if (mixed) {
-        k_bh_prep_mixed<<<ng, BH_BLOCK, 0, st>>>(ctl, t);
+        k_bh_prep_mixed<<<ng, BH_BLOCK, 0, st>>>(ctl, seg, t);
         /* CTAs per SM the walk's registers are capped for: the walk is bound
          * by the latency of its node loads, so occupancy is what counts */
         /* one wave of resident CTAs; their warps share the group queue */
         const int minb = cb.bh_shape == 1 ? 4 : cb.bh_shape == 2 ? 5 : 3;
         const int gw = g < cb.sms * minb ? g : cb.sms * minb;
         switch (cb.bh_shape) {
-        case 1: k_bh_force_mixed<4><<<gw, BH_BLOCK, 0, st>>>(cb.a, ctl, t.val[0], t); break;
-        case 2: k_bh_force_mixed<5><<<gw, BH_BLOCK, 0, st>>>(cb.a, ctl, t.val[0], t); break;
-        default: k_bh_force_mixed<3><<<gw, BH_BLOCK, 0, st>>>(cb.a, ctl, t.val[0], t); break;
+        case 1: k_bh_force_mixed<4><<<gw, BH_BLOCK, 0, st>>>(cb.a, ctl, seg, t.val[0], t); break;
+        case 2: k_bh_force_mixed<5><<<gw, BH_BLOCK, 0, st>>>(cb.a, ctl, seg, t.val[0], t); break;
+        default: k_bh_force_mixed<3><<<gw, BH_BLOCK, 0, st>>>(cb.a, ctl, seg, t.val[0], t); break;
         }
     } else {
-        k_bh_force<<<g, BH_BLOCK, 0, st>>>(cb.a, ctl, t.val[0], t);
+        k_bh_force<<<g, BH_BLOCK, 0, st>>>(cb.a, ctl, seg, t.val[0], t);
     }
-    k_bh_sun<<<64, BH_BLOCK, 0, st>>>(cb.a, ctl);
-    k_bh_collide<<<g, BH_BLOCK, 0, st>>>(cb.a, ctl, t.val[0], t, cb.ev_keys, cb.ev_cap);
+    k_bh_sun<<<64, BH_BLOCK, 0, st>>>(cb.a, ctl, seg);
+    k_bh_collide<<<g, BH_BLOCK, 0, st>>>(cb.a, ctl, seg, t.val[0], t, cb.ev_keys, cb.ev_cap);
+}
+
+int nbg_bh_launches(const CycleBufs &cb, bool mixed)
+{
+    const int passes = cb.seg.nsims > 1 ? 10 : 8;
+    /* reset, bounds, segs, keys; the sort; count, top, scan, roots, nodes;
+     * masses; (prep,) walk; suns; collisions */
+    return 4 + 3 * passes + 5 + (BH_LEVELS + 1) + (mixed ? 2 : 1) + 2;
 }

@@ -1441,9 +1441,9 @@ static void launch_cycle(nbg_ctx *ctx, int precision, long ev_base)
      * kernel; mixed adds reduce, the sort decision and 21 sort launches
      * (which return at once in cycles that keep the order), pack, tile
      * origins, i-body set-up, the output and 4 that carry the order through
-     * compaction; Barnes-Hut replaces the pair kernel with 55 (k_bh.cu) */
+     * compaction; Barnes-Hut replaces the pair kernel (nbg_bh_launches) */
     ctx->launches_per_cycle = (cb.ev_radix ? nbg_event_radix_launches(cb) : 0) +
-                              (cb.bh ? 13 + 55 + (precision == NBG_PRECISION_MIXED ? 1 : 0)
+                              (cb.bh ? 13 + nbg_bh_launches(cb, precision == NBG_PRECISION_MIXED)
                                      : precision == NBG_PRECISION_MIXED ? 45 : 13 + nbg_pair_fp64_launches(cb)) +
                               (cb.ring_head ? 1 : 0);
 }
@@ -1507,7 +1507,6 @@ struct LaunchWindow {
 int nbg_step(nbg_ctx *ctx, double dt, double R, int nsteps, nbg_step_info *info)
 {
     if (!ctx || nsteps < 0) return fail(ctx, NBG_E_ARG, "bad arguments");
-    if (ctx->cb.bh && ctx->cb.seg.nsims != 1) return fail(ctx, NBG_E_STATE, "Barnes-Hut needs a single collection");
     CK(cudaSetDevice(ctx->device));
     /* dt, R and the per-call accumulators */
     {
@@ -1661,7 +1660,6 @@ int nbg_force_pass(nbg_ctx *ctx)
 {
     if (!ctx) return NBG_E_ARG;
     CK(cudaSetDevice(ctx->device));
-    if (ctx->cb.bh && ctx->cb.seg.nsims != 1) return fail(ctx, NBG_E_STATE, "Barnes-Hut needs a single collection");
     {
         int rc = ensure_p64(ctx);
         if (rc != NBG_OK) return rc;

@@ -189,6 +189,14 @@ struct BhTree {
     float4 *fd;         /* collision query: the node's cube (centre xyz, half) in FP32 */
     int *skip, *start, *end, *first;
     unsigned char *level, *flags;
+    /* one tree per collection, all in one depth-first node array: per
+     * collection s its bounding box (sbox[6 s ..]: lo xyz, hi xyz as
+     * order-preserving integers), tree bodies (scount), first sorted
+     * position (stree, [nsims + 1]), root node (sroot, [nsims + 1]: the nodes
+     * of s are [sroot[s], sroot[s + 1])) and first 32-body walk group (sgrp,
+     * [nsims + 1]) */
+    ull *sbox;
+    ll *scount, *stree, *sroot, *sgrp;
     ll node_cap;
 };
 
@@ -367,6 +375,7 @@ __device__ static inline void nbg_emit_event(DevCtl *ctl, ull *keys, ll cap, ll 
 int nbg_bh_alloc(BhTree &t, ll cap, ll node_cap);
 void nbg_bh_free(BhTree &t);
 void nbg_launch_bh(const CycleBufs &cb, DevCtl *ctl, cudaStream_t st, bool mixed);
+int nbg_bh_launches(const CycleBufs &cb, bool mixed); /* kernels nbg_launch_bh launches */
 
 /* k_cycle.cu (compiled with --fmad=false) */
 void nbg_launch_begin(const CycleBufs &cb, DevCtl *ctl, cudaStream_t st);

@@ -11,10 +11,10 @@ import pytest
 
 from nbodygo_gb300 import _abi as A
 from nbodygo_gb300 import workloads as W
-from nbodygo_gb300.api import NbgError, Simulation
+from nbodygo_gb300.api import Simulation
 from oracle.oracle import OracleSim
 
-from helpers import assert_events_identical
+from helpers import assert_events_identical, assert_states_identical
 from test_gpu_plain_parity import dense_cluster
 
 pytestmark = pytest.mark.gpu
@@ -120,13 +120,57 @@ def test_bh_step_with_a_graph_equals_single_cycles():
         assert np.array_equal(a[f].view(np.uint64), c[f].view(np.uint64)), f
 
 
-def test_bh_needs_a_single_collection():
-    sim = Simulation("fp64")
-    sim.set_option(A.OPT_BARNES_HUT, 1)
-    sim.set_collections([W.plummer(300, seed=1), W.plummer(200, seed=2)])
-    with pytest.raises(NbgError) as e:
-        sim.step(0.01, 1.0, 1)
-    assert e.value.code == A.NBG_E_STATE
+def batched_bh_sets():
+    return [
+        dense_cluster(300, seed=51),                               # collisions of every behaviour
+        {k: np.asarray(v)[:0] for k, v in W.plummer(8, seed=1).items()},  # an empty collection
+        with_sun(W.disk(n=400, seed=52)),                          # a sun: summed directly
+        W.plummer(n=1500, seed=53, radius_range=(0.3, 1.5)),
+        dense_cluster(1, seed=54),                                 # a single body
+        W.uniform_ball(n=700, seed=55, R=60.0, radius=0.8, behavior=A.ELASTIC),
+    ]
+
+
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+def test_batched_bh_equals_each_collection_alone(prec):
+    """One tree per collection: every collection of a batched Barnes-Hut
+    context gets the tree, walk groups, sun sums and collision query it gets
+    alone, so its forces and its whole cycles are bit-identical to a context
+    holding that collection only (fragment ids aside: a batch draws them from
+    one counter)."""
+    from test_gpu_batch import split_state
+
+    sets = batched_bh_sets()
+    batch = Simulation(prec, seed=8)
+    batch.set_option(A.OPT_BARNES_HUT, 1)
+    batch.set_collections(sets)
+    alone = []
+    for b in sets:
+        s = Simulation(prec, seed=8)
+        s.set_option(A.OPT_BARNES_HUT, 1)
+        s.set_bodies(b)
+        alone.append(s)
+    f = np.array(batch.force_pass())
+    o = 0
+    for q, (s, b) in enumerate(zip(alone, sets)):
+        k = len(b["x"])
+        if k:
+            g = np.array(s.force_pass())
+            assert np.array_equal(f[:, o:o + k].view(np.uint64), g.view(np.uint64)), f"collection {q}"
+        o += k
+    for c in range(6):
+        batch.step(0.05, 0.9, 1)
+        for s in alone:
+            s.step(0.05, 0.9, 1)
+        counts = batch.sim_counts()
+        assert list(counts) == [s.count() for s in alone], f"cycle {c}"
+        for q, (s, got) in enumerate(zip(alone, split_state(batch.state(), counts))):
+            if counts[q]:
+                assert_states_identical(got, s.state(), fields=[k for k in got if k != "id"],
+                                        where=f"{prec} cycle {c} collection {q}")
+    batch.close()
+    for s in alone:
+        s.close()
 
 
 @pytest.mark.parametrize("name,bodies", [
