@@ -89,7 +89,10 @@ FIELD_DTYPES = {f: dt for f, _, dt, _ in SOA_FIELDS}
 
 
 class NbgSoa(C.Structure):
-    _fields_ = [(f, t) for f, t, _, _ in SOA_FIELDS]
+    # every field points into a host array (typed in nbgpu.h); void pointers
+    # here take the arrays' addresses as integers, with no ctypes cast per
+    # field on every call
+    _fields_ = [(f, C.c_void_p) for f, _, _, _ in SOA_FIELDS]
 
 
 class NbgStepInfo(C.Structure):
@@ -136,13 +139,14 @@ def soa_from_arrays(arrays):
     """
     soa = NbgSoa()
     keep = []
-    for f, t, dt, _ in SOA_FIELDS:
+    for f, _, dt, _ in SOA_FIELDS:
         a = arrays.get(f)
         if a is None:
             continue
-        a = np.ascontiguousarray(a, dtype=dt)
+        if not (isinstance(a, np.ndarray) and a.dtype == dt and a.flags.c_contiguous):
+            a = np.ascontiguousarray(a, dtype=dt)
         keep.append(a)
-        setattr(soa, f, a.ctypes.data_as(t))
+        setattr(soa, f, a.__array_interface__["data"][0])
     return soa, keep
 
 

@@ -650,27 +650,35 @@ static int upload_soa(nbg_ctx *ctx, BodyArrays &D, ll off, const nbg_soa *h, ll 
     if (rc0 != NBG_OK) return rc0;
     CK(cudaStreamSynchronize(ctx->st)); /* the staging's last copy is done */
     unsigned *flags = ctx->flags_h;
-    /* every behaviour is checked before anything is copied; then the flag
-     * words are composed in branch-free loops the compiler vectorises */
+    /* the flag words are composed into the host staging in branch-free
+     * loops the compiler vectorises, with the behaviours' range taken in the
+     * same pass; an out-of-range behaviour fails the call before anything
+     * is copied */
     const int32_t *coll = h->collision;
     const uint32_t *hf = h->flags;
+    const unsigned dflt_b = (unsigned)NBG_ELASTIC << NBG_BEHAVIOR_SHIFT;
     if (coll) {
         int32_t lo = coll[0], hi = coll[0];
-        for (ll k = 1; k < n; k++) {
-            lo = coll[k] < lo ? coll[k] : lo;
-            hi = coll[k] > hi ? coll[k] : hi;
-        }
+        if (hf)
+            for (ll k = 0; k < n; k++) {
+                const int32_t c = coll[k];
+                lo = c < lo ? c : lo;
+                hi = c > hi ? c : hi;
+                flags[k] = (hf[k] & 0xffu) | ((unsigned)c << NBG_BEHAVIOR_SHIFT);
+            }
+        else
+            for (ll k = 0; k < n; k++) {
+                const int32_t c = coll[k];
+                lo = c < lo ? c : lo;
+                hi = c > hi ? c : hi;
+                flags[k] = NBG_F_EXISTS | ((unsigned)c << NBG_BEHAVIOR_SHIFT);
+            }
         if (lo < NBG_NONE || hi > NBG_FRAGMENT) return fail(ctx, NBG_E_ARG, "collision behaviour out of range");
-    }
-    const unsigned dflt_b = (unsigned)NBG_ELASTIC << NBG_BEHAVIOR_SHIFT;
-    if (coll && hf)
-        for (ll k = 0; k < n; k++) flags[k] = (hf[k] & 0xffu) | ((unsigned)coll[k] << NBG_BEHAVIOR_SHIFT);
-    else if (coll)
-        for (ll k = 0; k < n; k++) flags[k] = NBG_F_EXISTS | ((unsigned)coll[k] << NBG_BEHAVIOR_SHIFT);
-    else if (hf)
+    } else if (hf) {
         for (ll k = 0; k < n; k++) flags[k] = (hf[k] & 0xffu) | dflt_b;
-    else
+    } else {
         for (ll k = 0; k < n; k++) flags[k] = NBG_F_EXISTS | dflt_b;
+    }
     int rc;
     CopyBatch cb;
     cb.n = 0;
