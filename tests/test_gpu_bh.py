@@ -201,3 +201,18 @@ def test_mixed_bh_first_cycle_events_are_exact():
     sim.step(0.05, 0.9, 1)
     ora.step(0.05, 0.9, 1)
     assert_events_identical(sim.events(), ora.events(), "cycle 0")
+
+
+def test_every_mixed_walk_shape_gives_the_same_forces():
+    """The walk shapes differ in the CTAs per SM their registers are capped
+    for, not in arithmetic: each group's terms, order and folds are fixed."""
+    b = W.plummer(n=5000, seed=61, radius_range=(0.3, 1.5))
+    out = []
+    for shape in range(3):
+        with Simulation("mixed") as s:
+            s.set_option(A.OPT_BARNES_HUT, 1)
+            s.set_option(A.OPT_BH_SHAPE, shape)
+            s.set_bodies(b)
+            out.append(np.array(s.force_pass()))
+    for shape, f in enumerate(out[1:], 1):
+        assert np.array_equal(f.view(np.uint64), out[0].view(np.uint64)), f"shape {shape}"
