@@ -87,6 +87,9 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="plummer_disk", choices=sorted(WORKLOADS))
     ap.add_argument("--n-each", type=int, default=65536, help="plummer_disk: bodies per component")
+    ap.add_argument("--bodies", type=int, default=None,
+                    help="uniform, uniform_bh_mixed: bodies in the ball (default 1,048,576), e.g. a smaller case "
+                         "for a profiler")
     ap.add_argument("--no-plain", action="store_true", help="skip the FP64 comparison run")
     ap.add_argument("--with-plain", action="store_true",
                     help="run the FP64 comparison on the uniform ball too (one FP64 force pass, ~2 min at 1M bodies)")
@@ -215,9 +218,12 @@ class Clocks:
                 "samples": len(sm)}
 
 
-def traffic_from_profiles(workload):
-    """DRAM bytes per launch of the pair kernel from the committed ncu summary."""
-    p = os.path.join(ROOT, "profiles", f"pair_mixed_{workload}.md")
+def traffic_from_profiles(workload, kernel="k_pair_mixed"):
+    """DRAM bytes per launch of the pair kernel from the committed ncu summary
+    (pair_mixed_<workload>.md, or pair_sym_<workload>.md for the symmetric
+    kernel)."""
+    stem = "pair_sym" if kernel == "k_pair_sym" else "pair_mixed"
+    p = os.path.join(ROOT, "profiles", f"{stem}_{workload}.md")
     try:
         txt = open(p).read()
     except OSError:
@@ -247,7 +253,7 @@ def shard_collections(sizes, ws):
     return [sorted(x) for x in shards]
 
 
-def make_workload(name, n_each, rank, ws=1):
+def make_workload(name, n_each, rank, ws=1, bodies=None):
     """(list of body dicts, one per simulation) for a workload.  The ensemble
     is one job split across the ranks (its collections are independent);
     every other workload is one replica per rank with its own seed."""
@@ -263,13 +269,13 @@ def make_workload(name, n_each, rank, ws=1):
             sims = [sims[k] for k in mine]
         return sims
     if name == "uniform":
-        return [W.uniform_ball(seed=4 + seed_off)]
+        return [W.uniform_ball(seed=4 + seed_off) if bodies is None else W.uniform_ball(bodies, seed=4 + seed_off)]
     if name == "plummer":
         return [W.plummer(seed=2 + seed_off)]
     if name in ("plummer_bh", "plummer_bh_mixed"):
         return [W.plummer(131072, seed=2 + seed_off)]
     if name == "uniform_bh_mixed":
-        return [W.uniform_ball(seed=4 + seed_off)]
+        return [W.uniform_ball(seed=4 + seed_off) if bodies is None else W.uniform_ball(bodies, seed=4 + seed_off)]
     return [W.disk(seed=1 + seed_off)]
 
 
@@ -498,7 +504,7 @@ def main():
     # stream, which nbg_set_stream does not take)
     stream = torch.cuda.Stream()
     torch.cuda.set_stream(stream)
-    sims = make_workload(args.workload, args.n_each, rank, ws)
+    sims = make_workload(args.workload, args.n_each, rank, ws, args.bodies)
     sharded = args.workload == "ensemble" and ws > 1
     n0 = int(sum(len(b["x"]) for b in sims))
     chunk = 10 if args.workload == "ensemble" else 1
@@ -524,7 +530,8 @@ def main():
         # Barnes-Hut: the shape of the mixed walk (CTAs per SM it is built for)
         sim.set_option(A.OPT_BH_SHAPE if bh else A.OPT_MIX_SHAPE, args.shape)
         tuned = {"shape": args.shape, "pair_kernel_ms": None, "candidates": 3 if bh else A.MIX_SHAPES,
-                 "fixed": True, "kernel": "k_bh_force_mixed" if bh else "k_pair_mixed"}
+                 "fixed": True, "kernel": "k_bh_force_mixed" if bh else
+                 "k_pair_sym" if args.shape in (A.MIX_SYM, A.MIX_SYM + 1) else "k_pair_mixed"}
     elif prec == "mixed" and not args.no_autotune and not bh:
         shape, tms = sim.autotune()
         tuned = {"shape": shape, "pair_kernel_ms": tms, "candidates": A.MIX_SHAPES}
@@ -716,7 +723,9 @@ def main():
             peak_src = f"DFMA-chain probe on this GPU at {mhz:.0f} MHz (MEASURED_PEAKS.json has no FP64 figure)"
     elif prec == "mixed":
         achieved = inter_t * FLOPS_PER_PAIR / (pair_ms * 1e-3) / 1e12
-        peak, kernel, bound = f32 / 1e12, "k_pair_mixed", "fp32_fma"
+        # shapes MIX_SYM and MIX_SYM + 1 are the symmetric kernel
+        sym = tuned is not None and tuned.get("shape") in (A.MIX_SYM, A.MIX_SYM + 1)
+        peak, kernel, bound = f32 / 1e12, "k_pair_sym" if sym else "k_pair_mixed", "fp32_fma"
         peak_src = f"FFMA-chain probe on this GPU at {mhz:.0f} MHz (MEASURED_PEAKS.json has no FP32 figure)"
     else:
         achieved = inter_t * FLOPS_PER_PAIR / (pair_ms * 1e-3) / 1e12
@@ -741,7 +750,7 @@ def main():
             "gpu_launches": int(launches),
             "roofline": {"bound": bound, "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                          "frac": achieved / peak if peak else None,
-                         "traffic": traffic_from_profiles(args.workload) if prec == "mixed" else None,
+                         "traffic": traffic_from_profiles(args.workload, kernel) if prec == "mixed" else None,
                          "kernel": kernel, "flops_per_pair": FLOPS_PER_PAIR, "pair_kernel_ms": pair_ms,
                          "peak_source": peak_src},
             "peaks": {"fp32_tflops": f32 / 1e12, "fp64_tflops": f64 / 1e12, "probe_sm_mhz": mhz,

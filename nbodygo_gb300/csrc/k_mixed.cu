@@ -1211,12 +1211,23 @@ __global__ void k_sym_out(BodyArrays A, DevCtl *ctl, SimSegs seg, const unsigned
             sy += o[SYM_B + li];
             sz += o[2 * SYM_B + li];
         }
+        /* the column's unit slots (aa, a), rows in order, as FP32 (hi, lo)
+         * TwoSum pairs: a column holds up to T - 1 slots (2,047 for 2^20
+         * bodies), and FP64 adds, at 1/64 of the FP32 rate, bound this loop.
+         * Unit (aa, a) is row_start(aa) + a - aa, and row_start(aa + 1) =
+         * row_start(aa) + T - aa. */
+        float hx = 0.f, lx = 0.f, hy = 0.f, ly = 0.f, hz = 0.f, lz = 0.f;
+        const float *q = jpart + (seg.item_off[sim] + a) * 3 * SYM_B + li;
+#pragma unroll 4
         for (ll aa = 0; aa < a; aa++) {
-            const float *q = jpart + (seg.item_off[sim] + sym_row_start(aa, T) + (a - aa)) * 3 * SYM_B;
-            sx += (double)q[li];
-            sy += (double)q[SYM_B + li];
-            sz += (double)q[2 * SYM_B + li];
+            two_sum_add(hx, lx, q[0]);
+            two_sum_add(hy, ly, q[SYM_B]);
+            two_sum_add(hz, lz, q[2 * SYM_B]);
+            q += (T - aa - 1) * 3 * SYM_B;
         }
+        sx += (double)hx + (double)lx;
+        sy += (double)hy + (double)ly;
+        sz += (double)hz + (double)lz;
         const double gm = NBG_G * A.m[i] * ms;
         A.fx[i] = gm * sx;
         A.fy[i] = gm * sy;

@@ -92,9 +92,13 @@ def test_ensemble_mixed_against_fp64_body_by_body():
     assert e.max() <= TOL, f"factor 0.15: worst body {e.max():.3e} of its term scale"
 
 
-def test_uniform_ball_1024_bodies_against_the_oracle():
+@pytest.mark.parametrize("shape", [0, A.MIX_SYM])
+def test_uniform_ball_1024_bodies_against_the_oracle(shape):
+    """The default one-sided shape, and the symmetric kernel the autotuner
+    picks for this workload (2.1 M block pairs, 13 GB of j partials)."""
     b = W.uniform_ball()
     with Simulation("mixed", capacity=len(b["x"])) as m:
+        m.set_option(A.OPT_MIX_SHAPE, shape)
         m.set_bodies(b)
         f = m.force_pass()
     ora = OracleSim(threads=8)
