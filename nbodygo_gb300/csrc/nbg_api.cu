@@ -390,10 +390,16 @@ static int ensure_jpart(nbg_ctx *ctx, ll need)
 {
     if (need <= ctx->cb.jpart_units) return NBG_OK;
     const ll units = need + need / 4 + 16;
+    const size_t bytes = (size_t)units * 3 * NBG_MIX_ITILE * sizeof(float);
     cudaFree(ctx->cb.jpart);
     ctx->cb.jpart = nullptr;
     ctx->cb.jpart_units = 0;
-    CK(cudaMalloc((void **)&ctx->cb.jpart, (size_t)units * 3 * NBG_MIX_ITILE * sizeof(float)));
+    /* the slots grow with the square of the body count (13 GB at 2^20
+     * bodies): past half of the free device memory the shape is refused */
+    size_t free_b = 0, total_b = 0;
+    if (cudaMemGetInfo(&free_b, &total_b) == cudaSuccess && bytes > free_b / 2)
+        return fail(ctx, NBG_E_CUDA, "the symmetric kernel's j partials would take over half of the free device memory");
+    CK(cudaMalloc((void **)&ctx->cb.jpart, bytes));
     ctx->cb.jpart_units = units;
     invalidate_graph(ctx);
     return NBG_OK;
@@ -1784,8 +1790,13 @@ int nbg_autotune(nbg_ctx *ctx, const char *cache_path, int *variant, double *bes
         const int prev = ctx->cb.mix_variant;
         for (int v = 0; v < NBG_MIX_VARIANTS; v++) {
             if ((rc = select_variant(ctx, v)) != NBG_OK) return rc;
-            /* one untimed force pass grows the buffers this shape needs */
+            /* one untimed force pass grows the buffers this shape needs; a
+             * symmetric shape whose j partials do not fit is passed over */
             if ((rc = nbg_force_pass(ctx)) != NBG_OK) {
+                if (nbg_mix_is_sym(v) && rc == NBG_E_CUDA) {
+                    cudaGetLastError();
+                    continue;
+                }
                 select_variant(ctx, prev);
                 return rc;
             }
@@ -1810,6 +1821,14 @@ int nbg_autotune(nbg_ctx *ctx, const char *cache_path, int *variant, double *bes
         }
     }
     if ((rc = select_variant(ctx, best)) != NBG_OK) return rc;
+    if (!nbg_mix_is_sym(best) && ctx->cb.jpart) {
+        /* a one-sided shape won: the symmetric kernel's slots go */
+        CK(cudaStreamSynchronize(ctx->st));
+        cudaFree(ctx->cb.jpart);
+        ctx->cb.jpart = nullptr;
+        ctx->cb.jpart_units = 0;
+        invalidate_graph(ctx);
+    }
     if (variant) *variant = best;
     if (best_ms) *best_ms = best_t;
     return NBG_OK;
