@@ -1629,8 +1629,11 @@ int nbg_step(nbg_ctx *ctx, double dt, double R, int nsteps, nbg_step_info *info)
         h->error = 0;
         int z = 0;
         CK(cudaMemcpyAsync(&ctx->ctl->error, &z, sizeof z, cudaMemcpyHostToDevice, ctx->st));
-        /* the failed cycle may have claimed a sort it never finished */
-        if ((rc = drop_order(ctx)) != NBG_OK) return rc;
+        /* the failed cycle may have claimed a sort it never finished - unless
+         * k_begin stopped it (partial-sum or j-partial slots) before any
+         * other kernel ran: then the order stands, as it would have without
+         * the retry (a resumed snapshot's cycles repeat the run's) */
+        if (h->error_what != 4 && h->error_what != 6 && (rc = drop_order(ctx)) != NBG_OK) return rc;
     }
     {
         /* a cycle with more events than one block sorts in shared memory
@@ -1681,10 +1684,9 @@ int nbg_force_pass(nbg_ctx *ctx)
     for (int attempt = 0;; attempt++) {
         int z = 0;
         CK(cudaMemcpyAsync(&ctx->ctl->error, &z, sizeof z, cudaMemcpyHostToDevice, ctx->st));
-        if (attempt > 0) {
-            int rc = drop_order(ctx);
-            if (rc != NBG_OK) return rc;
-        }
+        /* a retry follows a buffer k_begin found short (partial-sum or
+         * j-partial slots) or the octree's (Barnes-Hut, which keeps no Morton
+         * order): no kernel after k_begin ran, so the order stands */
         nbg_launch_begin(ctx->cb, ctx->ctl, ctx->st);
         if (ctx->cb.bh) {
             nbg_launch_bh(ctx->cb, ctx->ctl, ctx->st, ctx->precision == NBG_PRECISION_MIXED);

@@ -87,12 +87,24 @@ def test_snapshot_taken_mid_fragmentation_holds_fragment_state():
         assert_states_identical(t.state(), st, where="loaded state")
 
 
-def test_mixed_form_resumes_bit_exact_between_sorts():
+@pytest.mark.parametrize("shape", [0, A.MIX_SYM, 17])
+def test_mixed_form_resumes_bit_exact_between_sorts(shape):
     """The mixed form keeps its Morton order for 4 cycles; a snapshot taken
-    mid-interval carries the order, so the FP32 sums group the same bodies."""
+    mid-interval carries the order and the kernel shape (one-sided,
+    symmetric, bulk-copied tiles), so the FP32 sums group the same bodies."""
     bodies = W.plummer_disk(n_each=4096, seed=8)
-    a, b, _ = resumed(lambda: Simulation("mixed"), lambda s: s.set_bodies(bodies), 6, 7, 0.01, 1.0)
-    assert_states_identical(b.state(), a.state(), where="mixed resumed vs uninterrupted")
+
+    made = []
+
+    def make():
+        s = Simulation("mixed")
+        if not made:  # the resumed context takes its shape from the snapshot
+            s.set_option(A.OPT_MIX_SHAPE, shape)
+        made.append(s)
+        return s
+
+    a, b, _ = resumed(make, lambda s: s.set_bodies(bodies), 6, 7, 0.01, 1.0)
+    assert_states_identical(b.state(), a.state(), where=f"mixed shape {shape} resumed vs uninterrupted")
 
 
 def test_batched_context_with_staged_adds_resumes_bit_exact():
