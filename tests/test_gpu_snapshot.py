@@ -141,6 +141,21 @@ def test_barnes_hut_context_resumes_bit_exact(prec):
     assert_events_identical(b.events(), a.events(), where="last cycle")
 
 
+def test_batched_barnes_hut_context_resumes_bit_exact():
+    """One tree per collection, rebuilt every cycle: a batched Barnes-Hut
+    run resumes bit for bit too."""
+    sims = [dense_cluster(250, seed=42), W.plummer(n=700, seed=43, radius_range=(0.3, 1.5))]
+
+    def make():
+        s = Simulation("mixed", seed=6)
+        s.set_option(A.OPT_BARNES_HUT, 1)
+        return s
+
+    a, b, _ = resumed(make, lambda s: s.set_collections(sims), 4, 5, 0.05, 0.9)
+    assert list(b.sim_counts()) == list(a.sim_counts())
+    assert_states_identical(b.state(), a.state(), where="batched Barnes-Hut resumed vs uninterrupted")
+
+
 def test_snapshot_size_query_and_rejections():
     bodies = W.disk(n=100, seed=3)
     import ctypes as C
