@@ -12,7 +12,7 @@ from nbodygo_gb300 import workloads as W
 from nbodygo_gb300.api import NbgError, Simulation
 from oracle.oracle import OracleSim
 
-from helpers import assert_states_identical
+from helpers import assert_states_identical, rel_l2
 from test_gpu_batch import split_state
 from test_gpu_plain_parity import dense_cluster
 
@@ -114,3 +114,30 @@ def test_collection_index_is_checked():
         with pytest.raises(NbgError) as e:
             gpu.remove_bodies(3, sim=-1)
         assert e.value.code == A.NBG_E_ARG
+
+
+@pytest.mark.parametrize("shape", [0, 7, A.MIX_SYM])
+def test_mixed_batch_stays_right_through_edits(shape):
+    """The mixed form carries a Morton order between sorts; removals, adds
+    and edits addressed to single collections change bodies' indices and
+    positions.  After them the mixed forces must still be those of the
+    bodies now in the context: within 1e-6 of an FP64 force pass of the
+    same state."""
+    sims = [W.plummer(n=800, seed=s) for s in (71, 72, 73)]
+    m = Simulation("mixed", seed=5)
+    m.set_option(A.OPT_MIX_SHAPE, shape)
+    m.set_collections(sims)
+    m.step(0.01, 1.0, 2)
+    m.remove_bodies(100, sim=1)
+    m.add_bodies(W.plummer(n=50, seed=74), sim=2)
+    m.apply_edits([dict(id=int(sims[0]["id"][5]), mask=A.M_X | A.M_MASS, x=123.0, mass=5e13)], sim=0)
+    m.step(0.01, 1.0, 1)
+    counts = m.sim_counts()
+    assert counts[1] < 800 and counts[2] > 800
+    f = np.array(m.force_pass())
+    st = m.state()
+    with Simulation("fp64") as p:
+        p.set_collections(split_state(st, counts))
+        g = np.array(p.force_pass())
+    assert rel_l2(f, g) <= 1e-6
+    m.close()
