@@ -160,8 +160,8 @@ def test_flat_collections_match_separate_parts():
         b.set_collections_flat(flat, counts[:-1])
 
 
-@pytest.mark.parametrize("interval", [1, 4])
-def test_mixed_batch_graph_replay_equals_single_cycles(interval):
+@pytest.mark.parametrize("interval,shape", [(1, 0), (4, 0), (4, A.MIX_SYM), (4, 17)])
+def test_mixed_batch_graph_replay_equals_single_cycles(interval, shape):
     """The mixed form decides on the device when to sort and carries the
     order through compaction; with collisions in some collection every
     cycle, ten cycles replayed as one CUDA graph, as two graphs of five and
@@ -170,6 +170,7 @@ def test_mixed_batch_graph_replay_equals_single_cycles(interval):
     runs = []
     for cycles_per_graph, calls in ((10, [10]), (5, [5, 5]), (1, [1] * 10)):
         gpu = Simulation("mixed", seed=9)
+        gpu.set_option(A.OPT_MIX_SHAPE, shape)
         gpu.set_option(A.OPT_SORT_INTERVAL, interval)
         gpu.set_option(A.OPT_GRAPH_CYCLES, cycles_per_graph)
         gpu.set_collections(sims)

@@ -5,6 +5,7 @@ resultqueue.go:97-129) without a copy call."""
 import numpy as np
 import pytest
 
+from nbodygo_gb300 import _abi as A
 from nbodygo_gb300 import workloads as W
 from nbodygo_gb300.api import Simulation
 
@@ -51,3 +52,21 @@ def test_ring_attach_needs_sizes():
     with Simulation("fp64") as sim:
         with pytest.raises(NbgError):
             sim.set_render_ring(slots=0, slot_cap=10)
+
+
+@pytest.mark.parametrize("bh", [False, True])
+def test_ring_with_several_collections(bh):
+    """A batched context (direct sum or one Barnes-Hut tree per collection)
+    writes every collection's renderables into the ring, in body order."""
+    sims = [W.disk(n=400, seed=5), W.plummer(500, seed=6)]
+    with Simulation("mixed") as sim:
+        if bh:
+            sim.set_option(A.OPT_BARNES_HUT, 1)
+        sim.set_collections(sims)
+        head, rend = sim.set_render_ring(slots=2, slot_cap=2048)
+        for c in range(3):
+            sim.step(0.005, 1.0, 1)
+            s = c % 2
+            n = head[s]["count"]
+            assert head[s]["cycle"] == c and n == sim.count() and head[s]["written"] == n
+            same_rend(rend[s, :n], sim.renderables())
