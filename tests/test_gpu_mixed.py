@@ -302,3 +302,21 @@ def test_full_size_ensemble_forces_cancel_per_collection():
         worst = max(worst, _net_force_ratio(f, o, o + n))
         o += n
     assert worst <= 1e-5, f"worst net force {worst:.3e} of a collection's summed magnitudes"
+
+
+def test_autotune_cache_file(tmp_path):
+    """The first tuning of a collection appends its result to the cache
+    file; a context of the same size bucket takes the shape from the file
+    without measuring (the same shape and time come back)."""
+    path = str(tmp_path / "tune.txt")
+    b = W.plummer(n=9000, seed=17)
+    with Simulation("mixed") as s1:
+        s1.set_bodies(b)
+        shape1, ms1 = s1.autotune(path)
+    lines = open(path).read().split("\n")
+    assert len([ln for ln in lines if ln.strip()]) == 1 and lines[0].split()[1] == str(shape1)
+    with Simulation("mixed") as s2:
+        s2.set_bodies(W.plummer(n=10000, seed=18))  # the same power-of-two bucket
+        shape2, ms2 = s2.autotune(path)
+    assert (shape2, round(ms2, 4)) == (shape1, round(ms1, 4))
+    assert len([ln for ln in open(path).read().split("\n") if ln.strip()]) == 1
