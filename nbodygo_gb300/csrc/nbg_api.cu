@@ -24,7 +24,34 @@
 #include <string>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "nbg_internal.cuh"
+
+/* An NVTX range over one C-ABI call (domain "nbgpu"), so a timeline tool
+ * shows the host calls around the kernels; without a tool attached each
+ * push and pop is a check of a null function pointer. */
+namespace {
+nvtxDomainHandle_t nvtx_domain()
+{
+    static nvtxDomainHandle_t d = nvtxDomainCreateA("nbgpu");
+    return d;
+}
+struct NvtxRange {
+    explicit NvtxRange(const char *name)
+    {
+        nvtxEventAttributes_t a = {};
+        a.version = NVTX_VERSION;
+        a.size = NVTX_EVENT_ATTRIB_STRUCT_SIZE;
+        a.messageType = NVTX_MESSAGE_TYPE_ASCII;
+        a.message.ascii = name;
+        nvtxDomainRangePushEx(nvtx_domain(), &a);
+    }
+    ~NvtxRange() { nvtxDomainRangePop(nvtx_domain()); }
+    NvtxRange(const NvtxRange &) = delete;
+    NvtxRange &operator=(const NvtxRange &) = delete;
+};
+} // namespace
 
 struct nbg_ctx {
     int device = 0;
@@ -888,6 +915,7 @@ int nbg_set_cycle(nbg_ctx *ctx, uint64_t cycle)
 
 int nbg_set_collections(nbg_ctx *ctx, int64_t nsims, const int64_t *counts, const nbg_soa *host)
 {
+    NvtxRange nvtx("nbg_set_collections");
     if (!ctx || nsims < 1 || nsims > NBG_MAX_SIMS || !counts) return fail(ctx, NBG_E_ARG, "bad arguments");
     ll n = 0;
     for (ll s = 0; s < nsims; s++) {
@@ -920,6 +948,7 @@ int nbg_set_collections(nbg_ctx *ctx, int64_t nsims, const int64_t *counts, cons
 
 int nbg_set_bodies(nbg_ctx *ctx, const nbg_soa *host, int64_t n)
 {
+    NvtxRange nvtx("nbg_set_bodies");
     if (!ctx || n < 0 || (n > 0 && !host)) return fail(ctx, NBG_E_ARG, "bad arguments");
     const int64_t counts[1] = {n};
     return nbg_set_collections(ctx, 1, counts, host);
@@ -952,6 +981,7 @@ int nbg_count(nbg_ctx *ctx, int64_t *n)
 
 int nbg_get_state(nbg_ctx *ctx, nbg_soa *h, int64_t cap, int64_t *n_out)
 {
+    NvtxRange nvtx("nbg_get_state");
     if (!ctx || !h || cap < 0) return fail(ctx, NBG_E_ARG, "bad arguments");
     CK(cudaSetDevice(ctx->device));
     int rc = sync_ctl(ctx);
@@ -1287,6 +1317,7 @@ static int snap_copy_arrays(nbg_ctx *ctx, BodyArrays &A, char *blk, ll n, bool t
 
 int nbg_save_state(nbg_ctx *ctx, void *buf, int64_t cap, int64_t *size)
 {
+    NvtxRange nvtx("nbg_save_state");
     if (!ctx || !size || cap < 0) return fail(ctx, NBG_E_ARG, "bad arguments");
     CK(cudaSetDevice(ctx->device));
     int rc = sync_ctl(ctx);
@@ -1345,6 +1376,7 @@ int nbg_save_state(nbg_ctx *ctx, void *buf, int64_t cap, int64_t *size)
 
 int nbg_load_state(nbg_ctx *ctx, const void *buf, int64_t size)
 {
+    NvtxRange nvtx("nbg_load_state");
     if (!ctx || !buf || size < NBG_SNAP_HEADER_BYTES) return fail(ctx, NBG_E_ARG, "not a snapshot: too short");
     const char *in = (const char *)buf;
     SnapHeader H;
@@ -1520,6 +1552,7 @@ struct LaunchWindow {
 
 int nbg_step(nbg_ctx *ctx, double dt, double R, int nsteps, nbg_step_info *info)
 {
+    NvtxRange nvtx("nbg_step");
     if (!ctx || nsteps < 0) return fail(ctx, NBG_E_ARG, "bad arguments");
     CK(cudaSetDevice(ctx->device));
     /* dt, R and the per-call accumulators */
@@ -1675,6 +1708,7 @@ int nbg_cancel(nbg_ctx *ctx)
 
 int nbg_force_pass(nbg_ctx *ctx)
 {
+    NvtxRange nvtx("nbg_force_pass");
     if (!ctx) return NBG_E_ARG;
     CK(cudaSetDevice(ctx->device));
     {
@@ -1766,6 +1800,7 @@ static std::string tune_key(nbg_ctx *ctx, ll n)
 
 int nbg_autotune(nbg_ctx *ctx, const char *cache_path, int *variant, double *best_ms)
 {
+    NvtxRange nvtx("nbg_autotune");
     if (!ctx) return NBG_E_ARG;
     CK(cudaSetDevice(ctx->device));
     int rc = sync_ctl(ctx);
