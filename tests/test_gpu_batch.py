@@ -264,3 +264,70 @@ def test_empty_collections_in_a_batch(prec):
         assert counts[2] == 5 and counts[0] == 0 and counts[3] == 0 and counts[6] == 0
         part = split_state(gpu.state(), counts)[2]
         assert np.all(np.isin(part["mass"], add["mass"]))
+
+
+def _tiny_sets(count, seed):
+    """count small collections of 0-16 bodies (some empty), every behaviour"""
+    rng = np.random.default_rng(seed)
+    sizes = rng.integers(0, 17, count)
+    sets = []
+    for s, k in enumerate(sizes):
+        b = dense_cluster(max(int(k), 1), seed=1000 + s)
+        if k == 0:
+            b = {f: np.asarray(v)[:0] for f, v in b.items()}
+        sets.append(b)
+    return sets
+
+
+def test_the_most_collections_a_context_takes():
+    """2,048 collections (the Morton key's 11-bit collection field, the
+    largest count nbg_set_collections takes), of 0-16 bodies each: plain
+    cycles stay bit-identical to each collection's oracle run, the mixed
+    forces and the Barnes-Hut forests agree with FP64, and 2,049 are
+    refused."""
+    from nbodygo_gb300.api import NbgError
+
+    sets = _tiny_sets(2048, 5)
+    gpu = Simulation("fp64", seed=3)
+    gpu.set_collections(sets)
+    oracles = []
+    for b in sets:
+        o = OracleSim(seed=3, threads=1)
+        o.set_bodies(b)
+        oracles.append(o)
+    for c in range(3):
+        gpu.step(0.05, 0.9, 1)
+        for o in oracles:
+            o.step(0.05, 0.9, 1)
+        counts = gpu.sim_counts()
+        assert list(counts) == [o.count() for o in oracles], f"cycle {c}"
+        for q, (got, o) in enumerate(zip(split_state(gpu.state(), counts), oracles)):
+            if counts[q]:
+                assert_states_identical(got, o.state(), fields=[k for k in got if k != "id"],
+                                        where=f"cycle {c} collection {q}")
+    g = np.array(gpu.force_pass())
+    parts = split_state(gpu.state(), gpu.sim_counts())
+    gpu.close()
+
+    def forces(prec, bh):
+        with Simulation(prec) as s:
+            if bh:
+                s.set_option(A.OPT_BARNES_HUT, 1)
+            s.set_collections(parts)
+            return np.array(s.force_pass())
+
+    assert rel_l2(forces("mixed", False), g) <= 1e-6
+    # one tree per collection: against the oracle's octree of each
+    t = forces("fp64", True)
+    want = []
+    for b in parts:
+        if len(b["x"]):
+            o = OracleSim(threads=1)
+            o.set_barnes_hut(True)
+            o.set_bodies(b)
+            want.append(np.array(o.forces()))
+    assert rel_l2(t, np.concatenate(want, axis=1)) <= 1e-12
+    assert rel_l2(forces("mixed", True), t) <= 1e-6
+    with pytest.raises(NbgError):
+        with Simulation("mixed") as s:
+            s.set_collections(_tiny_sets(2049, 6))
