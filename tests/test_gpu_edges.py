@@ -94,3 +94,41 @@ def test_invalid_collision_behaviour_is_rejected_before_any_copy():
     with pytest.raises(NbgError):
         sim.set_bodies(bad)
     assert sim.count() == 100
+
+
+@pytest.mark.parametrize("prec,bh,shape", [("fp64", False, None), ("mixed", False, 0), ("mixed", False, 15),
+                                           ("fp64", True, None), ("mixed", True, None)])
+def test_reloading_other_sizes_leaves_nothing_stale(prec, bh, shape):
+    """One context loaded with 3,000 bodies, stepped through a CUDA graph,
+    reloaded with 9,000, stepped, then with 500: its force pass and next
+    cycles equal a fresh context's on the last set, bit for bit (buffers,
+    graphs, the Morton order and the trees are all rebuilt for the new
+    bodies)."""
+    from nbodygo_gb300 import workloads as W
+
+    def make():
+        s = Simulation(prec, seed=4)
+        if bh:
+            s.set_option(A.OPT_BARNES_HUT, 1)
+        if shape is not None:
+            s.set_option(A.OPT_MIX_SHAPE, shape)
+        s.set_option(A.OPT_GRAPH_CYCLES, 3)
+        return s
+
+    last = W.plummer(n=500, seed=33, radius_range=(0.5, 2.0))
+    with make() as a:
+        a.set_bodies(W.plummer(n=3000, seed=31, radius_range=(0.5, 2.0)))
+        a.step(0.01, 1.0, 6)
+        a.set_bodies(W.plummer(n=9000, seed=32, radius_range=(0.5, 2.0)))
+        a.step(0.01, 1.0, 4)
+        a.set_bodies(last)
+        fa = np.array(a.force_pass())
+        a.step(0.01, 1.0, 5)
+        sa = a.state()
+    with make() as b:
+        b.set_bodies(last)
+        fb = np.array(b.force_pass())
+        b.step(0.01, 1.0, 5)
+        sb = b.state()
+    assert np.array_equal(fa.view(np.uint64), fb.view(np.uint64))
+    assert_states_identical(sa, sb, where="reloaded vs fresh")
