@@ -132,3 +132,27 @@ def test_reloading_other_sizes_leaves_nothing_stale(prec, bh, shape):
         sb = b.state()
     assert np.array_equal(fa.view(np.uint64), fb.view(np.uint64))
     assert_states_identical(sa, sb, where="reloaded vs fresh")
+
+
+@pytest.mark.parametrize("first,then", [("fp64", "mixed"), ("mixed", "fp64")])
+def test_switching_precision_mid_run(first, then):
+    """nbg_set_precision on a stepped context: the cycles after the switch
+    equal those of a fresh context of the new form loaded with the state
+    reached, bit for bit (a switch to the plain form is the oracle's cycle
+    from there on)."""
+    from nbodygo_gb300 import workloads as W
+
+    b = W.plummer(n=2000, seed=35, radius_range=(0.5, 2.0))
+    with Simulation(first, seed=4) as a:
+        a.set_bodies(b)
+        a.step(0.01, 1.0, 3)
+        mid, nid = a.state(), a.next_id()
+        a.set_precision(then)
+        a.step(0.01, 1.0, 4)
+        sa = a.state()
+    with Simulation(then, seed=4) as c:
+        c.set_bodies(mid)
+        c.set_next_id(nid)
+        c.step(0.01, 1.0, 4)
+        sc = c.state()
+    assert_states_identical(sa, sc, where=f"{first} -> {then}")
