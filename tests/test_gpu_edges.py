@@ -156,3 +156,39 @@ def test_switching_precision_mid_run(first, then):
         c.step(0.01, 1.0, 4)
         sc = c.state()
     assert_states_identical(sa, sc, where=f"{first} -> {then}")
+
+
+@pytest.mark.parametrize("prec,bh", [("mixed", False), ("fp64", True), ("mixed", True)])
+def test_switching_between_one_and_several_collections(prec, bh):
+    """One context loaded with a single collection, then three, then one
+    again (the launch sequence changes: per-collection passes of the octree
+    sort, collection fields of the Morton keys): each stage equals a fresh
+    context's, bit for bit."""
+    from nbodygo_gb300 import workloads as W
+
+    def make():
+        s = Simulation(prec, seed=4)
+        if bh:
+            s.set_option(A.OPT_BARNES_HUT, 1)
+        s.set_option(A.OPT_GRAPH_CYCLES, 2)
+        return s
+
+    one = W.plummer(n=1500, seed=36, radius_range=(0.5, 2.0))
+    three = [W.plummer(n=600 + 100 * k, seed=37 + k, radius_range=(0.5, 2.0)) for k in range(3)]
+    with make() as a:
+        a.set_bodies(one)
+        a.step(0.01, 1.0, 4)
+        a.set_collections(three)
+        a.step(0.01, 1.0, 4)
+        s3 = a.state()
+        a.set_bodies(one)
+        a.step(0.01, 1.0, 4)
+        s1 = a.state()
+    with make() as b:
+        b.set_collections(three)
+        b.step(0.01, 1.0, 4)
+        assert_states_identical(s3, b.state(), where="three collections after one")
+    with make() as c:
+        c.set_bodies(one)
+        c.step(0.01, 1.0, 4)
+        assert_states_identical(s1, c.state(), where="one collection after three")

@@ -178,3 +178,22 @@ def test_snapshot_size_query_and_rejections():
             s.load_state(bytes(bad))
         # a refused load leaves the context as it was
         assert_states_identical(s.state(), before, where="after refused loads")
+
+
+def test_snapshot_carries_its_form_into_a_context_of_the_other():
+    """A mixed run's snapshot loaded into a context created for the plain
+    form resumes the mixed run (the form, the kernel shape and the Morton
+    order travel with it), bit for bit; and the other way round."""
+    bodies = W.plummer_disk(n_each=3000, seed=12)
+    for first, other in (("mixed", "fp64"), ("fp64", "mixed")):
+        a = Simulation(first, seed=2)
+        a.set_bodies(bodies)
+        a.step(0.01, 1.0, 5)
+        snap = a.save_state()
+        a.step(0.01, 1.0, 6)
+        b = Simulation(other, seed=2)
+        b.load_state(snap)
+        b.step(0.01, 1.0, 6)
+        assert_states_identical(b.state(), a.state(), where=f"{first} snapshot in a {other} context")
+        a.close()
+        b.close()
