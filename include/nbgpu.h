@@ -154,6 +154,9 @@ int nbg_create(int device, int precision, int64_t capacity, nbg_ctx **out);
 void nbg_destroy(nbg_ctx *ctx);
 const char *nbg_last_error(const nbg_ctx *ctx);
 int nbg_set_precision(nbg_ctx *ctx, int precision);
+/* The context's current form (NBG_PRECISION_*): the one it was created or
+ * set to, or the one a loaded snapshot carried. */
+int nbg_get_precision(nbg_ctx *ctx, int *precision);
 /* Runs the context's work on the caller's CUDA stream (a cudaStream_t passed
  * as void *; NULL restores the context's own stream). */
 int nbg_set_stream(nbg_ctx *ctx, void *stream);

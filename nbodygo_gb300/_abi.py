@@ -172,6 +172,7 @@ def declare(lib):
         "nbg_destroy": (None, [P]),
         "nbg_last_error": (C.c_char_p, [P]),
         "nbg_set_precision": (C.c_int, [P, C.c_int]),
+        "nbg_get_precision": (C.c_int, [P, C.POINTER(C.c_int)]),
         "nbg_set_stream": (C.c_int, [P, C.c_void_p]),
         "nbg_set_seed": (C.c_int, [P, C.c_uint64]),
         "nbg_set_next_id": (C.c_int, [P, C.c_int64]),

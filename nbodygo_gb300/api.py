@@ -266,6 +266,10 @@ class Simulation:
     def load_state(self, snapshot):
         data = bytes(snapshot)
         self._check(self.lib.nbg_load_state(self.ctx, data, len(data)))
+        # the snapshot carries the form of the run it came from
+        p = C.c_int()
+        self._check(self.lib.nbg_get_precision(self.ctx, C.byref(p)))
+        self.precision = "mixed" if p.value == A.PRECISION_MIXED else "fp64"
 
     # ---- the cycle ----
     def step(self, dt, R=1.0, nsteps=1):

@@ -864,6 +864,13 @@ int nbg_set_precision(nbg_ctx *ctx, int precision)
     return NBG_OK;
 }
 
+int nbg_get_precision(nbg_ctx *ctx, int *precision)
+{
+    if (!ctx || !precision) return fail(ctx, NBG_E_ARG, "bad arguments");
+    *precision = ctx->precision;
+    return NBG_OK;
+}
+
 int nbg_set_stream(nbg_ctx *ctx, void *stream)
 {
     if (!ctx) return NBG_E_ARG;

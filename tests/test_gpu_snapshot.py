@@ -193,6 +193,7 @@ def test_snapshot_carries_its_form_into_a_context_of_the_other():
         a.step(0.01, 1.0, 6)
         b = Simulation(other, seed=2)
         b.load_state(snap)
+        assert b.precision == first
         b.step(0.01, 1.0, 6)
         assert_states_identical(b.state(), a.state(), where=f"{first} snapshot in a {other} context")
         a.close()
