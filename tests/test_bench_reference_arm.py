@@ -38,3 +38,15 @@ def test_default_workload_is_timed_whole_on_the_cpu():
     assert "plummer_disk" in bench.CPU_FULL
     sims, what = bench.cpu_sample("plummer_disk", 64)
     assert len(sims) == 1 and len(sims[0]["x"]) == 128 and "full workload" in what
+
+
+def test_roofline_traffic_comes_from_the_summary_of_the_kernel_that_ran():
+    """The `traffic` of a bench line is read from the committed ncu summary
+    of the kernel and workload: the one-sided kernel on the headline
+    workload, the symmetric kernel on the uniform ball."""
+    sys.path.insert(0, ROOT)
+    import bench
+
+    assert bench.traffic_from_profiles("plummer_disk") == 100160512
+    assert bench.traffic_from_profiles("uniform", "k_pair_sym") == 1.64e10
+    assert bench.traffic_from_profiles("uniform") is None  # no one-sided summary of that workload
