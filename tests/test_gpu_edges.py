@@ -192,3 +192,35 @@ def test_switching_between_one_and_several_collections(prec, bh):
         c.set_bodies(one)
         c.step(0.01, 1.0, 4)
         assert_states_identical(s1, c.state(), where="one collection after three")
+
+
+def test_contexts_stepped_from_two_threads_at_once():
+    """Two contexts on one GPU, each driven by its own host thread at the
+    same time (ctypes drops the GIL during a call, so the calls overlap):
+    each ends exactly where it ends when run alone."""
+    import threading
+
+    from nbodygo_gb300 import workloads as W
+
+    jobs = [("mixed", W.plummer(n=6000, seed=41, radius_range=(0.5, 2.0))),
+            ("fp64", W.disk(n=1500, seed=42)),
+            ("mixed", W.plummer_disk(n_each=4096, seed=43))]
+
+    def run(prec, b, out, k):
+        with Simulation(prec, seed=7) as s:
+            s.set_bodies(b)
+            for _ in range(4):
+                s.step(0.01, 1.0, 3)
+            out[k] = s.state()
+
+    alone = [None] * len(jobs)
+    for k, (prec, b) in enumerate(jobs):
+        run(prec, b, alone, k)
+    together = [None] * len(jobs)
+    threads = [threading.Thread(target=run, args=(prec, b, together, k)) for k, (prec, b) in enumerate(jobs)]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    for k in range(len(jobs)):
+        assert_states_identical(together[k], alone[k], where=f"context {k} from a thread")
