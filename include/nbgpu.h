@@ -22,7 +22,9 @@
  *  - Inputs are copied before a call returns; no caller pointer is kept
  *    (this satisfies the cgo pointer-passing rules).
  *  - One thread drives a context at a time (the runner goroutine); calls on
- *    one context are not synchronised against each other.
+ *    one context are not synchronised against each other.  Different
+ *    contexts are independent: several host threads may each drive their
+ *    own at the same time, on one GPU or several.
  *  - Body order is the reference's array order: results depend on it exactly
  *    as in the reference (force summation order, event order, compaction).
  *  - Strings (Name, Class), colour and light intensity stay with the caller,
