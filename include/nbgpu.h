@@ -154,6 +154,8 @@ typedef struct nbg_edit {
  * Replaces NewComputationRunner's worker pool (computation-runner.go:81-98). */
 int nbg_create(int device, int precision, int64_t capacity, nbg_ctx **out);
 void nbg_destroy(nbg_ctx *ctx);
+/* the context's last error message; with NULL, the calling thread's last
+ * error of a call that had no context (nbg_create, the allocation-free pass) */
 const char *nbg_last_error(const nbg_ctx *ctx);
 int nbg_set_precision(nbg_ctx *ctx, int precision);
 /* The context's current form (NBG_PRECISION_*): the one it was created or

@@ -35,6 +35,7 @@
  * its own, and k_mix_out adds the shares in chunk order, so results do not
  * depend on scheduling.
  */
+#include <atomic>
 #include <type_traits>
 
 #include "nbg_internal.cuh"
@@ -1283,13 +1284,17 @@ MixVariantInfo nbg_mix_variant_info(int variant)
     }
 }
 
-static int g_mixed_slots_cache[64][NBG_MIX_VARIANTS];
+/* resident CTAs of each shape per device, filled on first use (relaxed
+ * atomics: threads driving contexts at once store the same value) */
+static std::atomic<int> g_mixed_slots_cache[64][NBG_MIX_VARIANTS];
 
 int nbg_mixed_slots(int device, int variant)
 {
     if (variant < 0 || variant >= NBG_MIX_VARIANTS) variant = 0;
-    if (device >= 0 && device < 64 && g_mixed_slots_cache[device][variant] > 0)
-        return g_mixed_slots_cache[device][variant];
+    if (device >= 0 && device < 64) {
+        const int cached = g_mixed_slots_cache[device][variant].load(std::memory_order_relaxed);
+        if (cached > 0) return cached;
+    }
     int per_sm = 0, sms = 0;
     switch (variant) {
 #define X(id, kind, b, k, jt, u, mb) \
@@ -1306,7 +1311,7 @@ int nbg_mixed_slots(int device, int variant)
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
     int slots = per_sm * sms;
     if (slots < 1) slots = 1;
-    if (device >= 0 && device < 64) g_mixed_slots_cache[device][variant] = slots;
+    if (device >= 0 && device < 64) g_mixed_slots_cache[device][variant].store(slots, std::memory_order_relaxed);
     return slots;
 }
 

@@ -135,7 +135,9 @@ static int set_segments(nbg_ctx *ctx, int nsims, const ll *counts, bool *reshape
     return NBG_OK;
 }
 
-static std::string g_last_error;
+/* one per host thread, as errno: threads that create contexts at once do
+ * not share it */
+static thread_local std::string g_last_error;
 
 /* error message of calls without a context (read by nbg_last_error(NULL)) */
 const char *nbg_set_global_error(const char *msg)
