@@ -95,7 +95,7 @@ struct DevCtl {
     unsigned pad2;
     /* Morton order of the mixed path (perm): valid while no body changed
      * index; re-sorted when invalid or sort_interval cycles after the last
-     * sort (0: NBG_SORT_INTERVAL_DEFAULT).  sort_now is this cycle's verdict. */
+     * sort (0: NBG_SORT_INTERVAL_DEFAULT).  sort_now is this cycle's decision. */
     int sort_valid;
     int sort_now;
     int sort_interval;
