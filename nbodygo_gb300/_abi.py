@@ -146,7 +146,7 @@ def soa_from_arrays(arrays):
         if not (isinstance(a, np.ndarray) and a.dtype == dt and a.flags.c_contiguous):
             a = np.ascontiguousarray(a, dtype=dt)
         keep.append(a)
-        setattr(soa, f, a.__array_interface__["data"][0])
+        setattr(soa, f, a.ctypes.data)
     return soa, keep
 
 
