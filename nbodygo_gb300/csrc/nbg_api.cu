@@ -1404,11 +1404,28 @@ int nbg_load_state(nbg_ctx *ctx, const void *buf, int64_t size)
     const ll *counts = (const ll *)(in + L.counts), *hadd = (const ll *)(in + L.hadd);
     ll nsum = 0, asum = 0;
     for (int s = 0; s < H.nsims; s++) {
-        if (counts[s] < 0 || hadd[s] < 0) return fail(ctx, NBG_E_ARG, "snapshot counts out of range");
+        if (counts[s] < 0 || hadd[s] < 0 || counts[s] > NBG_MAX_BODIES || hadd[s] > NBG_MAX_BODIES)
+            return fail(ctx, NBG_E_ARG, "snapshot counts out of range");
         nsum += counts[s];
         asum += hadd[s];
     }
     if (nsum != H.n || asum != H.pending_adds) return fail(ctx, NBG_E_ARG, "snapshot counts do not add up");
+    if (H.has_order) {
+        /* the kernels index the bodies through the order: it must map each
+         * collection's positions onto that collection's bodies, once each */
+        const unsigned *ord = (const unsigned *)(in + L.order);
+        std::vector<unsigned char> seen((size_t)H.n, 0);
+        ll o = 0;
+        for (int s = 0; s < H.nsims; s++) {
+            for (ll p = o; p < o + counts[s]; p++) {
+                const ll k = (ll)ord[p];
+                if (k < o || k >= o + counts[s] || seen[(size_t)k])
+                    return fail(ctx, NBG_E_ARG, "snapshot order is not a permutation of each collection");
+                seen[(size_t)k] = 1;
+            }
+            o += counts[s];
+        }
+    }
     CK(cudaSetDevice(ctx->device));
     CK(cudaStreamSynchronize(ctx->st));
     int rc;

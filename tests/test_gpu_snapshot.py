@@ -198,3 +198,38 @@ def test_snapshot_carries_its_form_into_a_context_of_the_other():
         assert_states_identical(b.state(), a.state(), where=f"{first} snapshot in a {other} context")
         a.close()
         b.close()
+
+
+def test_batched_mixed_context_resumes_bit_exact():
+    """Several collections in the mixed form: the Morton order travels with
+    the snapshot, each collection's positions over its own bodies."""
+    sims = [W.plummer(n=1500, seed=1, behavior=A.SUBSUME, radius_range=(0.5, 3.0)), W.disk(n=700, seed=2),
+            W.uniform_ball(n=2100, seed=3, R=300.0)]
+    a, b, _ = resumed(lambda: Simulation("mixed", seed=3), lambda s: s.set_collections(sims), 5, 6, 0.01, 1.0)
+    assert list(b.sim_counts()) == list(a.sim_counts())
+    assert_states_identical(b.state(), a.state(), where="batched mixed resumed vs uninterrupted")
+
+
+def test_snapshot_with_a_broken_order_is_refused():
+    """The kernels index the bodies through the snapshot's order, so a load
+    checks that it is a permutation of each collection: an index past the
+    collection or a repeated one is refused, and the context stays as it
+    was."""
+    bodies = W.plummer_disk(n_each=2000, seed=4)
+    with Simulation("mixed") as s:
+        s.set_bodies(bodies)
+        s.step(0.01, 1.0, 5)
+        snap = s.save_state()
+        n = s.count()
+        before = s.state()
+        start = len(snap) - (n * 4 + 7) // 8 * 8  # the order is the last section
+        order = np.frombuffer(snap, dtype=np.uint32, count=n, offset=start)
+        assert sorted(order.tolist()) == list(range(n))
+        for k, v in ((0, n), (1, int(order[0])), (n - 1, 0xFFFFFFFF)):
+            o = order.copy()
+            o[k] = v
+            with pytest.raises(NbgError) as e:
+                s.load_state(snap[:start] + o.tobytes() + snap[start + 4 * n:])
+            assert e.value.code == A.NBG_E_ARG and "order" in str(e.value)
+        assert_states_identical(s.state(), before, where="after refused loads")
+        s.load_state(snap)
