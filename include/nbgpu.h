@@ -41,7 +41,8 @@ extern "C" {
 
 /* status codes */
 #define NBG_OK 0
-#define NBG_E_CUDA 1     /* a CUDA runtime call failed */
+#define NBG_E_CUDA 1     /* a CUDA runtime call failed (a failed growth of the body capacity leaves
+                            the context with no bodies: load a collection again) */
 #define NBG_E_ARG 2      /* bad argument (null pointer, size, enum value) */
 #define NBG_E_OVERFLOW 3 /* a device buffer was too small; state is unchanged */
 #define NBG_E_TIMEOUT 4  /* nbg_step reached its deadline (NBG_OPT_STEP_DEADLINE_MS), or a device wait gave up */
@@ -408,6 +409,12 @@ int nbg_get_timing(nbg_ctx *ctx, nbg_timing *t);
    waits (bounded again) for its copies and leaves, and the cycle fails with
    NBG_E_TIMEOUT.  The context stays usable; 0 (default) turns it off. */
 #define NBG_OPT_TEST_WAIT_STALL 14
+/* test hook for a failed capacity growth: 1 makes the next growth of the
+   body capacity fail as a device out of memory would, after the old
+   buffers were released.  The call fails with NBG_E_CUDA and the context
+   is left with no bodies (one empty collection, no staged adds); it stays
+   usable, and the next load allocates again.  The hook clears itself. */
+#define NBG_OPT_TEST_FAIL_GROWTH 15
 #define NBG_OPT_NEAR_PPM 5   /* mixed: pairs closer than (value * 1e-6) x the i-body's
                                 distance from its tile origin take the near-pair
                                 pass: the exact hi/lo difference, FP64 for a

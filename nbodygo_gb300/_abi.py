@@ -49,6 +49,7 @@ OPT_SORT_INTERVAL = 10
 OPT_STEP_DEADLINE_MS = 12
 OPT_EVENT_SORT = 13
 OPT_TEST_WAIT_STALL = 14
+OPT_TEST_FAIL_GROWTH = 15
 OPT_P64_SPLIT_MAX = 11
 MIX_SHAPES = 19
 MIX_SYM = 15  # shapes 15 and 16: the symmetric kernel

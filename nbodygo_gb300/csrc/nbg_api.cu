@@ -92,6 +92,7 @@ struct nbg_ctx {
     ll deadline_ms = 0;
     int ev_sort_mode = 0; /* NBG_OPT_EVENT_SORT */
     int ev_radix_auto = 0; /* automatic choice for the next call */
+    bool test_fail_growth = false; /* NBG_OPT_TEST_FAIL_GROWTH: the next growth fails */
     cudaEvent_t win[2] = {nullptr, nullptr}; /* the last two launches in flight */
 };
 
@@ -218,21 +219,24 @@ static void free_arrays(BodyArrays &A)
     memset(&A, 0, sizeof A);
 }
 
+/* every array for cap bodies; on failure none stays allocated and A is
+ * zeroed */
 static cudaError_t alloc_arrays(BodyArrays &A, ll cap)
 {
     memset(&A, 0, sizeof A);
     size_t c = (size_t)(cap > 0 ? cap : 1);
     double **f[NBG_NF64];
     f64_fields(A, f);
-    for (int q = 0; q < NBG_NF64; q++) {
-        cudaError_t e = cudaMalloc((void **)f[q], c * sizeof(double));
-        if (e != cudaSuccess) return e;
+    cudaError_t e = cudaSuccess;
+    for (int q = 0; q < NBG_NF64 && e == cudaSuccess; q++) e = cudaMalloc((void **)f[q], c * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc((void **)&A.fr_cnt, c * sizeof(ll));
+    if (e == cudaSuccess) e = cudaMalloc((void **)&A.id, c * sizeof(ll));
+    if (e == cudaSuccess) e = cudaMalloc((void **)&A.flags, c * sizeof(unsigned));
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        free_arrays(A);
     }
-    cudaError_t e = cudaMalloc((void **)&A.fr_cnt, c * sizeof(ll));
-    if (e != cudaSuccess) return e;
-    e = cudaMalloc((void **)&A.id, c * sizeof(ll));
-    if (e != cudaSuccess) return e;
-    return cudaMalloc((void **)&A.flags, c * sizeof(unsigned));
+    return e;
 }
 
 static cudaError_t copy_arrays(BodyArrays &D, const BodyArrays &S, ll n, cudaStream_t st)
@@ -288,6 +292,30 @@ static int drop_order(nbg_ctx *ctx)
     return NBG_OK;
 }
 
+/* After a failed growth: the bodies, the staged adds and every buffer of
+ * the capacity are released, and the context holds one empty collection
+ * (it stays usable: the next load or cycle allocates again). */
+static void lose_bodies(nbg_ctx *ctx)
+{
+    cudaGetLastError();
+    cudaStreamSynchronize(ctx->st);
+    free_arrays(ctx->cb.a);
+    free_arrays(ctx->cb.b);
+    free_cap_buffers(ctx->cb);
+    ctx->cb.cap = 0;
+    ctx->n_host = 0;
+    ctx->pending_adds = 0;
+    ctx->add_sim.clear();
+    invalidate_graph(ctx);
+    const ll zero = 0;
+    bool reshaped = false;
+    if (set_segments(ctx, 1, &zero, &reshaped) == NBG_OK) {
+        k_set_loaded<<<1, 1, 0, ctx->st>>>(ctx->ctl, 0);
+        cudaStreamSynchronize(ctx->st);
+    }
+    cudaGetLastError();
+}
+
 static int ensure_cap(nbg_ctx *ctx, ll need, ll keep)
 {
     if (need <= ctx->cb.cap) return NBG_OK;
@@ -296,35 +324,54 @@ static int ensure_cap(nbg_ctx *ctx, ll need, ll keep)
     while (cap < need) cap *= 2;
     if (cap > NBG_MAX_BODIES) cap = NBG_MAX_BODIES;
     BodyArrays na;
-    CK(alloc_arrays(na, cap));
+    CK(alloc_arrays(na, cap)); /* nothing has changed if this fails */
     if (ctx->cb.cap > 0) {
-        CK(copy_arrays(na, ctx->cb.a, keep, ctx->st));
-        CK(cudaStreamSynchronize(ctx->st));
+        cudaError_t e = copy_arrays(na, ctx->cb.a, keep, ctx->st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->st);
+        if (e != cudaSuccess) {
+            free_arrays(na);
+            CK(e);
+        }
         free_arrays(ctx->cb.a);
         free_arrays(ctx->cb.b);
         free_cap_buffers(ctx->cb);
     }
+    /* the old buffers are gone: until every new one exists the capacity is
+     * 0, and a failure leaves a context with no bodies (lose_bodies) */
     ctx->cb.a = na;
-    CK(alloc_arrays(ctx->cb.b, cap));
-    CK(cudaMalloc((void **)&ctx->cb.rend, (size_t)cap * sizeof(nbg_renderable)));
-    ll nblk = (cap + NBG_SCAN_TILE - 1) / NBG_SCAN_TILE;
-    CK(cudaMalloc((void **)&ctx->cb.blk_sum, (size_t)nblk * sizeof(ll)));
-    CK(cudaMalloc((void **)&ctx->cb.blk_off, (size_t)nblk * sizeof(ll)));
-    ctx->cb.nblk_cap = nblk;
-    CK(cudaMalloc((void **)&ctx->cb.jhi, (size_t)cap * sizeof(float4)));
-    CK(cudaMalloc((void **)&ctx->cb.jlo, (size_t)cap * sizeof(float4)));
+    ctx->cb.cap = 0;
+    /* the test hook stands in for a device out of memory at this point */
+    cudaError_t e = ctx->test_fail_growth ? cudaErrorMemoryAllocation : alloc_arrays(ctx->cb.b, cap);
+    ctx->test_fail_growth = false;
+#define CAP_ALLOC(ptr, bytes) \
+    if (e == cudaSuccess) e = cudaMalloc((void **)&(ptr), (size_t)(bytes))
+    CAP_ALLOC(ctx->cb.rend, cap * sizeof(nbg_renderable));
+    const ll nblk = (cap + NBG_SCAN_TILE - 1) / NBG_SCAN_TILE;
+    CAP_ALLOC(ctx->cb.blk_sum, nblk * sizeof(ll));
+    CAP_ALLOC(ctx->cb.blk_off, nblk * sizeof(ll));
+    CAP_ALLOC(ctx->cb.jhi, cap * sizeof(float4));
+    CAP_ALLOC(ctx->cb.jlo, cap * sizeof(float4));
     /* every sim may end in a partial tile: at most cap / itile + nsims tiles */
-    ll tiles = (cap + NBG_MIX_MIN_ITILE - 1) / NBG_MIX_MIN_ITILE + NBG_MAX_SIMS + 1;
-    CK(cudaMalloc((void **)&ctx->cb.tile_c, (size_t)tiles * sizeof(float4)));
-    CK(cudaMalloc((void **)&ctx->cb.tile_t, (size_t)tiles * sizeof(float)));
-    CK(cudaMalloc((void **)&ctx->cb.iprep, (size_t)cap * sizeof(float4)));
-    ctx->cb.part_doubles = part_need(ctx, cap);
-    CK(cudaMalloc((void **)&ctx->cb.part, (size_t)ctx->cb.part_doubles * sizeof(double)));
-    CK(cudaMalloc((void **)&ctx->cb.perm, (size_t)cap * sizeof(unsigned)));
-    CK(cudaMalloc((void **)&ctx->cb.sval, (size_t)cap * sizeof(unsigned)));
-    CK(cudaMalloc((void **)&ctx->cb.skey[0], (size_t)cap * sizeof(unsigned)));
-    CK(cudaMalloc((void **)&ctx->cb.skey[1], (size_t)cap * sizeof(unsigned)));
-    CK(cudaMalloc((void **)&ctx->cb.shist, (size_t)nbg_sort_scratch_hist(cap) * sizeof(ll)));
+    const ll tiles = (cap + NBG_MIX_MIN_ITILE - 1) / NBG_MIX_MIN_ITILE + NBG_MAX_SIMS + 1;
+    CAP_ALLOC(ctx->cb.tile_c, tiles * sizeof(float4));
+    CAP_ALLOC(ctx->cb.tile_t, tiles * sizeof(float));
+    CAP_ALLOC(ctx->cb.iprep, cap * sizeof(float4));
+    const ll pdoubles = part_need(ctx, cap);
+    CAP_ALLOC(ctx->cb.part, pdoubles * sizeof(double));
+    CAP_ALLOC(ctx->cb.perm, cap * sizeof(unsigned));
+    CAP_ALLOC(ctx->cb.sval, cap * sizeof(unsigned));
+    CAP_ALLOC(ctx->cb.skey[0], cap * sizeof(unsigned));
+    CAP_ALLOC(ctx->cb.skey[1], cap * sizeof(unsigned));
+    CAP_ALLOC(ctx->cb.shist, nbg_sort_scratch_hist(cap) * sizeof(ll));
+#undef CAP_ALLOC
+    if (e != cudaSuccess) {
+        const std::string m = "buffers for " + std::to_string(cap) + " bodies: " + cudaGetErrorString(e) +
+                              " (the context now holds no bodies)";
+        lose_bodies(ctx);
+        return fail(ctx, NBG_E_CUDA, m);
+    }
+    ctx->cb.nblk_cap = nblk;
+    ctx->cb.part_doubles = pdoubles;
     ctx->cb.cap = cap;
     invalidate_graph(ctx);
     int rc = drop_order(ctx);
@@ -411,6 +458,15 @@ static void free_cap_buffers(CycleBufs &cb)
     cudaFree(cb.skey[0]);
     cudaFree(cb.skey[1]);
     cudaFree(cb.shist);
+    cb.rend = nullptr;
+    cb.blk_sum = cb.blk_off = nullptr;
+    cb.nblk_cap = 0;
+    cb.jhi = cb.jlo = cb.tile_c = cb.iprep = nullptr;
+    cb.tile_t = nullptr;
+    cb.part = nullptr;
+    cb.part_doubles = 0;
+    cb.perm = cb.sval = cb.skey[0] = cb.skey[1] = nullptr;
+    cb.shist = nullptr;
 }
 
 /* the symmetric mixed kernel's j-partial slots: at least `need` units (with
@@ -439,10 +495,13 @@ static int ensure_frag_cap(nbg_ctx *ctx, ll need)
     if (need <= ctx->cb.frag_cap) return NBG_OK;
     ll c = ctx->cb.frag_cap > 0 ? ctx->cb.frag_cap : 4096;
     while (c < need) c *= 2;
-    if (ctx->cb.frag_cap > 0) free_arrays(ctx->cb.frags);
+    /* no capacity until the new arrays exist: a cycle that would emit
+     * fragments then stops with the overflow status */
+    free_arrays(ctx->cb.frags);
+    ctx->cb.frag_cap = 0;
+    invalidate_graph(ctx);
     CK(alloc_arrays(ctx->cb.frags, c));
     ctx->cb.frag_cap = c;
-    invalidate_graph(ctx);
     return NBG_OK;
 }
 
@@ -454,8 +513,12 @@ static int ensure_adds_cap(nbg_ctx *ctx, ll need)
     BodyArrays na;
     CK(alloc_arrays(na, c));
     if (ctx->cb.adds_cap > 0) {
-        CK(copy_arrays(na, ctx->cb.adds, ctx->pending_adds, ctx->st));
-        CK(cudaStreamSynchronize(ctx->st));
+        cudaError_t e = copy_arrays(na, ctx->cb.adds, ctx->pending_adds, ctx->st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->st);
+        if (e != cudaSuccess) {
+            free_arrays(na);
+            CK(e);
+        }
         free_arrays(ctx->cb.adds);
     }
     ctx->cb.adds = na;
@@ -2068,6 +2131,10 @@ int nbg_set_option(nbg_ctx *ctx, int key, int64_t value)
         ctx->ctl_h->test_tx_extra = extra;
         return ctl_put(ctx, offsetof(DevCtl, test_tx_extra), &extra, sizeof extra);
     }
+    case NBG_OPT_TEST_FAIL_GROWTH:
+        if (value < 0 || value > 1) return fail(ctx, NBG_E_ARG, "growth-failure hook must be 0 or 1");
+        ctx->test_fail_growth = value != 0;
+        return NBG_OK;
     case NBG_OPT_STEP_DEADLINE_MS:
         if (value < 0 || value > ((ll)1 << 40)) return fail(ctx, NBG_E_ARG, "deadline must be 0..2^40 ms");
         ctx->deadline_ms = value;
@@ -2097,9 +2164,10 @@ int nbg_set_option(nbg_ctx *ctx, int key, int64_t value)
         CK(cudaSetDevice(ctx->device));
         CK(cudaStreamSynchronize(ctx->st));
         free_arrays(ctx->cb.frags);
+        ctx->cb.frag_cap = 0;
+        invalidate_graph(ctx);
         CK(alloc_arrays(ctx->cb.frags, value));
         ctx->cb.frag_cap = value;
-        invalidate_graph(ctx);
         return NBG_OK;
     }
     default:

@@ -6,7 +6,8 @@ import numpy as np
 import pytest
 
 from nbodygo_gb300 import _abi as A
-from nbodygo_gb300.api import Simulation
+from nbodygo_gb300 import workloads as W
+from nbodygo_gb300.api import NbgError, Simulation
 from oracle.oracle import OracleSim
 
 from helpers import assert_states_identical, body_set
@@ -224,3 +225,30 @@ def test_contexts_stepped_from_two_threads_at_once():
         t.join()
     for k in range(len(jobs)):
         assert_states_identical(together[k], alone[k], where=f"context {k} from a thread")
+
+
+def test_failed_capacity_growth_leaves_an_empty_usable_context():
+    """A growth of the body capacity that fails after the old buffers were
+    released (the host-side hook stands in for a device out of memory)
+    leaves one empty collection; stepping it is harmless, and the next load
+    runs as in a fresh context."""
+    small, big = W.plummer(n=1000, seed=31), W.plummer(n=5000, seed=32)
+    for prec in ("fp64", "mixed"):
+        with Simulation(prec) as ref:
+            ref.set_bodies(big)
+            ref.step(0.01, 1.0, 2)
+            exp = ref.state()
+        with Simulation(prec) as s:
+            s.set_bodies(small)
+            s.step(0.01, 1.0, 1)
+            s.add_bodies(W.plummer(n=3, seed=33))
+            s.set_option(A.OPT_TEST_FAIL_GROWTH, 1)
+            with pytest.raises(NbgError) as e:
+                s.set_bodies(big)
+            assert e.value.code == A.NBG_E_CUDA and "no bodies" in str(e.value)
+            assert s.count() == 0 and list(s.sim_counts()) == [0]
+            s.step(0.01, 1.0, 2)
+            assert s.count() == 0
+            s.set_bodies(big)
+            s.step(0.01, 1.0, 2)
+            assert_states_identical(s.state(), exp, where=f"{prec}: after a failed growth")
