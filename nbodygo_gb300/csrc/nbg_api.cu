@@ -1678,6 +1678,10 @@ int nbg_step(nbg_ctx *ctx, double dt, double R, int nsteps, nbg_step_info *info)
     while (done < nsteps) {
         int rc = ensure_cap(ctx, ctx->n_host + ctx->pending_adds + 1, ctx->n_host);
         if (rc != NBG_OK) return rc;
+        /* the event buffers exist (an earlier failed reallocation leaves
+         * none, and the cycle's kernels write the per-sim event ranges) */
+        if ((rc = ensure_ev_cap(ctx, 1)) != NBG_OK) return rc;
+        if (ctx->cb.bh && (rc = ensure_bh(ctx, 0)) != NBG_OK) return rc; /* likewise the octree's */
         if ((rc = ensure_p64(ctx)) != NBG_OK) return rc;
         const int todo = nsteps - done;
         if (ctx->timing || !ctx->use_graph || todo < ctx->graph_cycles || todo == 1) {
@@ -1803,6 +1807,8 @@ int nbg_force_pass(nbg_ctx *ctx)
     {
         int rc = ensure_p64(ctx);
         if (rc != NBG_OK) return rc;
+        /* the octree's buffers exist (a failed allocation leaves none) */
+        if (ctx->cb.bh && (rc = ensure_bh(ctx, 0)) != NBG_OK) return rc;
     }
     for (int attempt = 0;; attempt++) {
         int z = 0;
