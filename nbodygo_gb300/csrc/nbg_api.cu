@@ -104,23 +104,30 @@ struct nbg_ctx {
 static int set_segments(nbg_ctx *ctx, int nsims, const ll *counts, bool *reshaped)
 {
     *reshaped = nsims != ctx->cb.seg.nsims;
+    if (!ctx->seg_h) {
+        cudaError_t e = cudaMallocHost((void **)&ctx->seg_h, (size_t)(NBG_MAX_SIMS + 1) * sizeof(ll));
+        if (e != cudaSuccess) {
+            ctx->seg_h = nullptr;
+            ctx->err = std::string("segment staging: ") + cudaGetErrorString(e);
+            return NBG_E_CUDA;
+        }
+    }
     if (nsims > ctx->seg_cap) {
+        /* without the arrays the context holds no collection (nsims 0):
+         * the cycle refuses to run until a load succeeds */
         cudaFree(ctx->seg_mem);
         ctx->seg_mem = nullptr;
+        ctx->seg_cap = 0;
+        memset(&ctx->cb.seg, 0, sizeof ctx->cb.seg);
+        *reshaped = true;
         cudaError_t e = cudaMalloc(&ctx->seg_mem, NBG_SEG_BYTES(nsims));
         if (e != cudaSuccess) {
+            ctx->seg_mem = nullptr;
+            cudaGetLastError();
             ctx->err = std::string("segment allocation: ") + cudaGetErrorString(e);
             return NBG_E_CUDA;
         }
         ctx->seg_cap = nsims;
-        *reshaped = true;
-    }
-    if (!ctx->seg_h) {
-        cudaError_t e = cudaMallocHost((void **)&ctx->seg_h, (size_t)(NBG_MAX_SIMS + 1) * sizeof(ll));
-        if (e != cudaSuccess) {
-            ctx->err = std::string("segment staging: ") + cudaGetErrorString(e);
-            return NBG_E_CUDA;
-        }
     }
     ctx->cb.seg = nbg_seg_carve(ctx->seg_mem, nsims);
     ll *h = ctx->seg_h;
@@ -1202,6 +1209,7 @@ int nbg_apply_edits(nbg_ctx *ctx, const nbg_edit *edits, int64_t k, int32_t *res
 int nbg_apply_edits_in(nbg_ctx *ctx, int64_t sim, const nbg_edit *edits, int64_t k, int32_t *results)
 {
     if (!ctx || k < 0 || (k > 0 && !edits)) return fail(ctx, NBG_E_ARG, "bad arguments");
+    if (ctx->cb.seg.nsims < 1) return fail(ctx, NBG_E_STATE, "no collection is loaded (a segment allocation failed)");
     if (sim < -1 || sim >= ctx->cb.seg.nsims) return fail(ctx, NBG_E_ARG, "collection index out of range");
     if (k == 0) return NBG_OK;
     for (ll q = 0; q < k; q++)
@@ -1260,6 +1268,7 @@ int nbg_get_body(nbg_ctx *ctx, int64_t id, nbg_soa *h, int32_t *found)
 int nbg_get_body_in(nbg_ctx *ctx, int64_t sim, int64_t id, nbg_soa *h, int32_t *found)
 {
     if (!ctx || !h || !found) return fail(ctx, NBG_E_ARG, "bad arguments");
+    if (ctx->cb.seg.nsims < 1) return fail(ctx, NBG_E_STATE, "no collection is loaded (a segment allocation failed)");
     if (sim < -1 || sim >= ctx->cb.seg.nsims) return fail(ctx, NBG_E_ARG, "collection index out of range");
     CK(cudaSetDevice(ctx->device));
     int rc = ensure_scratch(ctx, sizeof(ll));
@@ -1643,6 +1652,7 @@ int nbg_step(nbg_ctx *ctx, double dt, double R, int nsteps, nbg_step_info *info)
 {
     NvtxRange nvtx("nbg_step");
     if (!ctx || nsteps < 0) return fail(ctx, NBG_E_ARG, "bad arguments");
+    if (ctx->cb.seg.nsims < 1) return fail(ctx, NBG_E_STATE, "no collection is loaded (a segment allocation failed)");
     CK(cudaSetDevice(ctx->device));
     /* dt, R and the per-call accumulators */
     {
@@ -1803,6 +1813,7 @@ int nbg_force_pass(nbg_ctx *ctx)
 {
     NvtxRange nvtx("nbg_force_pass");
     if (!ctx) return NBG_E_ARG;
+    if (ctx->cb.seg.nsims < 1) return fail(ctx, NBG_E_STATE, "no collection is loaded (a segment allocation failed)");
     CK(cudaSetDevice(ctx->device));
     {
         int rc = ensure_p64(ctx);
@@ -1897,6 +1908,7 @@ int nbg_autotune(nbg_ctx *ctx, const char *cache_path, int *variant, double *bes
 {
     NvtxRange nvtx("nbg_autotune");
     if (!ctx) return NBG_E_ARG;
+    if (ctx->cb.seg.nsims < 1) return fail(ctx, NBG_E_STATE, "no collection is loaded (a segment allocation failed)");
     CK(cudaSetDevice(ctx->device));
     int rc = sync_ctl(ctx);
     if (rc != NBG_OK) return rc;
@@ -2050,6 +2062,7 @@ int nbg_get_forces(nbg_ctx *ctx, double *fx, double *fy, double *fz, int64_t cap
 int nbg_energy(nbg_ctx *ctx, double *kinetic, double *potential, double momentum[3])
 {
     if (!ctx) return NBG_E_ARG;
+    if (ctx->cb.seg.nsims < 1) return fail(ctx, NBG_E_STATE, "no collection is loaded (a segment allocation failed)");
     CK(cudaSetDevice(ctx->device));
     int rc = sync_ctl(ctx);
     if (rc != NBG_OK) return rc;
