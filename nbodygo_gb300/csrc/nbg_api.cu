@@ -2116,6 +2116,7 @@ int nbg_set_option(nbg_ctx *ctx, int key, int64_t value)
         ctx->use_graph = value != 0;
         return NBG_OK;
     case NBG_OPT_MIX_SHAPE:
+        if (value < 0 || value >= NBG_MIX_VARIANTS) return fail(ctx, NBG_E_ARG, "unknown kernel shape");
         return select_variant(ctx, (int)value);
     case NBG_OPT_BH_SHAPE:
         if (value < 0 || value > 2) return fail(ctx, NBG_E_ARG, "Barnes-Hut walk shape must be 0..2");
