@@ -585,10 +585,14 @@ static int ensure_ev_cap(nbg_ctx *ctx, ll need)
 static int ensure_scratch(nbg_ctx *ctx, size_t bytes)
 {
     if (bytes <= ctx->scratch_bytes) return NBG_OK;
+    size_t b = 1 << 16;
+    while (b < bytes) {
+        if (b > ((size_t)1 << 46)) return fail(ctx, NBG_E_ARG, "scratch request too large");
+        b <<= 1;
+    }
     cudaFree(ctx->scratch);
     ctx->scratch = nullptr;
-    size_t b = 1 << 16;
-    while (b < bytes) b <<= 1;
+    ctx->scratch_bytes = 0;
     CK(cudaMalloc(&ctx->scratch, b));
     ctx->scratch_bytes = b;
     return NBG_OK;
@@ -999,8 +1003,11 @@ int nbg_set_collections(nbg_ctx *ctx, int64_t nsims, const int64_t *counts, cons
     ll n = 0;
     for (ll s = 0; s < nsims; s++) {
         if (counts[s] < 0) return fail(ctx, NBG_E_ARG, "negative body count");
+        /* bounded one by one, so the sum cannot wrap */
+        if (counts[s] > NBG_MAX_BODIES) return fail(ctx, NBG_E_ARG, "body count exceeds 2^30");
         n += counts[s];
     }
+    if (n > NBG_MAX_BODIES) return fail(ctx, NBG_E_ARG, "body count exceeds 2^30");
     if (n > 0 && !host) return fail(ctx, NBG_E_ARG, "host is NULL");
     CK(cudaSetDevice(ctx->device));
     CK(cudaStreamSynchronize(ctx->st));
@@ -1150,6 +1157,8 @@ int nbg_add_bodies_to(nbg_ctx *ctx, int64_t sim, const nbg_soa *host, int64_t n,
     if (!ctx || n < 0 || (n > 0 && !host)) return fail(ctx, NBG_E_ARG, "bad arguments");
     if (sim < 0 || sim >= ctx->cb.seg.nsims) return fail(ctx, NBG_E_ARG, "collection index out of range");
     if (n == 0) return NBG_OK;
+    if (n > NBG_MAX_BODIES || ctx->n_host + ctx->pending_adds + n > NBG_MAX_BODIES)
+        return fail(ctx, NBG_E_ARG, "body count exceeds 2^30");
     CK(cudaSetDevice(ctx->device));
     int rc = sync_ctl(ctx);
     if (rc != NBG_OK) return rc;
@@ -1208,7 +1217,7 @@ int nbg_apply_edits(nbg_ctx *ctx, const nbg_edit *edits, int64_t k, int32_t *res
 
 int nbg_apply_edits_in(nbg_ctx *ctx, int64_t sim, const nbg_edit *edits, int64_t k, int32_t *results)
 {
-    if (!ctx || k < 0 || (k > 0 && !edits)) return fail(ctx, NBG_E_ARG, "bad arguments");
+    if (!ctx || k < 0 || (k > 0 && !edits) || k > NBG_MAX_BODIES) return fail(ctx, NBG_E_ARG, "bad arguments");
     if (ctx->cb.seg.nsims < 1) return fail(ctx, NBG_E_STATE, "no collection is loaded (a segment allocation failed)");
     if (sim < -1 || sim >= ctx->cb.seg.nsims) return fail(ctx, NBG_E_ARG, "collection index out of range");
     if (k == 0) return NBG_OK;
